@@ -1,0 +1,1073 @@
+// Operator assembly kernels for the exterior Burton-Miller Galerkin P1/DP0
+// Helmholtz BEM (sm_103a).
+//
+// The reference assembles four dense operators S, D, K', H with one CUDA
+// thread per element pair and float atomics
+// (src/blab/solvers/julia_local/src/BeatEngineCudaRegularKernels.jl:1-406,
+// BeatEngineCudaSingular.jl:301-530), then forms the Burton-Miller matrix
+// 1/2 M - D + eta H with a broadcast (BeatEngineCore.jl:1197).  Here one fused
+// pass writes the requested linear combination  cD*D + cH*H + cM*M11  of the
+// P1 x P1 operators straight into a column-major matrix, and the right-hand
+// side  (cS*S + cK*K' + cM10*M10) q  is formed matrix-free from the driven
+// faces only.  The integrands are those of the reference CPU pair integrals
+// (BeatEngineCpuAssembly.jl:151-218 and 278-373).
+//
+// Data flow for one frequency:
+//   regular_*_kernel      face pairs that share no vertex, 6x6 quadrature
+//                         -> Rext[(g*3+b)][e]  (extended rows e, trial face g)
+//   singular_dyn_kernel   vertex-sharing pairs (Duffy rules): k-dependent part,
+//                         combined with the k-independent FP64 moments
+//                         precomputed once per mesh -> per-pair 3x3 blocks
+//   singular_scatter      adds the singular blocks into Rext (one thread per
+//                         trial face: deterministic, no atomics)
+//   gather_columns        A[:, j] = sum over (g, b) in star(j) of Rext[g*3+b],
+//                         then halo extended rows folded into their rows
+#include "bem_common.cuh"
+#include "bem_internal.h"
+#include "bem_kernels.h"
+
+namespace bem {
+
+namespace {
+
+__device__ __forceinline__ bool share_vertex(const int* a, int b0, int b1, int b2) {
+  return a[0] == b0 || a[0] == b1 || a[0] == b2 || a[1] == b0 || a[1] == b1 || a[1] == b2 || a[2] == b0 ||
+         a[2] == b1 || a[2] == b2;
+}
+
+// ------------------------------------------------------------------------
+// Regular pairs, compensated FP32.
+//
+// Phase: k*r is split as k*|C| + k*(r - |C|), C = anchor_g - anchor_f.  The
+// first term is formed in double-float once per pair and reduced mod 2pi; the
+// second is small (|r - |C|| <= element size) and is computed in FP32 from
+// r - |C| = (2 C.d + d.d) / (r + |C|), d = off_g - off_f, which has no
+// cancellation.  Plain FP32 k*r loses ~kr * 6e-8 rad; this keeps the phase
+// error near 1e-7 rad for any kr.
+// ------------------------------------------------------------------------
+struct PairF32 {
+  float Cf[3];   // C rounded to float
+  float R0;      // |C| rounded to float
+  float theta0;  // k|C| mod 2pi
+};
+
+__device__ __forceinline__ PairF32 pair_setup_f32(const float* ahi_g, const float* alo_g, const float* ahi_f,
+                                                  const float* alo_f, df kdf) {
+  PairF32 P;
+  df C[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    df s = two_sum(ahi_g[d], -ahi_f[d]);
+    s.lo += alo_g[d] - alo_f[d];
+    C[d] = quick_two_sum(s.hi, s.lo);
+    P.Cf[d] = C[d].hi + C[d].lo;
+  }
+  df r2 = df_add(df_add(df_mul(C[0], C[0]), df_mul(C[1], C[1])), df_mul(C[2], C[2]));
+  df R = df_sqrt(r2);
+  P.R0 = R.hi + R.lo;
+  P.theta0 = df_reduce_two_pi(df_mul(kdf, R));
+  return P;
+}
+
+// Green's function and the radial factor of its gradient at one q-pair.
+// Returns false when the points coincide (the reference skips r == 0).
+__device__ __forceinline__ void green_f32(const PairF32& P, const float* d, float k, float& rinv, float rv[3],
+                                          float2& G) {
+  rv[0] = P.Cf[0] + d[0];
+  rv[1] = P.Cf[1] + d[1];
+  rv[2] = P.Cf[2] + d[2];
+  float r2 = fmaf(rv[0], rv[0], fmaf(rv[1], rv[1], rv[2] * rv[2]));
+  rinv = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
+  float r = r2 * rinv;
+  float cd = fmaf(P.Cf[0], d[0], fmaf(P.Cf[1], d[1], P.Cf[2] * d[2]));
+  float dd = fmaf(d[0], d[0], fmaf(d[1], d[1], d[2] * d[2]));
+  float den = fmaxf(r + P.R0, 1e-30f);
+  float delta = __fdividef(fmaf(2.0f, cd, dd), den);
+  float theta = reduce_two_pi(fmaf(k, delta, P.theta0));
+  float s, c;
+  __sincosf(theta, &s, &c);
+  float sc = rinv * BEM_INV_FOUR_PI;
+  G = make_float2(c * sc, s * sc);
+}
+
+// cw[a*Q + q] = phi_a(xi_q) * w_q of the regular rule (kernel parameters, so
+// meshes with different rules can run concurrently on different streams).
+struct RegParamsF32 {
+  df kdf;      // wavenumber as double-float
+  float k, k2;
+  float2 cD, cH;  // LHS coefficients of D and H
+  float cw[3 * kMaxQ];
+};
+
+template <int Q, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) regular_f32_kernel(const FaceF32* __restrict__ faces, int nf,
+                                                                 const int* __restrict__ tile_group_ptr,
+                                                                 const LaneSlot* __restrict__ slots,
+                                                                 const int* __restrict__ tile_row_base,
+                                                                 int max_rows, float2* __restrict__ Rext,
+                                                                 long long ldR, RegParamsF32 p) {
+  extern __shared__ float2 smem_acc32[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile = blockIdx.y;
+  const int g = blockIdx.x * WARPS + warp;
+  const int base = tile_row_base[tile];
+  const int rows = tile_row_base[tile + 1] - base;
+  float2* acc = smem_acc32 + (size_t)warp * 3 * max_rows;
+  for (int i = lane; i < 3 * max_rows; i += 32) acc[i] = make_float2(0.0f, 0.0f);
+  __syncwarp();
+  if (g >= nf) return;
+
+  // trial face (warp-uniform)
+  const FaceF32& T = faces[g];
+  float ahi_g[3], alo_g[3], ng[3], og[Q][3], cg[9];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    ahi_g[d] = T.anchor_hi[d];
+    alo_g[d] = T.anchor_lo[d];
+    ng[d] = T.normal[d];
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) cg[i] = T.curls[i];
+#pragma unroll
+  for (int n = 0; n < Q; ++n)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) og[n][d] = T.off[3 * n + d];
+  const float a2g = T.area2;
+  const int gv0 = T.verts[0], gv1 = T.verts[1], gv2 = T.verts[2];
+
+  const int g0 = tile_group_ptr[tile], g1 = tile_group_ptr[tile + 1];
+  for (int grp = g0; grp < g1; ++grp) {
+    const LaneSlot s = slots[(size_t)grp * 32 + lane];
+    if (s.face >= 0) {
+      const FaceF32& F = faces[s.face];
+      int fv[3] = {F.verts[0], F.verts[1], F.verts[2]};
+      if (!share_vertex(fv, gv0, gv1, gv2)) {
+        float ahi_f[3], alo_f[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          ahi_f[d] = F.anchor_hi[d];
+          alo_f[d] = F.anchor_lo[d];
+        }
+        PairF32 P = pair_setup_f32(ahi_g, alo_g, ahi_f, alo_f, p.kdf);
+        float2 IG[3][3], ID[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) {
+            IG[a][b] = make_float2(0.f, 0.f);
+            ID[a][b] = make_float2(0.f, 0.f);
+          }
+#pragma unroll
+        for (int m = 0; m < Q; ++m) {
+          float of[3] = {F.off[3 * m], F.off[3 * m + 1], F.off[3 * m + 2]};
+          float2 u[3], v[3];
+#pragma unroll
+          for (int b = 0; b < 3; ++b) {
+            u[b] = make_float2(0.f, 0.f);
+            v[b] = make_float2(0.f, 0.f);
+          }
+#pragma unroll
+          for (int n = 0; n < Q; ++n) {
+            float d[3] = {og[n][0] - of[0], og[n][1] - of[1], og[n][2] - of[2]};
+            float rinv, rv[3];
+            float2 G;
+            green_f32(P, d, p.k, rinv, rv, G);
+            // double-layer kernel dG/dn_y = G (ik - 1/r) (r . n_y)/r
+            float t = fmaf(rv[0], ng[0], fmaf(rv[1], ng[1], rv[2] * ng[2])) * rinv;
+            float2 Dk = make_float2(t * (-G.x * rinv - G.y * p.k), t * (G.x * p.k - G.y * rinv));
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+              const float c = p.cw[b * Q + n];
+              u[b].x = fmaf(c, G.x, u[b].x);
+              u[b].y = fmaf(c, G.y, u[b].y);
+              v[b].x = fmaf(c, Dk.x, v[b].x);
+              v[b].y = fmaf(c, Dk.y, v[b].y);
+            }
+          }
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            const float c = p.cw[a * Q + m];
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+              IG[a][b].x = fmaf(c, u[b].x, IG[a][b].x);
+              IG[a][b].y = fmaf(c, u[b].y, IG[a][b].y);
+              ID[a][b].x = fmaf(c, v[b].x, ID[a][b].x);
+              ID[a][b].y = fmaf(c, v[b].y, ID[a][b].y);
+            }
+          }
+        }
+        // combine: L = jac * (cD * D + cH * (curl.curl S0 - k^2 nn IG))
+        float2 S0 = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) S0 = cadd(S0, IG[a][b]);
+        const float nn = fmaf(F.normal[0], ng[0], fmaf(F.normal[1], ng[1], F.normal[2] * ng[2]));
+        const float jac = F.area2 * a2g;
+        const float kk_nn = p.k2 * nn;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const float cf0 = F.curls[3 * a], cf1 = F.curls[3 * a + 1], cf2 = F.curls[3 * a + 2];
+#pragma unroll
+          for (int b = 0; b < 3; ++b) {
+            const float cc = fmaf(cf0, cg[3 * b], fmaf(cf1, cg[3 * b + 1], cf2 * cg[3 * b + 2]));
+            float2 H = make_float2(cc * S0.x - kk_nn * IG[a][b].x, cc * S0.y - kk_nn * IG[a][b].y);
+            float2 L = cadd(cmul(p.cD, ID[a][b]), cmul(p.cH, H));
+            float2* dst = &acc[b * max_rows + s.loc[a]];
+            float2 o = *dst;
+            o.x = fmaf(jac, L.x, o.x);
+            o.y = fmaf(jac, L.y, o.y);
+            *dst = o;
+          }
+        }
+      }
+    }
+    __syncwarp();
+  }
+  // write this warp's three extended-row segments
+  for (int i = lane; i < 3 * rows; i += 32) {
+    const int b = i / rows, loc = i - b * rows;
+    Rext[(size_t)(3 * g + b) * ldR + base + loc] = acc[b * max_rows + loc];
+  }
+}
+
+// ------------------------------------------------------------------------
+// Regular pairs, FP64 (the plain FP64 form).
+// ------------------------------------------------------------------------
+struct RegParamsF64 {
+  double k, k2;
+  double2 cD, cH;
+  double cw[3 * kMaxQ];
+};
+
+template <int Q, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) regular_f64_kernel(const FaceF64* __restrict__ faces, int nf,
+                                                                 const int* __restrict__ tile_group_ptr,
+                                                                 const LaneSlot* __restrict__ slots,
+                                                                 const int* __restrict__ tile_row_base,
+                                                                 int max_rows, double2* __restrict__ Rext,
+                                                                 long long ldR, RegParamsF64 p) {
+  extern __shared__ double2 smem_acc64[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile = blockIdx.y;
+  const int g = blockIdx.x * WARPS + warp;
+  const int base = tile_row_base[tile];
+  const int rows = tile_row_base[tile + 1] - base;
+  double2* acc = smem_acc64 + (size_t)warp * 3 * max_rows;
+  for (int i = lane; i < 3 * max_rows; i += 32) acc[i] = make_double2(0.0, 0.0);
+  __syncwarp();
+  if (g >= nf) return;
+  const FaceF64& T = faces[g];
+  double ag[3], ng[3], og[Q][3], cg[9];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    ag[d] = T.anchor[d];
+    ng[d] = T.normal[d];
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) cg[i] = T.curls[i];
+#pragma unroll
+  for (int n = 0; n < Q; ++n)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) og[n][d] = T.off[3 * n + d];
+  const double a2g = T.area2;
+  const int gv0 = T.verts[0], gv1 = T.verts[1], gv2 = T.verts[2];
+  const int g0 = tile_group_ptr[tile], g1 = tile_group_ptr[tile + 1];
+  for (int grp = g0; grp < g1; ++grp) {
+    const LaneSlot s = slots[(size_t)grp * 32 + lane];
+    if (s.face >= 0) {
+      const FaceF64& F = faces[s.face];
+      int fv[3] = {F.verts[0], F.verts[1], F.verts[2]};
+      if (!share_vertex(fv, gv0, gv1, gv2)) {
+        double C[3] = {ag[0] - F.anchor[0], ag[1] - F.anchor[1], ag[2] - F.anchor[2]};
+        double2 IG[3][3], ID[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) {
+            IG[a][b] = make_double2(0., 0.);
+            ID[a][b] = make_double2(0., 0.);
+          }
+#pragma unroll 1
+        for (int m = 0; m < Q; ++m) {
+          const double of[3] = {F.off[3 * m], F.off[3 * m + 1], F.off[3 * m + 2]};
+          double2 u[3], v[3];
+#pragma unroll
+          for (int b = 0; b < 3; ++b) {
+            u[b] = make_double2(0., 0.);
+            v[b] = make_double2(0., 0.);
+          }
+#pragma unroll
+          for (int n = 0; n < Q; ++n) {
+            const double rv[3] = {C[0] + (og[n][0] - of[0]), C[1] + (og[n][1] - of[1]), C[2] + (og[n][2] - of[2])};
+            const double r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+            if (r2 == 0.0) continue;
+            const double r = sqrt(r2);
+            const double rinv = 1.0 / r;
+            double s, c;
+            sincos(p.k * r, &s, &c);
+            const double sc = rinv * (0.25 / CUDART_PI);
+            const double2 G = make_double2(c * sc, s * sc);
+            const double t = (rv[0] * ng[0] + rv[1] * ng[1] + rv[2] * ng[2]) * rinv;
+            const double2 Dk = make_double2(t * (-G.x * rinv - G.y * p.k), t * (G.x * p.k - G.y * rinv));
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+              const double cw = p.cw[b * Q + n];
+              u[b].x += cw * G.x;
+              u[b].y += cw * G.y;
+              v[b].x += cw * Dk.x;
+              v[b].y += cw * Dk.y;
+            }
+          }
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            const double cw = p.cw[a * Q + m];
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+              IG[a][b].x += cw * u[b].x;
+              IG[a][b].y += cw * u[b].y;
+              ID[a][b].x += cw * v[b].x;
+              ID[a][b].y += cw * v[b].y;
+            }
+          }
+        }
+        double2 S0 = make_double2(0., 0.);
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) S0 = cadd(S0, IG[a][b]);
+        const double nn = F.normal[0] * ng[0] + F.normal[1] * ng[1] + F.normal[2] * ng[2];
+        const double jac = F.area2 * a2g;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+#pragma unroll
+          for (int b = 0; b < 3; ++b) {
+            const double cc = F.curls[3 * a] * cg[3 * b] + F.curls[3 * a + 1] * cg[3 * b + 1] +
+                              F.curls[3 * a + 2] * cg[3 * b + 2];
+            double2 H = make_double2(cc * S0.x - p.k2 * nn * IG[a][b].x, cc * S0.y - p.k2 * nn * IG[a][b].y);
+            double2 L = cadd(cmul(p.cD, ID[a][b]), cmul(p.cH, H));
+            double2* dst = &acc[b * max_rows + s.loc[a]];
+            double2 o = *dst;
+            o.x += jac * L.x;
+            o.y += jac * L.y;
+            *dst = o;
+          }
+        }
+      }
+    }
+    __syncwarp();
+  }
+  for (int i = lane; i < 3 * rows; i += 32) {
+    const int b = i / rows, loc = i - b * rows;
+    Rext[(size_t)(3 * g + b) * ldR + base + loc] = acc[b * max_rows + loc];
+  }
+}
+
+// ------------------------------------------------------------------------
+// Singular (vertex-sharing) pairs.
+//
+// The Green's function is split into a k-independent singular part and a
+// smooth k-dependent remainder, both integrated with the same Duffy points:
+//   G            = s + R,                 s = 1/(4 pi r),  R = s (e^{ikr} - 1)
+//   dG/dn_y      = -(r.n_y) s / r^2 + h(kr) (r.n_y) s / r^2
+//   adjoint      = +(r.n_x) s / r^2 - h(kr) (r.n_x) s / r^2
+//   h(z)         = e^{iz}(iz - 1) + 1 = (1 - cos z - z sin z) + i (z cos z - sin z)
+// The k-independent moments are integrated once per mesh in FP64; the
+// remainder is integrated per frequency (FP32 in the mixed form, FP64 in the
+// plain form).  The sum is the reference's Duffy quadrature of the full kernel
+// (BeatEngineCpuAssembly.jl:151-218) up to rounding.
+//
+// Static moments per pair (24 doubles, all times jac):
+//   [0..2]  SG0[a] = sum w phi_a(x) s
+//   [3..11] IG0[a][b] = sum w phi_a(x) phi_b(y) s
+//   [12..20] ID0[a][b] = sum w phi_a phi_b (-(r.n_y) s / r^2)
+//   [21..23] IK0[a] = sum w phi_a(x) (+(r.n_x) s / r^2)
+// ------------------------------------------------------------------------
+constexpr int kStatic = 24;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+struct SingularGeom {
+  const double* verts;  // nv x 3
+  const int* faces;     // nf x 3
+  const double* normal;
+};
+
+__global__ void singular_static_kernel(SingularGeom geo, const SingularPair* __restrict__ pairs, int npairs,
+                                       const int* __restrict__ rule_ptr, const double* __restrict__ duffy,
+                                       double* __restrict__ moments) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= npairs) return;
+  const SingularPair P = pairs[warp];
+  const int* ft = geo.faces + 3 * P.test;
+  const int* fr = geo.faces + 3 * P.trial;
+  double t0[3], e1t[3], e2t[3], d0[3], e1r[3], e2r[3], nt[3], nr[3];
+  for (int d = 0; d < 3; ++d) {
+    t0[d] = geo.verts[3 * ft[0] + d];
+    e1t[d] = geo.verts[3 * ft[1] + d] - t0[d];
+    e2t[d] = geo.verts[3 * ft[2] + d] - t0[d];
+    const double r0 = geo.verts[3 * fr[0] + d];
+    d0[d] = r0 - t0[d];
+    e1r[d] = geo.verts[3 * fr[1] + d] - r0;
+    e2r[d] = geo.verts[3 * fr[2] + d] - r0;
+    nt[d] = geo.normal[3 * P.test + d];
+    nr[d] = geo.normal[3 * P.trial + d];
+  }
+  double acc[kStatic];
+#pragma unroll
+  for (int i = 0; i < kStatic; ++i) acc[i] = 0.0;
+  const int q0 = rule_ptr[P.rule], q1 = rule_ptr[P.rule + 1];
+  for (int q = q0 + lane; q < q1; q += 32) {
+    const double* pt = duffy + 5 * (size_t)q;
+    const double tu = pt[0], tv = pt[1], ru = pt[2], rvv = pt[3], w = pt[4];
+    const double px[3] = {1.0 - tu - tv, tu, tv};
+    const double py[3] = {1.0 - ru - rvv, ru, rvv};
+    double rv[3];
+    for (int d = 0; d < 3; ++d) rv[d] = (d0[d] + ru * e1r[d] + rvv * e2r[d]) - (tu * e1t[d] + tv * e2t[d]);
+    const double r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+    if (r2 == 0.0) continue;
+    const double rinv = rsqrt(r2);
+    const double s = rinv * (0.25 / CUDART_PI);
+    const double dny = -(rv[0] * nr[0] + rv[1] * nr[1] + rv[2] * nr[2]) * s * rinv * rinv;
+    const double dnx = (rv[0] * nt[0] + rv[1] * nt[1] + rv[2] * nt[2]) * s * rinv * rinv;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double wa = w * px[a];
+      acc[a] += wa * s;
+      acc[21 + a] += wa * dnx;
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        acc[3 + 3 * a + b] += wa * py[b] * s;
+        acc[12 + 3 * a + b] += wa * py[b] * dny;
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < kStatic; ++i) {
+    const double v = warp_sum(acc[i]);
+    if (lane == 0) moments[(size_t)kStatic * warp + i] = v * P.jac;
+  }
+}
+
+template <typename R> struct SingParams;
+template <> struct SingParams<float> {
+  float k, k2;
+  float2 cD, cH, cM, cS, cK, cM10;
+};
+template <> struct SingParams<double> {
+  double k, k2;
+  double2 cD, cH, cM, cS, cK, cM10;
+};
+
+// Per pair output: 9 LHS block entries then 3 RHS-operator entries (complex).
+constexpr int kSingOut = 12;
+
+template <typename R>
+__global__ void singular_dyn_kernel(SingularGeom geo, const SingularPair* __restrict__ pairs, int npairs,
+                                    const int* __restrict__ rule_ptr, const double* __restrict__ duffy,
+                                    const double* __restrict__ moments, const double* __restrict__ curls,
+                                    const double* __restrict__ area, const double* __restrict__ m11m10,
+                                    SingParams<R> p, typename cplx<R>::type* __restrict__ out) {
+  typedef typename cplx<R>::type C2;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= npairs) return;
+  const SingularPair P = pairs[warp];
+  const int* ft = geo.faces + 3 * P.test;
+  const int* fr = geo.faces + 3 * P.trial;
+  R e1t[3], e2t[3], d0[3], e1r[3], e2r[3], nt[3], nr[3];
+  for (int d = 0; d < 3; ++d) {
+    const double t0 = geo.verts[3 * ft[0] + d];
+    const double r0 = geo.verts[3 * fr[0] + d];
+    e1t[d] = (R)(geo.verts[3 * ft[1] + d] - t0);
+    e2t[d] = (R)(geo.verts[3 * ft[2] + d] - t0);
+    d0[d] = (R)(r0 - t0);
+    e1r[d] = (R)(geo.verts[3 * fr[1] + d] - r0);
+    e2r[d] = (R)(geo.verts[3 * fr[2] + d] - r0);
+    nt[d] = (R)geo.normal[3 * P.test + d];
+    nr[d] = (R)geo.normal[3 * P.trial + d];
+  }
+  // accumulators: SR[3], IR[9], IDh[9], IKh[3] (complex) = 48 reals
+  R acc[48];
+#pragma unroll
+  for (int i = 0; i < 48; ++i) acc[i] = R(0);
+  const R inv4pi = R(0.25 / CUDART_PI);
+  const int q0 = rule_ptr[P.rule], q1 = rule_ptr[P.rule + 1];
+  for (int q = q0 + lane; q < q1; q += 32) {
+    const double* pt = duffy + 5 * (size_t)q;
+    const R tu = (R)pt[0], tv = (R)pt[1], ru = (R)pt[2], rvv = (R)pt[3], w = (R)pt[4];
+    const R px[3] = {R(1) - tu - tv, tu, tv};
+    const R py[3] = {R(1) - ru - rvv, ru, rvv};
+    R rv[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) rv[d] = (d0[d] + ru * e1r[d] + rvv * e2r[d]) - (tu * e1t[d] + tv * e2t[d]);
+    const R r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+    if (r2 == R(0)) continue;
+    R rinv, r, sh, ch;
+    if constexpr (sizeof(R) == 4) {
+      rinv = rsqrtf(r2);
+      r = r2 * rinv;
+      sincosf(R(0.5) * p.k * r, &sh, &ch);
+    } else {
+      rinv = rsqrt(r2);
+      r = r2 * rinv;
+      sincos(R(0.5) * p.k * r, &sh, &ch);
+    }
+    const R z = p.k * r;
+    const R s = rinv * inv4pi;
+    const R sinz = R(2) * sh * ch;
+    const R omc = R(2) * sh * sh;  // 1 - cos z
+    const R cosz = R(1) - omc;
+    // R = s (cos z - 1 + i sin z)
+    const R Rr = -s * omc, Ri = s * sinz;
+    // h(z) = (1 - cos z - z sin z) + i (z cos z - sin z)
+    const R hr = omc - z * sinz, hi = z * cosz - sinz;
+    const R fy = (rv[0] * nr[0] + rv[1] * nr[1] + rv[2] * nr[2]) * s * rinv * rinv;
+    const R fx = -(rv[0] * nt[0] + rv[1] * nt[1] + rv[2] * nt[2]) * s * rinv * rinv;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const R wa = w * px[a];
+      acc[2 * a] += wa * Rr;
+      acc[2 * a + 1] += wa * Ri;
+      acc[42 + 2 * a] += wa * hr * fx;
+      acc[42 + 2 * a + 1] += wa * hi * fx;
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const R wab = wa * py[b];
+        acc[6 + 2 * (3 * a + b)] += wab * Rr;
+        acc[6 + 2 * (3 * a + b) + 1] += wab * Ri;
+        acc[24 + 2 * (3 * a + b)] += wab * hr * fy;
+        acc[24 + 2 * (3 * a + b) + 1] += wab * hi * fy;
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 48; ++i) acc[i] = warp_sum(acc[i]);
+  if (lane != 0) return;
+  const double* M = moments + (size_t)kStatic * warp;
+  const R jac = (R)P.jac;
+  C2 SR[3], IR[9], IDh[9], IKh[3];
+  for (int a = 0; a < 3; ++a) {
+    SR[a] = cplx<R>::make(acc[2 * a] * jac, acc[2 * a + 1] * jac);
+    IKh[a] = cplx<R>::make(acc[42 + 2 * a] * jac, acc[42 + 2 * a + 1] * jac);
+  }
+  for (int i = 0; i < 9; ++i) {
+    IR[i] = cplx<R>::make(acc[6 + 2 * i] * jac, acc[6 + 2 * i + 1] * jac);
+    IDh[i] = cplx<R>::make(acc[24 + 2 * i] * jac, acc[24 + 2 * i + 1] * jac);
+  }
+  // S0 = sum w G (static + dynamic)
+  C2 S0 = cplx<R>::make((R)(M[0] + M[1] + M[2]), R(0));
+  for (int a = 0; a < 3; ++a) S0 = cadd(S0, SR[a]);
+  const double* ct = curls + 9 * (size_t)P.test;
+  const double* cr = curls + 9 * (size_t)P.trial;
+  const R kk_nn = p.k2 * (R)P.nprod;
+  const bool coincident = P.kind == 1;
+  const R a2 = (R)(2.0 * area[P.test]);
+  C2* o = out + (size_t)kSingOut * warp;
+  for (int a = 0; a < 3; ++a) {
+    for (int b = 0; b < 3; ++b) {
+      const R cc = (R)(ct[3 * a] * cr[3 * b] + ct[3 * a + 1] * cr[3 * b + 1] + ct[3 * a + 2] * cr[3 * b + 2]);
+      const int i = 3 * a + b;
+      C2 D = cplx<R>::make((R)M[12 + i] + IDh[i].x, IDh[i].y);
+      C2 IGt = cplx<R>::make((R)M[3 + i] + IR[i].x, IR[i].y);
+      C2 H = cplx<R>::make(cc * S0.x - kk_nn * IGt.x, cc * S0.y - kk_nn * IGt.y);
+      C2 L = cadd(cmul(p.cD, D), cmul(p.cH, H));
+      if (coincident) L = cadd(L, cscale(p.cM, a2 * (R)m11m10[i]));
+      o[i] = L;
+    }
+    C2 S = cplx<R>::make((R)M[a] + SR[a].x, SR[a].y);
+    C2 K = cplx<R>::make((R)M[21 + a] + IKh[a].x, IKh[a].y);
+    C2 rhs = cadd(cmul(p.cS, S), cmul(p.cK, K));
+    if (coincident) rhs = cadd(rhs, cscale(p.cM10, a2 * (R)m11m10[9 + a]));
+    o[9 + a] = rhs;
+  }
+}
+
+// One thread per trial face: add its singular blocks into the extended rows.
+template <typename C2>
+__global__ void singular_scatter_kernel(const SingularPair* __restrict__ pairs, const int* __restrict__ by_trial_ptr,
+                                        const int* __restrict__ face_ext, const C2* __restrict__ blocks, int nf,
+                                        C2* __restrict__ Rext, long long ldR) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nf) return;
+  for (int k = by_trial_ptr[g]; k < by_trial_ptr[g + 1]; ++k) {
+    const int f = pairs[k].test;
+    const C2* blk = blocks + (size_t)kSingOut * k;
+    for (int a = 0; a < 3; ++a) {
+      const int e = face_ext[3 * f + a];
+      for (int b = 0; b < 3; ++b) {
+        C2* dst = &Rext[(size_t)(3 * g + b) * ldR + e];
+        *dst = cadd(*dst, blk[3 * a + b]);
+      }
+    }
+  }
+}
+
+// One CTA per column: A[:, j] in permuted row order.
+template <typename C2>
+__global__ void gather_columns_kernel(const C2* __restrict__ Rext, long long ldR, const int* __restrict__ col_ptr,
+                                      const int* __restrict__ col_fb, const int* __restrict__ ext_row,
+                                      const int* __restrict__ halo_slot_of_ext, const int* __restrict__ halo_row_ptr,
+                                      const int* __restrict__ halo_row, int n_ext, int n_halo_rows,
+                                      C2* __restrict__ A, long long lda, C2* __restrict__ A2, int col0) {
+  extern __shared__ unsigned char smem_raw[];
+  C2* hb = reinterpret_cast<C2*>(smem_raw);
+  const int j = col0 + blockIdx.x;
+  const int k0 = col_ptr[j], k1 = col_ptr[j + 1];
+  C2* Aj = A + (size_t)j * lda;
+  C2* A2j = A2 ? A2 + (size_t)j * lda : nullptr;
+  for (int e = threadIdx.x; e < n_ext; e += blockDim.x) {
+    C2 v;
+    v.x = 0;
+    v.y = 0;
+    for (int k = k0; k < k1; ++k) v = cadd(v, Rext[(size_t)col_fb[k] * ldR + e]);
+    const int hs = halo_slot_of_ext[e];
+    if (hs < 0) {
+      Aj[ext_row[e]] = v;
+      if (A2j) A2j[ext_row[e]] = v;
+    } else {
+      hb[hs] = v;
+    }
+  }
+  __syncthreads();
+  for (int h = threadIdx.x; h < n_halo_rows; h += blockDim.x) {
+    C2 s;
+    s.x = 0;
+    s.y = 0;
+    for (int i = halo_row_ptr[h]; i < halo_row_ptr[h + 1]; ++i) s = cadd(s, hb[i]);
+    const int r = halo_row[h];
+    Aj[r] = cadd(Aj[r], s);
+    if (A2j) A2j[r] = cadd(A2j[r], s);
+  }
+}
+
+// ------------------------------------------------------------------------
+// Right-hand side, regular part: warp per test face, lanes over driven faces.
+//   rb[f][a][c] = sum_{g driven, not adjacent} q_c[g] (cS S_fg[a] + cK K'_fg[a])
+//                 + sum over singular pairs (f, g) of q_c[g] * block_rhs[a]
+// q_c[g] = qscale * drive[c][g]  (qscale = i rho omega).
+// ------------------------------------------------------------------------
+template <typename R> struct RhsParams;
+template <> struct RhsParams<float> {
+  df kdf;
+  float k;
+  float2 cS, cK, qscale;
+  float cw[3 * kMaxQ];
+};
+template <> struct RhsParams<double> {
+  double k;
+  double2 cS, cK, qscale;
+  double cw[3 * kMaxQ];
+};
+
+template <typename R> struct FaceRec;
+template <> struct FaceRec<float> { typedef FaceF32 type; };
+template <> struct FaceRec<double> { typedef FaceF64 type; };
+
+template <int Q>
+__device__ __forceinline__ void rhs_pair_f32(const FaceF32& F, const FaceF32& Gf, const RhsParams<float>& p,
+                                             float2 S[3], float2 K[3]) {
+  PairF32 P = pair_setup_f32(Gf.anchor_hi, Gf.anchor_lo, F.anchor_hi, F.anchor_lo, p.kdf);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    S[a] = make_float2(0.f, 0.f);
+    K[a] = make_float2(0.f, 0.f);
+  }
+#pragma unroll 1
+  for (int m = 0; m < Q; ++m) {
+    float of[3] = {F.off[3 * m], F.off[3 * m + 1], F.off[3 * m + 2]};
+    float2 us = make_float2(0.f, 0.f), uk = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int n = 0; n < Q; ++n) {
+      float d[3] = {Gf.off[3 * n] - of[0], Gf.off[3 * n + 1] - of[1], Gf.off[3 * n + 2] - of[2]};
+      float rinv, rv[3];
+      float2 G;
+      green_f32(P, d, p.k, rinv, rv, G);
+      // adjoint double layer: G (-1/r + ik) * (-(r . n_x)/r)
+      float t = -fmaf(rv[0], F.normal[0], fmaf(rv[1], F.normal[1], rv[2] * F.normal[2])) * rinv;
+      float2 Kk = make_float2(t * (-G.x * rinv - G.y * p.k), t * (G.x * p.k - G.y * rinv));
+      // DP0 trial basis: weight is w_n only (sum_b phi_b w_n)
+      float wn = p.cw[n] + p.cw[Q + n] + p.cw[2 * Q + n];
+      us.x = fmaf(wn, G.x, us.x);
+      us.y = fmaf(wn, G.y, us.y);
+      uk.x = fmaf(wn, Kk.x, uk.x);
+      uk.y = fmaf(wn, Kk.y, uk.y);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float c = p.cw[a * Q + m];
+      S[a].x = fmaf(c, us.x, S[a].x);
+      S[a].y = fmaf(c, us.y, S[a].y);
+      K[a].x = fmaf(c, uk.x, K[a].x);
+      K[a].y = fmaf(c, uk.y, K[a].y);
+    }
+  }
+  const float jac = F.area2 * Gf.area2;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    S[a] = cscale(S[a], jac);
+    K[a] = cscale(K[a], jac);
+  }
+}
+
+template <int Q>
+__device__ __forceinline__ void rhs_pair_f64(const FaceF64& F, const FaceF64& Gf, const RhsParams<double>& p,
+                                             double2 S[3], double2 K[3]) {
+  const double C[3] = {Gf.anchor[0] - F.anchor[0], Gf.anchor[1] - F.anchor[1], Gf.anchor[2] - F.anchor[2]};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    S[a] = make_double2(0., 0.);
+    K[a] = make_double2(0., 0.);
+  }
+#pragma unroll 1
+  for (int m = 0; m < Q; ++m) {
+    double2 us = make_double2(0., 0.), uk = make_double2(0., 0.);
+#pragma unroll
+    for (int n = 0; n < Q; ++n) {
+      double rv[3];
+      for (int d = 0; d < 3; ++d) rv[d] = C[d] + (Gf.off[3 * n + d] - F.off[3 * m + d]);
+      const double r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+      if (r2 == 0.0) continue;
+      const double r = sqrt(r2), rinv = 1.0 / r;
+      double s, c;
+      sincos(p.k * r, &s, &c);
+      const double sc = rinv * (0.25 / CUDART_PI);
+      const double2 G = make_double2(c * sc, s * sc);
+      const double t = -(rv[0] * F.normal[0] + rv[1] * F.normal[1] + rv[2] * F.normal[2]) * rinv;
+      const double2 Kk = make_double2(t * (-G.x * rinv - G.y * p.k), t * (G.x * p.k - G.y * rinv));
+      const double wn = p.cw[n] + p.cw[Q + n] + p.cw[2 * Q + n];
+      us.x += wn * G.x;
+      us.y += wn * G.y;
+      uk.x += wn * Kk.x;
+      uk.y += wn * Kk.y;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double c = p.cw[a * Q + m];
+      S[a].x += c * us.x;
+      S[a].y += c * us.y;
+      K[a].x += c * uk.x;
+      K[a].y += c * uk.y;
+    }
+  }
+  const double jac = F.area2 * Gf.area2;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    S[a] = cscale(S[a], jac);
+    K[a] = cscale(K[a], jac);
+  }
+}
+
+template <typename R, int Q, int NC>
+__global__ void rhs_faces_kernel(const typename FaceRec<R>::type* __restrict__ faces, int nf,
+                                 const int* __restrict__ driven, int ndriven,
+                                 const typename cplx<R>::type* __restrict__ drive,  // NC x nf
+                                 const SingularPair* __restrict__ pairs, const int* __restrict__ by_test_ptr,
+                                 const int* __restrict__ by_test, const typename cplx<R>::type* __restrict__ sblocks,
+                                 RhsParams<R> p, typename cplx<R>::type* __restrict__ rb) {
+  typedef typename cplx<R>::type C2;
+  const int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (f >= nf) return;
+  const auto& F = faces[f];
+  C2 acc[3][NC];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[a][c] = cplx<R>::make(0, 0);
+  for (int i = lane; i < ndriven; i += 32) {
+    const int g = driven[i];
+    const auto& Gf = faces[g];
+    if (share_vertex(F.verts, Gf.verts[0], Gf.verts[1], Gf.verts[2])) continue;
+    C2 S[3], K[3];
+    if constexpr (sizeof(R) == 4)
+      rhs_pair_f32<Q>(F, Gf, p, S, K);
+    else
+      rhs_pair_f64<Q>(F, Gf, p, S, K);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const C2 q = cmul(p.qscale, drive[(size_t)c * nf + g]);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) acc[a][c] = cadd(acc[a][c], cmul(q, cadd(cmul(p.cS, S[a]), cmul(p.cK, K[a]))));
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      acc[a][c].x = warp_sum(acc[a][c].x);
+      acc[a][c].y = warp_sum(acc[a][c].y);
+    }
+  if (lane != 0) return;
+  for (int k = by_test_ptr[f]; k < by_test_ptr[f + 1]; ++k) {
+    const int pid = by_test[k];
+    const int g = pairs[pid].trial;
+    const C2* blk = sblocks + (size_t)kSingOut * pid;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const C2 q = cmul(p.qscale, drive[(size_t)c * nf + g]);
+      if (q.x == 0 && q.y == 0) continue;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) acc[a][c] = cadd(acc[a][c], cmul(q, blk[9 + a]));
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < NC; ++c) rb[((size_t)c * nf + f) * 3 + a] = acc[a][c];
+}
+
+// b[row(j)][c] = sum over (f, a) in star(j) of rb[c][f][a]
+template <typename C2>
+__global__ void rhs_gather_kernel(const C2* __restrict__ rb, int nf, int nc, const int* __restrict__ col_ptr,
+                                  const int* __restrict__ col_fb, const int* __restrict__ vertex_row, int nv,
+                                  C2* __restrict__ b, long long ldb) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nv) return;
+  for (int c = 0; c < nc; ++c) {
+    C2 s;
+    s.x = 0;
+    s.y = 0;
+    for (int k = col_ptr[j]; k < col_ptr[j + 1]; ++k) s = cadd(s, rb[(size_t)c * nf * 3 + col_fb[k]]);
+    b[(size_t)c * ldb + vertex_row[j]] = s;
+  }
+}
+
+// Rows/columns of vertices that no face references: identity (pressure 0).
+template <typename C2>
+__global__ void isolated_identity_kernel(const int* __restrict__ iso, int n, const int* __restrict__ vertex_row,
+                                         C2* A, long long lda, C2* A2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int v = iso[i];
+  C2 one;
+  one.x = 1;
+  one.y = 0;
+  A[(size_t)v * lda + vertex_row[v]] = one;
+  if (A2) A2[(size_t)v * lda + vertex_row[v]] = one;
+}
+
+}  // namespace
+
+// --------------------------------------------------------------- launchers --
+
+static inline float2 f2(double2 v) { return make_float2((float)v.x, (float)v.y); }
+
+static df make_df(double x) {
+  df r;
+  r.hi = (float)x;
+  r.lo = (float)(x - (double)r.hi);
+  return r;
+}
+
+cudaError_t launch_regular(const DeviceMesh& m, Precision prec, double k, double2 cD, double2 cH, void* Rext,
+                           long long ldR, cudaStream_t stream) {
+  const int W = 4;
+  dim3 grid((m.nf + W - 1) / W, m.n_tiles);
+  if (prec == Precision::Mixed) {
+    RegParamsF32 p;
+    p.kdf = make_df(k);
+    p.k = (float)k;
+    p.k2 = (float)(k * k);
+    p.cD = f2(cD);
+    p.cH = f2(cH);
+    for (int i = 0; i < 3 * kMaxQ; ++i) p.cw[i] = (float)m.rule_cw[i];
+    size_t sm = (size_t)W * 3 * m.max_tile_rows * sizeof(float2);
+    auto launch = [&](auto kern) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      kern<<<grid, W * 32, sm, stream>>>(m.faces32, m.nf, m.tile_group_ptr, m.lane_slots, m.tile_row_base,
+                                         m.max_tile_rows, (float2*)Rext, ldR, p);
+    };
+    if (m.Q == 6)
+      launch(regular_f32_kernel<6, W>);
+    else if (m.Q == 3)
+      launch(regular_f32_kernel<3, W>);
+    else
+      launch(regular_f32_kernel<1, W>);
+  } else {
+    RegParamsF64 p;
+    p.k = k;
+    p.k2 = k * k;
+    p.cD = cD;
+    p.cH = cH;
+    for (int i = 0; i < 3 * kMaxQ; ++i) p.cw[i] = m.rule_cw[i];
+    size_t sm = (size_t)W * 3 * m.max_tile_rows * sizeof(double2);
+    auto launch = [&](auto kern) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      kern<<<grid, W * 32, sm, stream>>>(m.faces64, m.nf, m.tile_group_ptr, m.lane_slots, m.tile_row_base,
+                                         m.max_tile_rows, (double2*)Rext, ldR, p);
+    };
+    if (m.Q == 6)
+      launch(regular_f64_kernel<6, W>);
+    else if (m.Q == 3)
+      launch(regular_f64_kernel<3, W>);
+    else
+      launch(regular_f64_kernel<1, W>);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, cudaStream_t stream) {
+  if (m.npairs == 0) return cudaSuccess;
+  SingularGeom geo{m.verts, m.faces, m.normal};
+  const int threads = 256;
+  const int blocks = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
+  singular_static_kernel<<<blocks, threads, 0, stream>>>(geo, m.pairs, m.npairs, m.rule_ptr, m.duffy, moments);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, double k, const OperatorCoeffs& c,
+                                void* blocks, cudaStream_t stream) {
+  if (m.npairs == 0) return cudaSuccess;
+  SingularGeom geo{m.verts, m.faces, m.normal};
+  const int threads = 256;
+  const int nblk = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
+  if (prec == Precision::Mixed) {
+    SingParams<float> p;
+    p.k = (float)k;
+    p.k2 = (float)(k * k);
+    p.cD = f2(c.cD);
+    p.cH = f2(c.cH);
+    p.cM = f2(c.cM);
+    p.cS = f2(c.cS);
+    p.cK = f2(c.cK);
+    p.cM10 = f2(c.cM10);
+    singular_dyn_kernel<float><<<nblk, threads, 0, stream>>>(geo, m.pairs, m.npairs, m.rule_ptr, m.duffy,
+                                                             m.moments, m.curls, m.area, m.m11m10, p,
+                                                             (float2*)blocks);
+  } else {
+    SingParams<double> p;
+    p.k = k;
+    p.k2 = k * k;
+    p.cD = c.cD;
+    p.cH = c.cH;
+    p.cM = c.cM;
+    p.cS = c.cS;
+    p.cK = c.cK;
+    p.cM10 = c.cM10;
+    singular_dyn_kernel<double><<<nblk, threads, 0, stream>>>(geo, m.pairs, m.npairs, m.rule_ptr, m.duffy,
+                                                              m.moments, m.curls, m.area, m.m11m10, p,
+                                                              (double2*)blocks);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_singular_scatter(const DeviceMesh& m, Precision prec, const void* blocks, void* Rext,
+                                    long long ldR, cudaStream_t stream) {
+  const int threads = 128;
+  const int nblk = (m.nf + threads - 1) / threads;
+  if (prec == Precision::Mixed)
+    singular_scatter_kernel<float2><<<nblk, threads, 0, stream>>>(m.pairs, m.pairs_by_trial_ptr, m.face_ext,
+                                                                  (const float2*)blocks, m.nf, (float2*)Rext, ldR);
+  else
+    singular_scatter_kernel<double2><<<nblk, threads, 0, stream>>>(m.pairs, m.pairs_by_trial_ptr, m.face_ext,
+                                                                   (const double2*)blocks, m.nf, (double2*)Rext,
+                                                                   ldR);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const DeviceMesh& m, Precision prec, const void* Rext, long long ldR, void* A, long long lda,
+                          void* A2, cudaStream_t stream) {
+  const int threads = 256;
+  const int n_halo = m.n_halo;
+  if (prec == Precision::Mixed) {
+    size_t sm = (size_t)std::max(1, n_halo) * sizeof(float2);
+    if (sm > 48 * 1024) cudaFuncSetAttribute(gather_columns_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    gather_columns_kernel<float2><<<m.nv, threads, sm, stream>>>(
+        (const float2*)Rext, ldR, m.col_ptr, m.col_fb, m.ext_row, m.halo_slot_of_ext, m.halo_row_ptr, m.halo_row,
+        m.n_ext, m.n_halo_rows, (float2*)A, lda, (float2*)A2, 0);
+    if (m.n_isolated)
+      isolated_identity_kernel<float2><<<(m.n_isolated + 127) / 128, 128, 0, stream>>>(
+          m.isolated, m.n_isolated, m.vertex_row, (float2*)A, lda, (float2*)A2);
+  } else {
+    size_t sm = (size_t)std::max(1, n_halo) * sizeof(double2);
+    if (sm > 48 * 1024) cudaFuncSetAttribute(gather_columns_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    gather_columns_kernel<double2><<<m.nv, threads, sm, stream>>>(
+        (const double2*)Rext, ldR, m.col_ptr, m.col_fb, m.ext_row, m.halo_slot_of_ext, m.halo_row_ptr,
+        m.halo_row, m.n_ext, m.n_halo_rows, (double2*)A, lda, (double2*)A2, 0);
+    if (m.n_isolated)
+      isolated_identity_kernel<double2><<<(m.n_isolated + 127) / 128, 128, 0, stream>>>(
+          m.isolated, m.n_isolated, m.vertex_row, (double2*)A, lda, (double2*)A2);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rhs(const DeviceMesh& m, Precision prec, double k, const OperatorCoeffs& c, double2 qscale,
+                       const void* drive, int nc, const void* sblocks, void* rb, void* b, long long ldb,
+                       cudaStream_t stream) {
+  const int threads = 128;
+  const int nblk = (int)(((long long)m.nf * 32 + threads - 1) / threads);
+  if (prec == Precision::Mixed) {
+    RhsParams<float> p;
+    p.kdf = make_df(k);
+    p.k = (float)k;
+    p.cS = f2(c.cS);
+    p.cK = f2(c.cK);
+    p.qscale = f2(qscale);
+    for (int i = 0; i < 3 * kMaxQ; ++i) p.cw[i] = (float)m.rule_cw[i];
+#define BEM_RHS32(QQ, NCC)                                                                                   \
+  rhs_faces_kernel<float, QQ, NCC><<<nblk, threads, 0, stream>>>(m.faces32, m.nf, m.driven, m.ndriven,        \
+                                                                 (const float2*)drive, m.pairs,              \
+                                                                 m.pairs_by_test_ptr, m.pairs_by_test,       \
+                                                                 (const float2*)sblocks, p, (float2*)rb)
+#define BEM_RHS32_Q(NCC)        \
+  if (m.Q == 6)                 \
+    BEM_RHS32(6, NCC);          \
+  else if (m.Q == 3)            \
+    BEM_RHS32(3, NCC);          \
+  else                          \
+    BEM_RHS32(1, NCC);
+    switch (nc) {
+      case 1: BEM_RHS32_Q(1) break;
+      case 2: BEM_RHS32_Q(2) break;
+      case 3: BEM_RHS32_Q(3) break;
+      case 4: BEM_RHS32_Q(4) break;
+      default: return cudaErrorInvalidValue;
+    }
+    rhs_gather_kernel<float2><<<(m.nv + 127) / 128, 128, 0, stream>>>((const float2*)rb, m.nf, nc, m.col_ptr,
+                                                                       m.col_fb, m.vertex_row, m.nv, (float2*)b,
+                                                                       ldb);
+  } else {
+    RhsParams<double> p;
+    p.k = k;
+    p.cS = c.cS;
+    p.cK = c.cK;
+    p.qscale = qscale;
+    for (int i = 0; i < 3 * kMaxQ; ++i) p.cw[i] = m.rule_cw[i];
+#define BEM_RHS64(QQ, NCC)                                                                                   \
+  rhs_faces_kernel<double, QQ, NCC><<<nblk, threads, 0, stream>>>(m.faces64, m.nf, m.driven, m.ndriven,       \
+                                                                  (const double2*)drive, m.pairs,            \
+                                                                  m.pairs_by_test_ptr, m.pairs_by_test,      \
+                                                                  (const double2*)sblocks, p, (double2*)rb)
+#define BEM_RHS64_Q(NCC)        \
+  if (m.Q == 6)                 \
+    BEM_RHS64(6, NCC);          \
+  else if (m.Q == 3)            \
+    BEM_RHS64(3, NCC);          \
+  else                          \
+    BEM_RHS64(1, NCC);
+    switch (nc) {
+      case 1: BEM_RHS64_Q(1) break;
+      case 2: BEM_RHS64_Q(2) break;
+      case 3: BEM_RHS64_Q(3) break;
+      case 4: BEM_RHS64_Q(4) break;
+      default: return cudaErrorInvalidValue;
+    }
+    rhs_gather_kernel<double2><<<(m.nv + 127) / 128, 128, 0, stream>>>((const double2*)rb, m.nf, nc, m.col_ptr,
+                                                                        m.col_fb, m.vertex_row, m.nv,
+                                                                        (double2*)b, ldb);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace bem

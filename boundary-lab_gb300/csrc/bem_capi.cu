@@ -1,0 +1,665 @@
+// C ABI of the GB300 BEM library: contexts, meshes, the batched frequency
+// solve and the parity entry points.  See include/gb300_bem.h for the contract.
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <string>
+#include <vector>
+
+#include "../../include/gb300_bem.h"
+#include "bem_internal.h"
+#include "bem_kernels.h"
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+struct BemError {
+  int code;
+  std::string msg;
+};
+
+inline void ck(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  int code = (e == cudaErrorMemoryAllocation) ? BEM_ERR_OUT_OF_MEMORY : BEM_ERR_CUDA;
+  throw BemError{code, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+}  // namespace
+
+struct bem_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cublasHandle_t cublas = nullptr;
+  std::string err;
+  DevBuf rext, mats, mats2, ipiv, info, sblocks, rb, b32, b64, x64, r64, d32, fsrc, fout, norms, pout;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::vector<bem_mesh*> meshes;
+};
+
+struct bem_mesh {
+  bem_context* ctx = nullptr;
+  bem::MeshPlan plan;
+  bem::DeviceMesh dm;
+  std::vector<void*> allocs;
+  int nc = 0;
+  DevBuf drive32, drive64, obs;
+  int nobs = 0;
+  DevBuf driven;
+};
+
+namespace {
+
+template <typename T> T* upload(bem_mesh* m, const std::vector<T>& v) {
+  if (v.empty()) return nullptr;
+  void* p = nullptr;
+  ck(cudaMalloc(&p, v.size() * sizeof(T)), "cudaMalloc(mesh)");
+  m->allocs.push_back(p);
+  ck(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, m->ctx->stream), "upload");
+  return (T*)p;
+}
+
+int fail(bem_context* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+template <typename F> int guarded(bem_context* ctx, F&& f) {
+  try {
+    if (ctx) {
+      ctx->err.clear();
+      cudaSetDevice(ctx->device);
+    }
+    return f();
+  } catch (const BemError& e) {
+    return fail(ctx, e.code, e.msg);
+  } catch (const std::bad_alloc&) {
+    return fail(ctx, BEM_ERR_OUT_OF_MEMORY, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(ctx, BEM_ERR_INVALID_ARGUMENT, e.what());
+  }
+}
+
+inline long long round_up(long long x, long long a) { return (x + a - 1) / a * a; }
+
+bem::OperatorCoeffs bm_coeffs(double k) {
+  bem::OperatorCoeffs c;
+  const double eta = 1.0 / k;  // eta = i/k
+  c.cD = make_double2(-1.0, 0.0);
+  c.cH = make_double2(0.0, eta);
+  c.cM = make_double2(0.5, 0.0);
+  c.cS = make_double2(-1.0, 0.0);
+  c.cK = make_double2(0.0, -eta);
+  c.cM10 = make_double2(0.0, -0.5 * eta);
+  return c;
+}
+
+// Shapes of the scratch layout for one mesh / batch.
+struct Layout {
+  long long ldR, lda, ldb;
+  size_t esz;
+};
+Layout layout_for(const bem::DeviceMesh& dm, bem::Precision prec) {
+  Layout L;
+  L.esz = prec == bem::Precision::Mixed ? sizeof(float2) : sizeof(double2);
+  L.ldR = round_up(std::max(dm.n_ext, 1), 32);
+  L.lda = round_up(dm.nv, 32);
+  L.ldb = round_up(dm.nv, 32);
+  return L;
+}
+
+// Assemble the LHS (cD, cH, cM) into A (and A2 if given) and, if nc > 0, the RHS
+// into b (nc columns, leading dimension ldb, permuted rows) for one frequency.
+void assemble_one(bem_mesh* m, bem::Precision prec, double k, const bem::OperatorCoeffs& c, void* A, void* A2,
+                  double2 qscale, int nc, const void* drive, void* b) {
+  bem_context* ctx = m->ctx;
+  const bem::DeviceMesh& dm = m->dm;
+  Layout L = layout_for(dm, prec);
+  ck(ctx->rext.ensure((size_t)L.ldR * 3 * dm.nf * L.esz), "alloc extended rows");
+  ck(ctx->sblocks.ensure((size_t)std::max(dm.npairs, 1) * 12 * L.esz), "alloc singular blocks");
+  ck(bem::launch_singular_dyn(dm, prec, k, c, ctx->sblocks.p, ctx->stream), "singular kernel");
+  ck(bem::launch_regular(dm, prec, k, c.cD, c.cH, ctx->rext.p, L.ldR, ctx->stream), "regular kernel");
+  ck(bem::launch_singular_scatter(dm, prec, ctx->sblocks.p, ctx->rext.p, L.ldR, ctx->stream), "singular scatter");
+  if (dm.n_isolated) {
+    ck(cudaMemsetAsync(A, 0, (size_t)L.lda * dm.nv * L.esz, ctx->stream), "memset");
+    if (A2) ck(cudaMemsetAsync(A2, 0, (size_t)L.lda * dm.nv * L.esz, ctx->stream), "memset");
+  }
+  ck(bem::launch_gather(dm, prec, ctx->rext.p, L.ldR, A, L.lda, A2, ctx->stream), "gather kernel");
+  if (nc > 0) {
+    ck(ctx->rb.ensure((size_t)nc * dm.nf * 3 * L.esz), "alloc rhs faces");
+    ck(bem::launch_rhs(dm, prec, k, c, qscale, drive, nc, ctx->sblocks.p, ctx->rb.p, b, L.ldb, ctx->stream),
+       "rhs kernel");
+  }
+}
+
+void free_mesh_device(bem_mesh* m) {
+  for (void* p : m->allocs) cudaFree(p);
+  m->allocs.clear();
+  m->drive32.release();
+  m->drive64.release();
+  m->obs.release();
+  m->driven.release();
+}
+
+}  // namespace
+
+extern "C" {
+
+int bem_abi_version(void) { return GB300_BEM_ABI_VERSION; }
+
+const char* bem_last_error(const bem_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int bem_create_context(int device, bem_context** out) {
+  if (!out) return BEM_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return BEM_ERR_CUDA;
+  if (device < 0 || device >= count) return BEM_ERR_INVALID_ARGUMENT;
+  bem_context* ctx = new bem_context();
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return BEM_ERR_CUDA;
+  }
+  if (cublasCreate(&ctx->cublas) != CUBLAS_STATUS_SUCCESS) {
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return BEM_ERR_CUDA;
+  }
+  cublasSetStream(ctx->cublas, ctx->stream);
+  for (auto& e : ctx->ev) cudaEventCreate(&e);
+  *out = ctx;
+  return BEM_OK;
+}
+
+void bem_destroy_context(bem_context* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (bem_mesh* m : ctx->meshes) {
+    free_mesh_device(m);
+    delete m;
+  }
+  ctx->meshes.clear();
+  for (DevBuf* b : {&ctx->rext, &ctx->mats, &ctx->mats2, &ctx->ipiv, &ctx->info, &ctx->sblocks, &ctx->rb, &ctx->b32,
+                    &ctx->b64, &ctx->x64, &ctx->r64, &ctx->d32, &ctx->fsrc, &ctx->fout, &ctx->norms, &ctx->pout})
+    b->release();
+  for (auto& e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->cublas) cublasDestroy(ctx->cublas);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+int bem_upload_mesh(bem_context* ctx, const double* vertices, int n_vertices, const int* faces, int n_faces,
+                    int regular_order, int singular_order, bem_mesh** out) {
+  if (!ctx) return BEM_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&]() -> int {
+    if (!out || !vertices || !faces) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "null pointer argument");
+    *out = nullptr;
+    bem_mesh* m = new bem_mesh();
+    m->ctx = ctx;
+    std::string e = bem::build_mesh_plan(vertices, n_vertices, faces, n_faces, regular_order, singular_order, 512, m->plan);
+    if (!e.empty()) {
+      delete m;
+      return fail(ctx, BEM_ERR_INVALID_ARGUMENT, e);
+    }
+    try {
+      const bem::MeshPlan& P = m->plan;
+      bem::DeviceMesh& d = m->dm;
+      d.nv = P.nv;
+      d.nf = P.nf;
+      d.Q = P.Q;
+      d.n_tiles = P.n_tiles;
+      d.max_tile_rows = P.max_tile_rows;
+      d.n_ext = P.n_ext;
+      d.n_halo = (int)P.halo_ext.size();
+      d.n_halo_rows = (int)P.halo_row.size();
+      d.npairs = (int)P.pairs.size();
+      d.faces32 = upload(m, P.faces32);
+      d.faces64 = upload(m, P.faces64);
+      d.tile_group_ptr = upload(m, P.tile_group_ptr);
+      d.lane_slots = upload(m, P.lane_slots);
+      d.tile_row_base = upload(m, P.tile_row_base);
+      d.ext_row = upload(m, P.ext_row);
+      d.halo_slot_of_ext = upload(m, P.halo_slot_of_ext);
+      d.halo_row_ptr = upload(m, P.halo_row_ptr);
+      d.halo_row = upload(m, P.halo_row);
+      d.col_ptr = upload(m, P.col_ptr);
+      d.col_fb = upload(m, P.col_fb);
+      d.face_ext = upload(m, P.face_ext);
+      d.vertex_row = upload(m, P.vertex_row);
+      std::vector<int> iso;
+      for (int v = 0; v < P.nv; ++v)
+        if (P.col_ptr[v] == P.col_ptr[v + 1]) iso.push_back(v);
+      d.n_isolated = (int)iso.size();
+      d.isolated = upload(m, iso);
+      d.pairs = upload(m, P.pairs);
+      d.pairs_by_trial_ptr = upload(m, P.pairs_by_trial_ptr);
+      d.pairs_by_test_ptr = upload(m, P.pairs_by_test_ptr);
+      d.pairs_by_test = upload(m, P.pairs_by_test);
+      d.rule_ptr = upload(m, P.rule_ptr);
+      d.duffy = upload(m, P.duffy);
+      d.verts = upload(m, P.verts);
+      d.faces = upload(m, P.faces);
+      d.normal = upload(m, P.normal);
+      d.curls = upload(m, P.curls);
+      d.area = upload(m, P.area);
+      std::vector<double> mm(12);
+      for (int i = 0; i < 9; ++i) mm[i] = P.m11[i];
+      for (int i = 0; i < 3; ++i) mm[9 + i] = P.m10[i];
+      d.m11m10 = upload(m, mm);
+      for (int q = 0; q < P.Q; ++q) {
+        const double u = P.rule_pts[2 * q], v = P.rule_pts[2 * q + 1];
+        const double phi[3] = {1.0 - u - v, u, v};
+        d.rule_w[q] = P.rule_w[q];
+        for (int a = 0; a < 3; ++a) {
+          d.rule_phi[a * P.Q + q] = phi[a];
+          d.rule_cw[a * P.Q + q] = phi[a] * P.rule_w[q];
+        }
+      }
+      if (d.npairs > 0) {
+        void* mom = nullptr;
+        ck(cudaMalloc(&mom, (size_t)d.npairs * 24 * sizeof(double)), "cudaMalloc(moments)");
+        m->allocs.push_back(mom);
+        d.moments = (double*)mom;
+        ck(bem::launch_singular_static(d, d.moments, ctx->stream), "singular moments kernel");
+      }
+      ck(cudaStreamSynchronize(ctx->stream), "mesh upload");
+    } catch (...) {
+      free_mesh_device(m);
+      delete m;
+      throw;
+    }
+    ctx->meshes.push_back(m);
+    *out = m;
+    return BEM_OK;
+  });
+}
+
+void bem_release_mesh(bem_mesh* mesh) {
+  if (!mesh) return;
+  bem_context* ctx = mesh->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  free_mesh_device(mesh);
+  ctx->meshes.erase(std::remove(ctx->meshes.begin(), ctx->meshes.end(), mesh), ctx->meshes.end());
+  delete mesh;
+}
+
+int bem_mesh_info(const bem_mesh* mesh, int* n_vertices, int* n_faces, int* n_singular_pairs) {
+  if (!mesh) return BEM_ERR_INVALID_ARGUMENT;
+  if (n_vertices) *n_vertices = mesh->dm.nv;
+  if (n_faces) *n_faces = mesh->dm.nf;
+  if (n_singular_pairs) *n_singular_pairs = mesh->dm.npairs;
+  return BEM_OK;
+}
+
+int bem_set_excitation(bem_mesh* m, const double* unit_drive, int n_rhs) {
+  if (!m) return BEM_ERR_INVALID_ARGUMENT;
+  bem_context* ctx = m->ctx;
+  return guarded(ctx, [&]() -> int {
+    if (!unit_drive || n_rhs < 1 || n_rhs > 4) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "need 1..4 excitations");
+    const int nf = m->dm.nf;
+    std::vector<float2> d32((size_t)n_rhs * nf);
+    std::vector<double2> d64((size_t)n_rhs * nf);
+    std::vector<int> driven;
+    for (int f = 0; f < nf; ++f) {
+      bool any = false;
+      for (int c = 0; c < n_rhs; ++c) {
+        const double re = unit_drive[2 * ((size_t)c * nf + f)], im = unit_drive[2 * ((size_t)c * nf + f) + 1];
+        if (!std::isfinite(re) || !std::isfinite(im)) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "drive must be finite");
+        d32[(size_t)c * nf + f] = make_float2((float)re, (float)im);
+        d64[(size_t)c * nf + f] = make_double2(re, im);
+        any = any || re != 0.0 || im != 0.0;
+      }
+      if (any) driven.push_back(f);
+    }
+    ck(cudaStreamSynchronize(ctx->stream), "sync");
+    ck(m->drive32.ensure(d32.size() * sizeof(float2)), "alloc drive");
+    ck(m->drive64.ensure(d64.size() * sizeof(double2)), "alloc drive");
+    ck(m->driven.ensure(std::max<size_t>(1, driven.size()) * sizeof(int)), "alloc driven");
+    ck(cudaMemcpy(m->drive32.p, d32.data(), d32.size() * sizeof(float2), cudaMemcpyHostToDevice), "copy drive");
+    ck(cudaMemcpy(m->drive64.p, d64.data(), d64.size() * sizeof(double2), cudaMemcpyHostToDevice), "copy drive");
+    if (!driven.empty())
+      ck(cudaMemcpy(m->driven.p, driven.data(), driven.size() * sizeof(int), cudaMemcpyHostToDevice), "copy driven");
+    m->dm.driven = (int*)m->driven.p;
+    m->dm.ndriven = (int)driven.size();
+    m->nc = n_rhs;
+    return BEM_OK;
+  });
+}
+
+int bem_set_observation_points(bem_mesh* m, const double* points, int n_points) {
+  if (!m) return BEM_ERR_INVALID_ARGUMENT;
+  bem_context* ctx = m->ctx;
+  return guarded(ctx, [&]() -> int {
+    if (!points || n_points < 1) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "need at least one observation point");
+    for (long long i = 0; i < 3LL * n_points; ++i)
+      if (!std::isfinite(points[i])) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "observation points must be finite");
+    ck(cudaStreamSynchronize(ctx->stream), "sync");
+    ck(m->obs.ensure((size_t)n_points * 3 * sizeof(double)), "alloc observation points");
+    ck(cudaMemcpy(m->obs.p, points, (size_t)n_points * 3 * sizeof(double), cudaMemcpyHostToDevice), "copy points");
+    m->nobs = n_points;
+    return BEM_OK;
+  });
+}
+
+void bem_default_options(bem_solve_options* opt) {
+  if (!opt) return;
+  opt->precision = BEM_PRECISION_MIXED;
+  opt->sound_speed = 343.0;
+  opt->rho = 1.21;
+  opt->refine_tol = 1e-10;
+  opt->max_refine = 8;
+  opt->batch = 0;
+  opt->lu_block = 0;
+  opt->outputs_on_device = 0;
+}
+
+long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int npts, int batch, int precision) {
+  const long long esz = precision == BEM_PRECISION_MIXED ? 8 : 16;
+  const long long lda = round_up(nv, 32);
+  const long long n_ext = (long long)(nv * 1.3) + 64;
+  long long bytes = 0;
+  bytes += round_up(n_ext, 32) * 3LL * nf * esz;                            // extended rows
+  bytes += (long long)batch * lda * nv * esz * (precision == BEM_PRECISION_MIXED ? 2 : 1);  // matrices (+copy)
+  bytes += (long long)npairs * (12 * esz + 24 * 8 + 48);                    // singular blocks, moments, pairs
+  bytes += (long long)batch * nrhs * lda * (esz + 3 * 16 + 16);             // rhs, x, r, b64, d
+  bytes += (long long)batch * nrhs * ((long long)nf * 6 * esz + (long long)npts * 16);  // field sources + out
+  bytes += (long long)nf * (160 + 288 + 64);                                // face records and maps
+  bytes += 64LL << 20;                                                      // cuBLAS workspace and slack
+  return bytes;
+}
+
+int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const bem_solve_options* opt,
+                          double* pressure_out, double* field_out, bem_solve_stats* stats) {
+  if (!m) return BEM_ERR_INVALID_ARGUMENT;
+  bem_context* ctx = m->ctx;
+  return guarded(ctx, [&]() -> int {
+    bem_solve_options o;
+    bem_default_options(&o);
+    if (opt) o = *opt;
+    if (!freqs_hz || n_freq < 1) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "need at least one frequency");
+    if (m->nc < 1) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "no excitation set (bem_set_excitation)");
+    if (field_out && m->nobs < 1) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "no observation points set");
+    if (!(o.sound_speed > 0) || !(o.rho > 0)) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "sound_speed and rho must be > 0");
+    if (o.precision != BEM_PRECISION_FP64 && o.precision != BEM_PRECISION_MIXED)
+      return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "unknown precision");
+    for (int i = 0; i < n_freq; ++i)
+      if (!(freqs_hz[i] > 0) || !std::isfinite(freqs_hz[i]))
+        return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "frequencies must be finite and positive");
+    const bem::Precision prec = o.precision == BEM_PRECISION_MIXED ? bem::Precision::Mixed : bem::Precision::FP64;
+    const bool mixed = prec == bem::Precision::Mixed;
+    const bem::DeviceMesh& dm = m->dm;
+    const int nv = dm.nv, nc = m->nc;
+    Layout L = layout_for(dm, prec);
+    int B = o.batch > 0 ? std::min(o.batch, 64) : 0;
+    if (B == 0) {
+      // automatic: matrices of one batch within ~8 GiB, at most 16 frequencies
+      const double per = (double)L.lda * nv * L.esz * (mixed ? 2 : 1);
+      B = (int)std::max(1.0, std::min(16.0, std::floor(8.0 * (1ull << 30) / per)));
+    }
+    B = std::min(B, n_freq);
+    const int nb = o.lu_block > 0 ? std::min(o.lu_block, 64) : (mixed ? 64 : 32);
+    const size_t matsz = (size_t)L.lda * nv * L.esz;
+    ck(ctx->mats.ensure(matsz * B), "alloc matrices");
+    if (mixed) ck(ctx->mats2.ensure(matsz * B), "alloc matrix copies");
+    ck(ctx->ipiv.ensure((size_t)B * nv * sizeof(int)), "alloc pivots");
+    ck(ctx->info.ensure((size_t)B * sizeof(int)), "alloc info");
+    const size_t vecn = (size_t)B * nc * L.ldb;
+    ck(ctx->b32.ensure(vecn * L.esz), "alloc rhs");
+    if (mixed) {
+      ck(ctx->b64.ensure(vecn * sizeof(double2)), "alloc rhs64");
+      ck(ctx->x64.ensure(vecn * sizeof(double2)), "alloc x");
+      ck(ctx->r64.ensure(vecn * sizeof(double2)), "alloc r");
+      ck(ctx->d32.ensure(vecn * sizeof(float2)), "alloc d");
+      ck(ctx->norms.ensure((size_t)B * nc * 2 * sizeof(double)), "alloc norms");
+    }
+    if (field_out) {
+      const size_t srcb = (size_t)B * nc * dm.nf * dm.Q * L.esz;
+      ck(ctx->fsrc.ensure(round_up(srcb, 256) + 4096), "alloc field sources");
+      ck(ctx->fout.ensure((size_t)B * nc * m->nobs * sizeof(double2)), "alloc field out");
+      if (mixed) ck(ctx->pout.ensure(vecn * sizeof(float2)), "alloc pressure f32");
+    }
+    const void* drive = mixed ? m->drive32.p : m->drive64.p;
+    std::vector<double> norms((size_t)B * nc * 2);
+    std::vector<int> info(B);
+    double t_asm = 0, t_sol = 0, t_fld = 0, max_res = 0;
+    int max_steps = 0, batches = 0;
+    for (int f0 = 0; f0 < n_freq; f0 += B) {
+      const int bt = std::min(B, n_freq - f0);
+      ++batches;
+      std::vector<double> ks(bt);
+      std::vector<double2> qs(bt);
+      cudaEventRecord(ctx->ev[0], ctx->stream);
+      for (int i = 0; i < bt; ++i) {
+        const double omega = 2.0 * M_PI * freqs_hz[f0 + i];
+        const double k = omega / o.sound_speed;
+        ks[i] = k;
+        qs[i] = make_double2(0.0, o.rho * omega);
+        char* A = (char*)ctx->mats.p + matsz * i;
+        char* A2 = mixed ? (char*)ctx->mats2.p + matsz * i : nullptr;
+        char* b = (char*)ctx->b32.p + (size_t)i * nc * L.ldb * L.esz;
+        assemble_one(m, prec, k, bm_coeffs(k), A, A2, qs[i], nc, drive, b);
+      }
+      cudaEventRecord(ctx->ev[1], ctx->stream);
+      ck(cudaMemsetAsync(ctx->info.p, 0, (size_t)bt * sizeof(int), ctx->stream), "memset info");
+      ck(bem::lu_factor_batched(prec, ctx->mats.p, L.lda, nv, bt, (int*)ctx->ipiv.p, (int*)ctx->info.p, nb,
+                                ctx->cublas, ctx->stream),
+         "LU factorisation");
+      ck(cudaMemcpyAsync(info.data(), ctx->info.p, (size_t)bt * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream),
+         "copy info");
+      const long long nvec = (long long)bt * nc * L.ldb;
+      if (!mixed) {
+        ck(bem::lu_solve_batched(prec, ctx->mats.p, L.lda, nv, bt, (int*)ctx->ipiv.p, ctx->b32.p, L.ldb, nc, nb,
+                                 ctx->stream),
+           "LU solve");
+      } else {
+        double2* x = (double2*)ctx->x64.p;
+        double2* r = (double2*)ctx->r64.p;
+        double2* b64 = (double2*)ctx->b64.p;
+        float2* d = (float2*)ctx->d32.p;
+        ck(bem::convert_f32_to_f64((const float2*)ctx->b32.p, b64, nvec, ctx->stream), "convert rhs");
+        ck(cudaMemcpyAsync(d, ctx->b32.p, nvec * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream), "copy rhs");
+        ck(bem::lu_solve_batched(prec, ctx->mats.p, L.lda, nv, bt, (int*)ctx->ipiv.p, d, L.ldb, nc, nb, ctx->stream),
+           "LU solve");
+        ck(cudaMemsetAsync(x, 0, nvec * sizeof(double2), ctx->stream), "memset x");
+        ck(bem::axpy_f32_into_f64(d, x, nvec, ctx->stream), "axpy");
+        int steps = 0;
+        double worst = 0;
+        for (;;) {
+          ck(bem::residual_batched(prec, ctx->mats2.p, L.lda, nv, bt, x, b64, L.ldb, nc, r, ctx->stream), "residual");
+          ck(bem::norms_batched(r, b64, L.ldb, nv, bt * nc, (double*)ctx->norms.p, ctx->stream), "norms");
+          ck(cudaMemcpyAsync(norms.data(), ctx->norms.p, (size_t)bt * nc * 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                             ctx->stream),
+             "copy norms");
+          ck(cudaStreamSynchronize(ctx->stream), "refinement sync");
+          worst = 0;
+          for (int i = 0; i < bt * nc; ++i) {
+            const double rel = norms[2 * i + 1] > 0 ? std::sqrt(norms[2 * i] / norms[2 * i + 1]) : std::sqrt(norms[2 * i]);
+            if (!std::isfinite(rel)) worst = INFINITY;
+            else worst = std::max(worst, rel);
+          }
+          if (worst <= o.refine_tol || steps >= o.max_refine || !std::isfinite(worst)) break;
+          ck(bem::convert_f64_to_f32(r, d, nvec, ctx->stream), "convert residual");
+          ck(bem::lu_solve_batched(prec, ctx->mats.p, L.lda, nv, bt, (int*)ctx->ipiv.p, d, L.ldb, nc, nb,
+                                   ctx->stream),
+             "LU solve");
+          ck(bem::axpy_f32_into_f64(d, x, nvec, ctx->stream), "axpy");
+          ++steps;
+        }
+        max_steps = std::max(max_steps, steps);
+        max_res = std::max(max_res, worst);
+      }
+      cudaEventRecord(ctx->ev[2], ctx->stream);
+      ck(cudaStreamSynchronize(ctx->stream), "solve sync");
+      for (int i = 0; i < bt; ++i)
+        if (info[i] != 0) return fail(ctx, BEM_ERR_SINGULAR, "zero pivot in LU factorisation (frequency " +
+                                                                std::to_string(freqs_hz[f0 + i]) + " Hz)");
+      // solution (vertex order) as [bt][nc][ldb]
+      const void* sol = mixed ? (const void*)ctx->x64.p : (const void*)ctx->b32.p;
+      if (field_out) {
+        const void* p_for_field = sol;
+        if (mixed) {
+          ck(bem::convert_f64_to_f32((const double2*)ctx->x64.p, (float2*)ctx->pout.p, nvec, ctx->stream), "convert");
+          p_for_field = ctx->pout.p;
+        }
+        ck(bem::launch_field(dm, prec, bt, ks.data(), qs.data(), p_for_field, L.ldb, nc, drive, (const double*)m->obs.p,
+                             m->nobs, ctx->fsrc.p, (double2*)ctx->fout.p, ctx->stream),
+           "field kernel");
+        double* dst = field_out + 2 * (size_t)f0 * nc * m->nobs;
+        ck(cudaMemcpyAsync(dst, ctx->fout.p, (size_t)bt * nc * m->nobs * sizeof(double2),
+                           o.outputs_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream),
+           "copy field");
+      }
+      cudaEventRecord(ctx->ev[3], ctx->stream);
+      if (pressure_out) {
+        // [bt][nc][nv] complex128 from [bt][nc][ldb]
+        const cudaMemcpyKind kind = o.outputs_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        if (mixed) {
+          ck(cudaMemcpy2DAsync(pressure_out + 2 * (size_t)f0 * nc * nv, (size_t)nv * sizeof(double2), sol,
+                               (size_t)L.ldb * sizeof(double2), (size_t)nv * sizeof(double2), (size_t)bt * nc, kind,
+                               ctx->stream),
+             "copy pressure");
+        } else {
+          ck(cudaMemcpy2DAsync(pressure_out + 2 * (size_t)f0 * nc * nv, (size_t)nv * sizeof(double2), sol,
+                               (size_t)L.ldb * sizeof(double2), (size_t)nv * sizeof(double2), (size_t)bt * nc, kind,
+                               ctx->stream),
+             "copy pressure");
+        }
+      }
+      ck(cudaStreamSynchronize(ctx->stream), "batch sync");
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+      t_asm += ms * 1e-3;
+      cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+      t_sol += ms * 1e-3;
+      cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+      t_fld += ms * 1e-3;
+    }
+    if (stats) {
+      stats->assembly_s = t_asm;
+      stats->solve_s = t_sol;
+      stats->field_s = t_fld;
+      stats->max_refine_steps = max_steps;
+      stats->max_rel_residual = max_res;
+      stats->batches = batches;
+    }
+    if (mixed && !(max_res <= o.refine_tol)) {
+      ctx->err = "iterative refinement stopped at relative residual " + std::to_string(max_res);
+      return BEM_ERR_NOT_CONVERGED;
+    }
+    return BEM_OK;
+  });
+}
+
+int bem_assemble_lhs(bem_mesh* m, double k, int precision, const double* coeffs, double* out) {
+  if (!m) return BEM_ERR_INVALID_ARGUMENT;
+  bem_context* ctx = m->ctx;
+  return guarded(ctx, [&]() -> int {
+    if (!coeffs || !out || !(k > 0)) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "bad arguments");
+    const bem::Precision prec = precision == BEM_PRECISION_MIXED ? bem::Precision::Mixed : bem::Precision::FP64;
+    const bem::DeviceMesh& dm = m->dm;
+    Layout L = layout_for(dm, prec);
+    bem::OperatorCoeffs c{};
+    c.cD = make_double2(coeffs[0], coeffs[1]);
+    c.cH = make_double2(coeffs[2], coeffs[3]);
+    c.cM = make_double2(coeffs[4], coeffs[5]);
+    const size_t matsz = (size_t)L.lda * dm.nv * L.esz;
+    ck(ctx->mats.ensure(matsz), "alloc matrix");
+    assemble_one(m, prec, k, c, ctx->mats.p, nullptr, make_double2(0, 0), 0, nullptr, nullptr);
+    std::vector<char> host(matsz);
+    ck(cudaMemcpyAsync(host.data(), ctx->mats.p, matsz, cudaMemcpyDeviceToHost, ctx->stream), "copy matrix");
+    ck(cudaStreamSynchronize(ctx->stream), "sync");
+    const int nv = dm.nv;
+    for (int j = 0; j < nv; ++j)
+      for (int r = 0; r < nv; ++r) {
+        const int v = m->plan.row_vertex[r];
+        double re, im;
+        if (prec == bem::Precision::Mixed) {
+          const float2 x = ((const float2*)host.data())[(size_t)j * L.lda + r];
+          re = x.x;
+          im = x.y;
+        } else {
+          const double2 x = ((const double2*)host.data())[(size_t)j * L.lda + r];
+          re = x.x;
+          im = x.y;
+        }
+        out[2 * ((size_t)j * nv + v)] = re;
+        out[2 * ((size_t)j * nv + v) + 1] = im;
+      }
+    return BEM_OK;
+  });
+}
+
+int bem_apply_rhs_operator(bem_mesh* m, double k, int precision, const double* coeffs, const double* q, int n_rhs,
+                           double* out) {
+  if (!m) return BEM_ERR_INVALID_ARGUMENT;
+  bem_context* ctx = m->ctx;
+  return guarded(ctx, [&]() -> int {
+    if (!coeffs || !q || !out || n_rhs < 1 || n_rhs > 4 || !(k > 0))
+      return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "bad arguments");
+    const bem::Precision prec = precision == BEM_PRECISION_MIXED ? bem::Precision::Mixed : bem::Precision::FP64;
+    // route q through the excitation slots with qscale = 1
+    const int saved_nc = m->nc;
+    int rc = bem_set_excitation(m, q, n_rhs);
+    if (rc != BEM_OK) return rc;
+    const bem::DeviceMesh& dm = m->dm;
+    Layout L = layout_for(dm, prec);
+    bem::OperatorCoeffs c{};
+    c.cS = make_double2(coeffs[0], coeffs[1]);
+    c.cK = make_double2(coeffs[2], coeffs[3]);
+    c.cM10 = make_double2(coeffs[4], coeffs[5]);
+    const size_t matsz = (size_t)L.lda * dm.nv * L.esz;
+    ck(ctx->mats.ensure(matsz), "alloc matrix");
+    ck(ctx->b32.ensure((size_t)n_rhs * L.ldb * L.esz), "alloc rhs");
+    const void* drive = prec == bem::Precision::Mixed ? m->drive32.p : m->drive64.p;
+    assemble_one(m, prec, k, c, ctx->mats.p, nullptr, make_double2(1.0, 0.0), n_rhs, drive, ctx->b32.p);
+    std::vector<char> host((size_t)n_rhs * L.ldb * L.esz);
+    ck(cudaMemcpyAsync(host.data(), ctx->b32.p, host.size(), cudaMemcpyDeviceToHost, ctx->stream), "copy rhs");
+    ck(cudaStreamSynchronize(ctx->stream), "sync");
+    (void)saved_nc;
+    const int nv = dm.nv;
+    for (int c2 = 0; c2 < n_rhs; ++c2)
+      for (int r = 0; r < nv; ++r) {
+        const int v = m->plan.row_vertex[r];
+        double re, im;
+        if (prec == bem::Precision::Mixed) {
+          const float2 x = ((const float2*)host.data())[(size_t)c2 * L.ldb + r];
+          re = x.x;
+          im = x.y;
+        } else {
+          const double2 x = ((const double2*)host.data())[(size_t)c2 * L.ldb + r];
+          re = x.x;
+          im = x.y;
+        }
+        out[2 * ((size_t)c2 * nv + v)] = re;
+        out[2 * ((size_t)c2 * nv + v) + 1] = im;
+      }
+    return BEM_OK;
+  });
+}
+
+}  // extern "C"

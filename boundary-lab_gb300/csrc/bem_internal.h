@@ -1,0 +1,111 @@
+// Internal (non-ABI) structures shared by the host mesh planner and the
+// kernel launchers of the GB300 BEM library.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace bem {
+
+// Regular (6-point) rule and Duffy rules use the reference's orders; the
+// planner supports regular orders 1 (1 point), 2/3 (3 points) and 4 (6 points)
+// and singular (Duffy) orders 1..4.
+constexpr int kMaxQ = 6;
+constexpr int kLanes = 32;
+
+// Compensated-FP32 face record, 40 words (160 B, 16-byte aligned).
+//   anchor_hi/anchor_lo : face centroid as an unevaluated float sum (double-float)
+//   off                 : quadrature points minus the centroid (float, |off| ~ h)
+//   normal, area2 (=2A), curls[3], verts[3] (global vertex ids for adjacency)
+struct alignas(16) FaceF32 {
+  float anchor_hi[3];
+  float anchor_lo[3];
+  float normal[3];
+  float area2;
+  float curls[9];
+  float off[kMaxQ * 3];
+  int verts[3];
+};
+static_assert(sizeof(FaceF32) == 160, "FaceF32 layout");
+
+// FP64 face record (288 B).
+struct alignas(16) FaceF64 {
+  double anchor[3];
+  double normal[3];
+  double area2;
+  double curls[9];
+  double off[kMaxQ * 3];
+  int verts[3];
+  int pad;
+};
+static_assert(sizeof(FaceF64) % 16 == 0, "FaceF64 layout");
+
+// One lane slot of a tile group: test face id and the tile-local rows of its
+// three vertices (-1 face id = empty slot).
+struct alignas(16) LaneSlot {
+  int face;
+  int loc[3];
+};
+
+// Singular (vertex-sharing) pair.
+struct SingularPair {
+  int test, trial, rule, kind;  // kind 1 coincident, 2 edge, 3 vertex
+  double jac;                   // (2 A_test)(2 A_trial)
+  double nprod;                 // n_test . n_trial
+};
+
+struct MeshPlan {
+  int nv = 0, nf = 0, Q = 0, regular_order = 4, singular_order = 4;
+  // regular rule on the reference triangle
+  std::vector<double> rule_pts;  // Q x 2
+  std::vector<double> rule_w;    // Q
+  // per-face records
+  std::vector<FaceF32> faces32;
+  std::vector<FaceF64> faces64;
+  std::vector<int> faces;  // nf x 3 (input vertex ids)
+  std::vector<double> verts;  // nv x 3
+  std::vector<double> area;   // nf
+  std::vector<double> normal;  // nf x 3
+  std::vector<double> curls;   // nf x 9
+  // test-face tiles (the extended-row layout)
+  int tile_faces = 0;                 // max faces per tile
+  int n_tiles = 0;
+  int max_tile_rows = 0;              // max distinct vertices in one tile
+  std::vector<int> tile_group_ptr;    // n_tiles + 1, in units of groups
+  std::vector<LaneSlot> lane_slots;   // n_groups x 32
+  std::vector<int> tile_row_base;     // n_tiles + 1: extended-row offset of each tile
+  int n_ext = 0;                      // total extended rows
+  std::vector<int> ext_row;           // n_ext: matrix row (permuted order) of each extended row
+  std::vector<int> ext_is_halo;       // n_ext: 1 when the extended row is not the vertex's primary slot
+  // row permutation: matrix row r holds the equation of vertex row_vertex[r]
+  std::vector<int> row_vertex;        // nv
+  std::vector<int> vertex_row;        // nv
+  // halo gather: extended rows that are not primary, grouped by target matrix row
+  std::vector<int> halo_ext;          // n_halo: extended row ids, sorted by target row
+  std::vector<int> halo_row;          // n_halo_rows: target matrix rows (distinct)
+  std::vector<int> halo_row_ptr;      // n_halo_rows + 1 into halo_ext
+  std::vector<int> halo_slot_of_ext;  // n_ext: index into halo_ext or -1
+  // column gather: for vertex j, the (trial face, local vertex) pairs g*3+b
+  std::vector<int> col_ptr;           // nv + 1
+  std::vector<int> col_fb;            // 3 nf
+  // per-(face, local vertex) extended row of that face's tile
+  std::vector<int> face_ext;          // nf x 3
+  // singular pairs sorted by trial face, with CSR by trial face and by test face
+  std::vector<SingularPair> pairs;
+  std::vector<int> pairs_by_trial_ptr;  // nf + 1 (pairs are sorted by trial)
+  std::vector<int> pairs_by_test;       // pair ids grouped by test face
+  std::vector<int> pairs_by_test_ptr;   // nf + 1
+  // Duffy rules: concatenated points; rule r occupies [rule_ptr[r], rule_ptr[r+1])
+  std::vector<int> rule_ptr;
+  std::vector<double> duffy;  // 5 doubles per point: test xi, test eta, trial xi, trial eta, w
+  // mass element constants: m11[a][b] = sum_q w_q phi_a phi_b ; m10[a] = sum_q w_q phi_a
+  double m11[9] = {0};
+  double m10[3] = {0};
+};
+
+// Build the plan; returns an empty string on success, else an error message.
+std::string build_mesh_plan(const double* verts, int nv, const int* faces, int nf, int regular_order,
+                            int singular_order, int tile_faces, MeshPlan& plan);
+
+}  // namespace bem

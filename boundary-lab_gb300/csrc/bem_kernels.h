@@ -1,0 +1,102 @@
+// Internal launcher interface between the context layer (bem_capi.cu) and the
+// kernel files.  Not part of the public C ABI (see include/gb300_bem.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "bem_internal.h"
+
+namespace bem {
+
+enum class Precision : int { FP64 = 0, Mixed = 1 };
+
+// Linear-combination coefficients.  LHS = cD*D + cH*H + cM*M11;
+// RHS operator = cS*S + cK*K' + cM10*M10.  The Burton-Miller system of the
+// reference (BeatEngineCpuSolve.jl:45-53) is cD=-1, cH=i/k, cM=1/2,
+// cS=-1, cK=-i/k, cM10=-i/(2k).
+struct OperatorCoeffs {
+  double2 cD, cH, cM, cS, cK, cM10;
+};
+
+struct DeviceMesh {
+  int nv = 0, nf = 0, Q = 0;
+  int n_tiles = 0, max_tile_rows = 0, n_ext = 0, n_halo = 0, n_halo_rows = 0;
+  int npairs = 0, n_isolated = 0, ndriven = 0;
+  FaceF32* faces32 = nullptr;
+  FaceF64* faces64 = nullptr;
+  int* tile_group_ptr = nullptr;
+  LaneSlot* lane_slots = nullptr;
+  int* tile_row_base = nullptr;
+  int* ext_row = nullptr;
+  int* halo_slot_of_ext = nullptr;
+  int* halo_row_ptr = nullptr;
+  int* halo_row = nullptr;
+  int* col_ptr = nullptr;
+  int* col_fb = nullptr;
+  int* face_ext = nullptr;
+  int* vertex_row = nullptr;
+  int* isolated = nullptr;
+  SingularPair* pairs = nullptr;
+  int* pairs_by_trial_ptr = nullptr;
+  int* pairs_by_test_ptr = nullptr;
+  int* pairs_by_test = nullptr;
+  int* rule_ptr = nullptr;
+  double* duffy = nullptr;
+  double* moments = nullptr;
+  double* verts = nullptr;
+  int* faces = nullptr;
+  double* normal = nullptr;
+  double* curls = nullptr;
+  double* area = nullptr;
+  double* m11m10 = nullptr;  // 9 + 3 doubles
+  int* driven = nullptr;
+  // regular rule: weights w_q, basis values phi_a(xi_q) (a-major, 3 x Q) and
+  // their products cw[a*Q + q] = phi_a(xi_q) w_q
+  double rule_w[kMaxQ] = {0};
+  double rule_phi[3 * kMaxQ] = {0};
+  double rule_cw[3 * kMaxQ] = {0};
+};
+
+// assembly (bem_assembly.cu)
+cudaError_t launch_regular(const DeviceMesh& m, Precision prec, double k, double2 cD, double2 cH, void* Rext,
+                           long long ldR, cudaStream_t stream);
+cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, cudaStream_t stream);
+cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, double k, const OperatorCoeffs& c, void* blocks,
+                                cudaStream_t stream);
+cudaError_t launch_singular_scatter(const DeviceMesh& m, Precision prec, const void* blocks, void* Rext,
+                                    long long ldR, cudaStream_t stream);
+cudaError_t launch_gather(const DeviceMesh& m, Precision prec, const void* Rext, long long ldR, void* A, long long lda,
+                          void* A2, cudaStream_t stream);
+cudaError_t launch_rhs(const DeviceMesh& m, Precision prec, double k, const OperatorCoeffs& c, double2 qscale,
+                       const void* drive, int nc, const void* sblocks, void* rb, void* b, long long ldb,
+                       cudaStream_t stream);
+
+// dense LU and solves (bem_lu.cu).  Matrices are column-major, batched with a
+// stride of lda*n elements; pivots are 0-based, ipiv stride n.
+struct LuWorkspace;
+cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int batch, int* ipiv, int* info,
+                              int nb, void* cublas_handle, cudaStream_t stream);
+// Solve (LU) X = B in place for nrhs columns per matrix (B stride ldb*nrhs per matrix), working precision.
+cudaError_t lu_solve_batched(Precision prec, const void* LU, long long lda, int n, int batch, const int* ipiv,
+                             void* B, long long ldb, int nrhs, int nb, cudaStream_t stream);
+// r = b - A x in FP64 arithmetic: A (complex64 or complex128), x, b, r complex128.
+cudaError_t residual_batched(Precision prec, const void* A, long long lda, int n, int batch, const double2* x,
+                             const double2* b, long long ldb, int nrhs, double2* r, cudaStream_t stream);
+// Per (matrix, rhs): out[2*i] = ||r_i||^2 and out[2*i+1] = ||b_i||^2.
+cudaError_t norms_batched(const double2* r, const double2* b, long long ldb, int n, int count, double* out,
+                          cudaStream_t stream);
+// x += d (d complex64) ; copy / convert helpers
+cudaError_t axpy_f32_into_f64(const float2* d, double2* x, long long n, cudaStream_t stream);
+cudaError_t convert_f64_to_f32(const double2* src, float2* dst, long long n, cudaStream_t stream);
+cudaError_t convert_f32_to_f64(const float2* src, double2* dst, long long n, cudaStream_t stream);
+// undo the row permutation of the solution?  (columns are unpermuted: the
+// solution is already in vertex order)
+
+// far field (bem_field.cu)
+cudaError_t launch_field(const DeviceMesh& m, Precision prec, int batch, const double* k, const double2* qscale,
+                         const void* pressure, long long ldp, int nc, const void* drive, const double* obs, int nobs,
+                         void* sources, double2* out, cudaStream_t stream);
+
+}  // namespace bem

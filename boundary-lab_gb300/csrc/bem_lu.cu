@@ -1,0 +1,451 @@
+// Dense complex LU with partial pivoting, triangular solves and the FP64
+// residual for iterative refinement (sm_103a).
+//
+// The reference solves each Burton-Miller system with CUDA.jl's `\`
+// (cuSOLVER getrf + getrs, src/blab/solvers/julia_local/src/
+// BeatEngineCore.jl:1206) and refactors for every channel.  Here the matrix of
+// one frequency is factored once and every excitation is solved against the
+// factors; many frequencies are factored together as a batch so that
+// panel-factorisation latency of one matrix overlaps the work of others.
+//
+// Blocked right-looking LU, per block column k of width nb:
+//   lu_panel_kernel   pivot search (|re|+|im| as LAPACK's icamax), row swap,
+//                     scaling and rank-1 updates inside the panel; one CTA per
+//                     matrix of the batch
+//   lu_swap_kernel    the panel's row interchanges applied to the other columns
+//   lu_trsm_kernel    U12 = L11^{-1} A12 (unit lower), L11 staged in shared memory
+//   trailing update   A22 -= L21 U12 : a batched complex GEMM
+#include <cublas_v2.h>
+
+#include "bem_common.cuh"
+#include "bem_kernels.h"
+
+namespace bem {
+namespace {
+
+template <typename R> struct CT;
+template <> struct CT<float> { typedef float2 C2; };
+template <> struct CT<double> { typedef double2 C2; };
+
+template <typename C2> __device__ __forceinline__ auto cabs1(C2 v) -> decltype(v.x) { return fabs(v.x) + fabs(v.y); }
+
+template <typename C2> __device__ __forceinline__ C2 cinv(C2 d) {
+  auto m = d.x * d.x + d.y * d.y;
+  C2 r;
+  r.x = d.x / m;
+  r.y = -d.y / m;
+  return r;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(1024) lu_panel_kernel(typename CT<R>::C2* A, long long lda, long long strideA, int n,
+                                                        int k, int kb, int* ipiv, int* info) {
+  typedef typename CT<R>::C2 C2;
+  C2* M = A + (size_t)blockIdx.x * strideA;
+  int* piv = ipiv + (size_t)blockIdx.x * n;
+  __shared__ R s_val[32];
+  __shared__ int s_idx[32];
+  __shared__ C2 s_row[64];
+  __shared__ int s_p;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  for (int j = 0; j < kb; ++j) {
+    const int col = k + j;
+    const C2* Mc = M + (size_t)col * lda;
+    R best = R(-1);
+    int bi = n;
+    for (int r = col + tid; r < n; r += blockDim.x) {
+      R v = cabs1(Mc[r]);
+      if (v > best) {  // first maximum in row order within this thread's stride
+        best = v;
+        bi = r;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      R ov = __shfl_xor_sync(0xffffffffu, best, o);
+      int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) {
+        best = ov;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      s_val[wid] = best;
+      s_idx[wid] = bi;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      best = lane < nw ? s_val[lane] : R(-1);
+      bi = lane < nw ? s_idx[lane] : n;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        R ov = __shfl_xor_sync(0xffffffffu, best, o);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) {
+          best = ov;
+          bi = oi;
+        }
+      }
+      if (lane == 0) {
+        s_p = bi < n ? bi : col;
+        piv[col] = s_p;
+      }
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (p != col) {
+      for (int c = tid; c < kb; c += blockDim.x) {
+        C2* a = M + (size_t)(k + c) * lda;
+        C2 t = a[col];
+        a[col] = a[p];
+        a[p] = t;
+      }
+    }
+    __syncthreads();
+    for (int c = tid; c < kb; c += blockDim.x) s_row[c] = M[(size_t)(k + c) * lda + col];
+    __syncthreads();
+    const C2 d = s_row[j];
+    C2 inv;
+    if (d.x == R(0) && d.y == R(0)) {
+      inv.x = R(0);
+      inv.y = R(0);
+      if (tid == 0 && info[blockIdx.x] == 0) info[blockIdx.x] = col + 1;
+    } else {
+      inv = cinv(d);
+    }
+    for (int r = col + 1 + tid; r < n; r += blockDim.x) {
+      C2 l = cmul(M[(size_t)col * lda + r], inv);
+      M[(size_t)col * lda + r] = l;
+      for (int c = j + 1; c < kb; ++c) {
+        C2* a = M + (size_t)(k + c) * lda + r;
+        C2 u = s_row[c];
+        C2 v = *a;
+        v.x -= l.x * u.x - l.y * u.y;
+        v.y -= l.x * u.y + l.y * u.x;
+        *a = v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename C2>
+__global__ void lu_swap_kernel(C2* A, long long lda, long long strideA, int n, int k, int kb, const int* ipiv) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ncols = n - kb;
+  if (t >= ncols) return;
+  const int c = t < k ? t : t + kb;
+  C2* a = A + (size_t)blockIdx.y * strideA + (size_t)c * lda;
+  const int* piv = ipiv + (size_t)blockIdx.y * n;
+  for (int j = 0; j < kb; ++j) {
+    const int r1 = k + j, r2 = piv[k + j];
+    if (r2 != r1) {
+      C2 tmp = a[r1];
+      a[r1] = a[r2];
+      a[r2] = tmp;
+    }
+  }
+}
+
+// U12 = L11^{-1} A12 for columns [k+kb, n); 128 columns per CTA.
+template <typename C2>
+__global__ void lu_trsm_kernel(C2* A, long long lda, long long strideA, int n, int k, int kb) {
+  extern __shared__ unsigned char smem_raw[];
+  C2* L = reinterpret_cast<C2*>(smem_raw);  // kb x kb, column-major
+  C2* X = L + kb * kb;                      // kb x blockDim
+  C2* M = A + (size_t)blockIdx.y * strideA;
+  for (int i = threadIdx.x; i < kb * kb; i += blockDim.x) {
+    const int r = i % kb, c = i / kb;
+    L[i] = M[(size_t)(k + c) * lda + k + r];
+  }
+  const int col = k + kb + blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = col < n;
+  C2* a = M + (size_t)col * lda + k;
+  if (active)
+    for (int r = 0; r < kb; ++r) X[r * blockDim.x + threadIdx.x] = a[r];
+  __syncthreads();
+  if (!active) return;
+  for (int j = 0; j < kb; ++j) {
+    const C2 xj = X[j * blockDim.x + threadIdx.x];
+    for (int i = j + 1; i < kb; ++i) {
+      C2 l = L[j * kb + i];
+      C2 v = X[i * blockDim.x + threadIdx.x];
+      v.x -= l.x * xj.x - l.y * xj.y;
+      v.y -= l.x * xj.y + l.y * xj.x;
+      X[i * blockDim.x + threadIdx.x] = v;
+    }
+  }
+  for (int r = 0; r < kb; ++r) a[r] = X[r * blockDim.x + threadIdx.x];
+}
+
+// One CTA per (matrix, right-hand side): P, then L (unit lower), then U.
+template <typename R>
+__global__ void __launch_bounds__(1024) lu_solve_kernel(const typename CT<R>::C2* A, long long lda, long long strideA,
+                                                        int n, const int* ipiv, typename CT<R>::C2* B, long long ldb,
+                                                        int nrhs) {
+  typedef typename CT<R>::C2 C2;
+  const int mat = blockIdx.x / nrhs, rhs = blockIdx.x % nrhs;
+  const C2* M = A + (size_t)mat * strideA;
+  const int* piv = ipiv + (size_t)mat * n;
+  C2* b = B + ((size_t)mat * nrhs + rhs) * ldb;
+  __shared__ C2 xs[32];
+  const int tid = threadIdx.x, lane = tid & 31;
+  if (tid == 0)
+    for (int i = 0; i < n; ++i) {
+      const int p = piv[i];
+      if (p != i) {
+        C2 t = b[i];
+        b[i] = b[p];
+        b[p] = t;
+      }
+    }
+  __syncthreads();
+  // forward substitution, blocks of 32 rows
+  for (int k0 = 0; k0 < n; k0 += 32) {
+    const int kb = min(32, n - k0);
+    if (tid < 32) {
+      C2 v;
+      v.x = 0;
+      v.y = 0;
+      if (lane < kb) v = b[k0 + lane];
+      for (int j = 0; j < kb; ++j) {
+        C2 xj;
+        xj.x = __shfl_sync(0xffffffffu, v.x, j);
+        xj.y = __shfl_sync(0xffffffffu, v.y, j);
+        if (lane > j && lane < kb) {
+          const C2 l = M[(size_t)(k0 + j) * lda + k0 + lane];
+          v.x -= l.x * xj.x - l.y * xj.y;
+          v.y -= l.x * xj.y + l.y * xj.x;
+        }
+      }
+      if (lane < kb) {
+        b[k0 + lane] = v;
+        xs[lane] = v;
+      }
+    }
+    __syncthreads();
+    for (int r = k0 + kb + tid; r < n; r += blockDim.x) {
+      C2 v = b[r];
+      for (int j = 0; j < kb; ++j) {
+        const C2 l = M[(size_t)(k0 + j) * lda + r];
+        const C2 x = xs[j];
+        v.x -= l.x * x.x - l.y * x.y;
+        v.y -= l.x * x.y + l.y * x.x;
+      }
+      b[r] = v;
+    }
+    __syncthreads();
+  }
+  // backward substitution
+  const int nblk = (n + 31) / 32;
+  for (int bi = nblk - 1; bi >= 0; --bi) {
+    const int k0 = bi * 32;
+    const int kb = min(32, n - k0);
+    if (tid < 32) {
+      C2 v;
+      v.x = 0;
+      v.y = 0;
+      if (lane < kb) v = b[k0 + lane];
+      for (int j = kb - 1; j >= 0; --j) {
+        C2 xj;
+        if (lane == j) {
+          const C2 d = M[(size_t)(k0 + j) * lda + k0 + j];
+          v = cmul(v, cinv(d));
+        }
+        xj.x = __shfl_sync(0xffffffffu, v.x, j);
+        xj.y = __shfl_sync(0xffffffffu, v.y, j);
+        if (lane < j) {
+          const C2 u = M[(size_t)(k0 + j) * lda + k0 + lane];
+          v.x -= u.x * xj.x - u.y * xj.y;
+          v.y -= u.x * xj.y + u.y * xj.x;
+        }
+      }
+      if (lane < kb) {
+        b[k0 + lane] = v;
+        xs[lane] = v;
+      }
+    }
+    __syncthreads();
+    for (int r = tid; r < k0; r += blockDim.x) {
+      C2 v = b[r];
+      for (int j = 0; j < kb; ++j) {
+        const C2 u = M[(size_t)(k0 + j) * lda + r];
+        const C2 x = xs[j];
+        v.x -= u.x * x.x - u.y * x.y;
+        v.y -= u.x * x.y + u.y * x.x;
+      }
+      b[r] = v;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename C2>
+__global__ void residual_kernel(const C2* __restrict__ A, long long lda, long long strideA, int n,
+                                const double2* __restrict__ x, const double2* __restrict__ b, long long ldb, int nrhs,
+                                double2* __restrict__ r) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  const int mat = blockIdx.y / nrhs, rhs = blockIdx.y % nrhs;
+  if (row >= n) return;
+  const C2* M = A + (size_t)mat * strideA;
+  const size_t off = ((size_t)mat * nrhs + rhs) * ldb;
+  const double2* xv = x + off;
+  double sr = 0.0, si = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const C2 a = M[(size_t)j * lda + row];
+    const double2 xj = xv[j];
+    const double ar = (double)a.x, ai = (double)a.y;
+    sr = fma(ar, xj.x, sr);
+    sr = fma(-ai, xj.y, sr);
+    si = fma(ar, xj.y, si);
+    si = fma(ai, xj.x, si);
+  }
+  const double2 bb = b[off + row];
+  r[off + row] = make_double2(bb.x - sr, bb.y - si);
+}
+
+__global__ void norms_kernel(const double2* __restrict__ r, const double2* __restrict__ b, long long ldb, int n,
+                             double* out) {
+  const double2* rv = r + (size_t)blockIdx.x * ldb;
+  const double2* bv = b + (size_t)blockIdx.x * ldb;
+  double sr = 0.0, sb = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    sr += rv[i].x * rv[i].x + rv[i].y * rv[i].y;
+    sb += bv[i].x * bv[i].x + bv[i].y * bv[i].y;
+  }
+  __shared__ double s1[32], s2[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+    sb += __shfl_xor_sync(0xffffffffu, sb, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s1[threadIdx.x >> 5] = sr;
+    s2[threadIdx.x >> 5] = sb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0, c = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a += s1[w];
+      c += s2[w];
+    }
+    out[2 * blockIdx.x] = a;
+    out[2 * blockIdx.x + 1] = c;
+  }
+}
+
+__global__ void axpy_kernel(const float2* d, double2* x, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    x[i].x += (double)d[i].x;
+    x[i].y += (double)d[i].y;
+  }
+}
+__global__ void f64_to_f32_kernel(const double2* s, float2* d, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) d[i] = make_float2((float)s[i].x, (float)s[i].y);
+}
+__global__ void f32_to_f64_kernel(const float2* s, double2* d, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) d[i] = make_double2((double)s[i].x, (double)s[i].y);
+}
+
+}  // namespace
+
+cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int batch, int* ipiv, int* info, int nb,
+                              void* cublas_handle, cudaStream_t stream) {
+  cublasHandle_t h = (cublasHandle_t)cublas_handle;
+  cublasSetStream(h, stream);
+  const long long strideA = lda * (long long)n;
+  const bool mixed = prec == Precision::Mixed;
+  nb = std::max(1, std::min(nb, 64));
+  const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
+  for (int k = 0; k < n; k += nb) {
+    const int kb = std::min(nb, n - k);
+    if (mixed)
+      lu_panel_kernel<float><<<batch, 1024, 0, stream>>>((float2*)A, lda, strideA, n, k, kb, ipiv, info);
+    else
+      lu_panel_kernel<double><<<batch, 1024, 0, stream>>>((double2*)A, lda, strideA, n, k, kb, ipiv, info);
+    if (n - kb > 0) {
+      dim3 g((n - kb + 127) / 128, batch);
+      if (mixed)
+        lu_swap_kernel<float2><<<g, 128, 0, stream>>>((float2*)A, lda, strideA, n, k, kb, ipiv);
+      else
+        lu_swap_kernel<double2><<<g, 128, 0, stream>>>((double2*)A, lda, strideA, n, k, kb, ipiv);
+    }
+    const int rest = n - k - kb;
+    if (rest > 0) {
+      const int tpb = 128;
+      dim3 g((rest + tpb - 1) / tpb, batch);
+      const size_t sm = (size_t)kb * kb * esz + (size_t)kb * tpb * esz;
+      if (mixed) {
+        if (sm > 48 * 1024) cudaFuncSetAttribute(lu_trsm_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        lu_trsm_kernel<float2><<<g, tpb, sm, stream>>>((float2*)A, lda, strideA, n, k, kb);
+        const cuComplex alpha = make_cuComplex(-1.f, 0.f), beta = make_cuComplex(1.f, 0.f);
+        float2* base = (float2*)A;
+        cublasStatus_t st = cublasCgemmStridedBatched(
+            h, CUBLAS_OP_N, CUBLAS_OP_N, rest, rest, kb, &alpha, (const cuComplex*)(base + (k + kb) + (size_t)k * lda),
+            (int)lda, strideA, (const cuComplex*)(base + k + (size_t)(k + kb) * lda), (int)lda, strideA, &beta,
+            (cuComplex*)(base + (k + kb) + (size_t)(k + kb) * lda), (int)lda, strideA, batch);
+        if (st != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+      } else {
+        if (sm > 48 * 1024) cudaFuncSetAttribute(lu_trsm_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        lu_trsm_kernel<double2><<<g, tpb, sm, stream>>>((double2*)A, lda, strideA, n, k, kb);
+        const cuDoubleComplex alpha = make_cuDoubleComplex(-1.0, 0.0), beta = make_cuDoubleComplex(1.0, 0.0);
+        double2* base = (double2*)A;
+        cublasStatus_t st = cublasZgemmStridedBatched(
+            h, CUBLAS_OP_N, CUBLAS_OP_N, rest, rest, kb, &alpha,
+            (const cuDoubleComplex*)(base + (k + kb) + (size_t)k * lda), (int)lda, strideA,
+            (const cuDoubleComplex*)(base + k + (size_t)(k + kb) * lda), (int)lda, strideA, &beta,
+            (cuDoubleComplex*)(base + (k + kb) + (size_t)(k + kb) * lda), (int)lda, strideA, batch);
+        if (st != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+      }
+    }
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t lu_solve_batched(Precision prec, const void* LU, long long lda, int n, int batch, const int* ipiv, void* B,
+                             long long ldb, int nrhs, int /*nb*/, cudaStream_t stream) {
+  const long long strideA = lda * (long long)n;
+  if (prec == Precision::Mixed)
+    lu_solve_kernel<float><<<batch * nrhs, 1024, 0, stream>>>((const float2*)LU, lda, strideA, n, ipiv, (float2*)B,
+                                                             ldb, nrhs);
+  else
+    lu_solve_kernel<double><<<batch * nrhs, 1024, 0, stream>>>((const double2*)LU, lda, strideA, n, ipiv,
+                                                              (double2*)B, ldb, nrhs);
+  return cudaGetLastError();
+}
+
+cudaError_t residual_batched(Precision prec, const void* A, long long lda, int n, int batch, const double2* x,
+                             const double2* b, long long ldb, int nrhs, double2* r, cudaStream_t stream) {
+  const long long strideA = lda * (long long)n;
+  dim3 g((n + 255) / 256, batch * nrhs);
+  if (prec == Precision::Mixed)
+    residual_kernel<float2><<<g, 256, 0, stream>>>((const float2*)A, lda, strideA, n, x, b, ldb, nrhs, r);
+  else
+    residual_kernel<double2><<<g, 256, 0, stream>>>((const double2*)A, lda, strideA, n, x, b, ldb, nrhs, r);
+  return cudaGetLastError();
+}
+
+cudaError_t norms_batched(const double2* r, const double2* b, long long ldb, int n, int count, double* out,
+                          cudaStream_t stream) {
+  norms_kernel<<<count, 256, 0, stream>>>(r, b, ldb, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t axpy_f32_into_f64(const float2* d, double2* x, long long n, cudaStream_t stream) {
+  axpy_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(d, x, n);
+  return cudaGetLastError();
+}
+cudaError_t convert_f64_to_f32(const double2* src, float2* dst, long long n, cudaStream_t stream) {
+  f64_to_f32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(src, dst, n);
+  return cudaGetLastError();
+}
+cudaError_t convert_f32_to_f64(const float2* src, double2* dst, long long n, cudaStream_t stream) {
+  f32_to_f64_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(src, dst, n);
+  return cudaGetLastError();
+}
+
+}  // namespace bem

@@ -1,0 +1,518 @@
+// Host-side mesh planner for the GB300 BEM library.
+//
+// Turns a triangle mesh into the device-ready layout used by the assembly
+// kernels:
+//  * element geometry (normals, areas, surface curls) as in the reference's
+//    BoundaryMesh / surface_curls (src/blab/solvers/julia_local/src/
+//    BeatEngineCore.jl:236-256, 685-702);
+//  * the regular triangle rule (BeatEngineCore.jl:517-549) and the remapped
+//    Duffy rules for vertex-sharing pairs (BeatEngineCore.jl:551-915), with the
+//    same point order and orientation keys so the discretisation is identical;
+//  * test-face tiles: faces ordered by recursive coordinate bisection of their
+//    centroids and cut into compact tiles.  Each tile owns a block of
+//    "extended rows" (one per distinct vertex of the tile); a vertex shared by
+//    several tiles has one primary extended row (which defines its matrix row)
+//    and halo rows in the other tiles.  The assembly kernel accumulates test
+//    faces into extended rows without atomics, and the column gather folds
+//    halo rows back into matrix rows in a fixed order;
+//  * lane groups: each tile's faces are packed into groups of 32 faces that
+//    share no vertex, so the 32 lanes of a warp can accumulate one group into
+//    shared memory without conflicts.
+#include "bem_internal.h"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <map>
+#include <numeric>
+#include <set>
+#include <tuple>
+
+namespace bem {
+namespace {
+
+using V3 = std::array<double, 3>;
+inline V3 sub(const V3& a, const V3& b) { return {a[0] - b[0], a[1] - b[1], a[2] - b[2]}; }
+inline double dot(const V3& a, const V3& b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+inline V3 cross(const V3& a, const V3& b) {
+  return {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+}
+
+// Regular rule (BeatEngineCore.jl:517-549): literal constants of the order-4
+// six-point rule, including the asymmetric final digits of two points.
+void regular_rule(int order, std::vector<double>& pts, std::vector<double>& w) {
+  if (order <= 1) {
+    pts = {1.0 / 3.0, 1.0 / 3.0};
+    w = {0.5};
+  } else if (order == 4) {
+    pts = {0.4459484909159651, 0.4459484909159651, 0.0915762135097710, 0.0915762135097700,
+           0.1081030181680700, 0.4459484909159651, 0.4459484909159651, 0.1081030181680700,
+           0.8168475729804590, 0.0915762135097700, 0.0915762135097710, 0.8168475729804580};
+    const double ws[6] = {0.2233815896780110, 0.1099517436553220, 0.2233815896780110,
+                          0.2233815896780110, 0.1099517436553220, 0.1099517436553220};
+    w.clear();
+    for (double x : ws) w.push_back(0.5 * x);
+  } else {
+    pts = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0, 1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0};
+    w = {1.0 / 6.0, 1.0 / 6.0, 1.0 / 6.0};
+  }
+}
+
+// Gauss-Legendre on [0,1] (BeatEngineCore.jl:551-569).
+bool gauss01(int order, std::vector<double>& x, std::vector<double>& w) {
+  if (order == 1) {
+    x = {0.5};
+    w = {1.0};
+  } else if (order == 2) {
+    double a = 0.5 / std::sqrt(3.0);
+    x = {0.5 - a, 0.5 + a};
+    w = {0.5, 0.5};
+  } else if (order == 3) {
+    double a = std::sqrt(3.0 / 5.0) / 2.0;
+    x = {0.5 - a, 0.5, 0.5 + a};
+    w = {5.0 / 18.0, 4.0 / 9.0, 5.0 / 18.0};
+  } else if (order == 4) {
+    double x1 = std::sqrt(3.0 / 7.0 - 2.0 / 7.0 * std::sqrt(6.0 / 5.0)) / 2.0;
+    double x2 = std::sqrt(3.0 / 7.0 + 2.0 / 7.0 * std::sqrt(6.0 / 5.0)) / 2.0;
+    double w1 = (18.0 + std::sqrt(30.0)) / 72.0;
+    double w2 = (18.0 - std::sqrt(30.0)) / 72.0;
+    x = {0.5 - x2, 0.5 - x1, 0.5 + x1, 0.5 + x2};
+    w = {w2, w1, w1, w2};
+  } else {
+    return false;
+  }
+  return true;
+}
+
+// One Duffy point as (test xi, test eta, trial xi, trial eta, w).
+using DPoint = std::array<double, 5>;
+
+// Duffy rules on [0,1]^4 mapped to triangle pairs (BeatEngineCore.jl:571-631):
+// coincident (6 sub-maps), edge-adjacent (5), vertex-adjacent (2).
+std::vector<DPoint> duffy_base(int order, int kind) {
+  std::vector<double> x, w;
+  gauss01(order, x, w);
+  const int n = (int)x.size();
+  std::vector<DPoint> out;
+  auto push = [&](double tx, double ty, double rx, double ry, double weight) {
+    out.push_back({tx - ty, ty, rx - ry, ry, weight});
+  };
+  for (int ti = 0; ti < n * n; ++ti) {
+    for (int ri = 0; ri < n * n; ++ri) {
+      const double xsi = x[ti % n], e1 = x[ti / n], e2 = x[ri % n], e3 = x[ri / n];
+      const double base = (w[ti / n] * w[ti % n]) * (w[ri / n] * w[ri % n]);
+      const double e12 = e1 * e2, e123 = e12 * e3;
+      if (kind == 1) {
+        double wt = base * xsi * xsi * xsi * e1 * e1 * e2;
+        push(xsi, xsi * (1.0 - e1 + e12), xsi * (1.0 - e123), xsi * (1.0 - e1), wt);
+        push(xsi * (1.0 - e123), xsi * (1.0 - e1), xsi, xsi * (1.0 - e1 + e12), wt);
+        push(xsi, xsi * (e1 - e12 + e123), xsi * (1.0 - e12), xsi * (e1 - e12), wt);
+        push(xsi * (1.0 - e12), xsi * (e1 - e12), xsi, xsi * (e1 - e12 + e123), wt);
+        push(xsi * (1.0 - e123), xsi * (e1 - e123), xsi, xsi * (e1 - e12), wt);
+        push(xsi, xsi * (e1 - e12), xsi * (1.0 - e123), xsi * (e1 - e123), wt);
+      } else if (kind == 2) {
+        double wt = base * xsi * xsi * xsi * e1 * e1;
+        push(xsi, xsi * e1 * e3, xsi * (1.0 - e12), xsi * e1 * (1.0 - e2), wt);
+        push(xsi, xsi * e1, xsi * (1.0 - e123), xsi * e1 * e2 * (1.0 - e3), wt * e2);
+        push(xsi * (1.0 - e12), xsi * e1 * (1.0 - e2), xsi, xsi * e123, wt * e2);
+        push(xsi * (1.0 - e123), xsi * e12 * (1.0 - e3), xsi, xsi * e1, wt * e2);
+        push(xsi * (1.0 - e123), xsi * e1 * (1.0 - e2 * e3), xsi, xsi * e12, wt * e2);
+      } else {
+        double wt = base * xsi * xsi * xsi * e2;
+        push(xsi, xsi * e1, xsi * e2, xsi * e2 * e3, wt);
+        push(xsi * e2, xsi * e2 * e3, xsi, xsi * e1, wt);
+      }
+    }
+  }
+  return out;
+}
+
+// Shared-vertex / shared-edge reparametrisations (BeatEngineCore.jl:633-655),
+// vertex ids 1-based.
+inline void remap_vertex(double& u, double& v, int id) {
+  if (id == 2) {
+    u = 1.0 - u - v;
+  } else if (id == 3) {
+    v = 1.0 - u - v;
+  }
+}
+inline void remap_edge(double& u, double& v, int a, int b) {
+  static const double ref[3][2] = {{0.0, 0.0}, {1.0, 0.0}, {0.0, 1.0}};
+  const int c = 6 - a - b;
+  const double* p0 = ref[a - 1];
+  const double* p1 = ref[b - 1];
+  const double* p2 = ref[c - 1];
+  double nu = p0[0] + u * (p1[0] - p0[0]) + v * (p2[0] - p0[0]);
+  double nv = p0[1] + u * (p1[1] - p0[1]) + v * (p2[1] - p0[1]);
+  u = nu;
+  v = nv;
+}
+
+struct Adjacency {
+  int kind, ta, tb, ra, rb;
+};
+// BeatEngineCore.jl:453-479
+Adjacency classify(const int* fa, const int* fb) {
+  int sa[9], sb[9], n = 0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      if (fa[i] == fb[j]) {
+        sa[n] = i + 1;
+        sb[n] = j + 1;
+        ++n;
+      }
+  if (n >= 3) return {1, 0, 0, 0, 0};
+  if (n == 2) {
+    if (sb[1] < sb[0]) {
+      std::swap(sa[0], sa[1]);
+      std::swap(sb[0], sb[1]);
+    }
+    return {2, sa[0], sa[1], sb[0], sb[1]};
+  }
+  if (n == 1) return {3, sa[0], 0, sb[0], 0};
+  return {0, 0, 0, 0, 0};
+}
+
+// Recursive coordinate bisection of face centroids into leaves of <= cap faces.
+void rcb(std::vector<int>& ids, int lo, int hi, const std::vector<double>& cent, int cap,
+         std::vector<std::pair<int, int>>& leaves) {
+  if (hi - lo <= cap) {
+    leaves.push_back({lo, hi});
+    return;
+  }
+  double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+  for (int i = lo; i < hi; ++i)
+    for (int d = 0; d < 3; ++d) {
+      mn[d] = std::min(mn[d], cent[3 * ids[i] + d]);
+      mx[d] = std::max(mx[d], cent[3 * ids[i] + d]);
+    }
+  int axis = 0;
+  for (int d = 1; d < 3; ++d)
+    if (mx[d] - mn[d] > mx[axis] - mn[axis]) axis = d;
+  // split so that the left part holds a whole number of tiles when possible
+  int n = hi - lo;
+  int tiles = (n + cap - 1) / cap;
+  int left_tiles = tiles / 2;
+  int mid = lo + std::max(1, std::min(n - 1, (int)((long long)n * left_tiles / tiles)));
+  std::nth_element(ids.begin() + lo, ids.begin() + mid, ids.begin() + hi, [&](int a, int b) {
+    double ca = cent[3 * a + axis], cb = cent[3 * b + axis];
+    return ca < cb || (ca == cb && a < b);
+  });
+  rcb(ids, lo, mid, cent, cap, leaves);
+  rcb(ids, mid, hi, cent, cap, leaves);
+}
+
+}  // namespace
+
+std::string build_mesh_plan(const double* verts, int nv, const int* faces, int nf, int regular_order,
+                            int singular_order, int tile_faces, MeshPlan& P) {
+  if (nv <= 0 || nf <= 0) return "mesh must have at least one vertex and one face";
+  if (regular_order < 1 || regular_order > 4) return "regular quadrature order must be 1..4";
+  if (singular_order < 1 || singular_order > 4) return "Duffy 1D Gauss order must be between 1 and 4";
+  if (tile_faces < 32) tile_faces = 32;
+  P = MeshPlan();
+  P.nv = nv;
+  P.nf = nf;
+  P.regular_order = regular_order;
+  P.singular_order = singular_order;
+  P.verts.assign(verts, verts + 3 * (size_t)nv);
+  P.faces.assign(faces, faces + 3 * (size_t)nf);
+  for (int i = 0; i < 3 * nf; ++i)
+    if (faces[i] < 0 || faces[i] >= nv) return "face references a vertex index out of range";
+  for (int i = 0; i < 3 * nv; ++i)
+    if (!std::isfinite(verts[i])) return "vertex coordinates must be finite";
+
+  regular_rule(regular_order, P.rule_pts, P.rule_w);
+  const int Q = (int)P.rule_w.size();
+  P.Q = Q;
+  for (int q = 0; q < Q; ++q) {
+    double u = P.rule_pts[2 * q], v = P.rule_pts[2 * q + 1];
+    double phi[3] = {1.0 - u - v, u, v};
+    for (int a = 0; a < 3; ++a) {
+      P.m10[a] += P.rule_w[q] * phi[a];
+      for (int b = 0; b < 3; ++b) P.m11[3 * a + b] += P.rule_w[q] * phi[a] * phi[b];
+    }
+  }
+
+  // ---- geometry (BeatEngineCore.jl:236-256, 685-702)
+  P.area.resize(nf);
+  P.normal.resize(3 * (size_t)nf);
+  P.curls.resize(9 * (size_t)nf);
+  std::vector<double> cent(3 * (size_t)nf);
+  P.faces32.resize(nf);
+  P.faces64.resize(nf);
+  for (int f = 0; f < nf; ++f) {
+    V3 v[3];
+    for (int a = 0; a < 3; ++a)
+      for (int d = 0; d < 3; ++d) v[a][d] = verts[3 * faces[3 * f + a] + d];
+    V3 e1 = sub(v[1], v[0]), e2 = sub(v[2], v[0]);
+    V3 cp = cross(e1, e2);
+    double nn = std::sqrt(dot(cp, cp));
+    if (!(nn > 0.0)) return "mesh contains a degenerate (zero-area) triangle";
+    V3 n = {cp[0] / nn, cp[1] / nn, cp[2] / nn};
+    P.area[f] = nn / 2.0;
+    double g11 = dot(e1, e1), g12 = dot(e1, e2), g22 = dot(e2, e2);
+    double det = g11 * g22 - g12 * g12;
+    double i11 = g22 / det, i12 = -g12 / det, i22 = g11 / det;
+    const double rg[3][2] = {{-1.0, -1.0}, {1.0, 0.0}, {0.0, 1.0}};
+    V3 curl[3];
+    for (int a = 0; a < 3; ++a) {
+      double c1 = i11 * rg[a][0] + i12 * rg[a][1], c2 = i12 * rg[a][0] + i22 * rg[a][1];
+      V3 g = {e1[0] * c1 + e2[0] * c2, e1[1] * c1 + e2[1] * c2, e1[2] * c1 + e2[2] * c2};
+      curl[a] = cross(n, g);
+    }
+    V3 c = {(v[0][0] + v[1][0] + v[2][0]) / 3.0, (v[0][1] + v[1][1] + v[2][1]) / 3.0,
+            (v[0][2] + v[1][2] + v[2][2]) / 3.0};
+    for (int d = 0; d < 3; ++d) {
+      cent[3 * f + d] = c[d];
+      P.normal[3 * f + d] = n[d];
+    }
+    for (int a = 0; a < 3; ++a)
+      for (int d = 0; d < 3; ++d) P.curls[9 * f + 3 * a + d] = curl[a][d];
+
+    FaceF32& F = P.faces32[f];
+    FaceF64& G = P.faces64[f];
+    std::fill((float*)&F, (float*)&F + 40, 0.0f);
+    std::fill((double*)&G, (double*)&G + sizeof(FaceF64) / 8, 0.0);
+    for (int d = 0; d < 3; ++d) {
+      F.anchor_hi[d] = (float)c[d];
+      F.anchor_lo[d] = (float)(c[d] - (double)F.anchor_hi[d]);
+      F.normal[d] = (float)n[d];
+      G.anchor[d] = c[d];
+      G.normal[d] = n[d];
+    }
+    F.area2 = (float)nn;
+    G.area2 = nn;
+    for (int a = 0; a < 3; ++a)
+      for (int d = 0; d < 3; ++d) {
+        F.curls[3 * a + d] = (float)curl[a][d];
+        G.curls[3 * a + d] = curl[a][d];
+      }
+    for (int q = 0; q < Q; ++q) {
+      double u = P.rule_pts[2 * q], w2 = P.rule_pts[2 * q + 1];
+      for (int d = 0; d < 3; ++d) {
+        // quadrature point as in local_to_global (BeatEngineCore.jl:678-681)
+        double x = (1.0 - u - w2) * v[0][d] + u * v[1][d] + w2 * v[2][d];
+        F.off[3 * q + d] = (float)(x - c[d]);
+        G.off[3 * q + d] = x - c[d];
+      }
+    }
+    for (int a = 0; a < 3; ++a) {
+      F.verts[a] = faces[3 * f + a];
+      G.verts[a] = faces[3 * f + a];
+    }
+  }
+
+  // ---- test-face tiles by recursive coordinate bisection
+  std::vector<int> order(nf);
+  std::iota(order.begin(), order.end(), 0);
+  std::vector<std::pair<int, int>> leaves;
+  rcb(order, 0, nf, cent, tile_faces, leaves);
+  P.tile_faces = tile_faces;
+  P.n_tiles = (int)leaves.size();
+  std::vector<int> face_tile(nf);
+  std::vector<std::vector<int>> tile_face_list(P.n_tiles);
+  for (int t = 0; t < P.n_tiles; ++t) {
+    std::vector<int> fl(order.begin() + leaves[t].first, order.begin() + leaves[t].second);
+    std::sort(fl.begin(), fl.end());
+    for (int f : fl) face_tile[f] = t;
+    tile_face_list[t] = fl;
+  }
+  // primary tile of a vertex = first tile (in tile order) containing it
+  std::vector<int> primary(nv, -1);
+  for (int t = 0; t < P.n_tiles; ++t)
+    for (int f : tile_face_list[t])
+      for (int a = 0; a < 3; ++a)
+        if (primary[faces[3 * f + a]] < 0) primary[faces[3 * f + a]] = t;
+  for (int v = 0; v < nv; ++v)
+    if (primary[v] < 0) primary[v] = -2;  // unreferenced vertex: gets its own row below
+  // tile-local rows: primary vertices first (first-appearance order), then halo vertices
+  P.face_ext.assign(3 * (size_t)nf, -1);
+  P.tile_row_base.assign(P.n_tiles + 1, 0);
+  P.vertex_row.assign(nv, -1);
+  P.row_vertex.clear();
+  std::vector<std::vector<int>> tile_rows(P.n_tiles);
+  std::vector<std::map<int, int>> tile_loc(P.n_tiles);
+  for (int t = 0; t < P.n_tiles; ++t) {
+    std::vector<int> prim, halo;
+    std::set<int> seen;
+    for (int f : tile_face_list[t])
+      for (int a = 0; a < 3; ++a) {
+        int v = faces[3 * f + a];
+        if (seen.insert(v).second) (primary[v] == t ? prim : halo).push_back(v);
+      }
+    for (int v : prim) {
+      P.vertex_row[v] = (int)P.row_vertex.size();
+      P.row_vertex.push_back(v);
+    }
+    std::vector<int>& rows = tile_rows[t];
+    rows = prim;
+    rows.insert(rows.end(), halo.begin(), halo.end());
+    for (size_t i = 0; i < rows.size(); ++i) tile_loc[t][rows[i]] = (int)i;
+    P.tile_row_base[t + 1] = P.tile_row_base[t] + (int)rows.size();
+    P.max_tile_rows = std::max(P.max_tile_rows, (int)rows.size());
+  }
+  for (int v = 0; v < nv; ++v)
+    if (P.vertex_row[v] < 0) {  // vertex used by no face: identity-free zero row
+      P.vertex_row[v] = (int)P.row_vertex.size();
+      P.row_vertex.push_back(v);
+    }
+  P.n_ext = P.tile_row_base[P.n_tiles];
+  P.ext_row.resize(P.n_ext);
+  P.ext_is_halo.resize(P.n_ext);
+  for (int t = 0; t < P.n_tiles; ++t)
+    for (size_t i = 0; i < tile_rows[t].size(); ++i) {
+      int v = tile_rows[t][i];
+      P.ext_row[P.tile_row_base[t] + i] = P.vertex_row[v];
+      P.ext_is_halo[P.tile_row_base[t] + i] = primary[v] == t ? 0 : 1;
+    }
+  for (int f = 0; f < nf; ++f) {
+    int t = face_tile[f];
+    for (int a = 0; a < 3; ++a) P.face_ext[3 * f + a] = P.tile_row_base[t] + tile_loc[t][faces[3 * f + a]];
+  }
+  // halo gather lists, grouped by target row (ascending ext id within a row)
+  {
+    std::vector<std::pair<int, int>> h;  // (row, ext)
+    for (int e = 0; e < P.n_ext; ++e)
+      if (P.ext_is_halo[e]) h.push_back({P.ext_row[e], e});
+    std::sort(h.begin(), h.end());
+    P.halo_ext.clear();
+    P.halo_row.clear();
+    P.halo_row_ptr.assign(1, 0);
+    P.halo_slot_of_ext.assign(P.n_ext, -1);
+    for (size_t i = 0; i < h.size(); ++i) {
+      if (i == 0 || h[i].first != h[i - 1].first) {
+        if (i) P.halo_row_ptr.push_back((int)i);
+        P.halo_row.push_back(h[i].first);
+      }
+      P.halo_slot_of_ext[h[i].second] = (int)i;
+      P.halo_ext.push_back(h[i].second);
+    }
+    P.halo_row_ptr.push_back((int)h.size());
+    if (h.empty()) P.halo_row_ptr.assign(1, 0);
+  }
+  // lane groups: first-fit packing of each tile's faces into vertex-disjoint groups of 32
+  P.tile_group_ptr.assign(1, 0);
+  P.lane_slots.clear();
+  for (int t = 0; t < P.n_tiles; ++t) {
+    std::vector<std::vector<int>> groups;
+    std::vector<std::set<int>> gverts;
+    for (int f : tile_face_list[t]) {
+      int placed = -1;
+      for (size_t g = 0; g < groups.size(); ++g) {
+        if (groups[g].size() >= (size_t)kLanes) continue;
+        bool clash = false;
+        for (int a = 0; a < 3 && !clash; ++a) clash = gverts[g].count(faces[3 * f + a]) > 0;
+        if (!clash) {
+          placed = (int)g;
+          break;
+        }
+      }
+      if (placed < 0) {
+        groups.emplace_back();
+        gverts.emplace_back();
+        placed = (int)groups.size() - 1;
+      }
+      groups[placed].push_back(f);
+      for (int a = 0; a < 3; ++a) gverts[placed].insert(faces[3 * f + a]);
+    }
+    for (auto& g : groups) {
+      for (int l = 0; l < kLanes; ++l) {
+        LaneSlot s;
+        if (l < (int)g.size()) {
+          int f = g[l];
+          s.face = f;
+          for (int a = 0; a < 3; ++a) s.loc[a] = tile_loc[t][faces[3 * f + a]];
+        } else {
+          s.face = -1;
+          s.loc[0] = s.loc[1] = s.loc[2] = 0;
+        }
+        P.lane_slots.push_back(s);
+      }
+    }
+    P.tile_group_ptr.push_back(P.tile_group_ptr.back() + (int)groups.size());
+  }
+  // column gather CSR: vertex j <- (g, b)
+  P.col_ptr.assign(nv + 1, 0);
+  for (int i = 0; i < 3 * nf; ++i) P.col_ptr[faces[i] + 1]++;
+  for (int v = 0; v < nv; ++v) P.col_ptr[v + 1] += P.col_ptr[v];
+  P.col_fb.assign(3 * (size_t)nf, 0);
+  {
+    std::vector<int> fill(P.col_ptr.begin(), P.col_ptr.end() - 1);
+    for (int f = 0; f < nf; ++f)
+      for (int b = 0; b < 3; ++b) P.col_fb[fill[faces[3 * f + b]]++] = 3 * f + b;
+  }
+
+  // ---- singular pairs and remapped Duffy rules (BeatEngineCore.jl:784-915)
+  std::vector<std::vector<int>> v2f(nv);
+  for (int f = 0; f < nf; ++f)
+    for (int a = 0; a < 3; ++a) v2f[faces[3 * f + a]].push_back(f);
+  std::vector<DPoint> base[4];
+  for (int k = 1; k <= 3; ++k) base[k] = duffy_base(singular_order, k);
+  std::map<std::tuple<int, int, int, int, int>, int> rule_of_key;
+  P.rule_ptr.assign(1, 0);
+  P.duffy.clear();
+  std::vector<SingularPair> pairs;
+  for (int t = 0; t < nf; ++t) {
+    std::vector<int> cand;
+    std::set<int> seen;
+    for (int a = 0; a < 3; ++a)
+      for (int r : v2f[faces[3 * t + a]])
+        if (seen.insert(r).second) cand.push_back(r);
+    for (int r : cand) {
+      Adjacency adj = classify(&faces[3 * t], &faces[3 * r]);
+      if (adj.kind == 0) continue;
+      auto key = adj.kind == 1 ? std::make_tuple(1, 0, 0, 0, 0)
+                 : adj.kind == 2 ? std::make_tuple(2, adj.ta, adj.tb, adj.ra, adj.rb)
+                                 : std::make_tuple(3, adj.ta, 0, adj.ra, 0);
+      auto it = rule_of_key.find(key);
+      int rule;
+      if (it == rule_of_key.end()) {
+        rule = (int)rule_of_key.size();
+        rule_of_key[key] = rule;
+        for (const DPoint& p : base[adj.kind]) {
+          double tu = p[0], tv = p[1], ru = p[2], rv = p[3];
+          if (adj.kind == 2) {
+            remap_edge(tu, tv, adj.ta, adj.tb);
+            remap_edge(ru, rv, adj.ra, adj.rb);
+          } else if (adj.kind == 3) {
+            remap_vertex(tu, tv, adj.ta);
+            remap_vertex(ru, rv, adj.ra);
+          }
+          P.duffy.insert(P.duffy.end(), {tu, tv, ru, rv, p[4]});
+        }
+        P.rule_ptr.push_back((int)(P.duffy.size() / 5));
+      } else {
+        rule = it->second;
+      }
+      SingularPair sp;
+      sp.test = t;
+      sp.trial = r;
+      sp.rule = rule;
+      sp.kind = adj.kind;
+      sp.jac = (2.0 * P.area[t]) * (2.0 * P.area[r]);
+      sp.nprod = P.normal[3 * t] * P.normal[3 * r] + P.normal[3 * t + 1] * P.normal[3 * r + 1] +
+                 P.normal[3 * t + 2] * P.normal[3 * r + 2];
+      pairs.push_back(sp);
+    }
+  }
+  std::vector<int> idx(pairs.size());
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return pairs[a].trial < pairs[b].trial; });
+  P.pairs.resize(pairs.size());
+  for (size_t i = 0; i < idx.size(); ++i) P.pairs[i] = pairs[idx[i]];
+  P.pairs_by_trial_ptr.assign(nf + 1, 0);
+  for (const auto& sp : P.pairs) P.pairs_by_trial_ptr[sp.trial + 1]++;
+  for (int f = 0; f < nf; ++f) P.pairs_by_trial_ptr[f + 1] += P.pairs_by_trial_ptr[f];
+  P.pairs_by_test_ptr.assign(nf + 1, 0);
+  for (const auto& sp : P.pairs) P.pairs_by_test_ptr[sp.test + 1]++;
+  for (int f = 0; f < nf; ++f) P.pairs_by_test_ptr[f + 1] += P.pairs_by_test_ptr[f];
+  P.pairs_by_test.assign(P.pairs.size(), 0);
+  {
+    std::vector<int> fill(P.pairs_by_test_ptr.begin(), P.pairs_by_test_ptr.end() - 1);
+    for (size_t i = 0; i < P.pairs.size(); ++i) P.pairs_by_test[fill[P.pairs[i].test]++] = (int)i;
+  }
+  return std::string();
+}
+
+}  // namespace bem

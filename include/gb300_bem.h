@@ -1,0 +1,143 @@
+/*
+ * gb300_bem.h - C ABI of the GB300 exterior Helmholtz BEM backend.
+ *
+ * The reference (JWSound/boundary-lab) runs its exterior solve in a Julia
+ * worker process; the Python adapter talks to it over a JSON request file and
+ * NDJSON events (src/blab/solvers/beat_engine_backend.py:140-221, 286-462).
+ * This library replaces the numerical part of that worker: the per-frequency
+ * body of solve_request_impl (src/blab/solvers/julia_local/solver.jl:805-997),
+ * i.e. operator assembly, the Burton-Miller LU solve and the field evaluation.
+ * Each entry point below names the reference function it stands in for.
+ *
+ * Conventions
+ *  - Every function returns an int status (BEM_OK == 0); on failure the
+ *    context's last error message says why (bem_last_error).
+ *  - Plain pointers and sizes only.  Host buffers are owned by the caller;
+ *    device memory is owned by the context and freed by bem_destroy_context.
+ *  - Complex arrays are interleaved (re, im) doubles.
+ *  - Vertex and face indices are 0-based; faces are int32 triples.
+ *  - A context owns one CUDA stream on one device and is thread-compatible:
+ *    use one context per host thread (or serialise calls).
+ *  - Frequencies of one call are solved as batches; results are identical to
+ *    solving them one by one up to rounding order within FP32/FP64.
+ */
+#ifndef GB300_BEM_H
+#define GB300_BEM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB300_BEM_ABI_VERSION 1
+
+typedef struct bem_context bem_context;
+typedef struct bem_mesh bem_mesh;
+
+enum bem_status {
+  BEM_OK = 0,
+  BEM_ERR_INVALID_ARGUMENT = 1,
+  BEM_ERR_CUDA = 2,
+  BEM_ERR_OUT_OF_MEMORY = 3,
+  BEM_ERR_SINGULAR = 4,     /* zero pivot in the LU factorisation */
+  BEM_ERR_NOT_CONVERGED = 5 /* iterative refinement missed its tolerance */
+};
+
+enum bem_precision {
+  BEM_PRECISION_FP64 = 0,  /* FP64 assembly, FP64 LU, FP64 field ("plain FP64 GPU form") */
+  BEM_PRECISION_MIXED = 1  /* compensated FP32 assembly, FP32 LU, FP64 iterative refinement,
+                              FP64 singular moments, compensated FP32 field */
+};
+
+/* Library ABI version (GB300_BEM_ABI_VERSION). */
+int bem_abi_version(void);
+
+/* Create a context on CUDA device `device`.  Replaces the reference's
+ * accelerator set-up in solver.jl:752-767 (device caches built per job). */
+int bem_create_context(int device, bem_context** out);
+void bem_destroy_context(bem_context* ctx);
+/* Message of the last failed call on this context ("" if none). */
+const char* bem_last_error(const bem_context* ctx);
+
+/* Upload a triangle mesh and build every frequency-independent cache: face
+ * geometry and surface curls, the regular rule, singular (vertex-sharing) pair
+ * list with remapped Duffy rules, and the FP64 k-independent singular moments.
+ * Replaces load_combined_mesh + build_p1/dp0_space + triangle_rule +
+ * build_singular_correction_cache + build_cuda_regular_assembly_cache +
+ * build_cuda_singular_correction_cache (solver.jl:717-767,
+ * BeatEngineCore.jl:236-256, 517-549, 875-915).
+ * regular_order: 1..4 (4 = the six-point rule); singular_order: 1..4. */
+int bem_upload_mesh(bem_context* ctx, const double* vertices, int n_vertices, const int* faces, int n_faces,
+                    int regular_order, int singular_order, bem_mesh** out);
+void bem_release_mesh(bem_mesh* mesh);
+/* Sizes of an uploaded mesh (any output pointer may be NULL). */
+int bem_mesh_info(const bem_mesh* mesh, int* n_vertices, int* n_faces, int* n_singular_pairs);
+
+/* Excitations: n_rhs unit drive patterns, complex, row-major [n_rhs][n_faces].
+ * The Neumann data of excitation c at angular frequency w is
+ * q_c = i * rho * w * drive[c], as in pressure_for_drives (solver.jl:434-459).
+ * 1 <= n_rhs <= 4. */
+int bem_set_excitation(bem_mesh* mesh, const double* unit_drive, int n_rhs);
+/* Observation points, row-major [n_points][3] in metres (solver.jl:320-388). */
+int bem_set_observation_points(bem_mesh* mesh, const double* points, int n_points);
+
+typedef struct bem_solve_options {
+  int precision;         /* enum bem_precision */
+  double sound_speed;    /* m/s */
+  double rho;            /* kg/m^3 */
+  double refine_tol;     /* mixed form: stop when ||b - A x|| / ||b|| <= refine_tol (FP64 residual) */
+  int max_refine;        /* mixed form: maximum refinement steps */
+  int batch;             /* frequencies factored together (<= 64); 0 = automatic */
+  int lu_block;          /* LU block size (<= 64); 0 = automatic */
+  int outputs_on_device; /* 1: pressure_out / field_out are device pointers of the context's device */
+} bem_solve_options;
+
+typedef struct bem_solve_stats {
+  double assembly_s;      /* summed over the call, seconds (CUDA events) */
+  double solve_s;
+  double field_s;
+  int max_refine_steps;   /* over all frequencies and excitations */
+  double max_rel_residual;
+  int batches;
+} bem_solve_stats;
+
+void bem_default_options(bem_solve_options* opt);
+
+/* The hot path: for every frequency, assemble the Burton-Miller system
+ * 1/2 M - D + (i/k) H, factor it once, solve every excitation, and evaluate
+ * the exterior field at the observation points.  Replaces the per-frequency
+ * body of solve_request_impl (solver.jl:805-920): assemble_regular_galerkin_
+ * operators, pressure_for_drives / solve_burton_miller_neumann and
+ * field_for_points.
+ * pressure_out: [n_freq][n_rhs][n_vertices] complex (may be NULL)
+ * field_out:    [n_freq][n_rhs][n_points] complex (may be NULL)
+ * stats may be NULL. */
+int bem_solve_frequencies(bem_mesh* mesh, const double* freqs_hz, int n_freq, const bem_solve_options* opt,
+                          double* pressure_out, double* field_out, bem_solve_stats* stats);
+
+/* Parity entry point: the dense P1 x P1 operator cD*D + cH*H + cM*M11 at
+ * wavenumber k, written column-major [n_vertices][n_vertices] complex (row i
+ * of column j at out[2*(j*n + i)]).  coeffs = {cD.re, cD.im, cH.re, cH.im,
+ * cM.re, cM.im}.  The Burton-Miller left-hand side of
+ * burton_miller_neumann_matrices (BeatEngineCpuSolve.jl:45-53) is
+ * cD = -1, cH = i/k, cM = 1/2. */
+int bem_assemble_lhs(bem_mesh* mesh, double k, int precision, const double* coeffs, double* out);
+
+/* Parity entry point: out = (cS*S + cK*K' + cM10*M10) q for n_rhs face-data
+ * columns q (column-major [n_rhs][n_faces] complex); out is column-major
+ * [n_rhs][n_vertices] complex.  coeffs = {cS, cK, cM10} as (re, im) pairs.
+ * The Burton-Miller right-hand side operator of BeatEngineCpuSolve.jl:50 is
+ * cS = -1, cK = -i/k, cM10 = -i/(2k); this is the matrix-free right-hand side
+ * of _cuda_burton_miller_rhs (BeatEngineCore.jl:1178-1184). */
+int bem_apply_rhs_operator(bem_mesh* mesh, double k, int precision, const double* coeffs, const double* q, int n_rhs,
+                           double* out);
+
+/* Device bytes needed to solve `batch` frequencies of a mesh of this size
+ * (scratch + matrices + factors), for admission control by a scheduler. */
+long long bem_estimate_device_bytes(int n_vertices, int n_faces, int n_singular_pairs, int n_rhs, int n_points,
+                                    int batch, int precision);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB300_BEM_H */

@@ -1,0 +1,216 @@
+"""GPU parity: the CUDA path (through the C ABI) against the FP64 CPU oracle.
+
+Tolerances (relative, Frobenius / 2-norm unless stated):
+  FP64 form  : operators 1e-11, solutions and fields 1e-9 (rounding-order only)
+  mixed form : operators 2e-6 (compensated FP32 entries), solutions and fields 1e-5
+               (the benchmark spec's bound on far-field pressure vs the FP64 oracle)
+"""
+
+import numpy as np
+import pytest
+
+from conftest import pkg_module
+
+pytestmark = pytest.mark.gpu
+
+meshes = pkg_module("meshes")
+
+
+def _oracle():
+    from oracle import oracle
+
+    return oracle
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+@pytest.fixture(scope="module")
+def sphere320():
+    return meshes.sphere_with_cap(0.1, 2, 30.0)
+
+
+@pytest.fixture(scope="module")
+def box_small():
+    return meshes.box_with_piston((0.3, 0.2, 0.25), 600, 0.05, "+z")
+
+
+@pytest.mark.parametrize("freq", [100.0, 1000.0, 4000.0])
+def test_bm_lhs_fp64_matches_oracle(gpu_ctx, native, sphere320, freq):
+    O = _oracle()
+    k = 2 * np.pi * freq / 343.0
+    m = gpu_ctx.upload_mesh(sphere320.vertices, sphere320.faces)
+    try:
+        A = m.assemble_lhs(k, precision=native.BEM_PRECISION_FP64)
+    finally:
+        m.release()
+    ops = O.assemble(sphere320, k)
+    M11, M10 = O.mass(sphere320)
+    lhs, _ = O.burton_miller_matrices(ops, M11, M10, k)
+    assert rel(A, lhs) < 1e-11
+    assert np.max(np.abs(A - lhs)) < 1e-10 * np.max(np.abs(lhs))
+
+
+@pytest.mark.parametrize("which", ["D", "H", "M"])
+def test_single_operators_fp64(gpu_ctx, native, box_small, which):
+    O = _oracle()
+    k = 2 * np.pi * 2500.0 / 343.0
+    coeffs = {"D": (1.0, 0.0, 0.0), "H": (0.0, 1.0, 0.0), "M": (0.0, 0.0, 1.0)}[which]
+    m = gpu_ctx.upload_mesh(box_small.vertices, box_small.faces)
+    try:
+        A = m.assemble_lhs(k, coeffs=coeffs, precision=native.BEM_PRECISION_FP64)
+    finally:
+        m.release()
+    ops = O.assemble(box_small, k)
+    M11, _ = O.mass(box_small)
+    ref = {"D": ops.double_layer, "H": ops.hypersingular, "M": M11.astype(complex)}[which]
+    assert rel(A, ref) < 1e-11
+
+
+def test_bm_lhs_mixed_matches_oracle(gpu_ctx, native, box_small):
+    O = _oracle()
+    freq = 6000.0
+    k = 2 * np.pi * freq / 343.0
+    m = gpu_ctx.upload_mesh(box_small.vertices, box_small.faces)
+    try:
+        A = m.assemble_lhs(k, precision=native.BEM_PRECISION_MIXED)
+    finally:
+        m.release()
+    ops = O.assemble(box_small, k)
+    M11, M10 = O.mass(box_small)
+    lhs, _ = O.burton_miller_matrices(ops, M11, M10, k)
+    assert rel(A, lhs) < 2e-6
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-11), (1, 2e-6)])
+def test_rhs_operator_matches_oracle(gpu_ctx, native, box_small, precision, tol):
+    O = _oracle()
+    k = 2 * np.pi * 1500.0 / 343.0
+    rng = np.random.default_rng(7)
+    q = rng.normal(size=(box_small.n_faces, 2)) + 1j * rng.normal(size=(box_small.n_faces, 2))
+    ops = O.assemble(box_small, k)
+    M11, M10 = O.mass(box_small)
+    _, rhs_op = O.burton_miller_matrices(ops, M11, M10, k)
+    m = gpu_ctx.upload_mesh(box_small.vertices, box_small.faces)
+    try:
+        bm = m.apply_rhs_operator(k, q, precision=precision)
+        s_only = m.apply_rhs_operator(k, q[:, 0], coeffs=(1.0, 0.0, 0.0), precision=precision)
+        k_only = m.apply_rhs_operator(k, q[:, 0], coeffs=(0.0, 1.0, 0.0), precision=precision)
+    finally:
+        m.release()
+    assert rel(bm, rhs_op @ q) < tol
+    assert rel(s_only, ops.single_layer @ q[:, 0]) < tol
+    assert rel(k_only, ops.adjoint_double_layer @ q[:, 0]) < tol
+
+
+def _solve_both(gpu_ctx, native, mesh, freqs, precision, drives=None, points=None):
+    O = _oracle()
+    if drives is None:
+        drives = (mesh.tags == meshes.RADIATOR_TAG).astype(np.complex128)[None, :]
+    if points is None:
+        points = np.array([[0, 0, 2.0], [2.0, 0, 0], [0, 1.2, 1.6], [0, 0, -2.0], [1.0, 1.0, 1.0]])
+    c, rho = 343.0, 1.205
+    m = gpu_ctx.upload_mesh(mesh.vertices, mesh.faces)
+    try:
+        m.set_excitation(drives)
+        m.set_observation_points(points)
+        p, u, stats = m.solve(freqs, precision=precision, sound_speed=c, rho=rho)
+    finally:
+        m.release()
+    refs = []
+    for f in freqs:
+        omega = 2 * np.pi * f
+        q = (drives * (1j * rho * omega)).T
+        refs.append(O.solve_frequency(mesh, omega / c, q, points))
+    return p, u, stats, refs
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-9), (1, 1e-5)])
+def test_full_solve_matches_oracle(gpu_ctx, native, sphere320, precision, tol):
+    freqs = [150.0, 1200.0, 3000.0]
+    p, u, stats, refs = _solve_both(gpu_ctx, native, sphere320, freqs, precision)
+    for i, ref in enumerate(refs):
+        assert rel(p[i, 0], ref.pressure[:, 0]) < tol
+        assert rel(u[i, 0], ref.field[:, 0]) < tol
+    if precision == 1:
+        assert stats["max_rel_residual"] <= 1e-10
+
+
+def test_two_excitations_and_batching(gpu_ctx, native, box_small):
+    rng = np.random.default_rng(3)
+    drives = np.zeros((2, box_small.n_faces), np.complex128)
+    drives[0, box_small.tags == meshes.RADIATOR_TAG] = 1.0
+    drives[1, rng.choice(box_small.n_faces, 20, replace=False)] = 0.5 - 0.25j
+    freqs = [300.0, 2000.0, 5000.0]
+    p, u, _, refs = _solve_both(gpu_ctx, native, box_small, freqs, 1, drives=drives)
+    for i, ref in enumerate(refs):
+        for c in range(2):
+            assert rel(p[i, c], ref.pressure[:, c]) < 1e-5
+            assert rel(u[i, c], ref.field[:, c]) < 1e-5
+
+
+def test_batch_equals_single(gpu_ctx, native, sphere320):
+    drives = (sphere320.tags == meshes.RADIATOR_TAG).astype(np.complex128)[None, :]
+    pts = np.array([[0, 0, 2.0], [0, 2.0, 0]])
+    m = gpu_ctx.upload_mesh(sphere320.vertices, sphere320.faces)
+    try:
+        m.set_excitation(drives)
+        m.set_observation_points(pts)
+        freqs = [200.0, 700.0, 1900.0, 2600.0]
+        pb, ub, _ = m.solve(freqs, batch=4)
+        for i, f in enumerate(freqs):
+            ps, us, _ = m.solve([f], batch=1)
+            assert rel(ps[0], pb[i]) < 1e-12
+            assert rel(us[0], ub[i]) < 1e-12
+    finally:
+        m.release()
+
+
+def test_isolated_vertex_gets_zero_pressure(gpu_ctx, native, sphere320):
+    v = np.vstack([sphere320.vertices, [[5.0, 5.0, 5.0]]])
+    mesh = meshes.BoundaryMesh(v, sphere320.faces, sphere320.tags)
+    drives = (mesh.tags == meshes.RADIATOR_TAG).astype(np.complex128)[None, :]
+    m = gpu_ctx.upload_mesh(mesh.vertices, mesh.faces)
+    try:
+        m.set_excitation(drives)
+        m.set_observation_points(np.array([[0, 0, 2.0]]))
+        p, u, _ = m.solve([800.0])
+    finally:
+        m.release()
+    assert p[0, 0, -1] == 0
+    assert np.all(np.isfinite(p)) and np.all(np.isfinite(u))
+
+
+def test_single_triangle(gpu_ctx, native):
+    O = _oracle()
+    v = np.array([[0.0, 0.0, 0.0], [0.02, 0.0, 0.0], [0.0, 0.02, 0.0]])
+    f = np.array([[0, 1, 2]])
+    mesh = meshes.BoundaryMesh(v, f, np.array([2]))
+    k = 2 * np.pi * 1000 / 343.0
+    m = gpu_ctx.upload_mesh(v, f)
+    try:
+        A = m.assemble_lhs(k, precision=0)
+    finally:
+        m.release()
+    ops = O.assemble(mesh, k)
+    M11, M10 = O.mass(mesh)
+    lhs, _ = O.burton_miller_matrices(ops, M11, M10, k)
+    assert rel(A, lhs) < 1e-11
+
+
+def test_invalid_inputs_raise(gpu_ctx, native):
+    with pytest.raises(native.BemError):
+        gpu_ctx.upload_mesh(np.zeros((3, 3)), np.array([[0, 1, 2]]))  # zero-area triangle
+    with pytest.raises(native.BemError):
+        gpu_ctx.upload_mesh(np.eye(3), np.array([[0, 1, 5]]))  # index out of range
+    m = gpu_ctx.upload_mesh(np.eye(3), np.array([[0, 1, 2]]))
+    try:
+        with pytest.raises(native.BemError):
+            m.solve([100.0])  # no excitation yet
+        m.set_excitation(np.ones((1, 1)))
+        m.set_observation_points(np.array([[0, 0, 3.0]]))
+        with pytest.raises(native.BemError):
+            m.solve([-5.0])
+    finally:
+        m.release()
