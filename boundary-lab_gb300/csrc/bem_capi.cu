@@ -56,6 +56,11 @@ struct bem_context {
   DevBuf rext, mats, mats2, ipiv, info, sblocks, rb, b32, b64, x64, r64, d32, fsrc, fout, norms, pout;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<bem_mesh*> meshes;
+  // optional per-kernel-family timing (options.profile)
+  bool prof = false;
+  std::vector<cudaEvent_t> pev;
+  std::vector<int> pslot;
+  size_t pev_used = 0;
 };
 
 struct bem_mesh {
@@ -67,6 +72,7 @@ struct bem_mesh {
   DevBuf drive32, drive64, obs;
   int nobs = 0;
   DevBuf driven;
+  long long singular_points = 0;
 };
 
 namespace {
@@ -78,6 +84,35 @@ template <typename T> T* upload(bem_mesh* m, const std::vector<T>& v) {
   m->allocs.push_back(p);
   ck(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, m->ctx->stream), "upload");
   return (T*)p;
+}
+
+// Profiling marks: the time between two consecutive marks is charged to the
+// slot of the later mark.
+void prof_mark(bem_context* c, int slot) {
+  if (!c->prof) return;
+  if (c->pev_used == c->pev.size()) {
+    cudaEvent_t e;
+    ck(cudaEventCreate(&e), "cudaEventCreate");
+    c->pev.push_back(e);
+  }
+  ck(cudaEventRecord(c->pev[c->pev_used], c->stream), "cudaEventRecord");
+  c->pslot.push_back(slot);
+  c->pev_used++;
+}
+void prof_begin(bem_context* c) {
+  c->pev_used = 0;
+  c->pslot.clear();
+  prof_mark(c, -1);
+}
+void prof_collect(bem_context* c, double* acc) {
+  if (!c->prof) return;
+  for (size_t i = 1; i < c->pev_used; ++i) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->pev[i - 1], c->pev[i]);
+    if (c->pslot[i] >= 0 && c->pslot[i] < BEM_K_SLOTS) acc[c->pslot[i]] += ms * 1e-3;
+  }
+  c->pev_used = 0;
+  c->pslot.clear();
 }
 
 int fail(bem_context* ctx, int code, const std::string& msg) {
@@ -139,17 +174,21 @@ void assemble_one(bem_mesh* m, bem::Precision prec, double k, const bem::Operato
   ck(ctx->rext.ensure((size_t)L.ldR * 3 * dm.nf * L.esz), "alloc extended rows");
   ck(ctx->sblocks.ensure((size_t)std::max(dm.npairs, 1) * 12 * L.esz), "alloc singular blocks");
   ck(bem::launch_singular_dyn(dm, prec, k, c, ctx->sblocks.p, ctx->stream), "singular kernel");
+  prof_mark(ctx, BEM_K_SINGULAR);
   ck(bem::launch_regular(dm, prec, k, c.cD, c.cH, ctx->rext.p, L.ldR, ctx->stream), "regular kernel");
+  prof_mark(ctx, BEM_K_REGULAR);
   ck(bem::launch_singular_scatter(dm, prec, ctx->sblocks.p, ctx->rext.p, L.ldR, ctx->stream), "singular scatter");
   if (dm.n_isolated) {
     ck(cudaMemsetAsync(A, 0, (size_t)L.lda * dm.nv * L.esz, ctx->stream), "memset");
     if (A2) ck(cudaMemsetAsync(A2, 0, (size_t)L.lda * dm.nv * L.esz, ctx->stream), "memset");
   }
   ck(bem::launch_gather(dm, prec, ctx->rext.p, L.ldR, A, L.lda, A2, ctx->stream), "gather kernel");
+  prof_mark(ctx, BEM_K_GATHER);
   if (nc > 0) {
     ck(ctx->rb.ensure((size_t)nc * dm.nf * 3 * L.esz), "alloc rhs faces");
     ck(bem::launch_rhs(dm, prec, k, c, qscale, drive, nc, ctx->sblocks.p, ctx->rb.p, b, L.ldb, ctx->stream),
        "rhs kernel");
+    prof_mark(ctx, BEM_K_RHS);
   }
 }
 
@@ -169,6 +208,8 @@ extern "C" {
 int bem_abi_version(void) { return GB300_BEM_ABI_VERSION; }
 
 const char* bem_last_error(const bem_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+void* bem_context_stream(const bem_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
 int bem_create_context(int device, bem_context** out) {
   if (!out) return BEM_ERR_INVALID_ARGUMENT;
@@ -207,6 +248,7 @@ void bem_destroy_context(bem_context* ctx) {
     b->release();
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
+  for (auto& e : ctx->pev) cudaEventDestroy(e);
   if (ctx->cublas) cublasDestroy(ctx->cublas);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -279,6 +321,7 @@ int bem_upload_mesh(bem_context* ctx, const double* vertices, int n_vertices, co
           d.rule_cw[a * P.Q + q] = phi[a] * P.rule_w[q];
         }
       }
+      for (const auto& sp : P.pairs) m->singular_points += P.rule_ptr[sp.rule + 1] - P.rule_ptr[sp.rule];
       if (d.npairs > 0) {
         void* mom = nullptr;
         ck(cudaMalloc(&mom, (size_t)d.npairs * 24 * sizeof(double)), "cudaMalloc(moments)");
@@ -376,6 +419,7 @@ void bem_default_options(bem_solve_options* opt) {
   opt->batch = 0;
   opt->lu_block = 0;
   opt->outputs_on_device = 0;
+  opt->profile = 0;
 }
 
 long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int npts, int batch, int precision) {
@@ -446,6 +490,8 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
     const void* drive = mixed ? m->drive32.p : m->drive64.p;
     std::vector<double> norms((size_t)B * nc * 2);
     std::vector<int> info(B);
+    double kacc[BEM_K_SLOTS] = {0};
+    ctx->prof = o.profile != 0;
     double t_asm = 0, t_sol = 0, t_fld = 0, max_res = 0;
     int max_steps = 0, batches = 0;
     for (int f0 = 0; f0 < n_freq; f0 += B) {
@@ -454,6 +500,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       std::vector<double> ks(bt);
       std::vector<double2> qs(bt);
       cudaEventRecord(ctx->ev[0], ctx->stream);
+      prof_begin(ctx);
       for (int i = 0; i < bt; ++i) {
         const double omega = 2.0 * M_PI * freqs_hz[f0 + i];
         const double k = omega / o.sound_speed;
@@ -469,6 +516,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       ck(bem::lu_factor_batched(prec, ctx->mats.p, L.lda, nv, bt, (int*)ctx->ipiv.p, (int*)ctx->info.p, nb,
                                 ctx->cublas, ctx->stream),
          "LU factorisation");
+      prof_mark(ctx, BEM_K_LU);
       ck(cudaMemcpyAsync(info.data(), ctx->info.p, (size_t)bt * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream),
          "copy info");
       const long long nvec = (long long)bt * nc * L.ldb;
@@ -513,6 +561,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
         max_steps = std::max(max_steps, steps);
         max_res = std::max(max_res, worst);
       }
+      prof_mark(ctx, BEM_K_SOLVE);
       cudaEventRecord(ctx->ev[2], ctx->stream);
       ck(cudaStreamSynchronize(ctx->stream), "solve sync");
       for (int i = 0; i < bt; ++i)
@@ -529,6 +578,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
         ck(bem::launch_field(dm, prec, bt, ks.data(), qs.data(), p_for_field, L.ldb, nc, drive, (const double*)m->obs.p,
                              m->nobs, ctx->fsrc.p, (double2*)ctx->fout.p, ctx->stream),
            "field kernel");
+        prof_mark(ctx, BEM_K_FIELD);
         double* dst = field_out + 2 * (size_t)f0 * nc * m->nobs;
         ck(cudaMemcpyAsync(dst, ctx->fout.p, (size_t)bt * nc * m->nobs * sizeof(double2),
                            o.outputs_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream),
@@ -551,6 +601,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
         }
       }
       ck(cudaStreamSynchronize(ctx->stream), "batch sync");
+      prof_collect(ctx, kacc);
       float ms = 0;
       cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
       t_asm += ms * 1e-3;
@@ -566,6 +617,10 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       stats->max_refine_steps = max_steps;
       stats->max_rel_residual = max_res;
       stats->batches = batches;
+      for (int i = 0; i < 8; ++i) stats->kernel_s[i] = kacc[i];
+      stats->regular_pairs = (long long)dm.nf * dm.nf - dm.npairs;
+      stats->singular_pairs = dm.npairs;
+      stats->singular_points = m->singular_points;
     }
     if (mixed && !(max_res <= o.refine_tol)) {
       ctx->err = "iterative refinement stopped at relative residual " + std::to_string(max_res);

@@ -31,6 +31,7 @@ EXPORTED_SYMBOLS = (
     "bem_create_context",
     "bem_destroy_context",
     "bem_last_error",
+    "bem_context_stream",
     "bem_upload_mesh",
     "bem_release_mesh",
     "bem_mesh_info",
@@ -64,6 +65,7 @@ class SolveOptions(ctypes.Structure):
         ("batch", ctypes.c_int),
         ("lu_block", ctypes.c_int),
         ("outputs_on_device", ctypes.c_int),
+        ("profile", ctypes.c_int),
     ]
 
 
@@ -75,7 +77,19 @@ class SolveStats(ctypes.Structure):
         ("max_refine_steps", ctypes.c_int),
         ("max_rel_residual", ctypes.c_double),
         ("batches", ctypes.c_int),
+        ("kernel_s", ctypes.c_double * 8),
+        ("regular_pairs", ctypes.c_longlong),
+        ("singular_pairs", ctypes.c_longlong),
+        ("singular_points", ctypes.c_longlong),
     ]
+
+KERNEL_SLOTS = ("singular", "regular", "gather", "rhs", "lu", "solve", "field")
+
+
+def stats_dict(stats: "SolveStats") -> dict:
+    out = {name: getattr(stats, name) for name, _ in SolveStats._fields_ if name != "kernel_s"}
+    out["kernel_s"] = {name: stats.kernel_s[i] for i, name in enumerate(KERNEL_SLOTS)}
+    return out
 
 
 _lock = threading.Lock()
@@ -112,6 +126,8 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         lib.bem_destroy_context.restype = None
         lib.bem_last_error.argtypes = [vp]
         lib.bem_last_error.restype = ctypes.c_char_p
+        lib.bem_context_stream.argtypes = [vp]
+        lib.bem_context_stream.restype = vp
         lib.bem_upload_mesh.argtypes = [vp, dp, ip, ctypes.POINTER(ctypes.c_int), ip, ip, ip, ctypes.POINTER(vp)]
         lib.bem_upload_mesh.restype = ip
         lib.bem_release_mesh.argtypes = [vp]
@@ -165,6 +181,11 @@ class Context:
         if rc != BEM_OK:
             msg = self._lib.bem_last_error(self._h)
             raise BemError(rc, msg.decode("utf-8", "replace") if msg else "")
+
+    @property
+    def stream_handle(self) -> int:
+        """The context's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+        return int(self._lib.bem_context_stream(self._h) or 0)
 
     def close(self) -> None:
         if getattr(self, "_h", None):
@@ -220,7 +241,7 @@ class Mesh:
 
     def solve(self, freqs_hz, *, precision: int = BEM_PRECISION_MIXED, sound_speed: float = 343.0,
               rho: float = 1.21, refine_tol: float = 1e-10, max_refine: int = 8, batch: int = 0, lu_block: int = 0,
-              want_pressure: bool = True, want_field: bool = True):
+              want_pressure: bool = True, want_field: bool = True, profile: bool = False):
         """Returns (pressure [n_freq, n_rhs, n_vertices], field [n_freq, n_rhs, n_points], stats dict)."""
         f = np.ascontiguousarray(freqs_hz, dtype=np.float64).reshape(-1)
         opt = SolveOptions()
@@ -232,6 +253,7 @@ class Mesh:
         opt.max_refine = int(max_refine)
         opt.batch = int(batch)
         opt.lu_block = int(lu_block)
+        opt.profile = int(bool(profile))
         pressure = np.zeros((len(f), self.n_rhs, self.n_vertices), np.complex128) if want_pressure else None
         field = np.zeros((len(f), self.n_rhs, self.n_points), np.complex128) if want_field else None
         stats = SolveStats()
@@ -241,8 +263,7 @@ class Mesh:
             None if field is None else field.ctypes.data_as(ctypes.c_void_p),
             ctypes.byref(stats))
         self.ctx._check(rc)
-        info = {name: getattr(stats, name) for name, _ in SolveStats._fields_}
-        return pressure, field, info
+        return pressure, field, stats_dict(stats)
 
     def solve_device(self, freqs_hz, pressure_ptr: int, field_ptr: int, **kw) -> dict:
         """Same as solve() but writes into device buffers (pointers on the context's device)."""
@@ -257,7 +278,7 @@ class Mesh:
             self._h, _dptr(f), len(f), ctypes.byref(opt),
             ctypes.c_void_p(pressure_ptr) if pressure_ptr else None,
             ctypes.c_void_p(field_ptr) if field_ptr else None, ctypes.byref(stats)))
-        return {name: getattr(stats, name) for name, _ in SolveStats._fields_}
+        return stats_dict(stats)
 
     def assemble_lhs(self, k: float, coeffs=(-1.0, None, 0.5), precision: int = BEM_PRECISION_FP64) -> np.ndarray:
         """Dense cD*D + cH*H + cM*M11 (default: the Burton-Miller LHS, cH = i/k)."""

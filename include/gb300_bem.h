@@ -57,6 +57,9 @@ int bem_create_context(int device, bem_context** out);
 void bem_destroy_context(bem_context* ctx);
 /* Message of the last failed call on this context ("" if none). */
 const char* bem_last_error(const bem_context* ctx);
+/* The context's CUDA stream (a cudaStream_t), so a caller can order its own
+ * work or record timing events against the library's launches. */
+void* bem_context_stream(const bem_context* ctx);
 
 /* Upload a triangle mesh and build every frequency-independent cache: face
  * geometry and surface curls, the regular rule, singular (vertex-sharing) pair
@@ -89,7 +92,20 @@ typedef struct bem_solve_options {
   int batch;             /* frequencies factored together (<= 64); 0 = automatic */
   int lu_block;          /* LU block size (<= 64); 0 = automatic */
   int outputs_on_device; /* 1: pressure_out / field_out are device pointers of the context's device */
+  int profile;           /* 1: also time each kernel family with CUDA events (stats.kernel_s) */
 } bem_solve_options;
+
+/* stats.kernel_s slots (filled when options.profile == 1), seconds summed over the call */
+enum bem_kernel_slot {
+  BEM_K_SINGULAR = 0, /* singular (Duffy) pair blocks */
+  BEM_K_REGULAR = 1,  /* regular pair assembly */
+  BEM_K_GATHER = 2,   /* singular scatter + column gather */
+  BEM_K_RHS = 3,      /* matrix-free right-hand side */
+  BEM_K_LU = 4,       /* LU factorisation */
+  BEM_K_SOLVE = 5,    /* triangular solves and FP64 refinement */
+  BEM_K_FIELD = 6,    /* field sources + field evaluation */
+  BEM_K_SLOTS = 8
+};
 
 typedef struct bem_solve_stats {
   double assembly_s;      /* summed over the call, seconds (CUDA events) */
@@ -98,6 +114,10 @@ typedef struct bem_solve_stats {
   int max_refine_steps;   /* over all frequencies and excitations */
   double max_rel_residual;
   int batches;
+  double kernel_s[8];     /* per kernel family, see enum bem_kernel_slot */
+  long long regular_pairs;  /* face pairs integrated with the regular rule, per frequency */
+  long long singular_pairs; /* vertex-sharing pairs integrated with Duffy rules, per frequency */
+  long long singular_points; /* Duffy points summed over the singular pairs, per frequency */
 } bem_solve_stats;
 
 void bem_default_options(bem_solve_options* opt);
