@@ -320,4 +320,68 @@ cudaError_t launch_field(const DeviceMesh& m, Precision prec, int batch, const d
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Single-excitation, single-frequency field evaluation from caller-placed
+// buffers (face records, weighted sources, drive, parameter block).  Used by
+// the allocation-free entry point in bem_noalloc.cu; the parameter block is
+// written on the device by write_field_params so no host staging is needed.
+namespace {
+__global__ void write_field_params_f32(FieldParamsF32* prm, double k) {
+  df v;
+  v.hi = (float)k;
+  v.lo = (float)(k - (double)v.hi);
+  prm->kdf[0] = v;
+  prm->k[0] = (float)k;
+  prm->qscale[0] = make_float2(1.0f, 0.0f);
+}
+__global__ void write_field_params_f64(FieldParamsF64* prm, double k) {
+  prm->k[0] = k;
+  prm->qscale[0] = make_double2(1.0, 0.0);
+}
+}  // namespace
+
+size_t field_params_bytes() { return sizeof(FieldParamsF32) > sizeof(FieldParamsF64) ? sizeof(FieldParamsF32) : sizeof(FieldParamsF64); }
+
+cudaError_t launch_field_single(Precision prec, const void* faces, int nf, int Q, const double* rule_w,
+                                const double* rule_phi, const void* sources, const void* drive, const double* obs,
+                                int nobs, double k, void* params, double2* out, cudaStream_t stream) {
+  FieldRule<float> fr32;
+  FieldRule<double> fr64;
+  for (int i = 0; i < kMaxQ; ++i) {
+    fr32.w[i] = (float)rule_w[i];
+    fr64.w[i] = rule_w[i];
+  }
+  for (int i = 0; i < 3 * kMaxQ; ++i) {
+    fr32.phi[i] = (float)rule_phi[i];
+    fr64.phi[i] = rule_phi[i];
+  }
+  dim3 grid(nobs, 1);
+  if (prec == Precision::Mixed) {
+    FieldParamsF32* dp = (FieldParamsF32*)params;
+    write_field_params_f32<<<1, 1, 0, stream>>>(dp, k);
+    const FaceF32* f = (const FaceF32*)faces;
+    const float2* s = (const float2*)sources;
+    const float2* d = (const float2*)drive;
+    if (Q == 6)
+      field_f32_kernel<6, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32);
+    else if (Q == 3)
+      field_f32_kernel<3, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32);
+    else
+      field_f32_kernel<1, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32);
+  } else {
+    FieldParamsF64* dp = (FieldParamsF64*)params;
+    write_field_params_f64<<<1, 1, 0, stream>>>(dp, k);
+    const FaceF64* f = (const FaceF64*)faces;
+    const double2* s = (const double2*)sources;
+    const double2* d = (const double2*)drive;
+    if (Q == 6)
+      field_f64_kernel<6, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr64);
+    else if (Q == 3)
+      field_f64_kernel<3, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr64);
+    else
+      field_f64_kernel<1, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr64);
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace bem

@@ -98,5 +98,12 @@ cudaError_t convert_f32_to_f64(const float2* src, double2* dst, long long n, cud
 cudaError_t launch_field(const DeviceMesh& m, Precision prec, int batch, const double* k, const double2* qscale,
                          const void* pressure, long long ldp, int nc, const void* drive, const double* obs, int nobs,
                          void* sources, double2* out, cudaStream_t stream);
+// One frequency, one excitation, everything in caller-placed device buffers
+// (face records FaceF32/FaceF64, weighted sources, drive with qscale = 1, a
+// parameter block of field_params_bytes()).  Used by bem_noalloc.cu.
+size_t field_params_bytes();
+cudaError_t launch_field_single(Precision prec, const void* faces, int nf, int Q, const double* rule_w,
+                                const double* rule_phi, const void* sources, const void* drive, const double* obs,
+                                int nobs, double k, void* params, double2* out, cudaStream_t stream);
 
 }  // namespace bem

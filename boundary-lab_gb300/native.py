@@ -42,7 +42,22 @@ EXPORTED_SYMBOLS = (
     "bem_assemble_lhs",
     "bem_apply_rhs_operator",
     "bem_estimate_device_bytes",
+    "bem_evaluate_field_noalloc",
 )
+
+
+def evaluate_field_noalloc(d_vertices: int, n_vertices: int, d_faces: int, n_faces: int, k: float, d_pressure: int,
+                           d_neumann: int, d_points: int, n_points: int, d_field_out: int, *,
+                           precision: int = BEM_PRECISION_MIXED, regular_order: int = 4, stream: int = 0) -> None:
+    """Field at n_points from caller-owned device buffers, without any device allocation
+    (bem_evaluate_field_noalloc).  Pointers are integers (e.g. torch's data_ptr())."""
+    lib = load()
+    err = ctypes.create_string_buffer(256)
+    rc = lib.bem_evaluate_field_noalloc(d_vertices, n_vertices, d_faces, n_faces, regular_order, float(k), d_pressure,
+                                        d_neumann, d_points, n_points, int(precision), d_field_out,
+                                        ctypes.c_void_p(stream) if stream else None, err, len(err))
+    if rc != BEM_OK:
+        raise BemError(rc, err.value.decode("utf-8", "replace"))
 
 
 class NativeLibraryError(RuntimeError):
@@ -149,6 +164,10 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         lib.bem_apply_rhs_operator.restype = ip
         lib.bem_estimate_device_bytes.argtypes = [ip, ip, ip, ip, ip, ip, ip]
         lib.bem_estimate_device_bytes.restype = ctypes.c_longlong
+        # allocation-free field evaluation: every pointer is a caller-owned device buffer
+        lib.bem_evaluate_field_noalloc.argtypes = [vp, ip, vp, ip, ip, ctypes.c_double, vp, vp, vp, ip, ip, vp, vp,
+                                                   ctypes.c_char_p, ip]
+        lib.bem_evaluate_field_noalloc.restype = ip
         if lib.bem_abi_version() != 1:
             raise NativeLibraryError(f"unexpected ABI version {lib.bem_abi_version()} in {path}")
         _lib = lib
