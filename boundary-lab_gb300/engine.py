@@ -1,0 +1,87 @@
+"""Numerical engine behind a solve session.
+
+``CudaEngine`` drives the C ABI (one context per process and device, shared by
+sessions; a lock serialises calls on it, like the reference's per-worker lock,
+src/blab/solvers/beat_engine_backend.py:314-334).  Any object with the same
+three methods can stand in for it (``engine_factory`` arguments and the
+``GB300_BEM_ENGINE=module:callable`` environment variable), which is how the
+CPU tests drive the session and worker logic without a GPU.
+"""
+
+from __future__ import annotations
+
+import importlib
+import os
+import threading
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import native
+
+PRECISIONS = {"fp64": native.BEM_PRECISION_FP64, "mixed": native.BEM_PRECISION_MIXED}
+
+
+@dataclass
+class EngineResult:
+    pressure: np.ndarray  # [n_freq, n_rhs, n_vertices] complex128
+    field: np.ndarray  # [n_freq, n_rhs, n_points] complex128
+    stats: dict
+
+
+_contexts: dict[int, native.Context] = {}
+_context_locks: dict[int, threading.Lock] = {}
+_pool_lock = threading.Lock()
+
+
+def shared_context(device: int) -> tuple[native.Context, threading.Lock]:
+    with _pool_lock:
+        if device not in _contexts:
+            _contexts[device] = native.Context(device)
+            _context_locks[device] = threading.Lock()
+        return _contexts[device], _context_locks[device]
+
+
+class CudaEngine:
+    """One uploaded mesh on one GPU."""
+
+    name = "gb300_cuda"
+
+    def __init__(self, device: int = 0, precision: str = "mixed", batch: int = 0, refine_tol: float = 1e-10):
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
+        self.device = device
+        self.precision = precision
+        self.batch = batch
+        self.refine_tol = refine_tol
+        self.ctx, self.lock = shared_context(device)
+        self.mesh: native.Mesh | None = None
+
+    def prepare(self, vertices, faces, drives, points, regular_order: int = 4, singular_order: int = 4) -> None:
+        with self.lock:
+            self.mesh = self.ctx.upload_mesh(vertices, faces, regular_order, singular_order)
+            self.mesh.set_excitation(drives)
+            self.mesh.set_observation_points(points)
+
+    def solve(self, freqs_hz, sound_speed: float, rho: float) -> EngineResult:
+        if self.mesh is None:
+            raise RuntimeError("engine.prepare() must run before solve()")
+        with self.lock:
+            p, u, stats = self.mesh.solve(freqs_hz, precision=PRECISIONS[self.precision], sound_speed=sound_speed,
+                                          rho=rho, refine_tol=self.refine_tol, batch=self.batch)
+        return EngineResult(p, u, stats)
+
+    def close(self) -> None:
+        with self.lock:
+            if self.mesh is not None:
+                self.mesh.release()
+                self.mesh = None
+
+
+def engine_from_env(**kwargs):
+    """Engine factory named by GB300_BEM_ENGINE ("module:callable"), else CudaEngine."""
+    spec = os.environ.get("GB300_BEM_ENGINE", "").strip()
+    if not spec:
+        return CudaEngine(**kwargs)
+    module, _, attr = spec.partition(":")
+    return getattr(importlib.import_module(module), attr or "make_engine")(**kwargs)

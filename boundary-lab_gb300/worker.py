@@ -1,0 +1,113 @@
+"""NDJSON worker speaking the reference BEAT worker protocol on the GB300 engine.
+
+Same command line and events as src/blab/solvers/julia_local/solver.jl:
+  python worker.py --request request.json   one job, then exit
+  python worker.py --worker                 emit `ready`, then one job per stdin line
+                                            {"request": "<path>", "operation": "solve"}
+Events (one JSON object per stdout line): ready, initialized, status, result,
+cancelled, completed, failed (solver.jl:12-24, 703-715, 807, 957-996, 1019-1036).
+The cancel file named by the request's `cancel_path` is honoured between
+frequencies.  Because the command line matches, the reference's own adapter
+runs this worker unchanged:
+  BeatEngineBackend(julia_executable=sys.executable, solver_script=<this file>, julia_project=None)
+"""
+
+from __future__ import annotations
+
+import importlib
+import json
+import math
+import os
+import sys
+from pathlib import Path
+
+
+def _package():
+    root = Path(__file__).resolve().parent.parent
+    if str(root) not in sys.path:
+        sys.path.insert(0, str(root))
+    return importlib.import_module("boundary-lab_gb300")
+
+
+def _clean(value):
+    """JSON-safe copy: NaN/Inf become null (the reference's JSON writer cannot emit them either)."""
+    if isinstance(value, float):
+        return value if math.isfinite(value) else None
+    if isinstance(value, dict):
+        return {k: _clean(v) for k, v in value.items()}
+    if isinstance(value, (list, tuple)):
+        return [_clean(v) for v in value]
+    return value
+
+
+def emit(event_type: str, **payload) -> None:
+    event = {"type": event_type, **payload}
+    sys.stdout.write(json.dumps(_clean(event), separators=(",", ":")) + "\n")
+    sys.stdout.flush()
+
+
+def solve_request(request: dict) -> None:
+    _package()
+    job_mod = importlib.import_module("boundary-lab_gb300.job")
+    precision = os.environ.get("GB300_BEM_PRECISION", "mixed")
+    device = int(os.environ.get("GB300_BEM_DEVICE", "0"))
+    job = job_mod.ExteriorJob(request, status=lambda m: emit("status", message=m), precision=precision,
+                              device=device)
+    emit("initialized", **job.initialized_payload())
+    try:
+        for event in job.results():
+            emit("result", **event)
+    except job_mod.JobCancelled as exc:
+        emit("cancelled", solved_count=exc.solved_count)
+        return
+    finally:
+        job.close()
+    emit("completed", solved_count=len(job.frequencies))
+
+
+def worker_loop() -> None:
+    emit("ready", protocol="boundary_lab_julia_worker", pid=os.getpid())
+    for line in sys.stdin:
+        text = line.strip()
+        if not text:
+            continue
+        try:
+            message = json.loads(text)
+            with open(str(message["request"]), encoding="utf-8") as fh:
+                request = json.load(fh)
+            solve_request(request)
+        except Exception as exc:  # noqa: BLE001 - every failure becomes a `failed` event
+            emit("failed", error=f"{type(exc).__name__}: {exc}")
+
+
+def main(argv: list[str]) -> int:
+    request_path = None
+    worker = False
+    i = 0
+    while i < len(argv):
+        if argv[i] == "--request" and i + 1 < len(argv):
+            request_path = argv[i + 1]
+            i += 2
+        elif argv[i] == "--worker":
+            worker = True
+            i += 1
+        else:
+            emit("failed", error=f"Unknown argument: {argv[i]}")
+            return 1
+    try:
+        if worker:
+            worker_loop()
+            return 0
+        if request_path is None:
+            emit("failed", error="Missing --request path.")
+            return 1
+        with open(request_path, encoding="utf-8") as fh:
+            solve_request(json.load(fh))
+        return 0
+    except Exception as exc:  # noqa: BLE001
+        emit("failed", error=f"{type(exc).__name__}: {exc}")
+        return 1
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv[1:]))
