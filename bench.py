@@ -188,6 +188,8 @@ def main() -> None:
     ap.add_argument("--cpu-baseline", type=int, default=1, help="frequencies timed on the host for cpu_baseline")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-extras", action="store_true", help="skip FP64 form, e2e and CPU baseline (profiling runs)")
+    ap.add_argument("--lu-gemm", type=int, default=0, choices=[0, 1, 2],
+                    help="LU trailing update: 0 automatic, 1 cuBLAS cgemm, 2 tcgen05 3xTF32")
     args = ap.parse_args()
     if args.warmup < 3 and not args.no_extras:
         args.warmup = 3
@@ -219,7 +221,7 @@ def main() -> None:
     u_dev = torch.empty((B, 1, len(points)), dtype=torch.complex128, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     opts = dict(precision=native.BEM_PRECISION_MIXED, sound_speed=SOUND_SPEED, rho=RHO, batch=B, refine_tol=1e-10,
-                max_refine=8)
+                max_refine=8, lu_gemm=args.lu_gemm)
 
     def step_freqs(step: int):
         # weak scaling: rank r takes batch (step * world + r) of the sweep
@@ -279,6 +281,7 @@ def main() -> None:
         "stage_ms_per_freq": per_freq_ms,
         "step_ms": step_ms,
         "refine_steps_max": max(st["max_refine_steps"] for st in stats_list),
+        "lu_trailing_update": {1: "cublas cgemm", 2: "tcgen05 3xTF32"}.get(stats_list[0]["lu_gemm_used"]),
         "rel_residual_max": max(st["max_rel_residual"] for st in stats_list),
     }
 

@@ -19,7 +19,8 @@ CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIBRARY = BUILD / "libgb300_bem.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["bem_assembly.cu", "bem_lu.cu", "bem_field.cu", "bem_capi.cu", "bem_noalloc.cu"]
+CUDA_SOURCES = ["bem_assembly.cu", "bem_lu.cu", "bem_lu_cluster.cu", "bem_gemm_tc.cu", "bem_field.cu", "bem_capi.cu",
+                "bem_noalloc.cu"]
 CXX_SOURCES = ["bem_plan.cpp"]
 HEADERS = ["bem_common.cuh", "bem_internal.h", "bem_kernels.h"]
 

@@ -113,8 +113,11 @@ __global__ void __launch_bounds__(WARPS * 32) regular_f32_kernel(const FaceF32* 
   const int base = tile_row_base[tile];
   const int rows = tile_row_base[tile + 1] - base;
   float2* acc = smem_acc32 + (size_t)warp * 3 * max_rows;
+  // rule coefficients of the (not unrolled) test-point loop, indexed at run time
+  __shared__ float s_cw[3 * kMaxQ];
+  if (threadIdx.x < 3 * kMaxQ) s_cw[threadIdx.x] = p.cw[threadIdx.x];
   for (int i = lane; i < 3 * max_rows; i += 32) acc[i] = make_float2(0.0f, 0.0f);
-  __syncwarp();
+  __syncthreads();
   if (g >= nf) return;
 
   // trial face (warp-uniform)
@@ -157,7 +160,9 @@ __global__ void __launch_bounds__(WARPS * 32) regular_f32_kernel(const FaceF32* 
             IG[a][b] = make_float2(0.f, 0.f);
             ID[a][b] = make_float2(0.f, 0.f);
           }
-#pragma unroll
+        // The test-point loop is kept rolled: fully unrolling 6 x 6 Green
+        // evaluations overflowed the instruction cache (no_instruction stalls).
+#pragma unroll 1
         for (int m = 0; m < Q; ++m) {
           float of[3] = {F.off[3 * m], F.off[3 * m + 1], F.off[3 * m + 2]};
           float2 u[3], v[3];
@@ -186,7 +191,7 @@ __global__ void __launch_bounds__(WARPS * 32) regular_f32_kernel(const FaceF32* 
           }
 #pragma unroll
           for (int a = 0; a < 3; ++a) {
-            const float c = p.cw[a * Q + m];
+            const float c = s_cw[a * Q + m];
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
               IG[a][b].x = fmaf(c, u[b].x, IG[a][b].x);
@@ -474,7 +479,7 @@ constexpr int kSingOut = 12;
 
 template <typename R>
 __global__ void singular_dyn_kernel(SingularGeom geo, const SingularPair* __restrict__ pairs, int npairs,
-                                    const int* __restrict__ rule_ptr, const double* __restrict__ duffy,
+                                    const int* __restrict__ rule_ptr, const R* __restrict__ duffy,
                                     const double* __restrict__ moments, const double* __restrict__ curls,
                                     const double* __restrict__ area, const double* __restrict__ m11m10,
                                     SingParams<R> p, typename cplx<R>::type* __restrict__ out) {
@@ -504,8 +509,10 @@ __global__ void singular_dyn_kernel(SingularGeom geo, const SingularPair* __rest
   const R inv4pi = R(0.25 / CUDART_PI);
   const int q0 = rule_ptr[P.rule], q1 = rule_ptr[P.rule + 1];
   for (int q = q0 + lane; q < q1; q += 32) {
-    const double* pt = duffy + 5 * (size_t)q;
-    const R tu = (R)pt[0], tv = (R)pt[1], ru = (R)pt[2], rvv = (R)pt[3], w = (R)pt[4];
+    // Duffy points in the working precision (a float copy of the table for the
+    // mixed form: FP64->FP32 conversions run at the FP64 rate on this part)
+    const R* pt = duffy + 5 * (size_t)q;
+    const R tu = pt[0], tv = pt[1], ru = pt[2], rvv = pt[3], w = pt[4];
     const R px[3] = {R(1) - tu - tv, tu, tv};
     const R py[3] = {R(1) - ru - rvv, ru, rvv};
     R rv[3];
@@ -942,7 +949,7 @@ cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, double k, c
     p.cS = f2(c.cS);
     p.cK = f2(c.cK);
     p.cM10 = f2(c.cM10);
-    singular_dyn_kernel<float><<<nblk, threads, 0, stream>>>(geo, m.pairs, m.npairs, m.rule_ptr, m.duffy,
+    singular_dyn_kernel<float><<<nblk, threads, 0, stream>>>(geo, m.pairs, m.npairs, m.rule_ptr, m.duffy32,
                                                              m.moments, m.curls, m.area, m.m11m10, p,
                                                              (float2*)blocks);
   } else {

@@ -53,7 +53,7 @@ struct bem_context {
   cudaStream_t stream = nullptr;
   cublasHandle_t cublas = nullptr;
   std::string err;
-  DevBuf rext, mats, mats2, ipiv, info, sblocks, rb, b32, b64, x64, r64, d32, fsrc, fout, norms, pout;
+  DevBuf rext, mats, mats2, ipiv, perm, info, sblocks, rb, b32, b64, x64, r64, d32, fsrc, fout, norms, pout, tcws;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<bem_mesh*> meshes;
   // optional per-kernel-family timing (options.profile)
@@ -244,7 +244,7 @@ void bem_destroy_context(bem_context* ctx) {
   }
   ctx->meshes.clear();
   for (DevBuf* b : {&ctx->rext, &ctx->mats, &ctx->mats2, &ctx->ipiv, &ctx->info, &ctx->sblocks, &ctx->rb, &ctx->b32,
-                    &ctx->b64, &ctx->x64, &ctx->r64, &ctx->d32, &ctx->fsrc, &ctx->fout, &ctx->norms, &ctx->pout})
+                    &ctx->b64, &ctx->x64, &ctx->r64, &ctx->d32, &ctx->fsrc, &ctx->fout, &ctx->norms, &ctx->pout, &ctx->perm, &ctx->tcws})
     b->release();
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
@@ -303,6 +303,7 @@ int bem_upload_mesh(bem_context* ctx, const double* vertices, int n_vertices, co
       d.pairs_by_test = upload(m, P.pairs_by_test);
       d.rule_ptr = upload(m, P.rule_ptr);
       d.duffy = upload(m, P.duffy);
+      d.duffy32 = upload(m, std::vector<float>(P.duffy.begin(), P.duffy.end()));
       d.verts = upload(m, P.verts);
       d.faces = upload(m, P.faces);
       d.normal = upload(m, P.normal);
@@ -420,6 +421,7 @@ void bem_default_options(bem_solve_options* opt) {
   opt->lu_block = 0;
   opt->outputs_on_device = 0;
   opt->profile = 0;
+  opt->lu_gemm = 0;
 }
 
 long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int npts, int batch, int precision) {
@@ -463,7 +465,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
     if (B == 0) {
       // automatic: matrices of one batch within ~8 GiB, at most 16 frequencies
       const double per = (double)L.lda * nv * L.esz * (mixed ? 2 : 1);
-      B = (int)std::max(1.0, std::min(16.0, std::floor(8.0 * (1ull << 30) / per)));
+      B = (int)std::max(1.0, std::min(32.0, std::floor(16.0 * (1ull << 30) / per)));
     }
     B = std::min(B, n_freq);
     const int nb = o.lu_block > 0 ? std::min(o.lu_block, 64) : (mixed ? 64 : 32);
@@ -471,6 +473,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
     ck(ctx->mats.ensure(matsz * B), "alloc matrices");
     if (mixed) ck(ctx->mats2.ensure(matsz * B), "alloc matrix copies");
     ck(ctx->ipiv.ensure((size_t)B * nv * sizeof(int)), "alloc pivots");
+    ck(ctx->perm.ensure((size_t)B * nv * sizeof(int)), "alloc permutation");
     ck(ctx->info.ensure((size_t)B * sizeof(int)), "alloc info");
     const size_t vecn = (size_t)B * nc * L.ldb;
     ck(ctx->b32.ensure(vecn * L.esz), "alloc rhs");
@@ -491,6 +494,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
     std::vector<double> norms((size_t)B * nc * 2);
     std::vector<int> info(B);
     double kacc[BEM_K_SLOTS] = {0};
+    int gemm_used = 0;
     ctx->prof = o.profile != 0;
     double t_asm = 0, t_sol = 0, t_fld = 0, max_res = 0;
     int max_steps = 0, batches = 0;
@@ -513,16 +517,24 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       }
       cudaEventRecord(ctx->ev[1], ctx->stream);
       ck(cudaMemsetAsync(ctx->info.p, 0, (size_t)bt * sizeof(int), ctx->stream), "memset info");
+      bool used_tensor = false;
+      int* tc_err = nullptr;
+      void* tcws = nullptr;
+      if (mixed && o.lu_gemm != (int)bem::LuGemm::Cublas && bem::tc_gemm_available()) {
+        ck(ctx->tcws.ensure(bem::tc_gemm_workspace_bytes(nv, B)), "alloc tensor-core workspace");
+        tcws = ctx->tcws.p;
+      }
       ck(bem::lu_factor_batched(prec, ctx->mats.p, L.lda, nv, bt, (int*)ctx->ipiv.p, (int*)ctx->info.p, nb,
-                                ctx->cublas, ctx->stream),
+                                ctx->cublas, ctx->stream, (bem::LuGemm)o.lu_gemm, tcws, &used_tensor, &tc_err),
          "LU factorisation");
+      gemm_used = mixed ? (used_tensor ? 2 : 1) : 0;
+      ck(bem::lu_perm_batched((const int*)ctx->ipiv.p, nv, bt, (int*)ctx->perm.p, ctx->stream), "pivot permutation");
       prof_mark(ctx, BEM_K_LU);
       ck(cudaMemcpyAsync(info.data(), ctx->info.p, (size_t)bt * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream),
          "copy info");
       const long long nvec = (long long)bt * nc * L.ldb;
       if (!mixed) {
-        ck(bem::lu_solve_batched(prec, ctx->mats.p, L.lda, nv, bt, (int*)ctx->ipiv.p, ctx->b32.p, L.ldb, nc, nb,
-                                 ctx->stream),
+        ck(bem::lu_solve_cluster_batched(prec, ctx->mats.p, L.lda, nv, bt, (const int*)ctx->perm.p, ctx->b32.p, L.ldb, nc, ctx->stream),
            "LU solve");
       } else {
         double2* x = (double2*)ctx->x64.p;
@@ -531,7 +543,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
         float2* d = (float2*)ctx->d32.p;
         ck(bem::convert_f32_to_f64((const float2*)ctx->b32.p, b64, nvec, ctx->stream), "convert rhs");
         ck(cudaMemcpyAsync(d, ctx->b32.p, nvec * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream), "copy rhs");
-        ck(bem::lu_solve_batched(prec, ctx->mats.p, L.lda, nv, bt, (int*)ctx->ipiv.p, d, L.ldb, nc, nb, ctx->stream),
+        ck(bem::lu_solve_cluster_batched(prec, ctx->mats.p, L.lda, nv, bt, (const int*)ctx->perm.p, d, L.ldb, nc, ctx->stream),
            "LU solve");
         ck(cudaMemsetAsync(x, 0, nvec * sizeof(double2), ctx->stream), "memset x");
         ck(bem::axpy_f32_into_f64(d, x, nvec, ctx->stream), "axpy");
@@ -552,8 +564,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
           }
           if (worst <= o.refine_tol || steps >= o.max_refine || !std::isfinite(worst)) break;
           ck(bem::convert_f64_to_f32(r, d, nvec, ctx->stream), "convert residual");
-          ck(bem::lu_solve_batched(prec, ctx->mats.p, L.lda, nv, bt, (int*)ctx->ipiv.p, d, L.ldb, nc, nb,
-                                   ctx->stream),
+          ck(bem::lu_solve_cluster_batched(prec, ctx->mats.p, L.lda, nv, bt, (const int*)ctx->perm.p, d, L.ldb, nc, ctx->stream),
              "LU solve");
           ck(bem::axpy_f32_into_f64(d, x, nvec, ctx->stream), "axpy");
           ++steps;
@@ -564,6 +575,12 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       prof_mark(ctx, BEM_K_SOLVE);
       cudaEventRecord(ctx->ev[2], ctx->stream);
       ck(cudaStreamSynchronize(ctx->stream), "solve sync");
+      if (used_tensor && tc_err) {
+        int h = 0;
+        ck(cudaMemcpy(&h, tc_err, sizeof(int), cudaMemcpyDeviceToHost), "read tensor-core status");
+        if (h != 0)
+          return fail(ctx, BEM_ERR_CUDA, "tensor-core LU update gave up waiting (status " + std::to_string(h) + ")");
+      }
       for (int i = 0; i < bt; ++i)
         if (info[i] != 0) return fail(ctx, BEM_ERR_SINGULAR, "zero pivot in LU factorisation (frequency " +
                                                                 std::to_string(freqs_hz[f0 + i]) + " Hz)");
@@ -621,11 +638,76 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       stats->regular_pairs = (long long)dm.nf * dm.nf - dm.npairs;
       stats->singular_pairs = dm.npairs;
       stats->singular_points = m->singular_points;
+      stats->lu_gemm_used = gemm_used;
     }
     if (mixed && !(max_res <= o.refine_tol)) {
       ctx->err = "iterative refinement stopped at relative residual " + std::to_string(max_res);
       return BEM_ERR_NOT_CONVERGED;
     }
+    return BEM_OK;
+  });
+}
+
+int bem_lu_factor_dense(bem_context* ctx, int n, double* a, int* ipiv, int precision, int lu_gemm) {
+  if (!ctx) return BEM_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&]() -> int {
+    if (!a || !ipiv || n < 1) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "bad arguments");
+    const bool mixed = precision == BEM_PRECISION_MIXED;
+    const bem::Precision prec = mixed ? bem::Precision::Mixed : bem::Precision::FP64;
+    const long long lda = round_up(n, 32);
+    const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
+    ck(ctx->mats.ensure((size_t)lda * n * esz), "alloc matrix");
+    ck(ctx->ipiv.ensure((size_t)n * sizeof(int)), "alloc pivots");
+    ck(ctx->info.ensure(sizeof(int)), "alloc info");
+    std::vector<char> host((size_t)lda * n * esz, 0);
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const double re = a[2 * ((size_t)j * n + i)], im = a[2 * ((size_t)j * n + i) + 1];
+        if (mixed)
+          ((float2*)host.data())[(size_t)j * lda + i] = make_float2((float)re, (float)im);
+        else
+          ((double2*)host.data())[(size_t)j * lda + i] = make_double2(re, im);
+      }
+    ck(cudaMemcpyAsync(ctx->mats.p, host.data(), host.size(), cudaMemcpyHostToDevice, ctx->stream), "copy matrix");
+    ck(cudaMemsetAsync(ctx->info.p, 0, sizeof(int), ctx->stream), "memset info");
+    void* tcws = nullptr;
+    if (mixed && lu_gemm != (int)bem::LuGemm::Cublas && bem::tc_gemm_available()) {
+      ck(ctx->tcws.ensure(bem::tc_gemm_workspace_bytes(n, 1)), "alloc tensor-core workspace");
+      tcws = ctx->tcws.p;
+    }
+    bool used_tensor = false;
+    int* tc_err = nullptr;
+    ck(bem::lu_factor_batched(prec, ctx->mats.p, lda, n, 1, (int*)ctx->ipiv.p, (int*)ctx->info.p, 64, ctx->cublas,
+                              ctx->stream, (bem::LuGemm)lu_gemm, tcws, &used_tensor, &tc_err),
+       "LU factorisation");
+    int info = 0;
+    ck(cudaMemcpyAsync(host.data(), ctx->mats.p, host.size(), cudaMemcpyDeviceToHost, ctx->stream), "copy factors");
+    ck(cudaMemcpyAsync(ipiv, ctx->ipiv.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "copy pivots");
+    ck(cudaMemcpyAsync(&info, ctx->info.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "copy info");
+    ck(cudaStreamSynchronize(ctx->stream), "sync");
+    if (used_tensor && tc_err) {
+      int h = 0;
+      ck(cudaMemcpy(&h, tc_err, sizeof(int), cudaMemcpyDeviceToHost), "read tensor-core status");
+      if (h != 0) return fail(ctx, BEM_ERR_CUDA, "tensor-core LU update gave up waiting");
+    }
+    if (lu_gemm == (int)bem::LuGemm::Tensor && mixed && !used_tensor)
+      return fail(ctx, BEM_ERR_CUDA, "tensor-core trailing update unavailable");
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        double re, im;
+        if (mixed) {
+          const float2 x = ((const float2*)host.data())[(size_t)j * lda + i];
+          re = x.x;
+          im = x.y;
+        } else {
+          const double2 x = ((const double2*)host.data())[(size_t)j * lda + i];
+          re = x.x;
+          im = x.y;
+        }
+        a[2 * ((size_t)j * n + i)] = re;
+        a[2 * ((size_t)j * n + i) + 1] = im;
+      }
+    if (info != 0) return fail(ctx, BEM_ERR_SINGULAR, "zero pivot at column " + std::to_string(info - 1));
     return BEM_OK;
   });
 }

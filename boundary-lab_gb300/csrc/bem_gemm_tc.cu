@@ -1,0 +1,440 @@
+// Tensor-core (tcgen05) trailing update of the complex LU: C -= L21 * U12.
+//
+// The complex product is run as one real GEMM.  With complex entries stored
+// interleaved (re, im), a column of C or U12 is already a real column of twice
+// the length, and
+//     C' (2M x N) -= A' (2M x 2K) * B' (2K x N)
+// where B' is U12's memory read as reals and A' replaces every complex L21
+// entry a by the 2 x 2 real block [[re a, -im a], [im a, re a]].
+//
+// Precision: 3xTF32.  Every operand value x is split as x = hi + lo with hi
+// rounded to TF32 (low 13 mantissa bits zero) and lo = x - hi exact in FP32;
+// the MMA sums hi*hi + hi*lo + lo*hi with FP32 accumulation, which carries
+// about 2^-21 relative error per product (FP32 LU quality), so the FP64
+// refinement still converges in one or two steps.
+//
+// Kernel: one CTA (4 warps) per 128 x 256 tile of C'.  A prep kernel writes
+// A'hi, A'lo, B'hi, B'lo as K-major (K contiguous) buffers; TMA brings 32-wide
+// K blocks into 128-byte-swizzled shared memory through a 2-stage mbarrier
+// pipeline; one thread issues tcgen05.mma (kind::tf32, M=128, N=256, K=8)
+// into a TMEM accumulator; all four warps read it back with tcgen05.ld, stage
+// -D in shared memory 32 columns at a time (double buffered per warp) and
+// TMA reduce-add it into C (cp.reduce.async.bulk.tensor .add.f32), so C is
+// never read by the SM: the read-modify-write happens in L2, asynchronously.
+// Every wait is bounded: on timeout the kernel records an error, waits
+// (bounded) for its own copies, frees its TMEM and returns.
+//
+// TMA coordinates into C: the C map spans every whole matrix of the batch
+// (x = real row 0..2n, y = column 0..n, z = matrix), so a tile starts at
+// x = 2 (k + kb) + m0 + 32 w.  The innermost coordinate times 4 bytes must be a
+// multiple of 16: k + kb is even because the block width nb is even (the plan
+// refuses odd nb), and m0 + 32 w is a multiple of 32.  All coordinates are >= 0;
+// rows x >= 2n and columns y >= n are clipped by the map bounds.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bem_common.cuh"
+#include "bem_kernels.h"
+
+namespace bem {
+namespace {
+
+constexpr int TM = 128;       // tile rows of C' (real rows)
+constexpr int TN = 256;       // tile columns of C'
+constexpr int TK = 32;        // K block per stage (32 fp32 = 128 B rows)
+constexpr int KP = 128;       // K' = 2 * nb, nb <= 64 (zero padded)
+constexpr int STAGES = 2;
+constexpr int A_BYTES = TM * TK * 4;   // 16 KB
+constexpr int B_BYTES = TN * TK * 4;   // 32 KB
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi + lo of A and B: 96 KB
+constexpr int TMEM_COLS = 256;
+// mbarrier waits give up after kWaitLimit polls with a 1 us suspend hint each
+// (about one second), far above any healthy wait (microseconds).
+constexpr long long kWaitLimit = 1LL << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase), "r"(1000)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait; returns false (and records it) when the limit is hit.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, int* err, int code) {
+  for (long long i = 0; i < kWaitLimit; ++i)
+    if (mbar_try_wait(bar, phase)) return true;
+  atomicCAS(err, 0, code);
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of
+// 128 B packed in 1024-byte groups of 8 (SBO = 1024 B).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);        // start address
+  d |= (uint64_t)1 << 16;                        // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset
+  d |= (uint64_t)1 << 46;                        // descriptor version
+  d |= (uint64_t)2 << 61;                        // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor: kind::tf32, D = F32, A = B = TF32, both K-major, M = 128, N = 256.
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          dtmem),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld_32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%"
+      "20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// -D tile of one warp (32 real rows x 32 columns, rows contiguous) added into C by TMA.
+__device__ __forceinline__ void tma_reduce_add_3d(const CUtensorMap* map, const void* src, int x, int y, int z) {
+  asm volatile("cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+                   (uint64_t)map),
+               "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ float round_tf32(float x) {
+  uint32_t u = __float_as_uint(x);
+  if ((u & 0x7F800000u) != 0x7F800000u) u = (u + 0x1000u) & 0xFFFFE000u;
+  return __uint_as_float(u);
+}
+
+// A'hi / A'lo [batch][rows_pad][KP] from L21 (rows k+nb.., columns k..k+kb of each matrix).
+__global__ void prep_a_kernel(const float2* __restrict__ A, long long lda, long long strideA, int row0, int col0, int M,
+                              int kb, int rows_pad, float* __restrict__ ahi, float* __restrict__ alo) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long per = (long long)rows_pad * KP;
+  if (idx >= per) return;
+  const int b = blockIdx.y;
+  const int rr = (int)(idx / KP), kk = (int)(idx % KP);
+  float v = 0.f;
+  const int i = rr >> 1, k = kk >> 1;
+  if (i < M && k < kb) {
+    const float2 a = A[(size_t)b * strideA + (size_t)(col0 + k) * lda + row0 + i];
+    if ((rr & 1) == 0)
+      v = (kk & 1) == 0 ? a.x : -a.y;
+    else
+      v = (kk & 1) == 0 ? a.y : a.x;
+  }
+  const float hi = round_tf32(v);
+  const size_t o = (size_t)b * per + idx;
+  ahi[o] = hi;
+  alo[o] = v - hi;
+}
+
+// B'hi / B'lo [batch][cols_pad][KP] from U12 (rows k..k+kb, columns k+nb.. of each matrix).
+__global__ void prep_b_kernel(const float2* __restrict__ A, long long lda, long long strideA, int row0, int col0, int N,
+                              int kb, int cols_pad, float* __restrict__ bhi, float* __restrict__ blo) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long per = (long long)cols_pad * KP;
+  if (idx >= per) return;
+  const int b = blockIdx.y;
+  const int j = (int)(idx / KP), kk = (int)(idx % KP);
+  float v = 0.f;
+  const int k = kk >> 1;
+  if (j < N && k < kb) {
+    const float2 u = A[(size_t)b * strideA + (size_t)(col0 + j) * lda + row0 + k];
+    v = (kk & 1) == 0 ? u.x : u.y;
+  }
+  const float hi = round_tf32(v);
+  const size_t o = (size_t)b * per + idx;
+  bhi[o] = hi;
+  blo[o] = v - hi;
+}
+
+__global__ void __launch_bounds__(128, 1)
+    trailing_update_tf32x3(const __grid_constant__ CUtensorMap map_ahi, const __grid_constant__ CUtensorMap map_alo,
+                           const __grid_constant__ CUtensorMap map_bhi, const __grid_constant__ CUtensorMap map_blo,
+                           const __grid_constant__ CUtensorMap map_c, int x0, int y0, int M2, int N, int* err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-byte alignment for the swizzled tiles
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t full_bar[STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[STAGES];
+  __shared__ __align__(8) uint64_t done_bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_fail;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * TM, n0 = blockIdx.y * TN, bz = blockIdx.z;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    mbar_init(&done_bar, 1);
+    s_fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  const int KB = KP / TK;  // 4 K blocks
+
+  if (warp == 0 && lane == 0) {
+    // TMA producer
+    for (int kb = 0; kb < KB; ++kb) {
+      const int s = kb % STAGES;
+      if (kb >= STAGES && !mbar_wait(&empty_bar[s], ((kb / STAGES) - 1) & 1, err, 1)) {
+        s_fail = 1;
+        break;
+      }
+      unsigned char* st = base + (size_t)s * STAGE_BYTES;
+      mbar_expect_tx(&full_bar[s], STAGE_BYTES);
+      tma_load_3d(st, &map_ahi, &full_bar[s], kb * TK, m0, bz);
+      tma_load_3d(st + A_BYTES, &map_alo, &full_bar[s], kb * TK, m0, bz);
+      tma_load_3d(st + 2 * A_BYTES, &map_bhi, &full_bar[s], kb * TK, n0, bz);
+      tma_load_3d(st + 2 * A_BYTES + B_BYTES, &map_blo, &full_bar[s], kb * TK, n0, bz);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    bool ok = true;
+    for (int kb = 0; kb < KB && ok; ++kb) {
+      const int s = kb % STAGES;
+      if (!mbar_wait(&full_bar[s], (kb / STAGES) & 1, err, 2)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      unsigned char* st = base + (size_t)s * STAGE_BYTES;
+      const uint32_t a_hi = smem_u32(st), a_lo = smem_u32(st + A_BYTES);
+      const uint32_t b_hi = smem_u32(st + 2 * A_BYTES), b_lo = smem_u32(st + 2 * A_BYTES + B_BYTES);
+#pragma unroll
+      for (int ks = 0; ks < TK / 8; ++ks) {
+        const uint32_t off = ks * 32;  // 8 fp32 = 32 bytes along K inside the swizzled row
+        const uint32_t acc = (kb > 0 || ks > 0) ? 1u : 0u;
+        mma_tf32(tmem, smem_desc_sw128(a_hi + off), smem_desc_sw128(b_hi + off), acc);
+        mma_tf32(tmem, smem_desc_sw128(a_hi + off), smem_desc_sw128(b_lo + off), 1u);
+        mma_tf32(tmem, smem_desc_sw128(a_lo + off), smem_desc_sw128(b_hi + off), 1u);
+      }
+      mma_commit(&empty_bar[s]);
+    }
+    if (!ok) s_fail = 1;
+    mma_commit(&done_bar);  // arrives once every MMA issued above has completed
+  }
+  __syncwarp();
+  // epilogue: warp w owns TMEM lanes [32w, 32w+32) = rows m0 + 32w + lane
+  const bool done = mbar_wait(&done_bar, 0, err, 3);
+  if (!done) s_fail = 1;  // make the epilogue decision uniform across the CTA
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (s_fail == 0) {
+    // Every MMA has completed, so the stage buffers are free: warp w stages its
+    // -D chunks in two 4 KB buffers at base + 8 KB * w.
+    float* stg = (float*)(base + (size_t)warp * 8192);
+    const bool rows_live = m0 + warp * 32 < M2;
+    for (int cc = 0; cc < TN / 32; ++cc) {
+      float v[32];
+      tmem_ld_32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cc * 32), v);
+      const int col = n0 + cc * 32;
+      if (!rows_live || col >= N) continue;  // warp-uniform; columns only grow with cc
+      float* buf = stg + (cc & 1) * 1024;
+      // the group that last read this buffer (chunk cc - 2) must be done reading
+      if (lane == 0) bulk_wait_read<1>();
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < 32; ++j) buf[j * 32 + lane] = -v[j];
+      fence_async_smem();
+      __syncwarp();
+      if (lane == 0) {
+        tma_reduce_add_3d(&map_c, buf, x0 + m0 + warp * 32, y0 + col, bz);
+        bulk_commit();
+      }
+    }
+    if (lane == 0) bulk_wait_read<0>();
+    __syncwarp();
+  } else if (threadIdx.x == 0) {
+    // drain: wait (bounded) for any TMA copies this CTA started
+    for (int s = 0; s < STAGES; ++s) mbar_wait(&full_bar[s], 0, err, 4);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+bool make_map(CUtensorMap* map, float* buf, int rows_pad, int batch, int box_rows) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)KP, (cuuint64_t)rows_pad, (cuuint64_t)batch};
+  cuuint64_t strides[2] = {(cuuint64_t)KP * 4, (cuuint64_t)rows_pad * KP * 4};
+  cuuint32_t box[3] = {(cuuint32_t)TK, (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, buf, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// C map: every whole matrix of the batch as reals, x = real row (2n), y = column (n),
+// z = matrix; box 32 x 32, no swizzle.
+bool make_c_map(CUtensorMap* map, float* base, int n, long long lda, long long strideA, int batch) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)2 * n, (cuuint64_t)n, (cuuint64_t)batch};
+  cuuint64_t strides[2] = {(cuuint64_t)lda * 8, (cuuint64_t)strideA * 8};
+  cuuint32_t box[3] = {32, 32, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+}  // namespace bem
+
+namespace bem {
+// Workspace for one batched factorisation: split operand buffers sized for the
+// first (largest) trailing update, tensor maps built once, and an error word.
+struct TcGemmPlan {
+  float *ahi = nullptr, *alo = nullptr, *bhi = nullptr, *blo = nullptr;
+  int* err = nullptr;
+  int rows_pad = 0, cols_pad = 0, batch = 0;
+  CUtensorMap mahi, malo, mbhi, mblo, mc;
+};
+
+size_t tc_gemm_workspace_bytes(int n, int batch) {
+  const size_t rows_pad = ((size_t)2 * n + TM - 1) / TM * TM;
+  const size_t cols_pad = ((size_t)n + TN - 1) / TN * TN;
+  return (2 * rows_pad + 2 * cols_pad) * KP * 4 * batch + 256 * 5;
+}
+
+bool tc_gemm_available() { return encode_fn() != nullptr; }
+
+// Build the plan inside caller-provided workspace (tc_gemm_workspace_bytes(n, batch) bytes)
+// for the batch of matrices at A (column-major, leading dimension lda, lda * n apart).
+// Refuses (returns false) when a TMA coordinate or stride into A could break the
+// 16-byte rule: odd nb, odd lda, or A not 16-byte aligned.
+bool tc_gemm_plan(TcGemmPlan* p, void* workspace, int n, int batch, float2* A, long long lda, int nb) {
+  if ((nb & 1) || (lda & 1) || ((uintptr_t)A & 15)) return false;
+  const size_t rows_pad = ((size_t)2 * n + TM - 1) / TM * TM;
+  const size_t cols_pad = ((size_t)n + TN - 1) / TN * TN;
+  char* w = (char*)workspace;
+  auto take = [&](size_t bytes) {
+    char* r = w;
+    w += (bytes + 255) / 256 * 256;
+    return r;
+  };
+  p->rows_pad = (int)rows_pad;
+  p->cols_pad = (int)cols_pad;
+  p->batch = batch;
+  p->ahi = (float*)take(rows_pad * KP * 4 * batch);
+  p->alo = (float*)take(rows_pad * KP * 4 * batch);
+  p->bhi = (float*)take(cols_pad * KP * 4 * batch);
+  p->blo = (float*)take(cols_pad * KP * 4 * batch);
+  p->err = (int*)take(sizeof(int));
+  return make_map(&p->mahi, p->ahi, (int)rows_pad, batch, TM) && make_map(&p->malo, p->alo, (int)rows_pad, batch, TM) &&
+         make_map(&p->mbhi, p->bhi, (int)cols_pad, batch, TN) && make_map(&p->mblo, p->blo, (int)cols_pad, batch, TN) &&
+         make_c_map(&p->mc, (float*)A, n, lda, lda * (long long)n, batch);
+}
+
+// C -= L21 * U12 for the block column at k (width kb <= 64) of every matrix in the batch.
+cudaError_t tc_trailing_update(TcGemmPlan* p, float2* A, long long lda, long long strideA, int n, int k, int kb,
+                               cudaStream_t stream) {
+  const int M = n - k - kb, N = n - k - kb;
+  if (M <= 0 || N <= 0) return cudaSuccess;
+  const int M2 = 2 * M;
+  const int rows_used = (M2 + TM - 1) / TM * TM;
+  const int cols_used = (N + TN - 1) / TN * TN;
+  {
+    const long long per = (long long)rows_used * KP;
+    dim3 g((unsigned)((per + 255) / 256), p->batch);
+    prep_a_kernel<<<g, 256, 0, stream>>>(A, lda, strideA, k + kb, k, M, kb, p->rows_pad, p->ahi, p->alo);
+  }
+  {
+    const long long per = (long long)cols_used * KP;
+    dim3 g((unsigned)((per + 255) / 256), p->batch);
+    prep_b_kernel<<<g, 256, 0, stream>>>(A, lda, strideA, k, k + kb, N, kb, p->cols_pad, p->bhi, p->blo);
+  }
+  const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(trailing_update_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  if ((k + kb) & 1) return cudaErrorInvalidValue;  // x coordinate 2 (k + kb) must be a multiple of 4
+  dim3 grid(rows_used / TM, cols_used / TN, p->batch);
+  trailing_update_tf32x3<<<grid, 128, smem, stream>>>(p->mahi, p->malo, p->mbhi, p->mblo, p->mc, 2 * (k + kb), k + kb,
+                                                     M2, N, p->err);
+  return cudaGetLastError();
+}
+
+int* tc_gemm_error_word(TcGemmPlan* p) { return p->err; }
+
+size_t tc_gemm_plan_size() { return sizeof(TcGemmPlan); }
+
+}  // namespace bem

@@ -44,6 +44,7 @@ struct DeviceMesh {
   int* pairs_by_test = nullptr;
   int* rule_ptr = nullptr;
   double* duffy = nullptr;
+  float* duffy32 = nullptr;  // the same table rounded to float (mixed form)
   double* moments = nullptr;
   double* verts = nullptr;
   int* faces = nullptr;
@@ -75,9 +76,19 @@ cudaError_t launch_rhs(const DeviceMesh& m, Precision prec, double k, const Oper
 
 // dense LU and solves (bem_lu.cu).  Matrices are column-major, batched with a
 // stride of lda*n elements; pivots are 0-based, ipiv stride n.
-struct LuWorkspace;
+// Trailing-update GEMM of the mixed-precision LU: 0 = automatic (tensor cores
+// when available), 1 = cuBLAS cgemm (FP32), 2 = tcgen05 3xTF32 (bem_gemm_tc.cu).
+enum class LuGemm : int { Auto = 0, Cublas = 1, Tensor = 2 };
+struct TcGemmPlan;
+size_t tc_gemm_workspace_bytes(int n, int batch);
+bool tc_gemm_available();
+int* tc_gemm_error_word(TcGemmPlan* p);
+// Factor `batch` matrices in place.  tc_workspace (tc_gemm_workspace_bytes(n,
+// batch) bytes, may be null) enables the tensor-core update; *used_tensor tells
+// which update ran; *tc_err receives the device address of the kernel's error word.
 cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int batch, int* ipiv, int* info,
-                              int nb, void* cublas_handle, cudaStream_t stream);
+                              int nb, void* cublas_handle, cudaStream_t stream, LuGemm gemm = LuGemm::Cublas,
+                              void* tc_workspace = nullptr, bool* used_tensor = nullptr, int** tc_err = nullptr);
 // Solve (LU) X = B in place for nrhs columns per matrix (B stride ldb*nrhs per matrix), working precision.
 cudaError_t lu_solve_batched(Precision prec, const void* LU, long long lda, int n, int batch, const int* ipiv,
                              void* B, long long ldb, int nrhs, int nb, cudaStream_t stream);
@@ -87,12 +98,20 @@ cudaError_t residual_batched(Precision prec, const void* A, long long lda, int n
 // Per (matrix, rhs): out[2*i] = ||r_i||^2 and out[2*i+1] = ||b_i||^2.
 cudaError_t norms_batched(const double2* r, const double2* b, long long ldb, int n, int count, double* out,
                           cudaStream_t stream);
+// Cluster-resident panel (bem_lu_cluster.cu).  lu_cluster_plan picks the panel
+// width (64 or 32) and cluster size for an n x n matrix; false when no cluster
+// configuration fits (then the single-CTA panel is used).
+bool lu_cluster_plan(Precision prec, int n, int* nb, int* cl);
+cudaError_t lu_panel_cluster(Precision prec, void* A, long long lda, long long strideA, int n, int k, int kb, int nb,
+                             int cl, int batch, int* ipiv, int* info, cudaStream_t stream);
+// perm[i]: (P b)[i] = b[perm[i]]; then one cluster per right-hand side solves in place.
+cudaError_t lu_perm_batched(const int* ipiv, int n, int batch, int* perm, cudaStream_t stream);
+cudaError_t lu_solve_cluster_batched(Precision prec, const void* LU, long long lda, int n, int batch, const int* perm,
+                                     void* B, long long ldb, int nrhs, cudaStream_t stream);
 // x += d (d complex64) ; copy / convert helpers
 cudaError_t axpy_f32_into_f64(const float2* d, double2* x, long long n, cudaStream_t stream);
 cudaError_t convert_f64_to_f32(const double2* src, float2* dst, long long n, cudaStream_t stream);
 cudaError_t convert_f32_to_f64(const float2* src, double2* dst, long long n, cudaStream_t stream);
-// undo the row permutation of the solution?  (columns are unpermuted: the
-// solution is already in vertex order)
 
 // far field (bem_field.cu)
 cudaError_t launch_field(const DeviceMesh& m, Precision prec, int batch, const double* k, const double2* qscale,

@@ -17,6 +17,8 @@
 //   trailing update   A22 -= L21 U12 : a batched complex GEMM
 #include <cublas_v2.h>
 
+#include <vector>
+
 #include "bem_common.cuh"
 #include "bem_kernels.h"
 
@@ -353,17 +355,43 @@ __global__ void f32_to_f64_kernel(const float2* s, double2* d, long long n) {
 
 }  // namespace
 
+bool tc_gemm_plan(TcGemmPlan* p, void* workspace, int n, int batch, float2* A, long long lda, int nb);
+cudaError_t tc_trailing_update(TcGemmPlan* p, float2* A, long long lda, long long strideA, int n, int k, int kb,
+                               cudaStream_t stream);
+size_t tc_gemm_plan_size();
+
 cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int batch, int* ipiv, int* info, int nb,
-                              void* cublas_handle, cudaStream_t stream) {
+                              void* cublas_handle, cudaStream_t stream, LuGemm gemm, void* tc_workspace,
+                              bool* used_tensor, int** tc_err) {
   cublasHandle_t h = (cublasHandle_t)cublas_handle;
   cublasSetStream(h, stream);
   const long long strideA = lda * (long long)n;
   const bool mixed = prec == Precision::Mixed;
   nb = std::max(1, std::min(nb, 64));
   const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
+  int cnb = 0, ccl = 0;
+  const bool cluster_panel = lu_cluster_plan(prec, n, &cnb, &ccl);
+  if (cluster_panel) nb = cnb;
+  // tensor-core trailing update (mixed precision only; K = 2 nb <= 128)
+  std::vector<unsigned char> plan_storage;
+  TcGemmPlan* plan = nullptr;
+  if (mixed && gemm != LuGemm::Cublas && tc_workspace && nb <= 64 && tc_gemm_available()) {
+    plan_storage.resize(tc_gemm_plan_size());
+    plan = reinterpret_cast<TcGemmPlan*>(plan_storage.data());
+    if (!tc_gemm_plan(plan, tc_workspace, n, batch, (float2*)A, lda, nb)) plan = nullptr;
+  }
+  if (gemm == LuGemm::Tensor && mixed && !plan) return cudaErrorNotSupported;
+  if (used_tensor) *used_tensor = plan != nullptr;
+  if (plan) {
+    if (tc_err) *tc_err = tc_gemm_error_word(plan);
+    cudaMemsetAsync(tc_gemm_error_word(plan), 0, sizeof(int), stream);
+  }
   for (int k = 0; k < n; k += nb) {
     const int kb = std::min(nb, n - k);
-    if (mixed)
+    if (cluster_panel) {
+      cudaError_t e = lu_panel_cluster(prec, A, lda, strideA, n, k, kb, nb, ccl, batch, ipiv, info, stream);
+      if (e != cudaSuccess) return e;
+    } else if (mixed)
       lu_panel_kernel<float><<<batch, 1024, 0, stream>>>((float2*)A, lda, strideA, n, k, kb, ipiv, info);
     else
       lu_panel_kernel<double><<<batch, 1024, 0, stream>>>((double2*)A, lda, strideA, n, k, kb, ipiv, info);
@@ -382,6 +410,11 @@ cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int
       if (mixed) {
         if (sm > 48 * 1024) cudaFuncSetAttribute(lu_trsm_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         lu_trsm_kernel<float2><<<g, tpb, sm, stream>>>((float2*)A, lda, strideA, n, k, kb);
+        if (plan) {
+          cudaError_t e = tc_trailing_update(plan, (float2*)A, lda, strideA, n, k, kb, stream);
+          if (e != cudaSuccess) return e;
+          continue;
+        }
         const cuComplex alpha = make_cuComplex(-1.f, 0.f), beta = make_cuComplex(1.f, 0.f);
         float2* base = (float2*)A;
         cublasStatus_t st = cublasCgemmStridedBatched(

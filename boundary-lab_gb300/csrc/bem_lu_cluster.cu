@@ -1,0 +1,489 @@
+// Cluster-resident LU panel factorisation and cluster triangular solves (sm_103a).
+//
+// Panel: the m x nb panel of one matrix is spread over the shared memory of a
+// thread-block cluster (CL CTAs, each holding a contiguous block of panel rows,
+// column-major).  Each column step does a local pivot search, one cluster
+// barrier, a pivot decision from the CL candidates read through distributed
+// shared memory (DSMEM), a second barrier after the two rows to be swapped are
+// staged, then the swap, scaling and rank-1 update entirely in shared memory.
+// Nothing touches global memory between the initial load and the final store,
+// where the previous single-CTA kernel streamed the whole panel through L2 at
+// every column.  Pivot choice is LAPACK's (first maximum of |re| + |im|).
+//
+// Solves: pivots are turned into a row permutation once per factorisation
+// (lu_perm_kernel, in shared memory); each right-hand side is then solved by
+// one cluster whose CTAs own blocks of rows: the owner of a 32-row diagonal
+// block solves it with one warp, publishes the 32 values in a double-buffered
+// shared slot, and after one cluster barrier every CTA applies the block's
+// columns to its own rows.
+//
+// Cluster barriers are hardware barriers (barrier.cluster); every CTA of a
+// cluster executes the same sequence of them, and the kernels end with a
+// barrier so no CTA leaves while another may still read its shared memory.
+#include <cooperative_groups.h>
+#include <limits.h>
+
+#include "bem_common.cuh"
+#include "bem_kernels.h"
+
+namespace cg = cooperative_groups;
+
+namespace bem {
+namespace {
+
+template <typename R> struct CT2;
+template <> struct CT2<float> { typedef float2 C2; };
+template <> struct CT2<double> { typedef double2 C2; };
+
+template <typename C2> __device__ __forceinline__ auto abs1(C2 v) -> decltype(v.x) { return fabs(v.x) + fabs(v.y); }
+
+template <typename C2> __device__ __forceinline__ C2 inverse(C2 d) {
+  auto m = d.x * d.x + d.y * d.y;
+  C2 r;
+  r.x = d.x / m;
+  r.y = -d.y / m;
+  return r;
+}
+
+constexpr int kPanelThreads = 512;
+
+template <typename R, int NB>
+__global__ void __launch_bounds__(kPanelThreads) lu_panel_cluster_kernel(typename CT2<R>::C2* A, long long lda,
+                                                                         long long strideA, int n, int k, int kb,
+                                                                         int chunk, int* ipiv, int* info) {
+  typedef typename CT2<R>::C2 C2;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int CL = (int)cluster.num_blocks();
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  C2* M = A + (size_t)blockIdx.y * strideA;
+  int* piv = ipiv + (size_t)blockIdx.y * n;
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C2* P = reinterpret_cast<C2*>(smem_raw);  // [NB][chunk]
+  C2* prow = P + (size_t)NB * chunk;        // staged pivot row (read by other CTAs)
+  C2* crow = prow + NB;                     // staged diagonal row (read by other CTAs)
+  C2* urow = crow + NB;                     // local copy of the pivot row
+  R* cval = reinterpret_cast<R*>(urow + NB);
+  int* cidx = reinterpret_cast<int*>(cval + 1);
+  __shared__ R wval[32];
+  __shared__ int widx[32];
+  __shared__ int s_p;
+
+  const int m = n - k;
+  const int r0 = rank * chunk;
+  const int rows = max(0, min(chunk, m - r0));
+  for (int c = 0; c < kb; ++c) {
+    const C2* src = M + (size_t)(k + c) * lda + k + r0;
+    for (int i = tid; i < rows; i += blockDim.x) P[(size_t)c * chunk + i] = src[i];
+  }
+  __syncthreads();
+
+  for (int j = 0; j < kb; ++j) {
+    // local pivot candidate among panel rows >= j
+    R best = R(-1);
+    int bi = INT_MAX;
+    const C2* Pj = P + (size_t)j * chunk;
+    for (int i = tid; i < rows; i += blockDim.x) {
+      const int pr = r0 + i;
+      if (pr >= j) {
+        const R v = abs1(Pj[i]);
+        if (v > best || (v == best && pr < bi)) {
+          best = v;
+          bi = pr;
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const R ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) {
+        best = ov;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      wval[wid] = best;
+      widx[wid] = bi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      R b = R(-1);
+      int x = INT_MAX;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+        if (wval[w] > b || (wval[w] == b && widx[w] < x)) {
+          b = wval[w];
+          x = widx[w];
+        }
+      cval[0] = b;
+      cidx[0] = x;
+    }
+    cluster.sync();  // B1: every CTA's candidate is published
+    if (tid == 0) {
+      R b = R(-1);
+      int x = INT_MAX;
+      for (int q = 0; q < CL; ++q) {
+        const R v = *cluster.map_shared_rank(cval, q);
+        const int ix = *cluster.map_shared_rank(cidx, q);
+        if (v > b || (v == b && ix < x)) {
+          b = v;
+          x = ix;
+        }
+      }
+      s_p = (x == INT_MAX) ? j : x;
+    }
+    __syncthreads();
+    const int p = s_p;
+    const int owner_j = j / chunk, owner_p = p / chunk;
+    if (rank == owner_p)
+      for (int c = tid; c < kb; c += blockDim.x) prow[c] = P[(size_t)c * chunk + (p - r0)];
+    if (rank == owner_j)
+      for (int c = tid; c < kb; c += blockDim.x) crow[c] = P[(size_t)c * chunk + (j - r0)];
+    cluster.sync();  // B2: the two rows of the interchange are staged
+    {
+      const C2* rp = cluster.map_shared_rank(prow, owner_p);
+      for (int c = tid; c < kb; c += blockDim.x) urow[c] = rp[c];
+    }
+    __syncthreads();
+    if (p != j) {
+      if (rank == owner_j)
+        for (int c = tid; c < kb; c += blockDim.x) P[(size_t)c * chunk + (j - r0)] = urow[c];
+      if (rank == owner_p) {
+        const C2* rc = cluster.map_shared_rank(crow, owner_j);
+        for (int c = tid; c < kb; c += blockDim.x) P[(size_t)c * chunk + (p - r0)] = rc[c];
+      }
+    }
+    if (rank == 0 && tid == 0) piv[k + j] = k + p;
+    __syncthreads();
+    const C2 d = urow[j];
+    C2 inv;
+    if (d.x == R(0) && d.y == R(0)) {
+      inv.x = R(0);
+      inv.y = R(0);
+      if (rank == 0 && tid == 0 && info[blockIdx.y] == 0) info[blockIdx.y] = k + j + 1;
+    } else {
+      inv = inverse(d);
+    }
+    for (int i = tid; i < rows; i += blockDim.x) {
+      if (r0 + i <= j) continue;
+      C2 l = cmul(P[(size_t)j * chunk + i], inv);
+      P[(size_t)j * chunk + i] = l;
+#pragma unroll 4
+      for (int c = j + 1; c < kb; ++c) {
+        const C2 u = urow[c];
+        C2 v = P[(size_t)c * chunk + i];
+        v.x -= l.x * u.x - l.y * u.y;
+        v.y -= l.x * u.y + l.y * u.x;
+        P[(size_t)c * chunk + i] = v;
+      }
+    }
+    __syncthreads();
+  }
+  for (int c = 0; c < kb; ++c) {
+    C2* dst = M + (size_t)(k + c) * lda + k + r0;
+    for (int i = tid; i < rows; i += blockDim.x) dst[i] = P[(size_t)c * chunk + i];
+  }
+  cluster.sync();  // no CTA leaves while others may still read its shared memory
+}
+
+// perm[i] such that (P b)[i] = b[perm[i]], from LAPACK-style interchanges.
+__global__ void lu_perm_kernel(const int* __restrict__ ipiv, int n, int* __restrict__ perm) {
+  extern __shared__ int sp[];
+  const int* piv = ipiv + (size_t)blockIdx.x * n;
+  int* out = perm + (size_t)blockIdx.x * n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sp[i] = i;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int i = 0; i < n; ++i) {
+      const int p = piv[i];
+      if (p != i && p >= 0 && p < n) {
+        const int t = sp[i];
+        sp[i] = sp[p];
+        sp[p] = t;
+      }
+    }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = sp[i];
+}
+
+constexpr int kSolveThreads = 512;
+
+// One cluster per (matrix, right-hand side): x = U^{-1} L^{-1} (P b), in place in B.
+template <typename R>
+__global__ void __launch_bounds__(kSolveThreads) lu_solve_cluster_kernel(const typename CT2<R>::C2* A, long long lda,
+                                                                         long long strideA, int n,
+                                                                         const int* __restrict__ perm,
+                                                                         typename CT2<R>::C2* B, long long ldb,
+                                                                         int nrhs, int chunk) {
+  typedef typename CT2<R>::C2 C2;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int sys = blockIdx.y;
+  const int mat = sys / nrhs;
+  const C2* M = A + (size_t)mat * strideA;
+  C2* b = B + (size_t)sys * ldb;
+  const int* pm = perm + (size_t)mat * n;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C2* x = reinterpret_cast<C2*>(smem_raw);  // my rows [r0, r0 + chunk)
+  C2* pub = x + chunk;                      // [2][32] published block solutions
+  const int r0 = rank * chunk;
+  const int rows = max(0, min(chunk, n - r0));
+  for (int i = tid; i < rows; i += blockDim.x) x[i] = b[pm[r0 + i]];
+  cluster.sync();  // every CTA has read b before anyone writes it back
+  const int nblk = (n + 31) / 32;
+  // forward substitution with unit lower L
+  for (int t = 0; t < nblk; ++t) {
+    const int k0 = t * 32, kb = min(32, n - k0);
+    const int owner = k0 / chunk;
+    C2* slot = pub + 32 * (t & 1);
+    if (rank == owner && tid < 32) {
+      // this lane's row of the diagonal block, loaded up front (independent loads)
+      C2 Lr[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        if (j < kb && lane < kb) {
+          Lr[j] = M[(size_t)(k0 + j) * lda + k0 + lane];
+        } else {
+          Lr[j].x = 0;
+          Lr[j].y = 0;
+        }
+      }
+      C2 v;
+      v.x = 0;
+      v.y = 0;
+      if (lane < kb) v = x[k0 - r0 + lane];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        C2 xj;
+        xj.x = __shfl_sync(0xffffffffu, v.x, j);
+        xj.y = __shfl_sync(0xffffffffu, v.y, j);
+        if (lane > j) {
+          v.x -= Lr[j].x * xj.x - Lr[j].y * xj.y;
+          v.y -= Lr[j].x * xj.y + Lr[j].y * xj.x;
+        }
+      }
+      if (lane < kb) {
+        x[k0 - r0 + lane] = v;
+        slot[lane] = v;
+      }
+    }
+    cluster.sync();
+    __shared__ C2 xs[32];
+    if (tid < kb) xs[tid] = cluster.map_shared_rank(slot, owner)[tid];
+    __syncthreads();
+    for (int i = tid; i < rows; i += blockDim.x) {
+      const int r = r0 + i;
+      if (r < k0 + kb) continue;
+      C2 v = x[i];
+#pragma unroll 8
+      for (int j = 0; j < kb; ++j) {
+        const C2 l = M[(size_t)(k0 + j) * lda + r];
+        const C2 s = xs[j];
+        v.x -= l.x * s.x - l.y * s.y;
+        v.y -= l.x * s.y + l.y * s.x;
+      }
+      x[i] = v;
+    }
+    __syncthreads();
+  }
+  // backward substitution with U
+  for (int t = nblk - 1; t >= 0; --t) {
+    const int k0 = t * 32, kb = min(32, n - k0);
+    const int owner = k0 / chunk;
+    // the slot alternates over the whole sequence of blocks (forward then backward)
+    C2* slot = pub + 32 * ((nblk + (nblk - 1 - t)) & 1);
+    if (rank == owner && tid < 32) {
+      C2 Ur[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        if (j < kb && lane < kb) {
+          Ur[j] = M[(size_t)(k0 + j) * lda + k0 + lane];
+        } else {
+          Ur[j].x = 0;
+          Ur[j].y = 0;
+        }
+      }
+      C2 dinv;
+      dinv.x = 0;
+      dinv.y = 0;
+      if (lane < kb) dinv = inverse(M[(size_t)(k0 + lane) * lda + k0 + lane]);
+      C2 v;
+      v.x = 0;
+      v.y = 0;
+      if (lane < kb) v = x[k0 - r0 + lane];
+#pragma unroll
+      for (int j = 31; j >= 0; --j) {
+        if (lane == j) v = cmul(v, dinv);
+        C2 xj;
+        xj.x = __shfl_sync(0xffffffffu, v.x, j);
+        xj.y = __shfl_sync(0xffffffffu, v.y, j);
+        if (lane < j) {
+          v.x -= Ur[j].x * xj.x - Ur[j].y * xj.y;
+          v.y -= Ur[j].x * xj.y + Ur[j].y * xj.x;
+        }
+      }
+      if (lane < kb) {
+        x[k0 - r0 + lane] = v;
+        slot[lane] = v;
+      }
+    }
+    cluster.sync();
+    __shared__ C2 ys[32];
+    if (tid < kb) ys[tid] = cluster.map_shared_rank(slot, owner)[tid];
+    __syncthreads();
+    for (int i = tid; i < rows; i += blockDim.x) {
+      const int r = r0 + i;
+      if (r >= k0) continue;
+      C2 v = x[i];
+#pragma unroll 8
+      for (int j = 0; j < kb; ++j) {
+        const C2 u = M[(size_t)(k0 + j) * lda + r];
+        const C2 s = ys[j];
+        v.x -= u.x * s.x - u.y * s.y;
+        v.y -= u.x * s.y + u.y * s.x;
+      }
+      x[i] = v;
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < rows; i += blockDim.x) b[r0 + i] = x[i];
+  cluster.sync();
+}
+
+template <typename K>
+cudaError_t launch_cluster(K kern, dim3 grid, int threads, size_t smem, int cl, cudaStream_t stream,
+                           void** args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelExC(&cfg, (const void*)kern, args);
+}
+
+// Largest cluster size the kernel can be launched with at this shared-memory size.
+template <typename K> int max_cluster(K kern, int threads, size_t smem) {
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(16, 1);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  int cl = 0;
+  if (cudaOccupancyMaxPotentialClusterSize(&cl, (const void*)kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return cl;
+}
+
+constexpr size_t kPanelSmemBudget = 200 * 1024;
+
+template <typename R, int NB> size_t panel_smem(int chunk) {
+  typedef typename CT2<R>::C2 C2;
+  return (size_t)NB * chunk * sizeof(C2) + 3 * NB * sizeof(C2) + 64;
+}
+
+template <typename R> bool choose_panel(int n, int& nb, int& cl) {
+  // prefer nb = 64 (larger trailing GEMMs), then 32; smallest cluster that fits
+  for (int want_nb : {64, 32}) {
+    for (int c : {4, 8, 16}) {
+      const int chunk = (n + c - 1) / c;
+      const size_t sm = want_nb == 64 ? panel_smem<R, 64>(chunk) : panel_smem<R, 32>(chunk);
+      if (sm > kPanelSmemBudget) continue;
+      int maxcl = want_nb == 64 ? max_cluster(lu_panel_cluster_kernel<R, 64>, kPanelThreads, sm)
+                                : max_cluster(lu_panel_cluster_kernel<R, 32>, kPanelThreads, sm);
+      if (maxcl >= c) {
+        nb = want_nb;
+        cl = c;
+        return true;
+      }
+    }
+  }
+  return false;
+}
+
+}  // namespace
+
+bool lu_cluster_plan(Precision prec, int n, int* nb, int* cl) {
+  static thread_local int last_n[2] = {-1, -1}, last_nb[2] = {0, 0}, last_cl[2] = {0, 0};
+  static thread_local bool last_ok[2] = {false, false};
+  const int pi = prec == Precision::Mixed ? 1 : 0;
+  if (last_n[pi] != n) {
+    int b = 0, c = 0;
+    last_ok[pi] = prec == Precision::Mixed ? choose_panel<float>(n, b, c) : choose_panel<double>(n, b, c);
+    last_n[pi] = n;
+    last_nb[pi] = b;
+    last_cl[pi] = c;
+  }
+  *nb = last_nb[pi];
+  *cl = last_cl[pi];
+  return last_ok[pi];
+}
+
+cudaError_t lu_panel_cluster(Precision prec, void* A, long long lda, long long strideA, int n, int k, int kb, int nb,
+                             int cl, int batch, int* ipiv, int* info, cudaStream_t stream) {
+  const int m = n - k;
+  const int chunk = (m + cl - 1) / cl;
+  void* args[] = {&A, &lda, &strideA, &n, &k, &kb, (void*)&chunk, &ipiv, &info};
+  dim3 grid(cl, batch);
+  if (prec == Precision::Mixed) {
+    if (nb == 64) {
+      const size_t sm = panel_smem<float, 64>(chunk);
+      cudaFuncSetAttribute(lu_panel_cluster_kernel<float, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      cudaFuncSetAttribute(lu_panel_cluster_kernel<float, 64>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+      return launch_cluster(lu_panel_cluster_kernel<float, 64>, grid, kPanelThreads, sm, cl, stream, args);
+    }
+    const size_t sm = panel_smem<float, 32>(chunk);
+    cudaFuncSetAttribute(lu_panel_cluster_kernel<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaFuncSetAttribute(lu_panel_cluster_kernel<float, 32>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return launch_cluster(lu_panel_cluster_kernel<float, 32>, grid, kPanelThreads, sm, cl, stream, args);
+  }
+  if (nb == 64) {
+    const size_t sm = panel_smem<double, 64>(chunk);
+    cudaFuncSetAttribute(lu_panel_cluster_kernel<double, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaFuncSetAttribute(lu_panel_cluster_kernel<double, 64>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return launch_cluster(lu_panel_cluster_kernel<double, 64>, grid, kPanelThreads, sm, cl, stream, args);
+  }
+  const size_t sm = panel_smem<double, 32>(chunk);
+  cudaFuncSetAttribute(lu_panel_cluster_kernel<double, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaFuncSetAttribute(lu_panel_cluster_kernel<double, 32>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return launch_cluster(lu_panel_cluster_kernel<double, 32>, grid, kPanelThreads, sm, cl, stream, args);
+}
+
+cudaError_t lu_perm_batched(const int* ipiv, int n, int batch, int* perm, cudaStream_t stream) {
+  const size_t sm = (size_t)n * sizeof(int);
+  if (sm > 48 * 1024) cudaFuncSetAttribute(lu_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  lu_perm_kernel<<<batch, 256, sm, stream>>>(ipiv, n, perm);
+  return cudaGetLastError();
+}
+
+cudaError_t lu_solve_cluster_batched(Precision prec, const void* LU, long long lda, int n, int batch, const int* perm,
+                                     void* B, long long ldb, int nrhs, cudaStream_t stream) {
+  const long long strideA = lda * (long long)n;
+  const size_t esz = prec == Precision::Mixed ? sizeof(float2) : sizeof(double2);
+  // rows per CTA: a multiple of 32 so that each 32-row block has one owner
+  int cl = 8;
+  int chunk = ((n + cl - 1) / cl + 31) / 32 * 32;
+  const size_t sm = (size_t)(chunk + 64) * esz;
+  dim3 grid(cl, batch * nrhs);
+  if (prec == Precision::Mixed) {
+    cudaFuncSetAttribute(lu_solve_cluster_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    void* args[] = {&LU, &lda, (void*)&strideA, &n, &perm, &B, &ldb, &nrhs, &chunk};
+    return launch_cluster(lu_solve_cluster_kernel<float>, grid, kSolveThreads, sm, cl, stream, args);
+  }
+  cudaFuncSetAttribute(lu_solve_cluster_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  void* args[] = {&LU, &lda, (void*)&strideA, &n, &perm, &B, &ldb, &nrhs, &chunk};
+  return launch_cluster(lu_solve_cluster_kernel<double>, grid, kSolveThreads, sm, cl, stream, args);
+}
+
+}  // namespace bem

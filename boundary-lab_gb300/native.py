@@ -43,6 +43,7 @@ EXPORTED_SYMBOLS = (
     "bem_apply_rhs_operator",
     "bem_estimate_device_bytes",
     "bem_evaluate_field_noalloc",
+    "bem_lu_factor_dense",
 )
 
 
@@ -81,6 +82,7 @@ class SolveOptions(ctypes.Structure):
         ("lu_block", ctypes.c_int),
         ("outputs_on_device", ctypes.c_int),
         ("profile", ctypes.c_int),
+        ("lu_gemm", ctypes.c_int),
     ]
 
 
@@ -96,6 +98,7 @@ class SolveStats(ctypes.Structure):
         ("regular_pairs", ctypes.c_longlong),
         ("singular_pairs", ctypes.c_longlong),
         ("singular_points", ctypes.c_longlong),
+        ("lu_gemm_used", ctypes.c_int),
     ]
 
 KERNEL_SLOTS = ("singular", "regular", "gather", "rhs", "lu", "solve", "field")
@@ -162,6 +165,8 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         lib.bem_assemble_lhs.restype = ip
         lib.bem_apply_rhs_operator.argtypes = [vp, ctypes.c_double, ip, dp, dp, ip, dp]
         lib.bem_apply_rhs_operator.restype = ip
+        lib.bem_lu_factor_dense.argtypes = [vp, ip, dp, ctypes.POINTER(ctypes.c_int), ip, ip]
+        lib.bem_lu_factor_dense.restype = ip
         lib.bem_estimate_device_bytes.argtypes = [ip, ip, ip, ip, ip, ip, ip]
         lib.bem_estimate_device_bytes.restype = ctypes.c_longlong
         # allocation-free field evaluation: every pointer is a caller-owned device buffer
@@ -226,6 +231,17 @@ class Context:
                                               len(f), int(regular_order), int(singular_order), ctypes.byref(handle)))
         return Mesh(self, handle, len(v), len(f))
 
+    def lu_factor_dense(self, a: np.ndarray, precision: int = BEM_PRECISION_FP64, lu_gemm: int = 0):
+        """(LU, ipiv) of a dense complex matrix, LAPACK getrf conventions (0-based ipiv)."""
+        a = np.asarray(a, dtype=np.complex128)
+        n = a.shape[0]
+        buf = np.asfortranarray(a).copy(order="F")
+        ipiv = np.zeros(n, dtype=np.int32)
+        self._check(self._lib.bem_lu_factor_dense(self._h, n, _dptr(buf.reshape(-1, order="F").view(np.float64)),
+                                                  ipiv.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), int(precision),
+                                                  int(lu_gemm)))
+        return buf, ipiv
+
     def estimate_device_bytes(self, n_vertices: int, n_faces: int, n_pairs: int, n_rhs: int, n_points: int,
                               batch: int, precision: int) -> int:
         return int(self._lib.bem_estimate_device_bytes(n_vertices, n_faces, n_pairs, n_rhs, n_points, batch, precision))
@@ -260,7 +276,7 @@ class Mesh:
 
     def solve(self, freqs_hz, *, precision: int = BEM_PRECISION_MIXED, sound_speed: float = 343.0,
               rho: float = 1.21, refine_tol: float = 1e-10, max_refine: int = 8, batch: int = 0, lu_block: int = 0,
-              want_pressure: bool = True, want_field: bool = True, profile: bool = False):
+              want_pressure: bool = True, want_field: bool = True, profile: bool = False, lu_gemm: int = 0):
         """Returns (pressure [n_freq, n_rhs, n_vertices], field [n_freq, n_rhs, n_points], stats dict)."""
         f = np.ascontiguousarray(freqs_hz, dtype=np.float64).reshape(-1)
         opt = SolveOptions()
@@ -273,6 +289,7 @@ class Mesh:
         opt.batch = int(batch)
         opt.lu_block = int(lu_block)
         opt.profile = int(bool(profile))
+        opt.lu_gemm = int(lu_gemm)
         pressure = np.zeros((len(f), self.n_rhs, self.n_vertices), np.complex128) if want_pressure else None
         field = np.zeros((len(f), self.n_rhs, self.n_points), np.complex128) if want_field else None
         stats = SolveStats()

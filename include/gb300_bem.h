@@ -93,6 +93,8 @@ typedef struct bem_solve_options {
   int lu_block;          /* LU block size (<= 64); 0 = automatic */
   int outputs_on_device; /* 1: pressure_out / field_out are device pointers of the context's device */
   int profile;           /* 1: also time each kernel family with CUDA events (stats.kernel_s) */
+  int lu_gemm;           /* LU trailing update of the mixed form: 0 automatic (tensor cores when
+                            available), 1 cuBLAS cgemm (FP32), 2 tcgen05 3xTF32 tensor cores */
 } bem_solve_options;
 
 /* stats.kernel_s slots (filled when options.profile == 1), seconds summed over the call */
@@ -118,6 +120,7 @@ typedef struct bem_solve_stats {
   long long regular_pairs;  /* face pairs integrated with the regular rule, per frequency */
   long long singular_pairs; /* vertex-sharing pairs integrated with Duffy rules, per frequency */
   long long singular_points; /* Duffy points summed over the singular pairs, per frequency */
+  int lu_gemm_used;       /* trailing update that ran: 1 cuBLAS, 2 tensor cores (0 FP64 form) */
 } bem_solve_stats;
 
 void bem_default_options(bem_solve_options* opt);
@@ -173,6 +176,15 @@ int bem_evaluate_field_noalloc(const double* d_vertices, int n_vertices, const i
                                int regular_order, double k, const double* d_pressure, const double* d_neumann,
                                const double* d_points, int n_points, int precision, double* d_field_out,
                                void* stream, char* err, int err_cap);
+
+/* Parity entry point: LU factorisation with partial pivoting of one dense
+ * n x n matrix, as LAPACK getrf (the reference's `\` / lu!, BeatEngineCore.jl:1206,
+ * BeatEngineCpuSolve.jl:63).  a: column-major complex [n][n] (host), overwritten
+ * with L (unit lower, below the diagonal) and U; ipiv: 0-based row interchanges
+ * (row i was swapped with ipiv[i]).  precision selects FP64 or the mixed form's
+ * FP32 factorisation; lu_gemm as in bem_solve_options.  Returns BEM_ERR_SINGULAR
+ * on a zero pivot. */
+int bem_lu_factor_dense(bem_context* ctx, int n, double* a, int* ipiv, int precision, int lu_gemm);
 
 /* Device bytes needed to solve `batch` frequencies of a mesh of this size
  * (scratch + matrices + factors), for admission control by a scheduler. */
