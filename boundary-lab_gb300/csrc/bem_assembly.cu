@@ -69,23 +69,23 @@ __device__ __forceinline__ PairF32 pair_setup_f32(const float* ahi_g, const floa
   return P;
 }
 
-// Green's function and the radial factor of its gradient at one q-pair.
-// Returns false when the points coincide (the reference skips r == 0).
+// Green's function and the radial factor of its gradient at one q-pair
+// (points never coincide for the pairs this is used on).
 __device__ __forceinline__ void green_f32(const PairF32& P, const float* d, float k, float& rinv, float rv[3],
                                           float2& G) {
   rv[0] = P.Cf[0] + d[0];
   rv[1] = P.Cf[1] + d[1];
   rv[2] = P.Cf[2] + d[2];
   float r2 = fmaf(rv[0], rv[0], fmaf(rv[1], rv[1], rv[2] * rv[2]));
-  rinv = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
+  rinv = r2 > 1e-30f ? rsqrt_ftz(r2) : 0.0f;
   float r = r2 * rinv;
   float cd = fmaf(P.Cf[0], d[0], fmaf(P.Cf[1], d[1], P.Cf[2] * d[2]));
   float dd = fmaf(d[0], d[0], fmaf(d[1], d[1], d[2] * d[2]));
   float den = fmaxf(r + P.R0, 1e-30f);
-  float delta = __fdividef(fmaf(2.0f, cd, dd), den);
+  float delta = fmaf(2.0f, cd, dd) * rcp_ftz(den);
   float theta = reduce_two_pi(fmaf(k, delta, P.theta0));
   float s, c;
-  __sincosf(theta, &s, &c);
+  sincos_ftz(theta, &s, &c);
   float sc = rinv * BEM_INV_FOUR_PI;
   G = make_float2(c * sc, s * sc);
 }
@@ -95,12 +95,13 @@ __device__ __forceinline__ void green_f32(const PairF32& P, const float* d, floa
 struct RegParamsF32 {
   df kdf;      // wavenumber as double-float
   float k, k2;
+  float kturn;  // k / 2pi (phase in turns)
   float2 cD, cH;  // LHS coefficients of D and H
-  float cw[3 * kMaxQ];
+  float2 cw2[3 * kMaxQ];  // (cw, cw): operand pairs of the packed FP32x2 FMAs
 };
 
 template <int Q, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) regular_f32_kernel(const FaceF32* __restrict__ faces, int nf,
+__global__ void __launch_bounds__(WARPS * 32, 3) regular_f32_kernel(const FaceF32* __restrict__ faces, int nf,
                                                                  const int* __restrict__ tile_group_ptr,
                                                                  const LaneSlot* __restrict__ slots,
                                                                  const int* __restrict__ tile_row_base,
@@ -114,15 +115,15 @@ __global__ void __launch_bounds__(WARPS * 32) regular_f32_kernel(const FaceF32* 
   const int rows = tile_row_base[tile + 1] - base;
   float2* acc = smem_acc32 + (size_t)warp * 3 * max_rows;
   // rule coefficients of the (not unrolled) test-point loop, indexed at run time
-  __shared__ float s_cw[3 * kMaxQ];
-  if (threadIdx.x < 3 * kMaxQ) s_cw[threadIdx.x] = p.cw[threadIdx.x];
+  __shared__ float2 s_cw2[3 * kMaxQ];
+  if (threadIdx.x < 3 * kMaxQ) s_cw2[threadIdx.x] = p.cw2[threadIdx.x];
   for (int i = lane; i < 3 * max_rows; i += 32) acc[i] = make_float2(0.0f, 0.0f);
   __syncthreads();
   if (g >= nf) return;
 
-  // trial face (warp-uniform)
+  // trial face (warp-uniform): quadrature offsets og[n] with og.og and og.n_g
   const FaceF32& T = faces[g];
-  float ahi_g[3], alo_g[3], ng[3], og[Q][3], cg[9];
+  float ahi_g[3], alo_g[3], ng[3], og[Q][3], cg[9], gg[Q], gn[Q];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     ahi_g[d] = T.anchor_hi[d];
@@ -132,26 +133,63 @@ __global__ void __launch_bounds__(WARPS * 32) regular_f32_kernel(const FaceF32* 
 #pragma unroll
   for (int i = 0; i < 9; ++i) cg[i] = T.curls[i];
 #pragma unroll
-  for (int n = 0; n < Q; ++n)
+  for (int n = 0; n < Q; ++n) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) og[n][d] = T.off[3 * n + d];
+    gg[n] = fmaf(og[n][0], og[n][0], fmaf(og[n][1], og[n][1], og[n][2] * og[n][2]));
+    gn[n] = fmaf(og[n][0], ng[0], fmaf(og[n][1], ng[1], og[n][2] * ng[2]));
+  }
   const float a2g = T.area2;
   const int gv0 = T.verts[0], gv1 = T.verts[1], gv2 = T.verts[2];
 
+  // Software pipeline over the lane groups: the slot of group grp + 2 and the
+  // face header (vertices, anchor) of group grp + 1 are loaded while group grp
+  // is integrated, so the pair set-up never waits on a global load.
   const int g0 = tile_group_ptr[tile], g1 = tile_group_ptr[tile + 1];
+  LaneSlot s_next{-1, {0, 0, 0}}, s_cur{-1, {0, 0, 0}};
+  int hv[3] = {-1, -1, -1};
+  float hhi[3] = {0.f, 0.f, 0.f}, hlo[3] = {0.f, 0.f, 0.f};
+  auto load_head = [&](const LaneSlot& sl) {
+    if (sl.face >= 0) {
+      const FaceF32& H = faces[sl.face];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        hv[d] = H.verts[d];
+        hhi[d] = H.anchor_hi[d];
+        hlo[d] = H.anchor_lo[d];
+      }
+    }
+  };
+  if (g0 < g1) {
+    s_cur = slots[(size_t)g0 * 32 + lane];
+    load_head(s_cur);
+  }
+  if (g0 + 1 < g1) s_next = slots[(size_t)(g0 + 1) * 32 + lane];
   for (int grp = g0; grp < g1; ++grp) {
-    const LaneSlot s = slots[(size_t)grp * 32 + lane];
+    const LaneSlot s = s_cur;
+    const int fv[3] = {hv[0], hv[1], hv[2]};
+    const float ahi_f[3] = {hhi[0], hhi[1], hhi[2]}, alo_f[3] = {hlo[0], hlo[1], hlo[2]};
+    if (grp + 1 < g1) {
+      s_cur = s_next;
+      load_head(s_cur);
+    }
+    if (grp + 2 < g1) s_next = slots[(size_t)(grp + 2) * 32 + lane];
     if (s.face >= 0) {
       const FaceF32& F = faces[s.face];
-      int fv[3] = {F.verts[0], F.verts[1], F.verts[2]};
       if (!share_vertex(fv, gv0, gv1, gv2)) {
-        float ahi_f[3], alo_f[3];
+        // With C = anchor_g - anchor_f, x_n = anchor_g + og[n], y_m = anchor_f + of[m]
+        // and d = og[n] - of[m]:  r = |C + d|, and
+        //   r - |C| = (2 C.d + d.d) / (r + |C|),
+        //   2 C.d + d.d = Pg[n] + Pf[m] - 2 og[n].of[m],
+        //   Pg[n] = 2 C.og[n] + og[n].og[n],  Pf[m] = of[m].of[m] - 2 C.of[m],
+        // every term of size |C| h or h^2 (no cancellation against |C|^2).
+        const PairF32 P = pair_setup_f32(ahi_g, alo_g, ahi_f, alo_f, p.kdf);
+        const float R0 = fmaxf(P.R0, 1e-30f);
+        const float t0 = P.theta0 * BEM_INV_TWO_PI;  // k|C| in turns, |t0| <= 1/2
+        float Pg[Q];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          ahi_f[d] = F.anchor_hi[d];
-          alo_f[d] = F.anchor_lo[d];
-        }
-        PairF32 P = pair_setup_f32(ahi_g, alo_g, ahi_f, alo_f, p.kdf);
+        for (int n = 0; n < Q; ++n)
+          Pg[n] = fmaf(2.0f, fmaf(P.Cf[0], og[n][0], fmaf(P.Cf[1], og[n][1], P.Cf[2] * og[n][2])), gg[n]);
         float2 IG[3][3], ID[3][3];
 #pragma unroll
         for (int a = 0; a < 3; ++a)
@@ -162,9 +200,23 @@ __global__ void __launch_bounds__(WARPS * 32) regular_f32_kernel(const FaceF32* 
           }
         // The test-point loop is kept rolled: fully unrolling 6 x 6 Green
         // evaluations overflowed the instruction cache (no_instruction stalls).
+        // test-face data used after the loop, loaded now
+        const float nn = fmaf(F.normal[0], ng[0], fmaf(F.normal[1], ng[1], F.normal[2] * ng[2]));
+        const float jac = F.area2 * a2g * BEM_INV_FOUR_PI;
+        float nf0 = F.off[0], nf1 = F.off[1], nf2 = F.off[2];
 #pragma unroll 1
         for (int m = 0; m < Q; ++m) {
-          float of[3] = {F.off[3 * m], F.off[3 * m + 1], F.off[3 * m + 2]};
+          const float f0 = nf0, f1 = nf1, f2 = nf2;
+          {  // offsets of test point m + 1, consumed in the next iteration
+            const int mn = m + 1 < Q ? m + 1 : m;
+            nf0 = F.off[3 * mn];
+            nf1 = F.off[3 * mn + 1];
+            nf2 = F.off[3 * mn + 2];
+          }
+          const float cm0 = P.Cf[0] - f0, cm1 = P.Cf[1] - f1, cm2 = P.Cf[2] - f2;
+          const float Pf = fmaf(-2.0f, fmaf(P.Cf[0], f0, fmaf(P.Cf[1], f1, P.Cf[2] * f2)),
+                                fmaf(f0, f0, fmaf(f1, f1, f2 * f2)));
+          const float cmn = fmaf(cm0, ng[0], fmaf(cm1, ng[1], cm2 * ng[2]));
           float2 u[3], v[3];
 #pragma unroll
           for (int b = 0; b < 3; ++b) {
@@ -173,55 +225,62 @@ __global__ void __launch_bounds__(WARPS * 32) regular_f32_kernel(const FaceF32* 
           }
 #pragma unroll
           for (int n = 0; n < Q; ++n) {
-            float d[3] = {og[n][0] - of[0], og[n][1] - of[1], og[n][2] - of[2]};
-            float rinv, rv[3];
-            float2 G;
-            green_f32(P, d, p.k, rinv, rv, G);
-            // double-layer kernel dG/dn_y = G (ik - 1/r) (r . n_y)/r
-            float t = fmaf(rv[0], ng[0], fmaf(rv[1], ng[1], rv[2] * ng[2])) * rinv;
-            float2 Dk = make_float2(t * (-G.x * rinv - G.y * p.k), t * (G.x * p.k - G.y * rinv));
+            // r vector y_m -> x_n
+            const float r0 = cm0 + og[n][0], r1 = cm1 + og[n][1], r2v = cm2 + og[n][2];
+            const float r2 = fmaxf(fmaf(r0, r0, fmaf(r1, r1, r2v * r2v)), 1e-30f);
+            const float rinv = rsqrt_ftz(r2);
+            const float num = fmaf(-2.0f, fmaf(og[n][0], f0, fmaf(og[n][1], f1, og[n][2] * f2)), Pg[n] + Pf);
+            const float delta = num * rcp_ftz(fmaf(r2, rinv, R0));
+            float turn = fmaf(p.kturn, delta, t0);
+            turn -= round_nearest_small(turn);  // |turn| <= 1/2
+            float sn, cs;
+            sincos_ftz(turn * BEM_TWO_PI_HI, &sn, &cs);
+            // G * 4pi = e^{ikr} / r;  dG/dn_y * 4pi = G4 (ik - 1/r) (r . n_g) / r
+            const float Gx = cs * rinv, Gy = sn * rinv;
+            const float t = (cmn + gn[n]) * rinv;
+            const float2 G2 = make_float2(Gx, Gy);
+            const float2 Dk = make_float2(t * fmaf(-Gx, rinv, -Gy * p.k), t * fmaf(Gx, p.k, -Gy * rinv));
+            // complex accumulations as packed FP32x2 FMAs (re and im in one instruction)
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
-              const float c = p.cw[b * Q + n];
-              u[b].x = fmaf(c, G.x, u[b].x);
-              u[b].y = fmaf(c, G.y, u[b].y);
-              v[b].x = fmaf(c, Dk.x, v[b].x);
-              v[b].y = fmaf(c, Dk.y, v[b].y);
+              const float2 c = p.cw2[b * Q + n];
+              u[b] = __ffma2_rn(c, G2, u[b]);
+              v[b] = __ffma2_rn(c, Dk, v[b]);
             }
           }
 #pragma unroll
           for (int a = 0; a < 3; ++a) {
-            const float c = s_cw[a * Q + m];
+            const float2 c = s_cw2[a * Q + m];
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
-              IG[a][b].x = fmaf(c, u[b].x, IG[a][b].x);
-              IG[a][b].y = fmaf(c, u[b].y, IG[a][b].y);
-              ID[a][b].x = fmaf(c, v[b].x, ID[a][b].x);
-              ID[a][b].y = fmaf(c, v[b].y, ID[a][b].y);
+              IG[a][b] = __ffma2_rn(c, u[b], IG[a][b]);
+              ID[a][b] = __ffma2_rn(c, v[b], ID[a][b]);
             }
           }
         }
-        // combine: L = jac * (cD * D + cH * (curl.curl S0 - k^2 nn IG))
+        // combine: L = jac/(4pi) * (cD * D + cH * (curl.curl S0 - k^2 nn IG))
+        //            = A1 * ID + A3 * IG + curl.curl * B
         float2 S0 = make_float2(0.f, 0.f);
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
           for (int b = 0; b < 3; ++b) S0 = cadd(S0, IG[a][b]);
-        const float nn = fmaf(F.normal[0], ng[0], fmaf(F.normal[1], ng[1], F.normal[2] * ng[2]));
-        const float jac = F.area2 * a2g;
+        const float2 A1 = make_float2(jac * p.cD.x, jac * p.cD.y);
+        const float2 A2 = make_float2(jac * p.cH.x, jac * p.cH.y);
         const float kk_nn = p.k2 * nn;
+        const float2 A3 = make_float2(-kk_nn * A2.x, -kk_nn * A2.y);
+        const float2 Bc = cmul(A2, S0);
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
           const float cf0 = F.curls[3 * a], cf1 = F.curls[3 * a + 1], cf2 = F.curls[3 * a + 2];
 #pragma unroll
           for (int b = 0; b < 3; ++b) {
             const float cc = fmaf(cf0, cg[3 * b], fmaf(cf1, cg[3 * b + 1], cf2 * cg[3 * b + 2]));
-            float2 H = make_float2(cc * S0.x - kk_nn * IG[a][b].x, cc * S0.y - kk_nn * IG[a][b].y);
-            float2 L = cadd(cmul(p.cD, ID[a][b]), cmul(p.cH, H));
+            const float2 d = ID[a][b], i = IG[a][b];
             float2* dst = &acc[b * max_rows + s.loc[a]];
             float2 o = *dst;
-            o.x = fmaf(jac, L.x, o.x);
-            o.y = fmaf(jac, L.y, o.y);
+            o.x += fmaf(A1.x, d.x, fmaf(-A1.y, d.y, fmaf(A3.x, i.x, fmaf(-A3.y, i.y, cc * Bc.x))));
+            o.y += fmaf(A1.x, d.y, fmaf(A1.y, d.x, fmaf(A3.x, i.y, fmaf(A3.y, i.x, cc * Bc.y))));
             *dst = o;
           }
         }
@@ -886,9 +945,10 @@ cudaError_t launch_regular(const DeviceMesh& m, Precision prec, double k, double
     p.kdf = make_df(k);
     p.k = (float)k;
     p.k2 = (float)(k * k);
+    p.kturn = (float)(k / (2.0 * M_PI));
     p.cD = f2(cD);
     p.cH = f2(cH);
-    for (int i = 0; i < 3 * kMaxQ; ++i) p.cw[i] = (float)m.rule_cw[i];
+    for (int i = 0; i < 3 * kMaxQ; ++i) p.cw2[i] = make_float2((float)m.rule_cw[i], (float)m.rule_cw[i]);
     size_t sm = (size_t)W * 3 * m.max_tile_rows * sizeof(float2);
     auto launch = [&](auto kern) {
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);

@@ -74,11 +74,16 @@ BEM_D df df_mul_f(df a, float b) {
   p.lo = fmaf(a.lo, b, p.lo);
   return quick_two_sum(p.hi, p.lo);
 }
-// sqrt of a positive df: one Newton step on the FP32 root.
+// sqrt of a positive df: one Newton step on an FP32 root taken from the
+// approximate reciprocal root.  The step removes the root's error to second
+// order (relative error about 2^-44); a.hi <= 0 gives 0.
+BEM_D float rsqrt_ftz(float x);
 BEM_D df df_sqrt(df a) {
-  float s = sqrtf(a.hi);
+  if (!(a.hi > 0.0f)) return {0.0f, 0.0f};
+  const float y = rsqrt_ftz(a.hi);
+  const float s = a.hi * y;
   df s2 = two_prod(s, s);
-  float r = ((a.hi - s2.hi) - s2.lo + a.lo) / (2.0f * s);
+  float r = ((a.hi - s2.hi) - s2.lo + a.lo) * (0.5f * y);
   return quick_two_sum(s, r);
 }
 
@@ -88,6 +93,33 @@ BEM_D df df_sqrt(df a) {
 #define BEM_TWO_PI_LO -6.8604980400235275e-15f
 #define BEM_INV_TWO_PI 0.159154943091895336f
 #define BEM_INV_FOUR_PI 0.0795774715459476678f
+
+// Single-instruction approximations (PTX .approx.ftz: subnormal inputs and
+// results flush to zero).  The library is built without -ftz, and the non-ftz
+// forms of these PTX instructions carry subnormal handling around each one; the
+// hot loops only apply them to arguments clamped well away from the subnormal
+// range (r^2 >= 1e-30, |angle| <= pi + 1e-6).  Documented accuracy (PTX ISA):
+// rsqrt/rcp about 2^-22 relative (rcp: 1 ulp), sin/cos 2^-20.5 absolute on [-pi, pi].
+BEM_D float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+BEM_D float rcp_ftz(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+BEM_D void sincos_ftz(float x, float* s, float* c) {
+  asm("sin.approx.ftz.f32 %0, %1;" : "=f"(*s) : "f"(x));
+  asm("cos.approx.ftz.f32 %0, %1;" : "=f"(*c) : "f"(x));
+}
+// Nearest integer of |x| < 2^22 on the FMA pipe: adding 1.5 * 2^23 rounds away
+// every fraction bit (round to nearest even); subtracting it back is exact.
+BEM_D float round_nearest_small(float x) {
+  const float kMagic = 12582912.0f;
+  return (x + kMagic) - kMagic;
+}
 
 // theta = a - 2*pi*rint(a / 2pi) for a df angle; the result lies in [-pi, pi]
 // and is accurate to about 2^-44 * |a| + 2^-24.
@@ -101,7 +133,7 @@ BEM_D float df_reduce_two_pi(df a) {
 
 // Reduce an FP32 angle of moderate size (|t| < 2^20) into [-pi, pi].
 BEM_D float reduce_two_pi(float t) {
-  float n = rintf(t * BEM_INV_TWO_PI);
+  float n = round_nearest_small(t * BEM_INV_TWO_PI);
   t = fmaf(-n, BEM_TWO_PI_HI, t);
   return fmaf(-n, BEM_TWO_PI_MID, t);
 }

@@ -111,14 +111,14 @@ __global__ void __launch_bounds__(256) field_f32_kernel(const FaceF32* __restric
       const float d[3] = {F.off[3 * n], F.off[3 * n + 1], F.off[3 * n + 2]};
       const float rv[3] = {Cf[0] + d[0], Cf[1] + d[1], Cf[2] + d[2]};
       const float rr = fmaf(rv[0], rv[0], fmaf(rv[1], rv[1], rv[2] * rv[2]));
-      const float rinv = rr > 0.f ? rsqrtf(rr) : 0.f;
+      const float rinv = rr > 1e-30f ? rsqrt_ftz(rr) : 0.f;
       const float r = rr * rinv;
       const float cd = fmaf(Cf[0], d[0], fmaf(Cf[1], d[1], Cf[2] * d[2]));
       const float dd = fmaf(d[0], d[0], fmaf(d[1], d[1], d[2] * d[2]));
-      const float delta = __fdividef(fmaf(2.f, cd, dd), fmaxf(r + R0, 1e-30f));
+      const float delta = fmaf(2.f, cd, dd) * rcp_ftz(fmaxf(r + R0, 1e-30f));
       const float th = reduce_two_pi(fmaf(k, delta, theta0));
       float sn, cs;
-      __sincosf(th, &sn, &cs);
+      sincos_ftz(th, &sn, &cs);
       const float sc = rinv * BEM_INV_FOUR_PI;
       const float2 G = make_float2(cs * sc, sn * sc);
       const float t = fmaf(rv[0], F.normal[0], fmaf(rv[1], F.normal[1], rv[2] * F.normal[2])) * rinv;

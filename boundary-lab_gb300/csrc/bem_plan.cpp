@@ -204,6 +204,128 @@ void rcb(std::vector<int>& ids, int lo, int hi, const std::vector<double>& cent,
 
 }  // namespace
 
+// Pack faces (given by their three tile-local vertex rows) into groups of at
+// most kLanes faces in which no two faces share a vertex.  Target: the minimum
+// ceil(n / kLanes) groups.  Faces are dealt round-robin (consecutive faces of a
+// spatially ordered tile are often neighbours, so this spreads them), each to
+// the first group from its own start that has room and no shared vertex; a
+// face that fits nowhere is placed through a chain of displacements (below),
+// and otherwise opens an extra group.
+// Returns groups of indices into `fl`.
+static std::vector<std::vector<int>> pack_lane_groups(const std::vector<std::array<int, 3>>& fl, int n_rows) {
+  const int n = (int)fl.size();
+  const int G = std::max(1, (n + kLanes - 1) / kLanes);
+  std::vector<std::vector<int>> groups(G);
+  std::vector<std::vector<int>> owner(G, std::vector<int>(n_rows, -1));  // row -> face in group
+  // distinct faces of group g sharing a vertex with f: 0, 1 (that face in *who) or 2 (two or more)
+  auto clashes = [&](int g, int f, int* who) {
+    int first = -1;
+    for (int a = 0; a < 3; ++a) {
+      const int o = owner[g][fl[f][a]];
+      if (o < 0) continue;
+      if (first < 0)
+        first = o;
+      else if (o != first)
+        return 2;
+    }
+    *who = first;
+    return first < 0 ? 0 : 1;
+  };
+  auto put = [&](int g, int f) {
+    groups[g].push_back(f);
+    for (int a = 0; a < 3; ++a) owner[g][fl[f][a]] = f;
+  };
+  auto take = [&](int g, int f) {
+    groups[g].erase(std::find(groups[g].begin(), groups[g].end(), f));
+    for (int a = 0; a < 3; ++a) owner[g][fl[f][a]] = -1;
+  };
+  auto fits = [&](int g, int f) {
+    int who = -1;
+    return (int)groups[g].size() < kLanes && clashes(g, f, &who) == 0;
+  };
+  std::vector<int> left;
+  for (int f = 0; f < n; ++f) {
+    int placed = -1;
+    for (int i = 0; i < G && placed < 0; ++i) {
+      const int g = (f + i) % G;
+      if (fits(g, f)) placed = g;
+    }
+    if (placed >= 0)
+      put(placed, f);
+    else
+      left.push_back(f);
+  }
+  // Augmenting chains: f enters group g1 displacing its single clashing face
+  // y1, y1 enters g2 displacing y2, ..., the last face enters a group with room
+  // and no clash.  Breadth-first over faces, groups distinct along a chain.
+  std::vector<int> group_of(n, -1);
+  for (int g = 0; g < G; ++g)
+    for (int f : groups[g]) group_of[f] = g;
+  std::vector<int> still;
+  std::vector<int> parent(n), via(n), stamp(n, -1);
+  for (int f : left) {
+    std::vector<int> queue{f};
+    stamp[f] = f;
+    parent[f] = -1;
+    via[f] = -1;
+    int end_face = -1, end_group = -1;
+    for (size_t qi = 0; qi < queue.size() && end_face < 0 && queue.size() < 4096; ++qi) {
+      const int x = queue[qi];
+      // groups already on x's chain may not be reused
+      auto on_chain = [&](int g) {
+        for (int y = x; y >= 0; y = parent[y])
+          if (via[y] == g || group_of[y] == g) return true;
+        return false;
+      };
+      for (int g = 0; g < G && end_face < 0; ++g) {
+        if (on_chain(g)) continue;
+        int y = -1;
+        const int c = clashes(g, x, &y);
+        if (c == 0 && (int)groups[g].size() < kLanes) {
+          end_face = x;
+          end_group = g;
+        } else if (c == 1 && stamp[y] != f) {
+          stamp[y] = f;
+          parent[y] = x;
+          via[y] = g;  // y leaves g, x takes its place
+          queue.push_back(y);
+        }
+      }
+    }
+    if (end_face < 0) {
+      still.push_back(f);
+      continue;
+    }
+    // apply from the end: end_face -> end_group, then each displaced face's
+    // predecessor takes its slot
+    int x = end_face, g = end_group;
+    while (x >= 0) {
+      const int from = x == f ? -1 : via[x];  // group x is displaced from
+      if (from >= 0) take(from, x);
+      put(g, x);
+      group_of[x] = g;
+      g = from;
+      x = parent[x];
+    }
+  }
+  // extra groups, first fit
+  for (int f : still) {
+    int placed = -1;
+    for (int g = G; g < (int)groups.size() && placed < 0; ++g)
+      if (fits(g, f)) placed = g;
+    if (placed < 0) {
+      groups.emplace_back();
+      owner.emplace_back(n_rows, -1);
+      placed = (int)groups.size() - 1;
+    }
+    put(placed, f);
+  }
+  std::vector<std::vector<int>> out;
+  for (auto& g : groups)
+    if (!g.empty()) out.push_back(std::move(g));
+  return out;
+}
+
 std::string build_mesh_plan(const double* verts, int nv, const int* faces, int nf, int regular_order,
                             int singular_order, int tile_faces, MeshPlan& P) {
   if (nv <= 0 || nf <= 0) return "mesh must have at least one vertex and one face";
@@ -391,31 +513,18 @@ std::string build_mesh_plan(const double* verts, int nv, const int* faces, int n
     P.halo_row_ptr.push_back((int)h.size());
     if (h.empty()) P.halo_row_ptr.assign(1, 0);
   }
-  // lane groups: first-fit packing of each tile's faces into vertex-disjoint groups of 32
+  // lane groups: each tile's faces packed into ceil(n / 32) vertex-disjoint
+  // groups of 32 where possible (pack_lane_groups), so few lanes idle.
   P.tile_group_ptr.assign(1, 0);
   P.lane_slots.clear();
   for (int t = 0; t < P.n_tiles; ++t) {
-    std::vector<std::vector<int>> groups;
-    std::vector<std::set<int>> gverts;
-    for (int f : tile_face_list[t]) {
-      int placed = -1;
-      for (size_t g = 0; g < groups.size(); ++g) {
-        if (groups[g].size() >= (size_t)kLanes) continue;
-        bool clash = false;
-        for (int a = 0; a < 3 && !clash; ++a) clash = gverts[g].count(faces[3 * f + a]) > 0;
-        if (!clash) {
-          placed = (int)g;
-          break;
-        }
-      }
-      if (placed < 0) {
-        groups.emplace_back();
-        gverts.emplace_back();
-        placed = (int)groups.size() - 1;
-      }
-      groups[placed].push_back(f);
-      for (int a = 0; a < 3; ++a) gverts[placed].insert(faces[3 * f + a]);
-    }
+    std::vector<std::array<int, 3>> fl;
+    fl.reserve(tile_face_list[t].size());
+    for (int f : tile_face_list[t])
+      fl.push_back({tile_loc[t][faces[3 * f]], tile_loc[t][faces[3 * f + 1]], tile_loc[t][faces[3 * f + 2]]});
+    std::vector<std::vector<int>> groups = pack_lane_groups(fl, (int)tile_loc[t].size());
+    for (auto& g : groups)
+      for (int& i : g) i = tile_face_list[t][i];
     for (auto& g : groups) {
       for (int l = 0; l < kLanes; ++l) {
         LaneSlot s;

@@ -1,0 +1,97 @@
+"""Mesh planner checks on the CPU (no GPU): the lane groups of the regular
+assembly kernel.
+
+The regular kernel gives each warp one trial face and its 32 lanes one group of
+test faces, and every lane adds its 3 x 3 block into shared-memory rows of its
+face's vertices without atomics.  That is race-free only if the faces of one
+group share no vertex, i.e. their tile-local rows are pairwise distinct.  The
+planner (boundary-lab_gb300/csrc/bem_plan.cpp) is compiled here with a small
+driver (tests/plan_check.cpp) and its layout checked: every face in exactly one
+slot, rows distinct within a group and inside the tile, and the groups packed
+close to the lower bound max(ceil(faces / 32), largest vertex valence) per tile.
+"""
+
+import shutil
+import subprocess
+from collections import defaultdict
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import pkg_module
+
+ROOT = Path(__file__).resolve().parents[1]
+CSRC = ROOT / "boundary-lab_gb300" / "csrc"
+meshes = pkg_module("meshes")
+
+
+@pytest.fixture(scope="module")
+def plan_tool(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    exe = tmp_path_factory.mktemp("plan") / "plan_check"
+    subprocess.run(["g++", "-O2", "-std=c++17", f"-I{CSRC}", str(ROOT / "tests" / "plan_check.cpp"),
+                    str(CSRC / "bem_plan.cpp"), "-o", str(exe)], check=True, capture_output=True)
+    return exe
+
+
+def run_plan(tool, tmp_path, mesh, tile_faces=512):
+    path = tmp_path / "mesh.bin"
+    with open(path, "wb") as f:
+        np.array([mesh.n_vertices, len(mesh.faces)], np.int32).tofile(f)
+        np.ascontiguousarray(mesh.vertices, np.float64).tofile(f)
+        np.ascontiguousarray(mesh.faces, np.int32).tofile(f)
+    out = subprocess.run([str(tool), str(path), str(tile_faces)], check=True, capture_output=True, text=True).stdout
+    tiles = []
+    for line in out.splitlines():
+        w = line.split()
+        if w[0] == "tile":
+            tiles.append({"rows": int(w[3]), "groups": int(w[5]), "slots": defaultdict(list)})
+        elif w[0] == "slot":
+            g, face, *loc = map(int, w[1:])
+            tiles[-1]["slots"][g].append((face, loc))
+    return tiles
+
+
+def make_mesh(name, faces):
+    if name == "sphere":
+        return meshes.sphere_with_cap(0.1, 3, 30.0)
+    if name == "seeded":
+        return meshes.seeded_piston_mesh(faces, 7)
+    return meshes.box_with_piston((0.3, 0.2, 0.25), faces, 0.05, "+z")
+
+
+@pytest.mark.parametrize("name,faces,tile_faces", [
+    ("sphere", 1280, 512),
+    ("seeded", 3000, 512),
+    ("box", 5000, 512),
+    ("box", 10000, 512),
+    ("box", 10000, 256),
+])
+def test_lane_groups_are_vertex_disjoint_and_dense(plan_tool, tmp_path, name, faces, tile_faces):
+    mesh = make_mesh(name, faces)
+    tiles = run_plan(plan_tool, tmp_path, mesh, tile_faces)
+    seen = np.zeros(len(mesh.faces), dtype=int)
+    total_groups = minimum = 0
+    for t in tiles:
+        n_tile = 0
+        valence = defaultdict(int)
+        for g, members in t["slots"].items():
+            assert 1 <= len(members) <= 32
+            rows = [r for _, loc in members for r in loc]
+            assert len(set(rows)) == len(rows), f"group {g} shares a vertex row"
+            assert all(0 <= r < t["rows"] for r in rows)
+            for face, loc in members:
+                seen[face] += 1
+                for r in loc:
+                    valence[r] += 1
+            n_tile += len(members)
+        total_groups += t["groups"]
+        # lower bound: 32 faces per group, and the faces around one vertex in distinct groups
+        minimum += max(-(-n_tile // 32), max(valence.values()))
+    assert np.all(seen == 1), "every face in exactly one lane slot"
+    # 512-face tiles (the production size) pack to within a group or so of the
+    # bound; small tiles leave the packer fewer groups to trade faces between
+    slack = max(1, len(tiles) // 10) if tile_faces >= 512 else int(0.15 * minimum)
+    assert total_groups <= minimum + slack, (total_groups, minimum)
