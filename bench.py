@@ -188,6 +188,9 @@ def main() -> None:
     ap.add_argument("--cpu-baseline", type=int, default=1, help="frequencies timed on the host for cpu_baseline")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-extras", action="store_true", help="skip FP64 form, e2e and CPU baseline (profiling runs)")
+    ap.add_argument("--serving-jobs", type=int, default=40, help="jobs in the seeded Poisson serving stream (0: skip)")
+    ap.add_argument("--serving-rate", type=float, default=20.0, help="serving arrivals per second")
+    ap.add_argument("--serving-running", type=int, default=4, help="concurrent jobs on the GPU")
     ap.add_argument("--lu-gemm", type=int, default=0, choices=[0, 1, 2],
                     help="LU trailing update: 0 automatic, 1 cuBLAS cgemm, 2 tcgen05 3xTF32")
     args = ap.parse_args()
@@ -361,11 +364,19 @@ def main() -> None:
                 "sample": f"{len(ts)} frequency of the same workload: FP32 restatement of BEAT CPU assembly "
                           "(colored OpenMP), BM system, LAPACK cgetrf/cgetrs, field",
             }
-    # gpu_launches: our kernels per step (see the design doc for the count per stage)
+        # serving stream: seeded Poisson arrivals of mixed-size jobs, latency per job
+        if args.serving_jobs > 0:
+            result["serving"] = serving_run(args, local_rank)
+    # gpu_launches: our kernels per timed step.  Per batch of B frequencies with
+    # P = ceil(n/64) panels and R refinement steps: 6 assembly kernels per
+    # frequency; LU 6P - 4 (panel, swap, trsm, operand split x2, tcgen05 update)
+    # or 3P - 1 with the cuBLAS update; permutation, FP64 copy, 5 (R + 1) solve /
+    # residual kernels, 2 field kernels.
     nv = mesh.n_vertices
     panels = (nv + 63) // 64
     refine = result["refine_steps_max"]
-    per_batch = 6 * B + (3 * panels - 1) + (5 + 5 * refine) + 2
+    lu = 6 * panels - 4 if stats_list[0]["lu_gemm_used"] == 2 else 3 * panels - 1
+    per_batch = 6 * B + lu + 2 + 5 * (refine + 1) + 2
     result["gpu_launches"] = per_batch * args.steps
     m.release()
     ctx.close()
@@ -373,6 +384,24 @@ def main() -> None:
         print(json.dumps(result))
     if dist:
         dist.destroy_process_group()
+
+
+def serving_run(args, device: int) -> dict:
+    """The serving stream (seeded Poisson arrivals, sizes 1k-15k triangles, 1-32
+    frequencies each) replayed twice on the same GPU: with the GB300 scheduler
+    (concurrent jobs, smallest-work-first with aging) and one job at a time in
+    arrival order, the reference server's per-GPU policy."""
+    serving = pkg("serving")
+    out = {"stream": f"{args.serving_jobs} jobs, Poisson {args.serving_rate:g}/s (seed 0), sizes uniform over "
+                     "{1k, 2k, 5k, 10k, 15k} triangles (box or cube-sphere, seeded piston), 1-32 log-spaced "
+                     "freqs in 100 Hz-8 kHz, 2x73 polar + 1000 Fibonacci points; latency = arrival to last "
+                     "result, mixed form"}
+    for name, running, policy in (("gb300_scheduler", args.serving_running, "sjf"), ("one_job_at_a_time_fifo", 1, "fifo")):
+        stream = serving.poisson_jobs(args.serving_jobs, args.serving_rate, seed=0)
+        with serving.ServingScheduler(device, max_running=running, policy=policy) as sch:
+            jobs = serving.replay(sch, stream, timeout_s=900)
+        out[name] = {"max_running": running, "policy": policy, **serving.latency_summary(jobs)}
+    return out
 
 
 if __name__ == "__main__":

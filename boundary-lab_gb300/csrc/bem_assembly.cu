@@ -22,11 +22,27 @@
 //                         trial face: deterministic, no atomics)
 //   gather_columns        A[:, j] = sum over (g, b) in star(j) of Rext[g*3+b],
 //                         then halo extended rows folded into their rows
+#include <map>
+#include <mutex>
+
 #include "bem_common.cuh"
 #include "bem_internal.h"
 #include "bem_kernels.h"
 
 namespace bem {
+
+bool ensure_smem_limit(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> limit;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = limit[{dev, func}];
+  if (bytes <= std::max<size_t>(cur, 48 * 1024)) return true;
+  if (cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) return false;
+  cur = bytes;
+  return true;
+}
 
 namespace {
 
@@ -951,7 +967,7 @@ cudaError_t launch_regular(const DeviceMesh& m, Precision prec, double k, double
     for (int i = 0; i < 3 * kMaxQ; ++i) p.cw2[i] = make_float2((float)m.rule_cw[i], (float)m.rule_cw[i]);
     size_t sm = (size_t)W * 3 * m.max_tile_rows * sizeof(float2);
     auto launch = [&](auto kern) {
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      ensure_smem_limit((const void*)kern, sm);
       kern<<<grid, W * 32, sm, stream>>>(m.faces32, m.nf, m.tile_group_ptr, m.lane_slots, m.tile_row_base,
                                          m.max_tile_rows, (float2*)Rext, ldR, p);
     };
@@ -970,7 +986,7 @@ cudaError_t launch_regular(const DeviceMesh& m, Precision prec, double k, double
     for (int i = 0; i < 3 * kMaxQ; ++i) p.cw[i] = m.rule_cw[i];
     size_t sm = (size_t)W * 3 * m.max_tile_rows * sizeof(double2);
     auto launch = [&](auto kern) {
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      ensure_smem_limit((const void*)kern, sm);
       kern<<<grid, W * 32, sm, stream>>>(m.faces64, m.nf, m.tile_group_ptr, m.lane_slots, m.tile_row_base,
                                          m.max_tile_rows, (double2*)Rext, ldR, p);
     };
@@ -1049,7 +1065,7 @@ cudaError_t launch_gather(const DeviceMesh& m, Precision prec, const void* Rext,
   const int n_halo = m.n_halo;
   if (prec == Precision::Mixed) {
     size_t sm = (size_t)std::max(1, n_halo) * sizeof(float2);
-    if (sm > 48 * 1024) cudaFuncSetAttribute(gather_columns_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (sm > 48 * 1024) ensure_smem_limit((const void*)gather_columns_kernel<float2>, sm);
     gather_columns_kernel<float2><<<m.nv, threads, sm, stream>>>(
         (const float2*)Rext, ldR, m.col_ptr, m.col_fb, m.ext_row, m.halo_slot_of_ext, m.halo_row_ptr, m.halo_row,
         m.n_ext, m.n_halo_rows, (float2*)A, lda, (float2*)A2, 0);
@@ -1058,7 +1074,7 @@ cudaError_t launch_gather(const DeviceMesh& m, Precision prec, const void* Rext,
           m.isolated, m.n_isolated, m.vertex_row, (float2*)A, lda, (float2*)A2);
   } else {
     size_t sm = (size_t)std::max(1, n_halo) * sizeof(double2);
-    if (sm > 48 * 1024) cudaFuncSetAttribute(gather_columns_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (sm > 48 * 1024) ensure_smem_limit((const void*)gather_columns_kernel<double2>, sm);
     gather_columns_kernel<double2><<<m.nv, threads, sm, stream>>>(
         (const double2*)Rext, ldR, m.col_ptr, m.col_fb, m.ext_row, m.halo_slot_of_ext, m.halo_row_ptr,
         m.halo_row, m.n_ext, m.n_halo_rows, (double2*)A, lda, (double2*)A2, 0);

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <exception>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "../../include/gb300_bem.h"
@@ -16,20 +17,48 @@
 
 namespace {
 
+// Library memory pool of one device.  Every device allocation of the library
+// is stream-ordered (cudaMallocFromPoolAsync / cudaFreeAsync on the owning
+// context's stream): unlike cudaMalloc / cudaFree it implies no device-wide
+// synchronisation, so contexts on different streams keep running concurrently
+// while one of them grows or frees its scratch.  Freed memory stays cached in
+// the pool (no release threshold) until bem_trim_context trims it.
+cudaMemPool_t device_pool(int device) {
+  static std::mutex mu;
+  static std::vector<cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)pools.size() <= device) pools.resize(device + 1, nullptr);
+  if (!pools[device]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) return nullptr;
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[device] = pool;
+  }
+  return pools[device];
+}
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  cudaStream_t stream = nullptr;  // owning stream (set by the owner before first use)
+  cudaMemPool_t pool = nullptr;
   cudaError_t ensure(size_t n) {
     if (n <= bytes) return cudaSuccess;
-    if (p) cudaFree(p);
+    if (!pool) return cudaErrorInitializationError;
+    if (p) cudaFreeAsync(p, stream);
     p = nullptr;
     bytes = 0;
-    cudaError_t e = cudaMalloc(&p, n);
+    cudaError_t e = cudaMallocFromPoolAsync(&p, n, pool, stream);
     if (e == cudaSuccess) bytes = n;
     return e;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, stream);
     p = nullptr;
     bytes = 0;
   }
@@ -53,7 +82,12 @@ struct bem_context {
   cudaStream_t stream = nullptr;
   cublasHandle_t cublas = nullptr;
   std::string err;
+  cudaMemPool_t pool = nullptr;
   DevBuf rext, mats, mats2, ipiv, perm, info, sblocks, rb, b32, b64, x64, r64, d32, fsrc, fout, norms, pout, tcws;
+  std::vector<DevBuf*> scratch() {
+    return {&rext, &mats, &mats2, &ipiv, &perm, &info, &sblocks, &rb, &b32, &b64, &x64, &r64, &d32, &fsrc, &fout, &norms,
+            &pout, &tcws};
+  }
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<bem_mesh*> meshes;
   // optional per-kernel-family timing (options.profile)
@@ -77,11 +111,16 @@ struct bem_mesh {
 
 namespace {
 
+void* mesh_alloc(bem_mesh* m, size_t bytes, const char* what) {
+  void* p = nullptr;
+  ck(cudaMallocFromPoolAsync(&p, bytes, m->ctx->pool, m->ctx->stream), what);
+  m->allocs.push_back(p);
+  return p;
+}
+
 template <typename T> T* upload(bem_mesh* m, const std::vector<T>& v) {
   if (v.empty()) return nullptr;
-  void* p = nullptr;
-  ck(cudaMalloc(&p, v.size() * sizeof(T)), "cudaMalloc(mesh)");
-  m->allocs.push_back(p);
+  void* p = mesh_alloc(m, v.size() * sizeof(T), "allocate mesh data");
   ck(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, m->ctx->stream), "upload");
   return (T*)p;
 }
@@ -193,7 +232,7 @@ void assemble_one(bem_mesh* m, bem::Precision prec, double k, const bem::Operato
 }
 
 void free_mesh_device(bem_mesh* m) {
-  for (void* p : m->allocs) cudaFree(p);
+  for (void* p : m->allocs) cudaFreeAsync(p, m->ctx->stream);
   m->allocs.clear();
   m->drive32.release();
   m->drive64.release();
@@ -229,6 +268,17 @@ int bem_create_context(int device, bem_context** out) {
     return BEM_ERR_CUDA;
   }
   cublasSetStream(ctx->cublas, ctx->stream);
+  ctx->pool = device_pool(device);
+  if (!ctx->pool) {
+    cublasDestroy(ctx->cublas);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return BEM_ERR_CUDA;
+  }
+  for (DevBuf* b : ctx->scratch()) {
+    b->stream = ctx->stream;
+    b->pool = ctx->pool;
+  }
   for (auto& e : ctx->ev) cudaEventCreate(&e);
   *out = ctx;
   return BEM_OK;
@@ -243,15 +293,31 @@ void bem_destroy_context(bem_context* ctx) {
     delete m;
   }
   ctx->meshes.clear();
-  for (DevBuf* b : {&ctx->rext, &ctx->mats, &ctx->mats2, &ctx->ipiv, &ctx->info, &ctx->sblocks, &ctx->rb, &ctx->b32,
-                    &ctx->b64, &ctx->x64, &ctx->r64, &ctx->d32, &ctx->fsrc, &ctx->fout, &ctx->norms, &ctx->pout, &ctx->perm, &ctx->tcws})
-    b->release();
+  for (DevBuf* b : ctx->scratch()) b->release();
+  cudaStreamSynchronize(ctx->stream);
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : ctx->pev) cudaEventDestroy(e);
   if (ctx->cublas) cublasDestroy(ctx->cublas);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
+}
+
+int bem_trim_context(bem_context* ctx) {
+  if (!ctx) return BEM_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&]() -> int {
+    for (DevBuf* b : ctx->scratch()) b->release();
+    ck(cudaStreamSynchronize(ctx->stream), "trim scratch");
+    ck(cudaMemPoolTrimTo(ctx->pool, 0), "trim memory pool");
+    return BEM_OK;
+  });
+}
+
+long long bem_context_scratch_bytes(const bem_context* ctx) {
+  if (!ctx) return -1;
+  long long total = 0;
+  for (DevBuf* b : const_cast<bem_context*>(ctx)->scratch()) total += (long long)b->bytes;
+  return total;
 }
 
 int bem_upload_mesh(bem_context* ctx, const double* vertices, int n_vertices, const int* faces, int n_faces,
@@ -262,6 +328,10 @@ int bem_upload_mesh(bem_context* ctx, const double* vertices, int n_vertices, co
     *out = nullptr;
     bem_mesh* m = new bem_mesh();
     m->ctx = ctx;
+    for (DevBuf* b : {&m->drive32, &m->drive64, &m->obs, &m->driven}) {
+      b->stream = ctx->stream;
+      b->pool = ctx->pool;
+    }
     std::string e = bem::build_mesh_plan(vertices, n_vertices, faces, n_faces, regular_order, singular_order, 512, m->plan);
     if (!e.empty()) {
       delete m;
@@ -324,10 +394,7 @@ int bem_upload_mesh(bem_context* ctx, const double* vertices, int n_vertices, co
       }
       for (const auto& sp : P.pairs) m->singular_points += P.rule_ptr[sp.rule + 1] - P.rule_ptr[sp.rule];
       if (d.npairs > 0) {
-        void* mom = nullptr;
-        ck(cudaMalloc(&mom, (size_t)d.npairs * 24 * sizeof(double)), "cudaMalloc(moments)");
-        m->allocs.push_back(mom);
-        d.moments = (double*)mom;
+        d.moments = (double*)mesh_alloc(m, (size_t)d.npairs * 24 * sizeof(double), "allocate singular moments");
         ck(bem::launch_singular_static(d, d.moments, ctx->stream), "singular moments kernel");
       }
       ck(cudaStreamSynchronize(ctx->stream), "mesh upload");
@@ -384,10 +451,14 @@ int bem_set_excitation(bem_mesh* m, const double* unit_drive, int n_rhs) {
     ck(m->drive32.ensure(d32.size() * sizeof(float2)), "alloc drive");
     ck(m->drive64.ensure(d64.size() * sizeof(double2)), "alloc drive");
     ck(m->driven.ensure(std::max<size_t>(1, driven.size()) * sizeof(int)), "alloc driven");
-    ck(cudaMemcpy(m->drive32.p, d32.data(), d32.size() * sizeof(float2), cudaMemcpyHostToDevice), "copy drive");
-    ck(cudaMemcpy(m->drive64.p, d64.data(), d64.size() * sizeof(double2), cudaMemcpyHostToDevice), "copy drive");
+    ck(cudaMemcpyAsync(m->drive32.p, d32.data(), d32.size() * sizeof(float2), cudaMemcpyHostToDevice, ctx->stream),
+       "copy drive");
+    ck(cudaMemcpyAsync(m->drive64.p, d64.data(), d64.size() * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream),
+       "copy drive");
     if (!driven.empty())
-      ck(cudaMemcpy(m->driven.p, driven.data(), driven.size() * sizeof(int), cudaMemcpyHostToDevice), "copy driven");
+      ck(cudaMemcpyAsync(m->driven.p, driven.data(), driven.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream),
+         "copy driven");
+    ck(cudaStreamSynchronize(ctx->stream), "copy drive");
     m->dm.driven = (int*)m->driven.p;
     m->dm.ndriven = (int)driven.size();
     m->nc = n_rhs;
@@ -404,7 +475,9 @@ int bem_set_observation_points(bem_mesh* m, const double* points, int n_points) 
       if (!std::isfinite(points[i])) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "observation points must be finite");
     ck(cudaStreamSynchronize(ctx->stream), "sync");
     ck(m->obs.ensure((size_t)n_points * 3 * sizeof(double)), "alloc observation points");
-    ck(cudaMemcpy(m->obs.p, points, (size_t)n_points * 3 * sizeof(double), cudaMemcpyHostToDevice), "copy points");
+    ck(cudaMemcpyAsync(m->obs.p, points, (size_t)n_points * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+       "copy points");
+    ck(cudaStreamSynchronize(ctx->stream), "copy points");
     m->nobs = n_points;
     return BEM_OK;
   });
@@ -577,7 +650,8 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       ck(cudaStreamSynchronize(ctx->stream), "solve sync");
       if (used_tensor && tc_err) {
         int h = 0;
-        ck(cudaMemcpy(&h, tc_err, sizeof(int), cudaMemcpyDeviceToHost), "read tensor-core status");
+        ck(cudaMemcpyAsync(&h, tc_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "read tensor-core status");
+      ck(cudaStreamSynchronize(ctx->stream), "read tensor-core status");
         if (h != 0)
           return fail(ctx, BEM_ERR_CUDA, "tensor-core LU update gave up waiting (status " + std::to_string(h) + ")");
       }
@@ -687,7 +761,8 @@ int bem_lu_factor_dense(bem_context* ctx, int n, double* a, int* ipiv, int preci
     ck(cudaStreamSynchronize(ctx->stream), "sync");
     if (used_tensor && tc_err) {
       int h = 0;
-      ck(cudaMemcpy(&h, tc_err, sizeof(int), cudaMemcpyDeviceToHost), "read tensor-core status");
+      ck(cudaMemcpyAsync(&h, tc_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "read tensor-core status");
+      ck(cudaStreamSynchronize(ctx->stream), "read tensor-core status");
       if (h != 0) return fail(ctx, BEM_ERR_CUDA, "tensor-core LU update gave up waiting");
     }
     if (lu_gemm == (int)bem::LuGemm::Tensor && mixed && !used_tensor)

@@ -311,19 +311,18 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// Driver entry point of cuTensorMapEncodeTiled, resolved once (thread-safe
+// static initialisation); null when the driver does not provide it.
 EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  static const EncodeTiledFn fn = []() -> EncodeTiledFn {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiledFn)p;
-    else
-      cudaGetLastError();
-  }
+      return (EncodeTiledFn)p;
+    cudaGetLastError();
+    return nullptr;
+  }();
   return fn;
 }
 
@@ -421,11 +420,7 @@ cudaError_t tc_trailing_update(TcGemmPlan* p, float2* A, long long lda, long lon
     prep_b_kernel<<<g, 256, 0, stream>>>(A, lda, strideA, k, k + kb, N, kb, p->cols_pad, p->bhi, p->blo);
   }
   const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(trailing_update_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  if (!ensure_smem_limit((const void*)trailing_update_tf32x3, smem)) return cudaErrorInvalidValue;
   if ((k + kb) & 1) return cudaErrorInvalidValue;  // x coordinate 2 (k + kb) must be a multiple of 4
   dim3 grid(rows_used / TM, cols_used / TN, p->batch);
   trailing_update_tf32x3<<<grid, 128, smem, stream>>>(p->mahi, p->malo, p->mbhi, p->mblo, p->mc, 2 * (k + kb), k + kb,

@@ -10,6 +10,14 @@
 
 namespace bem {
 
+// Raise a kernel's dynamic shared-memory limit (cudaFuncAttributeMaxDynamic-
+// SharedMemorySize) to at least `bytes` on the current device.  The attribute
+// belongs to the function, process-wide: contexts on other threads launch the
+// same kernels with other sizes, so the limit only ever grows (under a lock) and
+// a concurrent caller can never lower it between another's set and launch.
+bool ensure_smem_limit(const void* func, size_t bytes);
+
+
 enum class Precision : int { FP64 = 0, Mixed = 1 };
 
 // Linear-combination coefficients.  LHS = cD*D + cH*H + cM*M11;

@@ -408,7 +408,7 @@ cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int
       dim3 g((rest + tpb - 1) / tpb, batch);
       const size_t sm = (size_t)kb * kb * esz + (size_t)kb * tpb * esz;
       if (mixed) {
-        if (sm > 48 * 1024) cudaFuncSetAttribute(lu_trsm_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (sm > 48 * 1024) ensure_smem_limit((const void*)lu_trsm_kernel<float2>, sm);
         lu_trsm_kernel<float2><<<g, tpb, sm, stream>>>((float2*)A, lda, strideA, n, k, kb);
         if (plan) {
           cudaError_t e = tc_trailing_update(plan, (float2*)A, lda, strideA, n, k, kb, stream);
@@ -423,7 +423,7 @@ cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int
             (cuComplex*)(base + (k + kb) + (size_t)(k + kb) * lda), (int)lda, strideA, batch);
         if (st != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
       } else {
-        if (sm > 48 * 1024) cudaFuncSetAttribute(lu_trsm_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (sm > 48 * 1024) ensure_smem_limit((const void*)lu_trsm_kernel<double2>, sm);
         lu_trsm_kernel<double2><<<g, tpb, sm, stream>>>((double2*)A, lda, strideA, n, k, kb);
         const cuDoubleComplex alpha = make_cuDoubleComplex(-1.0, 0.0), beta = make_cuDoubleComplex(1.0, 0.0);
         double2* base = (double2*)A;

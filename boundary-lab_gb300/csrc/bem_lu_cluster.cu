@@ -372,7 +372,7 @@ cudaError_t launch_cluster(K kern, dim3 grid, int threads, size_t smem, int cl, 
 
 // Largest cluster size the kernel can be launched with at this shared-memory size.
 template <typename K> int max_cluster(K kern, int threads, size_t smem) {
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+  if (!ensure_smem_limit((const void*)kern, smem)) return 0;
   cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(16, 1);
@@ -439,30 +439,30 @@ cudaError_t lu_panel_cluster(Precision prec, void* A, long long lda, long long s
   if (prec == Precision::Mixed) {
     if (nb == 64) {
       const size_t sm = panel_smem<float, 64>(chunk);
-      cudaFuncSetAttribute(lu_panel_cluster_kernel<float, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      ensure_smem_limit((const void*)lu_panel_cluster_kernel<float, 64>, sm);
       cudaFuncSetAttribute(lu_panel_cluster_kernel<float, 64>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
       return launch_cluster(lu_panel_cluster_kernel<float, 64>, grid, kPanelThreads, sm, cl, stream, args);
     }
     const size_t sm = panel_smem<float, 32>(chunk);
-    cudaFuncSetAttribute(lu_panel_cluster_kernel<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    ensure_smem_limit((const void*)lu_panel_cluster_kernel<float, 32>, sm);
     cudaFuncSetAttribute(lu_panel_cluster_kernel<float, 32>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     return launch_cluster(lu_panel_cluster_kernel<float, 32>, grid, kPanelThreads, sm, cl, stream, args);
   }
   if (nb == 64) {
     const size_t sm = panel_smem<double, 64>(chunk);
-    cudaFuncSetAttribute(lu_panel_cluster_kernel<double, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    ensure_smem_limit((const void*)lu_panel_cluster_kernel<double, 64>, sm);
     cudaFuncSetAttribute(lu_panel_cluster_kernel<double, 64>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     return launch_cluster(lu_panel_cluster_kernel<double, 64>, grid, kPanelThreads, sm, cl, stream, args);
   }
   const size_t sm = panel_smem<double, 32>(chunk);
-  cudaFuncSetAttribute(lu_panel_cluster_kernel<double, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  ensure_smem_limit((const void*)lu_panel_cluster_kernel<double, 32>, sm);
   cudaFuncSetAttribute(lu_panel_cluster_kernel<double, 32>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   return launch_cluster(lu_panel_cluster_kernel<double, 32>, grid, kPanelThreads, sm, cl, stream, args);
 }
 
 cudaError_t lu_perm_batched(const int* ipiv, int n, int batch, int* perm, cudaStream_t stream) {
   const size_t sm = (size_t)n * sizeof(int);
-  if (sm > 48 * 1024) cudaFuncSetAttribute(lu_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (sm > 48 * 1024) ensure_smem_limit((const void*)lu_perm_kernel, sm);
   lu_perm_kernel<<<batch, 256, sm, stream>>>(ipiv, n, perm);
   return cudaGetLastError();
 }
@@ -477,11 +477,11 @@ cudaError_t lu_solve_cluster_batched(Precision prec, const void* LU, long long l
   const size_t sm = (size_t)(chunk + 64) * esz;
   dim3 grid(cl, batch * nrhs);
   if (prec == Precision::Mixed) {
-    cudaFuncSetAttribute(lu_solve_cluster_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    ensure_smem_limit((const void*)lu_solve_cluster_kernel<float>, sm);
     void* args[] = {&LU, &lda, (void*)&strideA, &n, &perm, &B, &ldb, &nrhs, &chunk};
     return launch_cluster(lu_solve_cluster_kernel<float>, grid, kSolveThreads, sm, cl, stream, args);
   }
-  cudaFuncSetAttribute(lu_solve_cluster_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  ensure_smem_limit((const void*)lu_solve_cluster_kernel<double>, sm);
   void* args[] = {&LU, &lda, (void*)&strideA, &n, &perm, &B, &ldb, &nrhs, &chunk};
   return launch_cluster(lu_solve_cluster_kernel<double>, grid, kSolveThreads, sm, cl, stream, args);
 }

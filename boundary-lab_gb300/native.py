@@ -44,6 +44,8 @@ EXPORTED_SYMBOLS = (
     "bem_estimate_device_bytes",
     "bem_evaluate_field_noalloc",
     "bem_lu_factor_dense",
+    "bem_trim_context",
+    "bem_context_scratch_bytes",
 )
 
 
@@ -169,6 +171,10 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         lib.bem_lu_factor_dense.restype = ip
         lib.bem_estimate_device_bytes.argtypes = [ip, ip, ip, ip, ip, ip, ip]
         lib.bem_estimate_device_bytes.restype = ctypes.c_longlong
+        lib.bem_trim_context.argtypes = [vp]
+        lib.bem_trim_context.restype = ip
+        lib.bem_context_scratch_bytes.argtypes = [vp]
+        lib.bem_context_scratch_bytes.restype = ctypes.c_longlong
         # allocation-free field evaluation: every pointer is a caller-owned device buffer
         lib.bem_evaluate_field_noalloc.argtypes = [vp, ip, vp, ip, ip, ctypes.c_double, vp, vp, vp, ip, ip, vp, vp,
                                                    ctypes.c_char_p, ip]
@@ -245,6 +251,15 @@ class Context:
     def estimate_device_bytes(self, n_vertices: int, n_faces: int, n_pairs: int, n_rhs: int, n_points: int,
                               batch: int, precision: int) -> int:
         return int(self._lib.bem_estimate_device_bytes(n_vertices, n_faces, n_pairs, n_rhs, n_points, batch, precision))
+
+    def trim(self) -> None:
+        """Free this context's solve scratch and return unused pool memory (bem_trim_context)."""
+        self._check(self._lib.bem_trim_context(self._h))
+
+    @property
+    def scratch_bytes(self) -> int:
+        """Device bytes of solve scratch this context holds (bem_context_scratch_bytes)."""
+        return int(self._lib.bem_context_scratch_bytes(self._h))
 
 
 class Mesh:

@@ -61,6 +61,17 @@ const char* bem_last_error(const bem_context* ctx);
  * work or record timing events against the library's launches. */
 void* bem_context_stream(const bem_context* ctx);
 
+/* Scratch memory control for schedulers that run several contexts on one GPU
+ * (no direct counterpart in the reference, whose worker frees per-frequency
+ * operator storage with release_operator_storage!, solver.jl:956).  A context
+ * keeps its per-solve scratch (matrices, factors, right-hand sides) between
+ * calls; all library device memory comes from one stream-ordered pool per
+ * device.  bem_trim_context frees the context's scratch, waits for its stream
+ * and returns unused pool memory to the device; uploaded meshes stay valid.
+ * bem_context_scratch_bytes reports the scratch bytes the context holds now. */
+int bem_trim_context(bem_context* ctx);
+long long bem_context_scratch_bytes(const bem_context* ctx);
+
 /* Upload a triangle mesh and build every frequency-independent cache: face
  * geometry and surface curls, the regular rule, singular (vertex-sharing) pair
  * list with remapped Duffy rules, and the FP64 k-independent singular moments.
