@@ -83,10 +83,10 @@ struct bem_context {
   cublasHandle_t cublas = nullptr;
   std::string err;
   cudaMemPool_t pool = nullptr;
-  DevBuf rext, mats, mats2, ipiv, perm, info, sblocks, rb, b32, b64, x64, r64, d32, fsrc, fout, norms, pout, tcws;
+  DevBuf rext, mats, mats2, ipiv, perm, info, sblocks, rb, b32, b64, x64, r64, d32, fsrc, fout, norms, pout, tcws, rowmap;
   std::vector<DevBuf*> scratch() {
     return {&rext, &mats, &mats2, &ipiv, &perm, &info, &sblocks, &rb, &b32, &b64, &x64, &r64, &d32, &fsrc, &fout, &norms,
-            &pout, &tcws};
+            &pout, &tcws, &rowmap};
   }
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<bem_mesh*> meshes;
@@ -508,6 +508,8 @@ long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int np
   bytes += (long long)batch * nrhs * lda * (esz + 3 * 16 + 16);             // rhs, x, r, b64, d
   bytes += (long long)batch * nrhs * ((long long)nf * 6 * esz + (long long)npts * 16);  // field sources + out
   bytes += (long long)nf * (160 + 288 + 64);                                // face records and maps
+  if (precision == BEM_PRECISION_MIXED)                                      // tensor-core update operands
+    bytes += (long long)batch * (2 * round_up(2LL * nv, 128) + 2 * round_up(nv, 256)) * 128 * 4;
   bytes += 64LL << 20;                                                      // cuBLAS workspace and slack
   return bytes;
 }
@@ -548,6 +550,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
     ck(ctx->ipiv.ensure((size_t)B * nv * sizeof(int)), "alloc pivots");
     ck(ctx->perm.ensure((size_t)B * nv * sizeof(int)), "alloc permutation");
     ck(ctx->info.ensure((size_t)B * sizeof(int)), "alloc info");
+    ck(ctx->rowmap.ensure((size_t)B * bem::kRowmapStride * sizeof(int)), "alloc row map");
     const size_t vecn = (size_t)B * nc * L.ldb;
     ck(ctx->b32.ensure(vecn * L.esz), "alloc rhs");
     if (mixed) {
@@ -598,7 +601,8 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
         tcws = ctx->tcws.p;
       }
       ck(bem::lu_factor_batched(prec, ctx->mats.p, L.lda, nv, bt, (int*)ctx->ipiv.p, (int*)ctx->info.p, nb,
-                                ctx->cublas, ctx->stream, (bem::LuGemm)o.lu_gemm, tcws, &used_tensor, &tc_err),
+                                ctx->cublas, ctx->stream, (bem::LuGemm)o.lu_gemm, tcws, &used_tensor, &tc_err,
+                                (int*)ctx->rowmap.p),
          "LU factorisation");
       gemm_used = mixed ? (used_tensor ? 2 : 1) : 0;
       ck(bem::lu_perm_batched((const int*)ctx->ipiv.p, nv, bt, (int*)ctx->perm.p, ctx->stream), "pivot permutation");
@@ -733,6 +737,7 @@ int bem_lu_factor_dense(bem_context* ctx, int n, double* a, int* ipiv, int preci
     ck(ctx->mats.ensure((size_t)lda * n * esz), "alloc matrix");
     ck(ctx->ipiv.ensure((size_t)n * sizeof(int)), "alloc pivots");
     ck(ctx->info.ensure(sizeof(int)), "alloc info");
+    ck(ctx->rowmap.ensure(bem::kRowmapStride * sizeof(int)), "alloc row map");
     std::vector<char> host((size_t)lda * n * esz, 0);
     for (int j = 0; j < n; ++j)
       for (int i = 0; i < n; ++i) {
@@ -752,7 +757,7 @@ int bem_lu_factor_dense(bem_context* ctx, int n, double* a, int* ipiv, int preci
     bool used_tensor = false;
     int* tc_err = nullptr;
     ck(bem::lu_factor_batched(prec, ctx->mats.p, lda, n, 1, (int*)ctx->ipiv.p, (int*)ctx->info.p, 64, ctx->cublas,
-                              ctx->stream, (bem::LuGemm)lu_gemm, tcws, &used_tensor, &tc_err),
+                              ctx->stream, (bem::LuGemm)lu_gemm, tcws, &used_tensor, &tc_err, (int*)ctx->rowmap.p),
        "LU factorisation");
     int info = 0;
     ck(cudaMemcpyAsync(host.data(), ctx->mats.p, host.size(), cudaMemcpyDeviceToHost, ctx->stream), "copy factors");

@@ -13,9 +13,9 @@
 // about 2^-21 relative error per product (FP32 LU quality), so the FP64
 // refinement still converges in one or two steps.
 //
-// Kernel: one CTA (4 warps) per 128 x 256 tile of C'.  A prep kernel writes
-// A'hi, A'lo, B'hi, B'lo as K-major (K contiguous) buffers; TMA brings 32-wide
-// K blocks into 128-byte-swizzled shared memory through a 2-stage mbarrier
+// Kernel: one CTA (4 warps, two CTAs per SM) per 128 x 256 tile of C'.  A prep kernel writes
+// A'hi, A'lo, B'hi, B'lo as K-major (K contiguous) buffers; TMA brings 16-wide
+// K blocks into 64-byte-swizzled shared memory through a 2-stage mbarrier
 // pipeline; one thread issues tcgen05.mma (kind::tf32, M=128, N=256, K=8)
 // into a TMEM accumulator; all four warps read it back with tcgen05.ld, stage
 // -D in shared memory 32 columns at a time (double buffered per warp) and
@@ -42,12 +42,14 @@ namespace {
 
 constexpr int TM = 128;       // tile rows of C' (real rows)
 constexpr int TN = 256;       // tile columns of C'
-constexpr int TK = 32;        // K block per stage (32 fp32 = 128 B rows)
+constexpr int TK = 16;        // K block per stage (16 fp32 = 64 B rows, 64-byte swizzle)
 constexpr int KP = 128;       // K' = 2 * nb, nb <= 64 (zero padded)
 constexpr int STAGES = 2;
-constexpr int A_BYTES = TM * TK * 4;   // 16 KB
-constexpr int B_BYTES = TN * TK * 4;   // 32 KB
-constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi + lo of A and B: 96 KB
+constexpr int A_BYTES = TM * TK * 4;   // 8 KB
+constexpr int B_BYTES = TN * TK * 4;   // 16 KB
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi + lo of A and B: 48 KB
+// Two stages (96 KB) per CTA and 256 TMEM columns: two CTAs share an SM, so one
+// CTA's epilogue (TMA reduce-adds into C) overlaps the other's loads and MMAs.
 constexpr int TMEM_COLS = 256;
 // mbarrier waits give up after kWaitLimit polls with a 1 us suspend hint each
 // (about one second), far above any healthy wait (microseconds).
@@ -86,15 +88,15 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
       : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of
-// 128 B packed in 1024-byte groups of 8 (SBO = 1024 B).
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+// Shared-memory matrix descriptor: K-major operand, 64-byte swizzle, rows of
+// 64 B packed in 512-byte groups of 8 (SBO = 512 B).
+__device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t addr) {
   uint64_t d = 0;
   d |= (uint64_t)((addr >> 4) & 0x3FFF);        // start address
   d |= (uint64_t)1 << 16;                        // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset
+  d |= (uint64_t)(512 >> 4) << 32;               // stride byte offset
   d |= (uint64_t)1 << 46;                        // descriptor version
-  d |= (uint64_t)2 << 61;                        // 128-byte swizzle
+  d |= (uint64_t)4 << 61;                        // 64-byte swizzle
   return d;
 }
 
@@ -190,7 +192,7 @@ __global__ void prep_b_kernel(const float2* __restrict__ A, long long lda, long 
   blo[o] = v - hi;
 }
 
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128, 2)
     trailing_update_tf32x3(const __grid_constant__ CUtensorMap map_ahi, const __grid_constant__ CUtensorMap map_alo,
                            const __grid_constant__ CUtensorMap map_bhi, const __grid_constant__ CUtensorMap map_blo,
                            const __grid_constant__ CUtensorMap map_c, int x0, int y0, int M2, int N, int* err) {
@@ -224,7 +226,7 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
-  const int KB = KP / TK;  // 4 K blocks
+  const int KB = KP / TK;  // 8 K blocks
 
   if (warp == 0 && lane == 0) {
     // TMA producer
@@ -258,9 +260,9 @@ __global__ void __launch_bounds__(128, 1)
       for (int ks = 0; ks < TK / 8; ++ks) {
         const uint32_t off = ks * 32;  // 8 fp32 = 32 bytes along K inside the swizzled row
         const uint32_t acc = (kb > 0 || ks > 0) ? 1u : 0u;
-        mma_tf32(tmem, smem_desc_sw128(a_hi + off), smem_desc_sw128(b_hi + off), acc);
-        mma_tf32(tmem, smem_desc_sw128(a_hi + off), smem_desc_sw128(b_lo + off), 1u);
-        mma_tf32(tmem, smem_desc_sw128(a_lo + off), smem_desc_sw128(b_hi + off), 1u);
+        mma_tf32(tmem, smem_desc_sw64(a_hi + off), smem_desc_sw64(b_hi + off), acc);
+        mma_tf32(tmem, smem_desc_sw64(a_hi + off), smem_desc_sw64(b_lo + off), 1u);
+        mma_tf32(tmem, smem_desc_sw64(a_lo + off), smem_desc_sw64(b_hi + off), 1u);
       }
       mma_commit(&empty_bar[s]);
     }
@@ -334,7 +336,7 @@ bool make_map(CUtensorMap* map, float* buf, int rows_pad, int batch, int box_row
   cuuint32_t box[3] = {(cuuint32_t)TK, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, buf, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 

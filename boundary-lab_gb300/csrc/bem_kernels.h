@@ -94,9 +94,13 @@ int* tc_gemm_error_word(TcGemmPlan* p);
 // Factor `batch` matrices in place.  tc_workspace (tc_gemm_workspace_bytes(n,
 // batch) bytes, may be null) enables the tensor-core update; *used_tensor tells
 // which update ran; *tc_err receives the device address of the kernel's error word.
+// rowmap (batch * kRowmapStride ints, may be null) lets the cluster panel hand
+// the net row permutation of its interchanges to the row-swap kernel.
+constexpr int kRowmapStride = 512;
 cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int batch, int* ipiv, int* info,
                               int nb, void* cublas_handle, cudaStream_t stream, LuGemm gemm = LuGemm::Cublas,
-                              void* tc_workspace = nullptr, bool* used_tensor = nullptr, int** tc_err = nullptr);
+                              void* tc_workspace = nullptr, bool* used_tensor = nullptr, int** tc_err = nullptr,
+                              int* rowmap = nullptr);
 // Solve (LU) X = B in place for nrhs columns per matrix (B stride ldb*nrhs per matrix), working precision.
 cudaError_t lu_solve_batched(Precision prec, const void* LU, long long lda, int n, int batch, const int* ipiv,
                              void* B, long long ldb, int nrhs, int nb, cudaStream_t stream);
@@ -110,8 +114,13 @@ cudaError_t norms_batched(const double2* r, const double2* b, long long ldb, int
 // width (64 or 32) and cluster size for an n x n matrix; false when no cluster
 // configuration fits (then the single-CTA panel is used).
 bool lu_cluster_plan(Precision prec, int n, int* nb, int* cl);
+// rowmap: if not null, receives per matrix [count, (dst row, src row) x count]:
+// the net effect of the panel's kb interchanges on any column (at most 2 kb rows).
 cudaError_t lu_panel_cluster(Precision prec, void* A, long long lda, long long strideA, int n, int k, int kb, int nb,
-                             int cl, int batch, int* ipiv, int* info, cudaStream_t stream);
+                             int cl, int batch, int* ipiv, int* info, cudaStream_t stream, int* rowmap = nullptr);
+// Apply a panel's net row permutation (rowmap) to every column outside the panel.
+cudaError_t lu_swap_rows_batched(Precision prec, void* A, long long lda, long long strideA, int n, int k, int kb,
+                                 int batch, const int* rowmap, cudaStream_t stream);
 // perm[i]: (P b)[i] = b[perm[i]]; then one cluster per right-hand side solves in place.
 cudaError_t lu_perm_batched(const int* ipiv, int n, int batch, int* perm, cudaStream_t stream);
 cudaError_t lu_solve_cluster_batched(Precision prec, const void* LU, long long lda, int n, int batch, const int* perm,

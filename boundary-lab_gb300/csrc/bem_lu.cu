@@ -149,35 +149,62 @@ __global__ void lu_swap_kernel(C2* A, long long lda, long long strideA, int n, i
   }
 }
 
-// U12 = L11^{-1} A12 for columns [k+kb, n); 128 columns per CTA.
+// U12 = L11^{-1} A12 for columns [k+kb, n); blockDim columns per CTA.  The
+// column block is staged through shared memory with coalesced loads and stores
+// (a warp per column, lanes along its rows); the substitution runs one thread
+// per column.  X has a padded row stride so both access patterns are
+// conflict-free.
 template <typename C2>
 __global__ void lu_trsm_kernel(C2* A, long long lda, long long strideA, int n, int k, int kb) {
   extern __shared__ unsigned char smem_raw[];
   C2* L = reinterpret_cast<C2*>(smem_raw);  // kb x kb, column-major
-  C2* X = L + kb * kb;                      // kb x blockDim
+  C2* X = L + kb * kb;                      // kb x (blockDim + 1)
+  const int ldx = blockDim.x + 1;
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   C2* M = A + (size_t)blockIdx.y * strideA;
   for (int i = threadIdx.x; i < kb * kb; i += blockDim.x) {
     const int r = i % kb, c = i / kb;
     L[i] = M[(size_t)(k + c) * lda + k + r];
   }
-  const int col = k + kb + blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = col < n;
-  C2* a = M + (size_t)col * lda + k;
-  if (active)
-    for (int r = 0; r < kb; ++r) X[r * blockDim.x + threadIdx.x] = a[r];
+  const int c0 = k + kb + blockIdx.x * blockDim.x;
+  const int ncol = min((int)blockDim.x, n - c0);
+  // 8 columns x 2 row halves per warp and batch: 16 independent loads in flight
+  for (int cb = wid; cb < ncol; cb += 8 * nw) {
+    C2 v[8][2];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int cl = cb + u * nw, r = lane + 32 * h;
+        if (cl < ncol && r < kb) v[u][h] = M[(size_t)(c0 + cl) * lda + k + r];
+      }
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int cl = cb + u * nw, r = lane + 32 * h;
+        if (cl < ncol && r < kb) X[r * ldx + cl] = v[u][h];
+      }
+  }
   __syncthreads();
-  if (!active) return;
-  for (int j = 0; j < kb; ++j) {
-    const C2 xj = X[j * blockDim.x + threadIdx.x];
-    for (int i = j + 1; i < kb; ++i) {
-      C2 l = L[j * kb + i];
-      C2 v = X[i * blockDim.x + threadIdx.x];
-      v.x -= l.x * xj.x - l.y * xj.y;
-      v.y -= l.x * xj.y + l.y * xj.x;
-      X[i * blockDim.x + threadIdx.x] = v;
+  if ((int)threadIdx.x < ncol) {
+    const int t = threadIdx.x;
+    for (int j = 0; j < kb; ++j) {
+      const C2 xj = X[j * ldx + t];
+      for (int i = j + 1; i < kb; ++i) {
+        const C2 l = L[j * kb + i];
+        C2 v = X[i * ldx + t];
+        v.x -= l.x * xj.x - l.y * xj.y;
+        v.y -= l.x * xj.y + l.y * xj.x;
+        X[i * ldx + t] = v;
+      }
     }
   }
-  for (int r = 0; r < kb; ++r) a[r] = X[r * blockDim.x + threadIdx.x];
+  __syncthreads();
+  for (int cl = wid; cl < ncol; cl += nw) {
+    C2* dst = M + (size_t)(c0 + cl) * lda + k;
+    for (int r = lane; r < kb; r += 32) dst[r] = X[r * ldx + cl];
+  }
 }
 
 // One CTA per (matrix, right-hand side): P, then L (unit lower), then U.
@@ -306,6 +333,70 @@ __global__ void residual_kernel(const C2* __restrict__ A, long long lda, long lo
   r[off + row] = make_double2(bb.x - sr, bb.y - si);
 }
 
+// r = b - A x for an FP32 matrix A and FP64 x (the mixed form's refinement
+// residual) with no FP64 arithmetic in the inner loop: this part's FP64 rate is
+// a small fraction of its FP32 rate.  Per tile of 256 columns, x is split into
+// float pairs x = xh + xl in shared memory; every product a * xh is formed
+// exactly as p + fma(a, xh, -p), the p are summed in double-float (two_sum),
+// and the small terms (product errors and a * xl) in FP32.  The tile sums are
+// added in FP64, so the result carries about 2^-40 relative error per tile:
+// far below the 1e-10 refinement target.
+__device__ __forceinline__ void acc_exact_prod(float& sh, float& sl, float& e, float a, float xh, float xl) {
+  const float p = a * xh;
+  const float pe = fmaf(a, xh, -p);
+  const float t = sh + p;
+  const float bb = t - sh;
+  sl += (sh - (t - bb)) + (p - bb);
+  sh = t;
+  e = fmaf(a, xl, e + pe);
+}
+
+__global__ void __launch_bounds__(256) residual_f32a_kernel(const float2* __restrict__ A, long long lda,
+                                                            long long strideA, int n, const double2* __restrict__ x,
+                                                            const double2* __restrict__ b, long long ldb, int nrhs,
+                                                            double2* __restrict__ r) {
+  __shared__ float4 xs[256];
+  const int row = blockIdx.x * 256 + threadIdx.x;
+  const int mat = blockIdx.y / nrhs, rhs = blockIdx.y % nrhs;
+  const float2* M = A + (size_t)mat * strideA;
+  const size_t off = ((size_t)mat * nrhs + rhs) * ldb;
+  const double2* xv = x + off;
+  double accr = 0.0, acci = 0.0;
+  for (int j0 = 0; j0 < n; j0 += 256) {
+    __syncthreads();
+    {
+      const int j = j0 + threadIdx.x;
+      if (j < n) {
+        const double2 v = xv[j];
+        const float hr = (float)v.x, hi = (float)v.y;
+        xs[threadIdx.x] = make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
+      }
+    }
+    __syncthreads();
+    if (row < n) {
+      const int jn = min(256, n - j0);
+      const float2* col = M + (size_t)j0 * lda + row;
+      float srh = 0.f, srl = 0.f, er = 0.f, sih = 0.f, sil = 0.f, ei = 0.f;
+#pragma unroll 8
+      for (int t = 0; t < jn; ++t) {
+        const float2 a = col[(size_t)t * lda];
+        const float4 xt = xs[t];
+        // re += a.x xr - a.y xi ; im += a.x xi + a.y xr
+        acc_exact_prod(srh, srl, er, a.x, xt.x, xt.z);
+        acc_exact_prod(srh, srl, er, -a.y, xt.y, xt.w);
+        acc_exact_prod(sih, sil, ei, a.x, xt.y, xt.w);
+        acc_exact_prod(sih, sil, ei, a.y, xt.x, xt.z);
+      }
+      accr += (double)srh + ((double)srl + (double)er);
+      acci += (double)sih + ((double)sil + (double)ei);
+    }
+  }
+  if (row < n) {
+    const double2 bb = b[off + row];
+    r[off + row] = make_double2(bb.x - accr, bb.y - acci);
+  }
+}
+
 __global__ void norms_kernel(const double2* __restrict__ r, const double2* __restrict__ b, long long ldb, int n,
                              double* out) {
   const double2* rv = r + (size_t)blockIdx.x * ldb;
@@ -362,7 +453,7 @@ size_t tc_gemm_plan_size();
 
 cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int batch, int* ipiv, int* info, int nb,
                               void* cublas_handle, cudaStream_t stream, LuGemm gemm, void* tc_workspace,
-                              bool* used_tensor, int** tc_err) {
+                              bool* used_tensor, int** tc_err, int* rowmap) {
   cublasHandle_t h = (cublasHandle_t)cublas_handle;
   cublasSetStream(h, stream);
   const long long strideA = lda * (long long)n;
@@ -389,13 +480,16 @@ cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int
   for (int k = 0; k < n; k += nb) {
     const int kb = std::min(nb, n - k);
     if (cluster_panel) {
-      cudaError_t e = lu_panel_cluster(prec, A, lda, strideA, n, k, kb, nb, ccl, batch, ipiv, info, stream);
+      cudaError_t e = lu_panel_cluster(prec, A, lda, strideA, n, k, kb, nb, ccl, batch, ipiv, info, stream, rowmap);
       if (e != cudaSuccess) return e;
     } else if (mixed)
       lu_panel_kernel<float><<<batch, 1024, 0, stream>>>((float2*)A, lda, strideA, n, k, kb, ipiv, info);
     else
       lu_panel_kernel<double><<<batch, 1024, 0, stream>>>((double2*)A, lda, strideA, n, k, kb, ipiv, info);
-    if (n - kb > 0) {
+    if (n - kb > 0 && cluster_panel && rowmap) {
+      cudaError_t e = lu_swap_rows_batched(prec, A, lda, strideA, n, k, kb, batch, rowmap, stream);
+      if (e != cudaSuccess) return e;
+    } else if (n - kb > 0) {
       dim3 g((n - kb + 127) / 128, batch);
       if (mixed)
         lu_swap_kernel<float2><<<g, 128, 0, stream>>>((float2*)A, lda, strideA, n, k, kb, ipiv);
@@ -406,7 +500,7 @@ cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int
     if (rest > 0) {
       const int tpb = 128;
       dim3 g((rest + tpb - 1) / tpb, batch);
-      const size_t sm = (size_t)kb * kb * esz + (size_t)kb * tpb * esz;
+      const size_t sm = (size_t)kb * kb * esz + (size_t)kb * (tpb + 1) * esz;
       if (mixed) {
         if (sm > 48 * 1024) ensure_smem_limit((const void*)lu_trsm_kernel<float2>, sm);
         lu_trsm_kernel<float2><<<g, tpb, sm, stream>>>((float2*)A, lda, strideA, n, k, kb);
@@ -456,7 +550,7 @@ cudaError_t residual_batched(Precision prec, const void* A, long long lda, int n
   const long long strideA = lda * (long long)n;
   dim3 g((n + 255) / 256, batch * nrhs);
   if (prec == Precision::Mixed)
-    residual_kernel<float2><<<g, 256, 0, stream>>>((const float2*)A, lda, strideA, n, x, b, ldb, nrhs, r);
+    residual_f32a_kernel<<<g, 256, 0, stream>>>((const float2*)A, lda, strideA, n, x, b, ldb, nrhs, r);
   else
     residual_kernel<double2><<<g, 256, 0, stream>>>((const double2*)A, lda, strideA, n, x, b, ldb, nrhs, r);
   return cudaGetLastError();

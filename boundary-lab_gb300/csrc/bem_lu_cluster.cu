@@ -2,10 +2,10 @@
 //
 // Panel: the m x nb panel of one matrix is spread over the shared memory of a
 // thread-block cluster (CL CTAs, each holding a contiguous block of panel rows,
-// column-major).  Each column step does a local pivot search, one cluster
-// barrier, a pivot decision from the CL candidates read through distributed
-// shared memory (DSMEM), a second barrier after the two rows to be swapped are
-// staged, then the swap, scaling and rank-1 update entirely in shared memory.
+// column-major).  Each column step does a local pivot search, publishes the
+// CTA's candidate row, one cluster barrier, a pivot decision from the CL
+// candidates read through distributed shared memory (DSMEM), then the swap,
+// scaling and rank-1 update entirely in shared memory.
 // Nothing touches global memory between the initial load and the final store,
 // where the previous single-CTA kernel streamed the whole panel through L2 at
 // every column.  Pivot choice is LAPACK's (first maximum of |re| + |im|).
@@ -47,114 +47,230 @@ template <typename C2> __device__ __forceinline__ C2 inverse(C2 d) {
 
 constexpr int kPanelThreads = 512;
 
+// First maximum of (value, index): larger value wins, ties go to the smaller index
+// (LAPACK's first maximum of |re| + |im| when indices are row numbers).
+template <typename R> __device__ __forceinline__ void argmax_merge(R& b, int& x, R ov, int oi) {
+  if (ov > b || (ov == b && oi < x)) {
+    b = ov;
+    x = oi;
+  }
+}
+template <typename R> __device__ __forceinline__ void warp_argmax(R& b, int& x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) argmax_merge(b, x, __shfl_xor_sync(0xffffffffu, b, o), __shfl_xor_sync(0xffffffffu, x, o));
+}
+
+// Net row permutation of the interchanges (j, pivs[j]), j = 0..kb-1, applied in
+// order (LAPACK laswp): row r of every column ends up holding the data of row
+// src(r).  Computed by one warp: the rows of the diagonal block in top[], other
+// pivot rows in a list searched with a ballot.  Writes [count, (k + r, k + src(r))
+// for every moved row] (at most 2 kb pairs).
+template <int NB> __device__ void net_row_map(const int* pivs, int kb, int k, int* out) {
+  __shared__ int top[NB], erow[NB], econt[NB];
+  const int lane = threadIdx.x & 31;
+  for (int i = lane; i < kb; i += 32) top[i] = i;
+  __syncwarp();
+  int n_ext = 0;
+  for (int j = 0; j < kb; ++j) {
+    const int p = pivs[j];
+    if (p == j) continue;
+    if (p < kb) {
+      if (lane == 0) {
+        const int t = top[j];
+        top[j] = top[p];
+        top[p] = t;
+      }
+      __syncwarp();
+      continue;
+    }
+    int found = -1;
+    for (int base = 0; base < n_ext && found < 0; base += 32) {
+      const int idx = base + lane;
+      const unsigned hit = __ballot_sync(0xffffffffu, idx < n_ext && erow[idx] == p);
+      if (hit) found = base + __ffs(hit) - 1;
+    }
+    if (found < 0) {
+      found = n_ext++;
+      if (lane == 0) {
+        erow[found] = p;
+        econt[found] = p;
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      const int t = top[j];
+      top[j] = econt[found];
+      econt[found] = t;
+    }
+    __syncwarp();
+  }
+  if (lane == 0) {
+    int cnt = 0;
+    for (int r = 0; r < kb; ++r)
+      if (top[r] != r) {
+        out[1 + 2 * cnt] = k + r;
+        out[2 + 2 * cnt] = k + top[r];
+        ++cnt;
+      }
+    for (int e = 0; e < n_ext; ++e)
+      if (econt[e] != erow[e]) {
+        out[1 + 2 * cnt] = k + erow[e];
+        out[2 + 2 * cnt] = k + econt[e];
+        ++cnt;
+      }
+    out[0] = cnt;
+  }
+}
+
+// Apply a net row permutation to the columns outside the panel: one warp per
+// column loads every source row (at most 4 per lane, all in flight), then
+// stores every destination row.
+template <typename C2>
+__global__ void __launch_bounds__(256) lu_swap_rows_kernel(C2* A, long long lda, long long strideA, int n, int k,
+                                                          int kb, const int* rowmap) {
+  __shared__ int sdst[128], ssrc[128];
+  __shared__ int s_cnt;
+  const int* rm = rowmap + (size_t)blockIdx.y * kRowmapStride;
+  if (threadIdx.x == 0) s_cnt = min(max(rm[0], 0), 128);
+  __syncthreads();
+  const int cnt = s_cnt;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    sdst[e] = rm[1 + 2 * e];
+    ssrc[e] = rm[2 + 2 * e];
+  }
+  __syncthreads();
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = blockIdx.x * (blockDim.x >> 5) + wid;
+  if (cnt == 0 || t >= n - kb) return;
+  const int c = t < k ? t : t + kb;
+  C2* a = A + (size_t)blockIdx.y * strideA + (size_t)c * lda;
+  C2 v[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int e = lane + 32 * q;
+    if (e < cnt && (unsigned)ssrc[e] < (unsigned)n) v[q] = a[ssrc[e]];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int e = lane + 32 * q;
+    if (e < cnt && (unsigned)ssrc[e] < (unsigned)n && (unsigned)sdst[e] < (unsigned)n) a[sdst[e]] = v[q];
+  }
+}
+
+// One column step has a single cluster barrier.  Before it, every CTA
+// publishes its local pivot candidate (value, row) and the candidate's whole
+// panel row, and the owner of row j publishes row j, into slot j & 1.  After
+// it, every CTA reads the CL candidates (one lane each), takes the first
+// maximum, copies the winning row and row j from their owners' slots, and
+// finishes the column locally.  A slot is rewritten two columns later, after
+// the next barrier, by which time every CTA has finished reading it.
 template <typename R, int NB>
 __global__ void __launch_bounds__(kPanelThreads) lu_panel_cluster_kernel(typename CT2<R>::C2* A, long long lda,
                                                                          long long strideA, int n, int k, int kb,
-                                                                         int chunk, int* ipiv, int* info) {
+                                                                         int chunk, int* ipiv, int* info,
+                                                                         int* rowmap) {
   typedef typename CT2<R>::C2 C2;
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const int CL = (int)cluster.num_blocks();
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int NW = blockDim.x >> 5;
+  __shared__ int s_pivs[NB];  // pivot row of each column, panel-local (rank 0)
   C2* M = A + (size_t)blockIdx.y * strideA;
   int* piv = ipiv + (size_t)blockIdx.y * n;
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C2* P = reinterpret_cast<C2*>(smem_raw);  // [NB][chunk]
-  C2* prow = P + (size_t)NB * chunk;        // staged pivot row (read by other CTAs)
-  C2* crow = prow + NB;                     // staged diagonal row (read by other CTAs)
-  C2* urow = crow + NB;                     // local copy of the pivot row
-  R* cval = reinterpret_cast<R*>(urow + NB);
-  int* cidx = reinterpret_cast<int*>(cval + 1);
+  C2* P = reinterpret_cast<C2*>(smem_raw);  // [NB][chunk], this CTA's panel rows
+  C2* pub = P + (size_t)NB * chunk;         // [2][NB] published candidate row
+  C2* dg = pub + 2 * NB;                    // [2][NB] published row j (owner of row j)
+  C2* urow = dg + 2 * NB;                   // pivot row after the interchange
+  C2* drow = urow + NB;                     // row j before the interchange
+  R* cval = reinterpret_cast<R*>(drow + NB);         // [2] published candidate value
+  int* cidx = reinterpret_cast<int*>(cval + 2);      // [2] published candidate row
   __shared__ R wval[32];
   __shared__ int widx[32];
-  __shared__ int s_p;
+  __shared__ int s_bi, s_p, s_fallback;
 
   const int m = n - k;
   const int r0 = rank * chunk;
   const int rows = max(0, min(chunk, m - r0));
-  for (int c = 0; c < kb; ++c) {
-    const C2* src = M + (size_t)(k + c) * lda + k + r0;
-    for (int i = tid; i < rows; i += blockDim.x) P[(size_t)c * chunk + i] = src[i];
+  // panel load: each thread owns rows, 16 independent column loads in flight
+  for (int i = tid; i < rows; i += blockDim.x) {
+    const C2* src = M + (size_t)k * lda + k + r0 + i;
+#pragma unroll 16
+    for (int c = 0; c < NB; ++c)
+      if (c < kb) P[(size_t)c * chunk + i] = src[(size_t)c * lda];
   }
   __syncthreads();
 
   for (int j = 0; j < kb; ++j) {
-    // local pivot candidate among panel rows >= j
+    const int s = j & 1;
+    const int owner_j = j / chunk;
+    // local pivot candidate among this CTA's panel rows >= j
     R best = R(-1);
     int bi = INT_MAX;
     const C2* Pj = P + (size_t)j * chunk;
-    for (int i = tid; i < rows; i += blockDim.x) {
-      const int pr = r0 + i;
-      if (pr >= j) {
-        const R v = abs1(Pj[i]);
-        if (v > best || (v == best && pr < bi)) {
-          best = v;
-          bi = pr;
-        }
-      }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const R ov = __shfl_xor_sync(0xffffffffu, best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov > best || (ov == best && oi < bi)) {
-        best = ov;
-        bi = oi;
-      }
-    }
+    for (int i = max(0, j - r0) + tid; i < rows; i += blockDim.x) argmax_merge(best, bi, abs1(Pj[i]), r0 + i);
+    warp_argmax(best, bi);
     if (lane == 0) {
       wval[wid] = best;
       widx[wid] = bi;
     }
     __syncthreads();
-    if (tid == 0) {
-      R b = R(-1);
-      int x = INT_MAX;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
-        if (wval[w] > b || (wval[w] == b && widx[w] < x)) {
-          b = wval[w];
-          x = widx[w];
-        }
-      cval[0] = b;
-      cidx[0] = x;
-    }
-    cluster.sync();  // B1: every CTA's candidate is published
-    if (tid == 0) {
-      R b = R(-1);
-      int x = INT_MAX;
-      for (int q = 0; q < CL; ++q) {
-        const R v = *cluster.map_shared_rank(cval, q);
-        const int ix = *cluster.map_shared_rank(cidx, q);
-        if (v > b || (v == b && ix < x)) {
-          b = v;
-          x = ix;
-        }
+    if (wid == 0) {
+      R b = lane < NW ? wval[lane] : R(-1);
+      int x = lane < NW ? widx[lane] : INT_MAX;
+      warp_argmax(b, x);
+      if (lane == 0) {
+        cval[s] = b;
+        cidx[s] = x;
+        s_bi = x;
       }
-      s_p = (x == INT_MAX) ? j : x;
+    }
+    __syncthreads();
+    const int bi_loc = s_bi;
+    if (bi_loc != INT_MAX)
+      for (int c = tid; c < kb; c += blockDim.x) pub[s * NB + c] = P[(size_t)c * chunk + (bi_loc - r0)];
+    if (rank == owner_j)
+      for (int c = tid; c < kb; c += blockDim.x) dg[s * NB + c] = P[(size_t)c * chunk + (j - r0)];
+    cluster.sync();  // candidates, candidate rows and row j of this column are published
+    if (wid == 0) {
+      R b = R(-1);
+      int x = INT_MAX;
+      if (lane < CL) {
+        b = *cluster.map_shared_rank(cval + s, lane);
+        x = *cluster.map_shared_rank(cidx + s, lane);
+      }
+      warp_argmax(b, x);
+      if (lane == 0) {
+        s_fallback = x == INT_MAX;  // no comparable candidate (all NaN): keep row j
+        s_p = x == INT_MAX ? j : x;
+      }
     }
     __syncthreads();
     const int p = s_p;
-    const int owner_j = j / chunk, owner_p = p / chunk;
-    if (rank == owner_p)
-      for (int c = tid; c < kb; c += blockDim.x) prow[c] = P[(size_t)c * chunk + (p - r0)];
-    if (rank == owner_j)
-      for (int c = tid; c < kb; c += blockDim.x) crow[c] = P[(size_t)c * chunk + (j - r0)];
-    cluster.sync();  // B2: the two rows of the interchange are staged
+    const int owner_p = p / chunk;
     {
-      const C2* rp = cluster.map_shared_rank(prow, owner_p);
-      for (int c = tid; c < kb; c += blockDim.x) urow[c] = rp[c];
+      const C2* src_u = s_fallback ? cluster.map_shared_rank(dg + s * NB, owner_j)
+                                   : cluster.map_shared_rank(pub + s * NB, owner_p);
+      const C2* src_d = cluster.map_shared_rank(dg + s * NB, owner_j);
+      for (int c = tid; c < kb; c += blockDim.x) {
+        urow[c] = src_u[c];
+        drow[c] = src_d[c];
+      }
     }
     __syncthreads();
     if (p != j) {
       if (rank == owner_j)
         for (int c = tid; c < kb; c += blockDim.x) P[(size_t)c * chunk + (j - r0)] = urow[c];
-      if (rank == owner_p) {
-        const C2* rc = cluster.map_shared_rank(crow, owner_j);
-        for (int c = tid; c < kb; c += blockDim.x) P[(size_t)c * chunk + (p - r0)] = rc[c];
-      }
+      if (rank == owner_p)
+        for (int c = tid; c < kb; c += blockDim.x) P[(size_t)c * chunk + (p - r0)] = drow[c];
     }
-    if (rank == 0 && tid == 0) piv[k + j] = k + p;
+    if (rank == 0 && tid == 0) {
+      piv[k + j] = k + p;
+      s_pivs[j] = p;
+    }
     __syncthreads();
     const C2 d = urow[j];
     C2 inv;
@@ -165,25 +281,31 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_cluster_kernel(typenam
     } else {
       inv = inverse(d);
     }
-    for (int i = tid; i < rows; i += blockDim.x) {
-      if (r0 + i <= j) continue;
-      C2 l = cmul(P[(size_t)j * chunk + i], inv);
-      P[(size_t)j * chunk + i] = l;
-#pragma unroll 4
-      for (int c = j + 1; c < kb; ++c) {
-        const C2 u = urow[c];
-        C2 v = P[(size_t)c * chunk + i];
+    const int i0 = min(rows, max(0, j + 1 - r0));  // first local row below the diagonal
+    C2* Pcol = P + (size_t)j * chunk;
+    for (int i = i0 + tid; i < rows; i += blockDim.x) Pcol[i] = cmul(Pcol[i], inv);
+    __syncthreads();
+    // rank-1 update of columns j+1.. : warps take columns, lanes take rows
+    for (int c = j + 1 + wid; c < kb; c += NW) {
+      const C2 u = urow[c];
+      C2* Pc = P + (size_t)c * chunk;
+      for (int i = i0 + lane; i < rows; i += 32) {
+        const C2 l = Pcol[i];
+        C2 v = Pc[i];
         v.x -= l.x * u.x - l.y * u.y;
         v.y -= l.x * u.y + l.y * u.x;
-        P[(size_t)c * chunk + i] = v;
+        Pc[i] = v;
       }
     }
     __syncthreads();
   }
-  for (int c = 0; c < kb; ++c) {
-    C2* dst = M + (size_t)(k + c) * lda + k + r0;
-    for (int i = tid; i < rows; i += blockDim.x) dst[i] = P[(size_t)c * chunk + i];
+  for (int i = tid; i < rows; i += blockDim.x) {
+    C2* dst = M + (size_t)k * lda + k + r0 + i;
+#pragma unroll 16
+    for (int c = 0; c < NB; ++c)
+      if (c < kb) dst[(size_t)c * lda] = P[(size_t)c * chunk + i];
   }
+  if (rank == 0 && wid == 0 && rowmap != nullptr) net_row_map<NB>(s_pivs, kb, k, rowmap + (size_t)blockIdx.y * kRowmapStride);
   cluster.sync();  // no CTA leaves while others may still read its shared memory
 }
 
@@ -390,7 +512,7 @@ constexpr size_t kPanelSmemBudget = 200 * 1024;
 
 template <typename R, int NB> size_t panel_smem(int chunk) {
   typedef typename CT2<R>::C2 C2;
-  return (size_t)NB * chunk * sizeof(C2) + 3 * NB * sizeof(C2) + 64;
+  return (size_t)NB * chunk * sizeof(C2) + 6 * NB * sizeof(C2) + 64;
 }
 
 template <typename R> bool choose_panel(int n, int& nb, int& cl) {
@@ -431,10 +553,10 @@ bool lu_cluster_plan(Precision prec, int n, int* nb, int* cl) {
 }
 
 cudaError_t lu_panel_cluster(Precision prec, void* A, long long lda, long long strideA, int n, int k, int kb, int nb,
-                             int cl, int batch, int* ipiv, int* info, cudaStream_t stream) {
+                             int cl, int batch, int* ipiv, int* info, cudaStream_t stream, int* rowmap) {
   const int m = n - k;
   const int chunk = (m + cl - 1) / cl;
-  void* args[] = {&A, &lda, &strideA, &n, &k, &kb, (void*)&chunk, &ipiv, &info};
+  void* args[] = {&A, &lda, &strideA, &n, &k, &kb, (void*)&chunk, &ipiv, &info, &rowmap};
   dim3 grid(cl, batch);
   if (prec == Precision::Mixed) {
     if (nb == 64) {
@@ -458,6 +580,17 @@ cudaError_t lu_panel_cluster(Precision prec, void* A, long long lda, long long s
   ensure_smem_limit((const void*)lu_panel_cluster_kernel<double, 32>, sm);
   cudaFuncSetAttribute(lu_panel_cluster_kernel<double, 32>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   return launch_cluster(lu_panel_cluster_kernel<double, 32>, grid, kPanelThreads, sm, cl, stream, args);
+}
+
+cudaError_t lu_swap_rows_batched(Precision prec, void* A, long long lda, long long strideA, int n, int k, int kb,
+                                 int batch, const int* rowmap, cudaStream_t stream) {
+  if (n - kb <= 0) return cudaSuccess;
+  dim3 g((unsigned)((n - kb + 7) / 8), batch);
+  if (prec == Precision::Mixed)
+    lu_swap_rows_kernel<float2><<<g, 256, 0, stream>>>((float2*)A, lda, strideA, n, k, kb, rowmap);
+  else
+    lu_swap_rows_kernel<double2><<<g, 256, 0, stream>>>((double2*)A, lda, strideA, n, k, kb, rowmap);
+  return cudaGetLastError();
 }
 
 cudaError_t lu_perm_batched(const int* ipiv, int n, int batch, int* perm, cudaStream_t stream) {
