@@ -121,6 +121,38 @@ BEM_D float round_nearest_small(float x) {
   return (x + kMagic) - kMagic;
 }
 
+// sin x and cos x with RELATIVE accuracy for small |x| (sin(z/2) feeds
+// 1 - cos z = 2 sin^2(z/2), where an absolute-accuracy approximation loses all
+// relative accuracy as z -> 0).  x is reduced by the nearest multiple n*pi (pi
+// split in two floats; each multiple flips both signs), then the Taylor series
+// in x^2: sin to x^13, cos to x^12, coefficients (-1)^j / (2j+1)! and
+// (-1)^j / (2j)!; the truncation error is below 7e-9 on |x| <= pi/2.
+// For |x| < 2^20.
+BEM_D void sincos_taylor(float x, float* s, float* c) {
+  const float n = round_nearest_small(x * 0.318309873342514f);
+  float r = fmaf(-n, 3.14159274101257324f, x);
+  r = fmaf(-n, -8.742278012618954e-08f, r);
+  const float r2 = r * r;
+  float ps = 1.6059043836821613e-10f;
+  ps = fmaf(ps, r2, -2.505210838544172e-08f);
+  ps = fmaf(ps, r2, 2.7557319223985893e-06f);
+  ps = fmaf(ps, r2, -1.984126984126984e-04f);
+  ps = fmaf(ps, r2, 8.333333333333333e-03f);
+  ps = fmaf(ps, r2, -1.6666666666666666e-01f);
+  float sv = fmaf(ps * r2, r, r);
+  float pc = 2.08767569878681e-09f;
+  pc = fmaf(pc, r2, -2.755731922398589e-07f);
+  pc = fmaf(pc, r2, 2.48015873015873e-05f);
+  pc = fmaf(pc, r2, -1.388888888888889e-03f);
+  pc = fmaf(pc, r2, 4.1666666666666664e-02f);
+  pc = fmaf(pc, r2, -0.5f);
+  float cv = fmaf(pc, r2, 1.0f);
+  // (-1)^n from the parity of n (|n| < 2^20, exact in float)
+  const bool odd = (((int)n) & 1) != 0;
+  *s = odd ? -sv : sv;
+  *c = odd ? -cv : cv;
+}
+
 // theta = a - 2*pi*rint(a / 2pi) for a df angle; the result lies in [-pi, pi]
 // and is accurate to about 2^-44 * |a| + 2^-24.
 BEM_D float df_reduce_two_pi(df a) {

@@ -10,8 +10,9 @@
 // (BeatEngineCudaField.jl:102-189).
 //
 // Here: a prologue kernel forms the weighted sources p_s w_s (all frequencies
-// and excitations of a batch), then one CTA per (observation point,
-// frequency) sweeps the faces.  The mixed form uses the same compensated
+// and excitations of a batch), then the FP32 kernel runs one CTA per (32
+// observation points, frequency) and the FP64 kernel one CTA per (observation
+// point, frequency), each sweeping the faces.  The mixed form uses the same compensated
 // phase as the assembly (double-float k|c_g - x| per face, FP32 correction per
 // point), Kahan-compensated FP32 partial sums per thread and an FP64 block
 // reduction; the far field sits at kr ~ 500 rad at 16 kHz, where plain FP32
@@ -62,6 +63,14 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
   s = t;
 }
 
+// One CTA per (32 observation points, frequency): lane = observation point,
+// warp w sweeps faces w, w + 8, ...  Every lane of a warp works on the same
+// face, so face records, sources and drives are broadcast loads, and the
+// compensated phase set-up (double-float k|c_g - x|) is done once per
+// (point, face).  The Q point terms of a face are summed in FP32 and added to
+// a Kahan-compensated per-lane sum; the 8 warps' sums are added in FP64.
+constexpr int kFieldWarps = 8;
+
 template <int Q, int NC>
 __global__ void __launch_bounds__(256) field_f32_kernel(const FaceF32* __restrict__ faces, int nf,
                                                         const float2* __restrict__ src,
@@ -69,8 +78,11 @@ __global__ void __launch_bounds__(256) field_f32_kernel(const FaceF32* __restric
                                                         const double* __restrict__ obs, int nobs,
                                                         const FieldParamsF32* __restrict__ prm,
                                                         double2* __restrict__ out, FieldRule<float> fr) {
-  const int o = blockIdx.x, bt = blockIdx.y;
-  const double xo[3] = {obs[3 * o], obs[3 * o + 1], obs[3 * o + 2]};
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int o = blockIdx.x * 32 + lane, bt = blockIdx.y;
+  const bool live = o < nobs;
+  const int oc = live ? o : nobs - 1;  // idle lanes repeat a live point; their result is dropped
+  const double xo[3] = {obs[3 * oc], obs[3 * oc + 1], obs[3 * oc + 2]};
   float xhi[3], xlo[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -88,7 +100,7 @@ __global__ void __launch_bounds__(256) field_f32_kernel(const FaceF32* __restric
     br[c] = 0.f;
     bcmp[c] = 0.f;
   }
-  for (int g = threadIdx.x; g < nf; g += blockDim.x) {
+  for (int g = wid; g < nf; g += kFieldWarps) {
     const FaceF32& F = faces[g];
     // base phase k|c_g - x| in double-float
     df C[3];
@@ -103,9 +115,13 @@ __global__ void __launch_bounds__(256) field_f32_kernel(const FaceF32* __restric
     const float R0 = R.hi + R.lo;
     const float theta0 = df_reduce_two_pi(df_mul(kdf, R));
     const float Cf[3] = {C[0].hi + C[0].lo, C[1].hi + C[1].lo, C[2].hi + C[2].lo};
-    float2 qg[NC];
+    const float Cn = fmaf(Cf[0], F.normal[0], fmaf(Cf[1], F.normal[1], Cf[2] * F.normal[2]));
+    float2 qg[NC], fs[NC];
 #pragma unroll
-    for (int c = 0; c < NC; ++c) qg[c] = cscale(cmul(qs, drive[(size_t)c * nf + g]), F.area2);
+    for (int c = 0; c < NC; ++c) {
+      qg[c] = cscale(cmul(qs, drive[(size_t)c * nf + g]), F.area2);
+      fs[c] = make_float2(0.f, 0.f);
+    }
 #pragma unroll
     for (int n = 0; n < Q; ++n) {
       const float d[3] = {F.off[3 * n], F.off[3 * n + 1], F.off[3 * n + 2]};
@@ -121,44 +137,38 @@ __global__ void __launch_bounds__(256) field_f32_kernel(const FaceF32* __restric
       sincos_ftz(th, &sn, &cs);
       const float sc = rinv * BEM_INV_FOUR_PI;
       const float2 G = make_float2(cs * sc, sn * sc);
-      const float t = fmaf(rv[0], F.normal[0], fmaf(rv[1], F.normal[1], rv[2] * F.normal[2])) * rinv;
+      // (r . n_y) / r with r . n_y = C . n + d . n (d . n = 0 for points on the face plane, kept for generality)
+      const float t = (Cn + fmaf(d[0], F.normal[0], fmaf(d[1], F.normal[1], d[2] * F.normal[2]))) * rinv;
       const float2 Dk = make_float2(t * (-G.x * rinv - G.y * k), t * (G.x * k - G.y * rinv));
       const float wn = fr.w[n];
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         const float2 ps = src[(((size_t)bt * NC + c) * nf + g) * Q + n];
         const float2 qq = cscale(qg[c], wn);
-        const float2 term = csub(cmul(Dk, ps), cmul(G, qq));
-        kahan_add(ar[c], ac[c], term.x);
-        kahan_add(br[c], bcmp[c], term.y);
+        fs[c] = cadd(fs[c], csub(cmul(Dk, ps), cmul(G, qq)));
       }
     }
-  }
-  __shared__ double red[2 * NC][8];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-  for (int c = 0; c < NC; ++c) {
-    double vr = (double)ar[c] - (double)ac[c];
-    double vi = (double)br[c] - (double)bcmp[c];
-#pragma unroll
-    for (int s = 16; s > 0; s >>= 1) {
-      vr += __shfl_xor_sync(0xffffffffu, vr, s);
-      vi += __shfl_xor_sync(0xffffffffu, vi, s);
-    }
-    if (lane == 0) {
-      red[2 * c][wid] = vr;
-      red[2 * c + 1][wid] = vi;
+    for (int c = 0; c < NC; ++c) {
+      kahan_add(ar[c], ac[c], fs[c].x);
+      kahan_add(br[c], bcmp[c], fs[c].y);
     }
   }
+  __shared__ double2 red[kFieldWarps][NC][32];
+#pragma unroll
+  for (int c = 0; c < NC; ++c)
+    red[wid][c][lane] = make_double2((double)ar[c] - (double)ac[c], (double)br[c] - (double)bcmp[c]);
   __syncthreads();
-  if (threadIdx.x < NC) {
-    const int c = threadIdx.x;
-    double vr = 0, vi = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      vr += red[2 * c][w];
-      vi += red[2 * c + 1][w];
+  if (wid == 0 && live) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      double vr = 0.0, vi = 0.0;
+      for (int w = 0; w < kFieldWarps; ++w) {
+        vr += red[w][c][lane].x;
+        vi += red[w][c][lane].y;
+      }
+      out[((size_t)bt * NC + c) * nobs + o] = make_double2(vr, vi);
     }
-    out[((size_t)bt * NC + c) * nobs + o] = make_double2(vr, vi);
   }
 }
 
@@ -261,6 +271,7 @@ cudaError_t launch_field(const DeviceMesh& m, Precision prec, int batch, const d
   }
   const int total = batch * nc * m.nf * m.Q;
   dim3 grid(nobs, batch);
+  dim3 grid32((nobs + 31) / 32, batch);  // FP32 kernel: 32 observation points per CTA
   if (prec == Precision::Mixed) {
     field_sources_kernel<float><<<(total + 255) / 256, 256, 0, stream>>>(m.faces, m.area, m.nf, m.Q, nc,
                                                                          (const float2*)pressure, ldp,
@@ -274,7 +285,7 @@ cudaError_t launch_field(const DeviceMesh& m, Precision prec, int batch, const d
     FieldParamsF32* dp = (FieldParamsF32*)((char*)sources + (((size_t)total * sizeof(float2) + 255) / 256) * 256);
     cudaMemcpyAsync(dp, &hp, sizeof(hp), cudaMemcpyHostToDevice, stream);
 #define BEM_F32(QQ, NCC)                                                                                   \
-  field_f32_kernel<QQ, NCC><<<grid, 256, 0, stream>>>(m.faces32, m.nf, (const float2*)sources,             \
+  field_f32_kernel<QQ, NCC><<<grid32, 256, 0, stream>>>(m.faces32, m.nf, (const float2*)sources,           \
                                                       (const float2*)drive, obs, nobs, dp, out, fr32)
 #define BEM_F32_Q(NCC)    \
   if (m.Q == 6)           \
@@ -356,6 +367,7 @@ cudaError_t launch_field_single(Precision prec, const void* faces, int nf, int Q
     fr64.phi[i] = rule_phi[i];
   }
   dim3 grid(nobs, 1);
+  dim3 grid32((nobs + 31) / 32, 1);
   if (prec == Precision::Mixed) {
     FieldParamsF32* dp = (FieldParamsF32*)params;
     write_field_params_f32<<<1, 1, 0, stream>>>(dp, k);
@@ -363,11 +375,11 @@ cudaError_t launch_field_single(Precision prec, const void* faces, int nf, int Q
     const float2* s = (const float2*)sources;
     const float2* d = (const float2*)drive;
     if (Q == 6)
-      field_f32_kernel<6, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32);
+      field_f32_kernel<6, 1><<<grid32, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32);
     else if (Q == 3)
-      field_f32_kernel<3, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32);
+      field_f32_kernel<3, 1><<<grid32, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32);
     else
-      field_f32_kernel<1, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32);
+      field_f32_kernel<1, 1><<<grid32, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32);
   } else {
     FieldParamsF64* dp = (FieldParamsF64*)params;
     write_field_params_f64<<<1, 1, 0, stream>>>(dp, k);
