@@ -226,11 +226,11 @@ def main() -> None:
     opts = dict(precision=native.BEM_PRECISION_MIXED, sound_speed=SOUND_SPEED, rho=RHO, batch=B, refine_tol=1e-10,
                 max_refine=8, lu_gemm=args.lu_gemm)
 
+    sharding = pkg("sharding")
+
     def step_freqs(step: int):
         # weak scaling: rank r takes batch (step * world + r) of the sweep
-        start = ((step * world + rank) * B) % len(freqs)
-        idx = [(start + i) % len(freqs) for i in range(B)]
-        return freqs[idx]
+        return freqs[sharding.step_batch(step, rank, world, B, len(freqs))]
 
     for s in range(args.warmup):
         m.solve_device(step_freqs(s), p_dev.data_ptr(), u_dev.data_ptr(), **opts)
@@ -303,7 +303,10 @@ def main() -> None:
         "peak": fp32_peak,
         "unit": "TFLOP/s",
         "frac": (achieved / fp32_peak) if achieved else None,
-        "traffic": None,
+        # DRAM bytes per launch from one ncu capture of this kernel at this workload
+        # (dram__bytes_read.sum + dram__bytes_write.sum, current source); the
+        # algorithmic bytes are the extended-row output, 3 x N_f x ldR x 8 B = 1.360e9
+        "traffic": 1.3146e9 if args.faces == 10000 else None,
         "peak_source": "152 SMs x 128 FP32 lanes x 2 flop x median SM clock sampled during the run "
                        "(MEASURED_PEAKS.json has no FP32 figure)",
         "work_per_launch": f"{regular_qpairs:.4g} q-pairs x {flops_per_qpair} flop",
