@@ -26,6 +26,7 @@ import os
 import statistics
 import subprocess
 import sys
+import threading
 import time
 from pathlib import Path
 
@@ -44,22 +45,50 @@ def pkg(name: str):
     return importlib.import_module("boundary-lab_gb300." + name)
 
 
-def workload(faces: int = 10000):
+# The synthetic workloads of the benchmark, by name: mesh, observation points,
+# frequencies, form.  "box10k" is the headline configuration (mixed form).
+WORKLOADS = {
+    "sphere1280": dict(mesh="sphere1280", f=(100.0, 3000.0, 16), polar=False, n_far=1000, form="fp64",
+                       text="rigid sphere r=0.1 m, icosphere {nf} triangles ({nv} dofs), unit-velocity cap (polar "
+                            "angle < 30 deg, {nr} faces); 16 log-spaced freqs 100 Hz-3 kHz; FP64 form; 1000 "
+                            "Fibonacci points at 2 m"),
+    "box5k": dict(mesh="box5k", f=(50.0, 10000.0, 200), polar=False, n_far=2000, form="mixed",
+                  text="closed box 0.3x0.2x0.25 m, {nf} triangles ({nv} dofs), circular piston r=5 cm on +z ({nr} "
+                       "faces); 200 log-spaced freqs 50 Hz-10 kHz; 2000 Fibonacci points at 2 m"),
+    "box10k": dict(mesh="box10k", f=(200.0, 12000.0, 64), polar=True, n_far=2000, form="mixed",
+                   text="closed box 0.3x0.2x0.25 m, {nf} triangles ({nv} P1 dofs), circular piston r=5 cm on +z "
+                        "({nr} faces); 64 log-spaced freqs 200 Hz-12 kHz; {npt} observation points (2x73 polar + "
+                        "2000 Fibonacci at 2 m)"),
+    "horn20k": dict(mesh="horn20k", f=(500.0, 16000.0, 32), polar=False, n_far=5000, form="mixed",
+                    text="exponential horn (throat r=2.5 cm, mouth r=15 cm, length 20 cm) in a 0.5x0.4x0.4 m box, "
+                         "{nf} triangles ({nv} dofs), driven throat disc ({nr} faces); 32 log-spaced freqs "
+                         "500 Hz-16 kHz; 5000 Fibonacci points at 2 m"),
+}
+
+
+def workload(name: str = "box10k", faces: int | None = None):
+    """(mesh, points, freqs, drive, spec) of a named workload; ``faces`` re-meshes the box."""
     meshes = pkg("meshes")
     request = pkg("request")
-    mesh = meshes.box_with_piston((0.3, 0.2, 0.25), faces, 0.05, "+z")
-    _, horizontal, vertical, _ = request.polar_observation_points({"step_size": 5.0, "distance": 2.0})
-    sphere = request.fibonacci_sphere(2000, 2.0)
-    points = np.vstack([horizontal, vertical, sphere])
-    freqs = np.logspace(np.log10(200.0), np.log10(12000.0), 64)
+    spec = WORKLOADS[name]
+    if faces is not None and name.startswith("box"):
+        mesh = meshes.box_with_piston((0.3, 0.2, 0.25), faces, 0.05, "+z")
+    else:
+        mesh = meshes.config_mesh(spec["mesh"])
+    parts = []
+    if spec["polar"]:
+        _, horizontal, vertical, _ = request.polar_observation_points({"step_size": 5.0, "distance": 2.0})
+        parts += [horizontal, vertical]
+    parts.append(request.fibonacci_sphere(spec["n_far"], 2.0))
+    points = np.vstack(parts)
+    lo, hi, n = spec["f"]
+    freqs = np.logspace(np.log10(lo), np.log10(hi), n)
     drive = (mesh.tags == meshes.RADIATOR_TAG).astype(np.complex128)[None, :]
-    return mesh, points, freqs, drive
+    return mesh, points, freqs, drive, spec
 
 
-def describe(mesh, points, freqs) -> str:
-    return (f"closed box 0.3x0.2x0.25 m, {mesh.n_faces} triangles ({mesh.n_vertices} P1 dofs), circular piston r=5 cm "
-            f"on +z ({int((mesh.tags == 2).sum())} faces); {len(freqs)} log-spaced freqs 200 Hz-12 kHz; "
-            f"{len(points)} observation points (2x73 polar + 2000 Fibonacci at 2 m)")
+def describe(mesh, points, spec) -> str:
+    return spec["text"].format(nf=mesh.n_faces, nv=mesh.n_vertices, nr=int((mesh.tags == 2).sum()), npt=len(points))
 
 
 class ClockSampler:
@@ -73,6 +102,15 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.lines: list[str] = []
+        self._first = threading.Event()
+        self._reader = None
+
+    def _read(self) -> None:
+        for ln in self.proc.stdout:
+            if ln.strip():
+                self.lines.append(ln)
+                self._first.set()
+        self._first.set()
 
     def __enter__(self):
         try:
@@ -81,17 +119,24 @@ class ClockSampler:
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
+            return self
+        self._reader = threading.Thread(target=self._read, daemon=True)
+        self._reader.start()
+        # nvidia-smi's first start on a box initialises NVML, which stalls this
+        # process's CUDA calls for a few hundred ms: start timing after its first sample
+        self._first.wait(timeout=15)
         return self
 
     def __exit__(self, *exc):
         if self.proc is not None:
             self.proc.terminate()
             try:
-                out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
-                out, _ = self.proc.communicate()
-            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+                self.proc.wait()
+            if self._reader is not None:
+                self._reader.join(timeout=5)
         return False
 
     def summary(self) -> dict:
@@ -119,35 +164,39 @@ def measured_peaks() -> dict:
     return {}
 
 
-def cpu_oracle_step(mesh, points, freq, drive, threads: int) -> float:
-    """One frequency of the reference algorithm in FP32 on the host (assembly, BM system, LU, field)."""
+def cpu_oracle_step(mesh, points, freq, drive, threads: int, precision: str = "f32"):
+    """One frequency of the reference algorithm on the host (assembly, BM system, LU,
+    field): FP32 as the reference's engine computes, or FP64.  Returns (seconds, solution)."""
     from oracle import oracle
 
     t0 = time.perf_counter()
     omega = 2 * np.pi * freq
-    q = (drive[0] * (1j * RHO * omega)).astype(np.complex64)
-    oracle.solve_frequency(mesh, omega / SOUND_SPEED, q, points, precision="f32", threads=threads)
-    return time.perf_counter() - t0
+    q = drive[0] * (1j * RHO * omega)
+    if precision == "f32":
+        q = q.astype(np.complex64)
+    sol = oracle.solve_frequency(mesh, omega / SOUND_SPEED, q, points, precision=precision, threads=threads)
+    return time.perf_counter() - t0, sol
 
 
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    mesh, points, freqs, drive = workload(args.faces)
+    mesh, points, freqs, drive, spec = workload(args.workload, args.faces)
     threads = os.cpu_count() or 1
+    cpu_prec = "f64" if spec["form"] == "fp64" else "f32"
     from oracle.build import build_oracle
 
     build_oracle()
     # The host path has nothing to warm up beyond one small solve (page-in of the
     # library and of OpenBLAS); timed steps are capped at 6 full-size frequencies so
     # the run stays within a few minutes whatever --steps asks for.
-    small_mesh, small_points, _, small_drive = workload(600)
+    small_mesh, small_points, _, small_drive, _ = workload("box10k", 600)
     for _ in range(args.warmup):
         cpu_oracle_step(small_mesh, small_points[:64], 500.0, small_drive, threads)
     timed = min(args.steps, 6)
     sel = [freqs[(i * 13) % len(freqs)] for i in range(timed)]
-    times = [cpu_oracle_step(mesh, points, f, drive, threads) for f in sel]
+    times = [cpu_oracle_step(mesh, points, f, drive, threads, cpu_prec)[0] for f in sel]
     total = sum(times)
     value = len(times) / total
     line = {
@@ -162,14 +211,14 @@ def run_reference(args) -> None:
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": "f64" if cpu_prec == "f64" else "f32",
         "data": "synthetic",
-        "config": {"workload": describe(mesh, points, freqs), "step": "1 frequency (bounded sample)",
+        "config": {"workload": describe(mesh, points, spec), "step": "1 frequency (bounded sample)",
                    "timed_steps": len(times), "warmup": "one small solve per warm-up step"},
         "cpu_baseline": {
             "value": value, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "1 frequency of the 10k-triangle box per step: FP32 restatement of BEAT CPU assembly "
-                      "(colored OpenMP), BM system, LAPACK cgetrf/cgetrs (scipy OpenBLAS), field",
+            "sample": f"1 frequency of the workload per step: {cpu_prec.upper()} restatement of BEAT CPU assembly "
+                      "(colored OpenMP), BM system, LAPACK getrf/getrs (scipy OpenBLAS), field",
         },
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -183,7 +232,9 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=16)
-    ap.add_argument("--faces", type=int, default=10000)
+    ap.add_argument("--workload", default="box10k", choices=sorted(WORKLOADS),
+                    help="synthetic workload (box10k: the headline mixed-form configuration)")
+    ap.add_argument("--faces", type=int, default=None, help="re-mesh the box workloads to about this many triangles")
     ap.add_argument("--fp64-freqs", type=int, default=2, help="frequencies timed in the plain FP64 form")
     ap.add_argument("--cpu-baseline", type=int, default=1, help="frequencies timed on the host for cpu_baseline")
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -191,6 +242,8 @@ def main() -> None:
     ap.add_argument("--serving-jobs", type=int, default=40, help="jobs in the seeded Poisson serving stream (0: skip)")
     ap.add_argument("--serving-rate", type=float, default=20.0, help="serving arrivals per second")
     ap.add_argument("--serving-running", type=int, default=4, help="concurrent jobs on the GPU")
+    ap.add_argument("--lu-block", type=int, default=0, choices=[0, 32, 64], help="LU panel width (0 automatic)")
+    ap.add_argument("--form", default=None, choices=["mixed", "fp64"], help="override the workload's precision form")
     ap.add_argument("--lu-gemm", type=int, default=0, choices=[0, 1, 2],
                     help="LU trailing update: 0 automatic, 1 cuBLAS cgemm, 2 tcgen05 3xTF32")
     args = ap.parse_args()
@@ -213,8 +266,11 @@ def main() -> None:
     torch.cuda.set_device(local_rank)
     native = pkg("native")
     native.load()
-    mesh, points, freqs, drive = workload(args.faces)
-    B = args.batch
+    mesh, points, freqs, drive, spec = workload(args.workload, args.faces)
+    if args.form:
+        spec = {**spec, "form": args.form}
+    fp64_workload = spec["form"] == "fp64"
+    B = min(args.batch, len(freqs))
     ctx = native.Context(local_rank)
     m = ctx.upload_mesh(mesh.vertices, mesh.faces)
     m.set_excitation(drive)
@@ -223,8 +279,9 @@ def main() -> None:
     p_dev = torch.empty((B, 1, mesh.n_vertices), dtype=torch.complex128, device="cuda")
     u_dev = torch.empty((B, 1, len(points)), dtype=torch.complex128, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    opts = dict(precision=native.BEM_PRECISION_MIXED, sound_speed=SOUND_SPEED, rho=RHO, batch=B, refine_tol=1e-10,
-                max_refine=8, lu_gemm=args.lu_gemm)
+    form = native.BEM_PRECISION_FP64 if fp64_workload else native.BEM_PRECISION_MIXED
+    opts = dict(precision=form, sound_speed=SOUND_SPEED, rho=RHO, batch=B, refine_tol=1e-10,
+                max_refine=8, lu_gemm=args.lu_gemm, lu_block=args.lu_block)
 
     sharding = pkg("sharding")
 
@@ -240,17 +297,24 @@ def main() -> None:
     ev_start = torch.cuda.Event(enable_timing=True)
     ev_end = torch.cuda.Event(enable_timing=True)
     step_events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    flush.fill_(-1.0)  # first use loads torch's fill kernel (hundreds of ms on a fresh box): not in the timed region
+    torch.cuda.synchronize()
     stats_list = []
+    host_ms = []
     with ClockSampler(local_rank) as clocks:
         torch.cuda.synchronize()
         with torch.cuda.stream(stream):
             ev_start.record(stream)
             for s in range(args.steps):
+                h0 = time.perf_counter()
                 flush.fill_(float(s))  # write 256 MiB (> 129 MB L2) between steps
                 step_events[s][0].record(stream)
+                h1 = time.perf_counter()
                 stats_list.append(m.solve_device(step_freqs(args.warmup + s), p_dev.data_ptr(), u_dev.data_ptr(),
                                                  profile=1, **opts))
+                h2 = time.perf_counter()
                 step_events[s][1].record(stream)
+                host_ms.append((1e3 * (h1 - h0), 1e3 * (h2 - h1)))
             ev_end.record(stream)
         torch.cuda.synchronize()
     elapsed = ev_start.elapsed_time(ev_end) / 1e3
@@ -275,23 +339,26 @@ def main() -> None:
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 (compensated) + f64 refinement",
+        "dtype": "f64" if fp64_workload else "f32 (compensated) + f64 refinement",
         "data": "synthetic",
-        "config": {"workload": describe(mesh, points, freqs), "form": "mixed", "batch": B,
+        "config": {"workload": describe(mesh, points, spec), "name": args.workload, "form": spec["form"], "batch": B,
                    "l2": "256 MiB buffer written before every timed step (> 129 MB L2)",
                    "parallelism": f"replicas x{world}, frequencies sharded"},
         "clocks": clocks.summary(),
         "stage_ms_per_freq": per_freq_ms,
         "step_ms": step_ms,
+        # timed region minus the steps: the L2 flushes and host time between steps
+        "between_steps_ms": 1e3 * elapsed - sum(step_ms),
+        "host_ms": [[round(a, 3), round(b, 3)] for a, b in host_ms],  # (flush + event, solve call) per step
         "refine_steps_max": max(st["max_refine_steps"] for st in stats_list),
         "lu_trailing_update": {1: "cublas cgemm", 2: "tcgen05 3xTF32"}.get(stats_list[0]["lu_gemm_used"]),
         "rel_residual_max": max(st["max_rel_residual"] for st in stats_list),
     }
 
-    # dominant kernel roofline: regular-pair assembly, FP32 pipe
+    # dominant kernel roofline: regular-pair assembly, FP32 pipe (mixed form)
     st0 = stats_list[0]
     regular_qpairs = st0["regular_pairs"] * 36
-    flops_per_qpair = 101  # counted from regular_f32_kernel (FMA = 2 flop), see the design doc
+    flops_per_qpair = 101  # counted from the regular_f32_kernel source (FMA = 2 flop)
     reg_s = kernel_s["regular"] / (args.steps * B)
     achieved = regular_qpairs * flops_per_qpair / reg_s / 1e12 if reg_s > 0 else None
     clock = result["clocks"]["sm_mhz"] or 1920.0
@@ -306,18 +373,42 @@ def main() -> None:
         # DRAM bytes per launch from one ncu capture of this kernel at this workload
         # (dram__bytes_read.sum + dram__bytes_write.sum, current source); the
         # algorithmic bytes are the extended-row output, 3 x N_f x ldR x 8 B = 1.360e9
-        "traffic": 1.3146e9 if args.faces == 10000 else None,
+        "traffic": 1.3146e9 if args.workload == "box10k" and args.faces in (None, 10000) else None,
         "peak_source": "152 SMs x 128 FP32 lanes x 2 flop x median SM clock sampled during the run "
                        "(MEASURED_PEAKS.json has no FP32 figure)",
         "work_per_launch": f"{regular_qpairs:.4g} q-pairs x {flops_per_qpair} flop",
     }
 
-    if not args.no_extras and rank == 0:
+    if fp64_workload:
+        result["roofline"] = None
+        result["roofline_note"] = "FP64 workload: the regular assembly runs regular_f64_kernel on the FP64 pipe"
+
+    if not args.no_extras and rank == 0 and fp64_workload:
+        # the FP64 GPU form against the FP64 CPU oracle on one frequency
+        from oracle.build import build_oracle
+
+        build_oracle()
+        f_chk = freqs[len(freqs) // 2]
+        p_g, u_g, _ = m.solve(np.array([f_chk]), **{**opts, "batch": 1})
+        _, ref = cpu_oracle_step(mesh, points, f_chk, drive, os.cpu_count() or 1, "f64")
+        result["max_rel_far_field_err_vs_cpu_fp64"] = float(
+            np.linalg.norm(u_g[0, 0] - ref.field[:, 0]) / np.linalg.norm(ref.field[:, 0]))
+        result["max_rel_surface_pressure_err_vs_cpu_fp64"] = float(
+            np.linalg.norm(p_g[0, 0] - ref.pressure[:, 0]) / np.linalg.norm(ref.pressure[:, 0]))
+    if not args.no_extras and rank == 0 and not fp64_workload:
         # plain FP64 form on a subset, and the mixed-form error against it
-        sel = freqs[[10, 50, 30, 60][: args.fp64_freqs]]
+        n_f = len(freqs)
+        if args.fp64_freqs <= 4:
+            sel = freqs[[int(x * (n_f - 1)) for x in (0.16, 0.8, 0.48, 0.95)][: args.fp64_freqs]]
+        else:  # accuracy sweep: evenly spread frequencies, at most one batch of 64
+            sel = freqs[np.unique(np.linspace(0, n_f - 1, min(args.fp64_freqs, 64)).round().astype(int))]
         ev_a, ev_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         p64 = torch.empty((len(sel), 1, mesh.n_vertices), dtype=torch.complex128, device="cuda")
         u64 = torch.empty((len(sel), 1, len(points)), dtype=torch.complex128, device="cuda")
+        # warm-up: the FP64 form's first call loads its kernels (cuBLAS zgemm, FP64 kernels) lazily
+        m.solve_device(sel[:1], p64.data_ptr(), u64.data_ptr(), precision=native.BEM_PRECISION_FP64,
+                       sound_speed=SOUND_SPEED, rho=RHO, batch=1)
+        torch.cuda.synchronize()
         with torch.cuda.stream(stream):
             ev_a.record(stream)
             st64 = m.solve_device(sel, p64.data_ptr(), u64.data_ptr(), precision=native.BEM_PRECISION_FP64,
@@ -333,11 +424,13 @@ def main() -> None:
         perr = [float(torch.linalg.norm(pm[i] - p64[i]) / torch.linalg.norm(p64[i])) for i in range(len(sel))]
         v64 = len(sel) / t64
         result["fp64_form"] = {"value": v64, "unit": UNIT, "freqs_hz": [float(f) for f in sel],
-                               "stage_ms_per_freq": {k: 1e3 * v / len(sel) for k, v in st64["kernel_s"].items()}}
+                               "stage_ms_per_freq": {k: 1e3 * v / len(sel) for k, v in st64["kernel_s"].items()},
+                               "far_field_err_per_freq": errs, "surface_pressure_err_per_freq": perr}
         result["speedup_vs_fp64"] = value / world / v64
         result["max_rel_far_field_err_vs_fp64"] = max(errs)
         result["max_rel_surface_pressure_err_vs_fp64"] = max(perr)
 
+    if not args.no_extras and rank == 0:
         # end to end through the C ABI with host buffers: upload mesh + caches, solve a batch, copy results back
         e2e_times = []
         h2d = mesh.vertices.nbytes + mesh.faces.astype(np.int32).nbytes + drive.nbytes + points.nbytes + B * 8
@@ -361,26 +454,20 @@ def main() -> None:
             from oracle.build import build_oracle
 
             build_oracle()
-            ts = [cpu_oracle_step(mesh, points, freqs[32 + i], drive, threads) for i in range(args.cpu_baseline)]
+            cpu_prec = "f64" if fp64_workload else "f32"
+            ts = [cpu_oracle_step(mesh, points, freqs[(len(freqs) // 2 + i) % len(freqs)], drive, threads,
+                                  cpu_prec)[0] for i in range(args.cpu_baseline)]
             result["cpu_baseline"] = {
                 "value": len(ts) / sum(ts), "unit": UNIT, "cores": threads, "kind": "port",
-                "sample": f"{len(ts)} frequency of the same workload: FP32 restatement of BEAT CPU assembly "
-                          "(colored OpenMP), BM system, LAPACK cgetrf/cgetrs, field",
+                "sample": f"{len(ts)} frequency of the same workload: {cpu_prec.upper()} restatement of BEAT CPU "
+                          "assembly (colored OpenMP), BM system, LAPACK getrf/getrs, field",
             }
         # serving stream: seeded Poisson arrivals of mixed-size jobs, latency per job
-        if args.serving_jobs > 0:
+        if args.serving_jobs > 0 and args.workload == "box10k":
             result["serving"] = serving_run(args, local_rank)
-    # gpu_launches: our kernels per timed step.  Per batch of B frequencies with
-    # P = ceil(n/64) panels and R refinement steps: 6 assembly kernels per
-    # frequency; LU 6P - 4 (panel, swap, trsm, operand split x2, tcgen05 update)
-    # or 3P - 1 with the cuBLAS update; permutation, FP64 copy, 5 (R + 1) solve /
-    # residual kernels, 2 field kernels.
-    nv = mesh.n_vertices
-    panels = (nv + 63) // 64
-    refine = result["refine_steps_max"]
-    lu = 6 * panels - 4 if stats_list[0]["lu_gemm_used"] == 2 else 3 * panels - 1
-    per_batch = 6 * B + lu + 2 + 5 * (refine + 1) + 2
-    result["gpu_launches"] = per_batch * args.steps
+    # gpu_launches: this library's kernels launched in the timed region, counted by
+    # the library itself per call (bem_solve_stats.kernel_launches)
+    result["gpu_launches"] = int(sum(st["kernel_launches"] for st in stats_list))
     m.release()
     ctx.close()
     if rank == 0:

@@ -509,7 +509,7 @@ long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int np
   bytes += (long long)batch * nrhs * ((long long)nf * 6 * esz + (long long)npts * 16);  // field sources + out
   bytes += (long long)nf * (160 + 288 + 64);                                // face records and maps
   if (precision == BEM_PRECISION_MIXED)                                      // tensor-core update operands
-    bytes += (long long)batch * (2 * round_up(2LL * nv, 128) + 2 * round_up(nv, 256)) * 128 * 4;
+    bytes += (long long)batch * (2 * round_up(2LL * nv, 128) + 2 * round_up(nv, 256)) * 256 * 4;
   bytes += 64LL << 20;                                                      // cuBLAS workspace and slack
   return bytes;
 }
@@ -543,7 +543,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       B = (int)std::max(1.0, std::min(32.0, std::floor(16.0 * (1ull << 30) / per)));
     }
     B = std::min(B, n_freq);
-    const int nb = o.lu_block > 0 ? std::min(o.lu_block, 64) : (mixed ? 64 : 32);
+    const int nb = o.lu_block > 0 ? std::min(o.lu_block, 64) : 0;  // 0: the LU chooses
     const size_t matsz = (size_t)L.lda * nv * L.esz;
     ck(ctx->mats.ensure(matsz * B), "alloc matrices");
     if (mixed) ck(ctx->mats2.ensure(matsz * B), "alloc matrix copies");
@@ -571,6 +571,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
     std::vector<int> info(B);
     double kacc[BEM_K_SLOTS] = {0};
     int gemm_used = 0;
+    long long launches = 0;
     ctx->prof = o.profile != 0;
     double t_asm = 0, t_sol = 0, t_fld = 0, max_res = 0;
     int max_steps = 0, batches = 0;
@@ -600,10 +601,14 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
         ck(ctx->tcws.ensure(bem::tc_gemm_workspace_bytes(nv, B)), "alloc tensor-core workspace");
         tcws = ctx->tcws.p;
       }
+      int lu_launches = 0;
       ck(bem::lu_factor_batched(prec, ctx->mats.p, L.lda, nv, bt, (int*)ctx->ipiv.p, (int*)ctx->info.p, nb,
                                 ctx->cublas, ctx->stream, (bem::LuGemm)o.lu_gemm, tcws, &used_tensor, &tc_err,
-                                (int*)ctx->rowmap.p),
+                                (int*)ctx->rowmap.p, &lu_launches),
          "LU factorisation");
+      // kernels of this batch: 6 per frequency in assembly (+1 with isolated vertices), the
+      // LU, the permutation, the solves (mixed: 5 + 5 per refinement step), the field (2, +1 mixed)
+      launches += (long long)bt * (6 + (dm.n_isolated ? 1 : 0)) + lu_launches + 1;
       gemm_used = mixed ? (used_tensor ? 2 : 1) : 0;
       ck(bem::lu_perm_batched((const int*)ctx->ipiv.p, nv, bt, (int*)ctx->perm.p, ctx->stream), "pivot permutation");
       prof_mark(ctx, BEM_K_LU);
@@ -613,6 +618,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       if (!mixed) {
         ck(bem::lu_solve_cluster_batched(prec, ctx->mats.p, L.lda, nv, bt, (const int*)ctx->perm.p, ctx->b32.p, L.ldb, nc, ctx->stream),
            "LU solve");
+        launches += 1;
       } else {
         double2* x = (double2*)ctx->x64.p;
         double2* r = (double2*)ctx->r64.p;
@@ -648,6 +654,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
         }
         max_steps = std::max(max_steps, steps);
         max_res = std::max(max_res, worst);
+        launches += 5 + 5LL * steps;
       }
       prof_mark(ctx, BEM_K_SOLVE);
       cudaEventRecord(ctx->ev[2], ctx->stream);
@@ -673,6 +680,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
         ck(bem::launch_field(dm, prec, bt, ks.data(), qs.data(), p_for_field, L.ldb, nc, drive, (const double*)m->obs.p,
                              m->nobs, ctx->fsrc.p, (double2*)ctx->fout.p, ctx->stream),
            "field kernel");
+        launches += mixed ? 3 : 2;
         prof_mark(ctx, BEM_K_FIELD);
         double* dst = field_out + 2 * (size_t)f0 * nc * m->nobs;
         ck(cudaMemcpyAsync(dst, ctx->fout.p, (size_t)bt * nc * m->nobs * sizeof(double2),
@@ -717,6 +725,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       stats->singular_pairs = dm.npairs;
       stats->singular_points = m->singular_points;
       stats->lu_gemm_used = gemm_used;
+      stats->kernel_launches = launches;
     }
     if (mixed && !(max_res <= o.refine_tol)) {
       ctx->err = "iterative refinement stopped at relative residual " + std::to_string(max_res);
@@ -756,7 +765,7 @@ int bem_lu_factor_dense(bem_context* ctx, int n, double* a, int* ipiv, int preci
     }
     bool used_tensor = false;
     int* tc_err = nullptr;
-    ck(bem::lu_factor_batched(prec, ctx->mats.p, lda, n, 1, (int*)ctx->ipiv.p, (int*)ctx->info.p, 64, ctx->cublas,
+    ck(bem::lu_factor_batched(prec, ctx->mats.p, lda, n, 1, (int*)ctx->ipiv.p, (int*)ctx->info.p, 0, ctx->cublas,
                               ctx->stream, (bem::LuGemm)lu_gemm, tcws, &used_tensor, &tc_err, (int*)ctx->rowmap.p),
        "LU factorisation");
     int info = 0;

@@ -24,12 +24,18 @@
 // Every wait is bounded: on timeout the kernel records an error, waits
 // (bounded) for its own copies, frees its TMEM and returns.
 //
+// General block update (tc_update): C[row0:row0+M, col0:col0+N] -= L U with
+// L = A[row0:, kcol0:kcol0+K] and U = A[kcol0:kcol0+K, col0:], K <= 128, so one
+// kernel serves the trailing update, the updates inside a wide panel and the
+// blocked triangular solve of its U rows.
+//
 // TMA coordinates into C: the C map spans every whole matrix of the batch
 // (x = real row 0..2n, y = column 0..n, z = matrix), so a tile starts at
-// x = 2 (k + kb) + m0 + 32 w.  The innermost coordinate times 4 bytes must be a
-// multiple of 16: k + kb is even because the block width nb is even (the plan
-// refuses odd nb), and m0 + 32 w is a multiple of 32.  All coordinates are >= 0;
-// rows x >= 2n and columns y >= n are clipped by the map bounds.
+// x = 2 row0 + m0 + 32 w.  The innermost coordinate times 4 bytes must be a
+// multiple of 16: row0 is even (checked; block widths are even, the plan
+// refuses odd nb) and m0 + 32 w is a multiple of 32.  All coordinates are >= 0;
+// rows x >= 2n and columns y >= n are clipped by the map bounds, and rows or
+// columns of a tile beyond M or N receive -0 from zero-padded operands.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -43,7 +49,7 @@ namespace {
 constexpr int TM = 128;       // tile rows of C' (real rows)
 constexpr int TN = 256;       // tile columns of C'
 constexpr int TK = 16;        // K block per stage (16 fp32 = 64 B rows, 64-byte swizzle)
-constexpr int KP = 128;       // K' = 2 * nb, nb <= 64 (zero padded)
+constexpr int KP_MAX = 256;   // K' = 2 K <= 256 (K <= 128 complex), row stride of the split operands
 constexpr int STAGES = 2;
 constexpr int A_BYTES = TM * TK * 4;   // 8 KB
 constexpr int B_BYTES = TN * TK * 4;   // 16 KB
@@ -149,14 +155,15 @@ __device__ __forceinline__ float round_tf32(float x) {
   return __uint_as_float(u);
 }
 
-// A'hi / A'lo [batch][rows_pad][KP] from L21 (rows k+nb.., columns k..k+kb of each matrix).
+// A'hi / A'lo [batch][rows_pad][KP_MAX] from L (rows row0.., columns col0..col0+kb of
+// each matrix); rows_used x kp entries are written (zero beyond M rows / 2 kb).
 __global__ void prep_a_kernel(const float2* __restrict__ A, long long lda, long long strideA, int row0, int col0, int M,
-                              int kb, int rows_pad, float* __restrict__ ahi, float* __restrict__ alo) {
+                              int kb, int rows_pad, int rows_used, int kp, float* __restrict__ ahi,
+                              float* __restrict__ alo) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long per = (long long)rows_pad * KP;
-  if (idx >= per) return;
+  if (idx >= (long long)rows_used * kp) return;
   const int b = blockIdx.y;
-  const int rr = (int)(idx / KP), kk = (int)(idx % KP);
+  const int rr = (int)(idx / kp), kk = (int)(idx % kp);
   float v = 0.f;
   const int i = rr >> 1, k = kk >> 1;
   if (i < M && k < kb) {
@@ -167,19 +174,20 @@ __global__ void prep_a_kernel(const float2* __restrict__ A, long long lda, long 
       v = (kk & 1) == 0 ? a.y : a.x;
   }
   const float hi = round_tf32(v);
-  const size_t o = (size_t)b * per + idx;
+  const size_t o = ((size_t)b * rows_pad + rr) * KP_MAX + kk;
   ahi[o] = hi;
   alo[o] = v - hi;
 }
 
-// B'hi / B'lo [batch][cols_pad][KP] from U12 (rows k..k+kb, columns k+nb.. of each matrix).
+// B'hi / B'lo [batch][cols_pad][KP_MAX] from U (rows row0..row0+kb, columns col0.. of
+// each matrix); cols_used x kp entries are written (zero beyond N columns / 2 kb).
 __global__ void prep_b_kernel(const float2* __restrict__ A, long long lda, long long strideA, int row0, int col0, int N,
-                              int kb, int cols_pad, float* __restrict__ bhi, float* __restrict__ blo) {
+                              int kb, int cols_pad, int cols_used, int kp, float* __restrict__ bhi,
+                              float* __restrict__ blo) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long per = (long long)cols_pad * KP;
-  if (idx >= per) return;
+  if (idx >= (long long)cols_used * kp) return;
   const int b = blockIdx.y;
-  const int j = (int)(idx / KP), kk = (int)(idx % KP);
+  const int j = (int)(idx / kp), kk = (int)(idx % kp);
   float v = 0.f;
   const int k = kk >> 1;
   if (j < N && k < kb) {
@@ -187,7 +195,7 @@ __global__ void prep_b_kernel(const float2* __restrict__ A, long long lda, long 
     v = (kk & 1) == 0 ? u.x : u.y;
   }
   const float hi = round_tf32(v);
-  const size_t o = (size_t)b * per + idx;
+  const size_t o = ((size_t)b * cols_pad + j) * KP_MAX + kk;
   bhi[o] = hi;
   blo[o] = v - hi;
 }
@@ -195,7 +203,8 @@ __global__ void prep_b_kernel(const float2* __restrict__ A, long long lda, long 
 __global__ void __launch_bounds__(128, 2)
     trailing_update_tf32x3(const __grid_constant__ CUtensorMap map_ahi, const __grid_constant__ CUtensorMap map_alo,
                            const __grid_constant__ CUtensorMap map_bhi, const __grid_constant__ CUtensorMap map_blo,
-                           const __grid_constant__ CUtensorMap map_c, int x0, int y0, int M2, int N, int* err) {
+                           const __grid_constant__ CUtensorMap map_c, int x0, int y0, int M2, int N, int KB,
+                           int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-byte alignment for the swizzled tiles
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -226,7 +235,6 @@ __global__ void __launch_bounds__(128, 2)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
-  const int KB = KP / TK;  // 8 K blocks
 
   if (warp == 0 && lane == 0) {
     // TMA producer
@@ -331,8 +339,8 @@ EncodeTiledFn encode_fn() {
 bool make_map(CUtensorMap* map, float* buf, int rows_pad, int batch, int box_rows) {
   EncodeTiledFn enc = encode_fn();
   if (!enc) return false;
-  cuuint64_t dims[3] = {(cuuint64_t)KP, (cuuint64_t)rows_pad, (cuuint64_t)batch};
-  cuuint64_t strides[2] = {(cuuint64_t)KP * 4, (cuuint64_t)rows_pad * KP * 4};
+  cuuint64_t dims[3] = {(cuuint64_t)KP_MAX, (cuuint64_t)rows_pad, (cuuint64_t)batch};
+  cuuint64_t strides[2] = {(cuuint64_t)KP_MAX * 4, (cuuint64_t)rows_pad * KP_MAX * 4};
   cuuint32_t box[3] = {(cuuint32_t)TK, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, buf, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -371,7 +379,7 @@ struct TcGemmPlan {
 size_t tc_gemm_workspace_bytes(int n, int batch) {
   const size_t rows_pad = ((size_t)2 * n + TM - 1) / TM * TM;
   const size_t cols_pad = ((size_t)n + TN - 1) / TN * TN;
-  return (2 * rows_pad + 2 * cols_pad) * KP * 4 * batch + 256 * 5;
+  return (2 * rows_pad + 2 * cols_pad) * KP_MAX * 4 * batch + 256 * 5;
 }
 
 bool tc_gemm_available() { return encode_fn() != nullptr; }
@@ -393,41 +401,53 @@ bool tc_gemm_plan(TcGemmPlan* p, void* workspace, int n, int batch, float2* A, l
   p->rows_pad = (int)rows_pad;
   p->cols_pad = (int)cols_pad;
   p->batch = batch;
-  p->ahi = (float*)take(rows_pad * KP * 4 * batch);
-  p->alo = (float*)take(rows_pad * KP * 4 * batch);
-  p->bhi = (float*)take(cols_pad * KP * 4 * batch);
-  p->blo = (float*)take(cols_pad * KP * 4 * batch);
+  p->ahi = (float*)take(rows_pad * KP_MAX * 4 * batch);
+  p->alo = (float*)take(rows_pad * KP_MAX * 4 * batch);
+  p->bhi = (float*)take(cols_pad * KP_MAX * 4 * batch);
+  p->blo = (float*)take(cols_pad * KP_MAX * 4 * batch);
   p->err = (int*)take(sizeof(int));
   return make_map(&p->mahi, p->ahi, (int)rows_pad, batch, TM) && make_map(&p->malo, p->alo, (int)rows_pad, batch, TM) &&
          make_map(&p->mbhi, p->bhi, (int)cols_pad, batch, TN) && make_map(&p->mblo, p->blo, (int)cols_pad, batch, TN) &&
          make_c_map(&p->mc, (float*)A, n, lda, lda * (long long)n, batch);
 }
 
-// C -= L21 * U12 for the block column at k (width kb <= 64) of every matrix in the batch.
-cudaError_t tc_trailing_update(TcGemmPlan* p, float2* A, long long lda, long long strideA, int n, int k, int kb,
-                               cudaStream_t stream) {
-  const int M = n - k - kb, N = n - k - kb;
-  if (M <= 0 || N <= 0) return cudaSuccess;
+// C[row0:row0+M, col0:col0+N] -= A[row0:row0+M, kcol0:kcol0+K] * A[kcol0:kcol0+K, col0:col0+N]
+// for every matrix of the batch (K <= 128).  Rows beyond M and columns beyond N
+// inside the last tiles receive -0 (their split operands are zero).
+cudaError_t tc_update(TcGemmPlan* p, float2* A, long long lda, long long strideA, int row0, int M, int col0, int N,
+                      int kcol0, int K, cudaStream_t stream) {
+  if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
+  if (2 * K > KP_MAX) return cudaErrorInvalidValue;
+  if (row0 & 1) return cudaErrorInvalidValue;  // x coordinate 2 row0 must be a multiple of 4
   const int M2 = 2 * M;
   const int rows_used = (M2 + TM - 1) / TM * TM;
   const int cols_used = (N + TN - 1) / TN * TN;
+  if (rows_used > p->rows_pad || cols_used > p->cols_pad) return cudaErrorInvalidValue;
+  const int kp = (2 * K + TK - 1) / TK * TK;
   {
-    const long long per = (long long)rows_used * KP;
-    dim3 g((unsigned)((per + 255) / 256), p->batch);
-    prep_a_kernel<<<g, 256, 0, stream>>>(A, lda, strideA, k + kb, k, M, kb, p->rows_pad, p->ahi, p->alo);
+    const long long total = (long long)rows_used * kp;
+    dim3 g((unsigned)((total + 255) / 256), p->batch);
+    prep_a_kernel<<<g, 256, 0, stream>>>(A, lda, strideA, row0, kcol0, M, K, p->rows_pad, rows_used, kp, p->ahi,
+                                         p->alo);
   }
   {
-    const long long per = (long long)cols_used * KP;
-    dim3 g((unsigned)((per + 255) / 256), p->batch);
-    prep_b_kernel<<<g, 256, 0, stream>>>(A, lda, strideA, k, k + kb, N, kb, p->cols_pad, p->bhi, p->blo);
+    const long long total = (long long)cols_used * kp;
+    dim3 g((unsigned)((total + 255) / 256), p->batch);
+    prep_b_kernel<<<g, 256, 0, stream>>>(A, lda, strideA, kcol0, col0, N, K, p->cols_pad, cols_used, kp, p->bhi,
+                                         p->blo);
   }
   const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024;
   if (!ensure_smem_limit((const void*)trailing_update_tf32x3, smem)) return cudaErrorInvalidValue;
-  if ((k + kb) & 1) return cudaErrorInvalidValue;  // x coordinate 2 (k + kb) must be a multiple of 4
   dim3 grid(rows_used / TM, cols_used / TN, p->batch);
-  trailing_update_tf32x3<<<grid, 128, smem, stream>>>(p->mahi, p->malo, p->mbhi, p->mblo, p->mc, 2 * (k + kb), k + kb,
-                                                     M2, N, p->err);
+  trailing_update_tf32x3<<<grid, 128, smem, stream>>>(p->mahi, p->malo, p->mbhi, p->mblo, p->mc, 2 * row0, col0, M2, N,
+                                                     kp / TK, p->err);
   return cudaGetLastError();
+}
+
+// C -= L21 * U12 for the block column at k (width kb) of every matrix in the batch.
+cudaError_t tc_trailing_update(TcGemmPlan* p, float2* A, long long lda, long long strideA, int n, int k, int kb,
+                               cudaStream_t stream) {
+  return tc_update(p, A, lda, strideA, k + kb, n - k - kb, k + kb, n - k - kb, k, kb, stream);
 }
 
 int* tc_gemm_error_word(TcGemmPlan* p) { return p->err; }

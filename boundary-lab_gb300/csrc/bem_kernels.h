@@ -97,10 +97,15 @@ int* tc_gemm_error_word(TcGemmPlan* p);
 // rowmap (batch * kRowmapStride ints, may be null) lets the cluster panel hand
 // the net row permutation of its interchanges to the row-swap kernel.
 constexpr int kRowmapStride = 512;
+// Outer block width of the two-level LU (trailing-update depth); a multiple of
+// every cluster panel width (32, 64) and at most the tcgen05 update's K (128).
+constexpr int kOuterBlock = 128;
+// Kernels the two-level LU launches for one batch (cuBLAS kernels not counted).
+int lu_launch_count(int n, int nb, int NB, bool tensor);
 cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int batch, int* ipiv, int* info,
                               int nb, void* cublas_handle, cudaStream_t stream, LuGemm gemm = LuGemm::Cublas,
                               void* tc_workspace = nullptr, bool* used_tensor = nullptr, int** tc_err = nullptr,
-                              int* rowmap = nullptr);
+                              int* rowmap = nullptr, int* n_launches = nullptr);
 // Solve (LU) X = B in place for nrhs columns per matrix (B stride ldb*nrhs per matrix), working precision.
 cudaError_t lu_solve_batched(Precision prec, const void* LU, long long lda, int n, int batch, const int* ipiv,
                              void* B, long long ldb, int nrhs, int nb, cudaStream_t stream);
@@ -113,7 +118,7 @@ cudaError_t norms_batched(const double2* r, const double2* b, long long ldb, int
 // Cluster-resident panel (bem_lu_cluster.cu).  lu_cluster_plan picks the panel
 // width (64 or 32) and cluster size for an n x n matrix; false when no cluster
 // configuration fits (then the single-CTA panel is used).
-bool lu_cluster_plan(Precision prec, int n, int* nb, int* cl);
+bool lu_cluster_plan(Precision prec, int n, int want_nb, int batch, int* nb, int* cl);
 // rowmap: if not null, receives per matrix [count, (dst row, src row) x count]:
 // the net effect of the panel's kb interchanges on any column (at most 2 kb rows).
 cudaError_t lu_panel_cluster(Precision prec, void* A, long long lda, long long strideA, int n, int k, int kb, int nb,

@@ -149,13 +149,14 @@ __global__ void lu_swap_kernel(C2* A, long long lda, long long strideA, int n, i
   }
 }
 
-// U12 = L11^{-1} A12 for columns [k+kb, n); blockDim columns per CTA.  The
+// U12 = L11^{-1} A12 for rows [k, k+kb) and columns [c_begin, c_end), with L11 the
+// unit lower triangle of A[k:k+kb, k:k+kb]; blockDim columns per CTA.  The
 // column block is staged through shared memory with coalesced loads and stores
 // (a warp per column, lanes along its rows); the substitution runs one thread
 // per column.  X has a padded row stride so both access patterns are
 // conflict-free.
 template <typename C2>
-__global__ void lu_trsm_kernel(C2* A, long long lda, long long strideA, int n, int k, int kb) {
+__global__ void lu_trsm_kernel(C2* A, long long lda, long long strideA, int n, int k, int kb, int c_begin, int c_end) {
   extern __shared__ unsigned char smem_raw[];
   C2* L = reinterpret_cast<C2*>(smem_raw);  // kb x kb, column-major
   C2* X = L + kb * kb;                      // kb x (blockDim + 1)
@@ -166,8 +167,8 @@ __global__ void lu_trsm_kernel(C2* A, long long lda, long long strideA, int n, i
     const int r = i % kb, c = i / kb;
     L[i] = M[(size_t)(k + c) * lda + k + r];
   }
-  const int c0 = k + kb + blockIdx.x * blockDim.x;
-  const int ncol = min((int)blockDim.x, n - c0);
+  const int c0 = c_begin + blockIdx.x * blockDim.x;
+  const int ncol = min((int)blockDim.x, c_end - c0);
   // 8 columns x 2 row halves per warp and batch: 16 independent loads in flight
   for (int cb = wid; cb < ncol; cb += 8 * nw) {
     C2 v[8][2];
@@ -449,19 +450,138 @@ __global__ void f32_to_f64_kernel(const float2* s, double2* d, long long n) {
 bool tc_gemm_plan(TcGemmPlan* p, void* workspace, int n, int batch, float2* A, long long lda, int nb);
 cudaError_t tc_trailing_update(TcGemmPlan* p, float2* A, long long lda, long long strideA, int n, int k, int kb,
                                cudaStream_t stream);
+cudaError_t tc_update(TcGemmPlan* p, float2* A, long long lda, long long strideA, int row0, int M, int col0, int N,
+                      int kcol0, int K, cudaStream_t stream);
 size_t tc_gemm_plan_size();
+
+namespace {
+
+// State of one batched factorisation for the two-level driver.
+struct LuJob {
+  Precision prec;
+  void* A;
+  long long lda, strideA;
+  int n, batch, nb, cl;
+  int* ipiv;
+  int* info;
+  int* rowmap;
+  TcGemmPlan* plan;  // tcgen05 updates (mixed form); null: cuBLAS
+  cublasHandle_t h;
+  cudaStream_t stream;
+};
+
+// U rows [k, k+kb) of columns [c0, c1): U = L^{-1} A with L the unit lower triangle of A[k:k+kb, k:k+kb].
+cudaError_t trsm_cols(const LuJob& j, int k, int kb, int c0, int c1) {
+  if (c1 <= c0 || kb <= 0) return cudaSuccess;
+  const int tpb = 128;
+  dim3 g((unsigned)((c1 - c0 + tpb - 1) / tpb), j.batch);
+  if (j.prec == Precision::Mixed) {
+    const size_t sm = (size_t)kb * kb * sizeof(float2) + (size_t)kb * (tpb + 1) * sizeof(float2);
+    if (sm > 48 * 1024) ensure_smem_limit((const void*)lu_trsm_kernel<float2>, sm);
+    lu_trsm_kernel<float2><<<g, tpb, sm, j.stream>>>((float2*)j.A, j.lda, j.strideA, j.n, k, kb, c0, c1);
+  } else {
+    const size_t sm = (size_t)kb * kb * sizeof(double2) + (size_t)kb * (tpb + 1) * sizeof(double2);
+    if (sm > 48 * 1024) ensure_smem_limit((const void*)lu_trsm_kernel<double2>, sm);
+    lu_trsm_kernel<double2><<<g, tpb, sm, j.stream>>>((double2*)j.A, j.lda, j.strideA, j.n, k, kb, c0, c1);
+  }
+  return cudaGetLastError();
+}
+
+// A[r0:r0+M, c0:c0+N] -= A[r0:r0+M, kc:kc+K] * A[kc:kc+K, c0:c0+N] for every matrix.
+cudaError_t block_update(const LuJob& j, int r0, int M, int c0, int N, int kc, int K) {
+  if (M <= 0 || N <= 0 || K <= 0) return cudaSuccess;
+  if (j.plan) return tc_update(j.plan, (float2*)j.A, j.lda, j.strideA, r0, M, c0, N, kc, K, j.stream);
+  const int ld = (int)j.lda;
+  if (j.prec == Precision::Mixed) {
+    const cuComplex alpha = make_cuComplex(-1.f, 0.f), beta = make_cuComplex(1.f, 0.f);
+    const cuComplex* base = (const cuComplex*)j.A;
+    const cublasStatus_t st = cublasCgemmStridedBatched(
+        j.h, CUBLAS_OP_N, CUBLAS_OP_N, M, N, K, &alpha, base + r0 + (size_t)kc * j.lda, ld, j.strideA,
+        base + kc + (size_t)c0 * j.lda, ld, j.strideA, &beta, (cuComplex*)j.A + r0 + (size_t)c0 * j.lda, ld, j.strideA,
+        j.batch);
+    return st == CUBLAS_STATUS_SUCCESS ? cudaSuccess : cudaErrorUnknown;
+  }
+  const cuDoubleComplex alpha = make_cuDoubleComplex(-1.0, 0.0), beta = make_cuDoubleComplex(1.0, 0.0);
+  const cuDoubleComplex* base = (const cuDoubleComplex*)j.A;
+  const cublasStatus_t st = cublasZgemmStridedBatched(
+      j.h, CUBLAS_OP_N, CUBLAS_OP_N, M, N, K, &alpha, base + r0 + (size_t)kc * j.lda, ld, j.strideA,
+      base + kc + (size_t)c0 * j.lda, ld, j.strideA, &beta, (cuDoubleComplex*)j.A + r0 + (size_t)c0 * j.lda, ld,
+      j.strideA, j.batch);
+  return st == CUBLAS_STATUS_SUCCESS ? cudaSuccess : cudaErrorUnknown;
+}
+
+#define BEM_TRY(x)                          \
+  do {                                      \
+    const cudaError_t e_ = (x);             \
+    if (e_ != cudaSuccess) return e_;       \
+  } while (0)
+
+// Two-level right-looking LU.  The matrix is factored in outer block columns of
+// width NB (128): each is factored as sub-panels of width nb (the cluster panel
+// width, 32 or 64) with their row interchanges applied to every other column
+// and the rest of the outer block updated after each sub-panel; then the outer
+// block's U rows are solved block by block and the trailing matrix takes one
+// update of depth NB.  The trailing matrix is read and written once per NB
+// columns instead of once per nb, which at block depth 64 bounds the LU by HBM.
+cudaError_t lu_two_level(const LuJob& j, int NB) {
+  const int n = j.n, nb = j.nb;
+  for (int k0 = 0; k0 < n; k0 += NB) {
+    const int KB = std::min(NB, n - k0);
+    for (int j0 = 0; j0 < KB; j0 += nb) {
+      const int kb = std::min(nb, KB - j0), kk = k0 + j0;
+      BEM_TRY(lu_panel_cluster(j.prec, j.A, j.lda, j.strideA, n, kk, kb, nb, j.cl, j.batch, j.ipiv, j.info, j.stream,
+                               j.rowmap));
+      BEM_TRY(lu_swap_rows_batched(j.prec, j.A, j.lda, j.strideA, n, kk, kb, j.batch, j.rowmap, j.stream));
+      if (j0 + kb < KB) {  // the rest of the outer block
+        BEM_TRY(trsm_cols(j, kk, kb, kk + kb, k0 + KB));
+        BEM_TRY(block_update(j, kk + kb, n - kk - kb, kk + kb, k0 + KB - kk - kb, kk, kb));
+      }
+    }
+    if (k0 + KB < n) {
+      // U rows of the outer block for the trailing columns: blocked forward substitution
+      for (int i0 = 0; i0 < KB; i0 += nb) {
+        const int kb = std::min(nb, KB - i0), kk = k0 + i0;
+        BEM_TRY(trsm_cols(j, kk, kb, k0 + KB, n));
+        if (i0 + kb < KB) BEM_TRY(block_update(j, kk + kb, k0 + KB - kk - kb, k0 + KB, n - k0 - KB, kk, kb));
+      }
+      BEM_TRY(block_update(j, k0 + KB, n - k0 - KB, k0 + KB, n - k0 - KB, k0, KB));
+    }
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int lu_launch_count(int n, int nb, int NB, bool tensor) {
+  const int per_update = tensor ? 3 : 0;  // operand split x2 + tcgen05 kernel (cuBLAS kernels are not counted)
+  int count = 0;
+  for (int k0 = 0; k0 < n; k0 += NB) {
+    const int KB = std::min(NB, n - k0);
+    for (int j0 = 0; j0 < KB; j0 += nb) {
+      const int kb = std::min(nb, KB - j0);
+      count += 2;                                        // panel, row swaps
+      if (j0 + kb < KB) count += 1 + (n - k0 - j0 - kb > 0 ? per_update : 0);
+    }
+    if (k0 + KB < n) {
+      for (int i0 = 0; i0 < KB; i0 += nb) count += 1 + (i0 + std::min(nb, KB - i0) < KB ? per_update : 0);
+      count += per_update;
+    }
+  }
+  return count;
+}
 
 cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int batch, int* ipiv, int* info, int nb,
                               void* cublas_handle, cudaStream_t stream, LuGemm gemm, void* tc_workspace,
-                              bool* used_tensor, int** tc_err, int* rowmap) {
+                              bool* used_tensor, int** tc_err, int* rowmap, int* n_launches) {
   cublasHandle_t h = (cublasHandle_t)cublas_handle;
   cublasSetStream(h, stream);
   const long long strideA = lda * (long long)n;
   const bool mixed = prec == Precision::Mixed;
-  nb = std::max(1, std::min(nb, 64));
+  const int want_nb = (nb == 32 || nb == 64) ? nb : 0;  // 0: automatic
+  nb = nb > 0 ? std::min(nb, 64) : (mixed ? 64 : 32);
   const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
   int cnb = 0, ccl = 0;
-  const bool cluster_panel = lu_cluster_plan(prec, n, &cnb, &ccl);
+  const bool cluster_panel = lu_cluster_plan(prec, n, want_nb, batch, &cnb, &ccl);
   if (cluster_panel) nb = cnb;
   // tensor-core trailing update (mixed precision only; K = 2 nb <= 128)
   std::vector<unsigned char> plan_storage;
@@ -477,8 +597,18 @@ cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int
     if (tc_err) *tc_err = tc_gemm_error_word(plan);
     cudaMemsetAsync(tc_gemm_error_word(plan), 0, sizeof(int), stream);
   }
+  // The two-level schedule serves the HBM-bound tcgen05 update; cuBLAS (the FP64
+  // form, or lu_gemm = 1) keeps one level: its kernels for the skinny panel
+  // shapes of the two-level schedule are slow.
+  if (cluster_panel && rowmap && plan) {
+    LuJob job{prec, A, lda, strideA, n, batch, nb, ccl, ipiv, info, rowmap, plan, h, stream};
+    if (n_launches) *n_launches = lu_launch_count(n, nb, kOuterBlock, plan != nullptr);
+    return lu_two_level(job, kOuterBlock);
+  }
+  if (n_launches) *n_launches = 0;
   for (int k = 0; k < n; k += nb) {
     const int kb = std::min(nb, n - k);
+    if (n_launches) *n_launches += 2 + (n - k - kb > 0 ? 1 + (plan ? 3 : 0) : 0);
     if (cluster_panel) {
       cudaError_t e = lu_panel_cluster(prec, A, lda, strideA, n, k, kb, nb, ccl, batch, ipiv, info, stream, rowmap);
       if (e != cudaSuccess) return e;
@@ -503,7 +633,7 @@ cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int
       const size_t sm = (size_t)kb * kb * esz + (size_t)kb * (tpb + 1) * esz;
       if (mixed) {
         if (sm > 48 * 1024) ensure_smem_limit((const void*)lu_trsm_kernel<float2>, sm);
-        lu_trsm_kernel<float2><<<g, tpb, sm, stream>>>((float2*)A, lda, strideA, n, k, kb);
+        lu_trsm_kernel<float2><<<g, tpb, sm, stream>>>((float2*)A, lda, strideA, n, k, kb, k + kb, n);
         if (plan) {
           cudaError_t e = tc_trailing_update(plan, (float2*)A, lda, strideA, n, k, kb, stream);
           if (e != cudaSuccess) return e;
@@ -518,7 +648,7 @@ cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int
         if (st != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
       } else {
         if (sm > 48 * 1024) ensure_smem_limit((const void*)lu_trsm_kernel<double2>, sm);
-        lu_trsm_kernel<double2><<<g, tpb, sm, stream>>>((double2*)A, lda, strideA, n, k, kb);
+        lu_trsm_kernel<double2><<<g, tpb, sm, stream>>>((double2*)A, lda, strideA, n, k, kb, k + kb, n);
         const cuDoubleComplex alpha = make_cuDoubleComplex(-1.0, 0.0), beta = make_cuDoubleComplex(1.0, 0.0);
         double2* base = (double2*)A;
         cublasStatus_t st = cublasZgemmStridedBatched(

@@ -515,35 +515,77 @@ template <typename R, int NB> size_t panel_smem(int chunk) {
   return (size_t)NB * chunk * sizeof(C2) + 6 * NB * sizeof(C2) + 64;
 }
 
-template <typename R> bool choose_panel(int n, int& nb, int& cl) {
-  // prefer nb = 64 (larger trailing GEMMs), then 32; smallest cluster that fits
-  for (int want_nb : {64, 32}) {
+// Clusters of size cl that can be resident at once for this kernel and shared memory.
+template <typename K> int active_clusters(K kern, int threads, size_t smem, int cl) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(cl, 1);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int num = 0;
+  if (cudaOccupancyMaxActiveClusters(&num, (const void*)kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return num;
+}
+
+// Panel width and cluster size for an n x n batch.  The panel is latency-bound
+// (a cluster barrier per column), so the batch's panels should run in as few
+// waves of clusters as possible: among the (width, cluster size) pairs whose
+// panel fits in shared memory, take the fewest waves (batch / resident
+// clusters), then the wider panel, then the smaller cluster.  want_nb > 0 fixes
+// the width.
+template <typename R> bool choose_panel(int n, int want_nb, int batch, int& nb, int& cl) {
+  bool found = false;
+  int best_waves = 0;
+  for (int w : {64, 32}) {
+    if (want_nb > 0 && w != want_nb) continue;
     for (int c : {4, 8, 16}) {
       const int chunk = (n + c - 1) / c;
-      const size_t sm = want_nb == 64 ? panel_smem<R, 64>(chunk) : panel_smem<R, 32>(chunk);
+      const size_t sm = w == 64 ? panel_smem<R, 64>(chunk) : panel_smem<R, 32>(chunk);
       if (sm > kPanelSmemBudget) continue;
-      int maxcl = want_nb == 64 ? max_cluster(lu_panel_cluster_kernel<R, 64>, kPanelThreads, sm)
+      const int maxcl = w == 64 ? max_cluster(lu_panel_cluster_kernel<R, 64>, kPanelThreads, sm)
                                 : max_cluster(lu_panel_cluster_kernel<R, 32>, kPanelThreads, sm);
-      if (maxcl >= c) {
-        nb = want_nb;
+      if (maxcl < c) continue;
+      const int act = w == 64 ? active_clusters(lu_panel_cluster_kernel<R, 64>, kPanelThreads, sm, c)
+                              : active_clusters(lu_panel_cluster_kernel<R, 32>, kPanelThreads, sm, c);
+      if (act < 1) continue;
+      const int waves = (std::max(batch, 1) + act - 1) / act;
+      if (!found || waves < best_waves) {  // candidates come wider first, then smaller clusters
+        found = true;
+        best_waves = waves;
+        nb = w;
         cl = c;
-        return true;
       }
     }
   }
-  return false;
+  return found;
 }
 
 }  // namespace
 
-bool lu_cluster_plan(Precision prec, int n, int* nb, int* cl) {
-  static thread_local int last_n[2] = {-1, -1}, last_nb[2] = {0, 0}, last_cl[2] = {0, 0};
+bool lu_cluster_plan(Precision prec, int n, int want_nb, int batch, int* nb, int* cl) {
+  struct Key {
+    int n = -1, want = 0, batch = 0;
+  };
+  static thread_local Key last[2];
+  static thread_local int last_nb[2] = {0, 0}, last_cl[2] = {0, 0};
   static thread_local bool last_ok[2] = {false, false};
   const int pi = prec == Precision::Mixed ? 1 : 0;
-  if (last_n[pi] != n) {
+  if (last[pi].n != n || last[pi].want != want_nb || last[pi].batch != batch) {
     int b = 0, c = 0;
-    last_ok[pi] = prec == Precision::Mixed ? choose_panel<float>(n, b, c) : choose_panel<double>(n, b, c);
-    last_n[pi] = n;
+    last_ok[pi] = prec == Precision::Mixed ? choose_panel<float>(n, want_nb, batch, b, c)
+                                           : choose_panel<double>(n, want_nb, batch, b, c);
+    last[pi].n = n;
+    last[pi].want = want_nb;
+    last[pi].batch = batch;
     last_nb[pi] = b;
     last_cl[pi] = c;
   }

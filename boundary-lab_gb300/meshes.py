@@ -510,5 +510,5 @@ def config_mesh(name: str) -> BoundaryMesh:
     if name == "box10k":
         return box_with_piston((0.3, 0.2, 0.25), 10000, 0.05, "+z")
     if name == "horn20k":
-        return horn_in_box()
+        return horn_in_box(target_faces=22300)  # 20,032 triangles (10,018 dofs)
     raise ValueError(f"unknown synthetic mesh {name!r}")

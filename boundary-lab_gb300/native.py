@@ -101,6 +101,7 @@ class SolveStats(ctypes.Structure):
         ("singular_pairs", ctypes.c_longlong),
         ("singular_points", ctypes.c_longlong),
         ("lu_gemm_used", ctypes.c_int),
+        ("kernel_launches", ctypes.c_longlong),
     ]
 
 KERNEL_SLOTS = ("singular", "regular", "gather", "rhs", "lu", "solve", "field")

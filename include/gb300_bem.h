@@ -101,7 +101,8 @@ typedef struct bem_solve_options {
   double refine_tol;     /* mixed form: stop when ||b - A x|| / ||b|| <= refine_tol (FP64 residual) */
   int max_refine;        /* mixed form: maximum refinement steps */
   int batch;             /* frequencies factored together (<= 64); 0 = automatic */
-  int lu_block;          /* LU block size (<= 64); 0 = automatic */
+  int lu_block;          /* LU panel width, 32 or 64 (trailing updates are 128 deep);
+                            0 = automatic (the width whose panels run in the fewest waves) */
   int outputs_on_device; /* 1: pressure_out / field_out are device pointers of the context's device */
   int profile;           /* 1: also time each kernel family with CUDA events (stats.kernel_s) */
   int lu_gemm;           /* LU trailing update of the mixed form: 0 automatic (tensor cores when
@@ -132,6 +133,7 @@ typedef struct bem_solve_stats {
   long long singular_pairs; /* vertex-sharing pairs integrated with Duffy rules, per frequency */
   long long singular_points; /* Duffy points summed over the singular pairs, per frequency */
   int lu_gemm_used;       /* trailing update that ran: 1 cuBLAS, 2 tensor cores (0 FP64 form) */
+  long long kernel_launches; /* kernels of this library launched by the call (cuBLAS kernels not counted) */
 } bem_solve_stats;
 
 void bem_default_options(bem_solve_options* opt);

@@ -3,7 +3,7 @@
 Tolerances (relative, Frobenius / 2-norm unless stated):
   FP64 form  : operators 1e-11, solutions and fields 1e-9 (rounding-order only)
   mixed form : operators 2e-6 (compensated FP32 entries), solutions and fields 1e-5
-               (the benchmark spec's bound on far-field pressure vs the FP64 oracle)
+               (the required bound on far-field pressure vs the FP64 oracle)
 """
 
 import numpy as np
