@@ -29,7 +29,7 @@ LABEL = "GB300 BEM (CUDA, sm_103a)"
 CAPABILITIES = contract.SolverCapabilities(
     supports_remote_assets=False,
     supports_parallel_workers=False,
-    supports_symmetry=False,
+    supports_symmetry=True,
     supports_channel_resynthesis=True,
     is_remote=False,
 )

@@ -46,6 +46,9 @@ bool ensure_smem_limit(const void* func, size_t bytes) {
 
 namespace {
 
+__device__ __forceinline__ double tr_sign_x(int tr) { return (tr & 1) ? -1.0 : 1.0; }
+__device__ __forceinline__ double tr_sign_y(int tr) { return (tr & 2) ? -1.0 : 1.0; }
+
 __device__ __forceinline__ bool share_vertex(const int* a, int b0, int b1, int b2) {
   return a[0] == b0 || a[0] == b1 || a[0] == b2 || a[1] == b0 || a[1] == b1 || a[1] == b2 || a[2] == b0 ||
          a[2] == b1 || a[2] == b2;
@@ -122,7 +125,8 @@ __global__ void __launch_bounds__(WARPS * 32, 3) regular_f32_kernel(const FaceF3
                                                                  const LaneSlot* __restrict__ slots,
                                                                  const int* __restrict__ tile_row_base,
                                                                  int max_rows, float2* __restrict__ Rext,
-                                                                 long long ldR, RegParamsF32 p) {
+                                                                 long long ldR, RegParamsF32 p, int ntr, int4 trs,
+                                                                 const unsigned char* __restrict__ fix_mask) {
   extern __shared__ float2 smem_acc32[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tile = blockIdx.y;
@@ -158,6 +162,40 @@ __global__ void __launch_bounds__(WARPS * 32, 3) regular_f32_kernel(const FaceF3
   const float a2g = T.area2;
   const int gv0 = T.verts[0], gv1 = T.verts[1], gv2 = T.verts[2];
 
+  // Symmetry images of the trial face (BeatEngineCpuAssembly.jl:411-445): the
+  // same test faces against the reflected trial face, added to the same trial
+  // columns.  The trial data are reflected in place from one transform to the
+  // next; pairs whose faces touch on the reflecting planes are left to the
+  // singular (Duffy) pass, like vertex-sharing pairs of the identity.
+  int prev_tr = 0;
+  for (int ti = 0; ti < ntr; ++ti) {
+    const int tr = ti == 0 ? trs.x : ti == 1 ? trs.y : ti == 2 ? trs.z : trs.w;
+    {
+      const int dlt = tr ^ prev_tr;
+      const float fx = (dlt & 1) ? -1.f : 1.f, fy = (dlt & 2) ? -1.f : 1.f, dr = fx * fy;
+      ahi_g[0] *= fx;
+      ahi_g[1] *= fy;
+      alo_g[0] *= fx;
+      alo_g[1] *= fy;
+      ng[0] *= fx;
+      ng[1] *= fy;
+#pragma unroll
+      for (int n = 0; n < Q; ++n) {
+        og[n][0] *= fx;
+        og[n][1] *= fy;
+      }
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        cg[3 * b] *= fx * dr;
+        cg[3 * b + 1] *= fy * dr;
+        cg[3 * b + 2] *= dr;
+      }
+      prev_tr = tr;
+    }
+    const int sv0 = (tr == 0 || (fix_mask[gv0] & tr) == tr) ? gv0 : -2;
+    const int sv1 = (tr == 0 || (fix_mask[gv1] & tr) == tr) ? gv1 : -2;
+    const int sv2 = (tr == 0 || (fix_mask[gv2] & tr) == tr) ? gv2 : -2;
+
   // Software pipeline over the lane groups: the slot of group grp + 2 and the
   // face header (vertices, anchor) of group grp + 1 are loaded while group grp
   // is integrated, so the pair set-up never waits on a global load.
@@ -192,7 +230,7 @@ __global__ void __launch_bounds__(WARPS * 32, 3) regular_f32_kernel(const FaceF3
     if (grp + 2 < g1) s_next = slots[(size_t)(grp + 2) * 32 + lane];
     if (s.face >= 0) {
       const FaceF32& F = faces[s.face];
-      if (!share_vertex(fv, gv0, gv1, gv2)) {
+      if (!share_vertex(fv, sv0, sv1, sv2)) {
         // With C = anchor_g - anchor_f, x_n = anchor_g + og[n], y_m = anchor_f + of[m]
         // and d = og[n] - of[m]:  r = |C + d|, and
         //   r - |C| = (2 C.d + d.d) / (r + |C|),
@@ -304,6 +342,7 @@ __global__ void __launch_bounds__(WARPS * 32, 3) regular_f32_kernel(const FaceF3
     }
     __syncwarp();
   }
+  }  // symmetry transforms
   // write this warp's three extended-row segments
   for (int i = lane; i < 3 * rows; i += 32) {
     const int b = i / rows, loc = i - b * rows;
@@ -326,7 +365,8 @@ __global__ void __launch_bounds__(WARPS * 32) regular_f64_kernel(const FaceF64* 
                                                                  const LaneSlot* __restrict__ slots,
                                                                  const int* __restrict__ tile_row_base,
                                                                  int max_rows, double2* __restrict__ Rext,
-                                                                 long long ldR, RegParamsF64 p) {
+                                                                 long long ldR, RegParamsF64 p, int ntr, int4 trs,
+                                                                 const unsigned char* __restrict__ fix_mask) {
   extern __shared__ double2 smem_acc64[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tile = blockIdx.y;
@@ -353,12 +393,38 @@ __global__ void __launch_bounds__(WARPS * 32) regular_f64_kernel(const FaceF64* 
   const double a2g = T.area2;
   const int gv0 = T.verts[0], gv1 = T.verts[1], gv2 = T.verts[2];
   const int g0 = tile_group_ptr[tile], g1 = tile_group_ptr[tile + 1];
+  int prev_tr = 0;
+  for (int ti = 0; ti < ntr; ++ti) {  // symmetry images, as in regular_f32_kernel
+    const int tr = ti == 0 ? trs.x : ti == 1 ? trs.y : ti == 2 ? trs.z : trs.w;
+    {
+      const int dlt = tr ^ prev_tr;
+      const double fx = (dlt & 1) ? -1.0 : 1.0, fy = (dlt & 2) ? -1.0 : 1.0, dr = fx * fy;
+      ag[0] *= fx;
+      ag[1] *= fy;
+      ng[0] *= fx;
+      ng[1] *= fy;
+#pragma unroll
+      for (int n = 0; n < Q; ++n) {
+        og[n][0] *= fx;
+        og[n][1] *= fy;
+      }
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        cg[3 * b] *= fx * dr;
+        cg[3 * b + 1] *= fy * dr;
+        cg[3 * b + 2] *= dr;
+      }
+      prev_tr = tr;
+    }
+    const int sv0 = (tr == 0 || (fix_mask[gv0] & tr) == tr) ? gv0 : -2;
+    const int sv1 = (tr == 0 || (fix_mask[gv1] & tr) == tr) ? gv1 : -2;
+    const int sv2 = (tr == 0 || (fix_mask[gv2] & tr) == tr) ? gv2 : -2;
   for (int grp = g0; grp < g1; ++grp) {
     const LaneSlot s = slots[(size_t)grp * 32 + lane];
     if (s.face >= 0) {
       const FaceF64& F = faces[s.face];
       int fv[3] = {F.verts[0], F.verts[1], F.verts[2]};
-      if (!share_vertex(fv, gv0, gv1, gv2)) {
+      if (!share_vertex(fv, sv0, sv1, sv2)) {
         double C[3] = {ag[0] - F.anchor[0], ag[1] - F.anchor[1], ag[2] - F.anchor[2]};
         double2 IG[3][3], ID[3][3];
 #pragma unroll
@@ -437,6 +503,7 @@ __global__ void __launch_bounds__(WARPS * 32) regular_f64_kernel(const FaceF64* 
     }
     __syncwarp();
   }
+  }  // symmetry transforms
   for (int i = lane; i < 3 * rows; i += 32) {
     const int b = i / rows, loc = i - b * rows;
     Rext[(size_t)(3 * g + b) * ldR + base + loc] = acc[b * max_rows + loc];
@@ -493,15 +560,17 @@ __global__ void singular_static_kernel(SingularGeom geo, const SingularPair* __r
   const int* fr = geo.faces + 3 * P.trial;
   double t0[3], e1t[3], e2t[3], d0[3], e1r[3], e2r[3], nt[3], nr[3];
   for (int d = 0; d < 3; ++d) {
+    // image pairs: the trial face reflected by P.tr (points and normal S p)
+    const double sd = d == 0 ? tr_sign_x(P.tr) : d == 1 ? tr_sign_y(P.tr) : 1.0;
     t0[d] = geo.verts[3 * ft[0] + d];
     e1t[d] = geo.verts[3 * ft[1] + d] - t0[d];
     e2t[d] = geo.verts[3 * ft[2] + d] - t0[d];
-    const double r0 = geo.verts[3 * fr[0] + d];
+    const double r0 = sd * geo.verts[3 * fr[0] + d];
     d0[d] = r0 - t0[d];
-    e1r[d] = geo.verts[3 * fr[1] + d] - r0;
-    e2r[d] = geo.verts[3 * fr[2] + d] - r0;
+    e1r[d] = sd * geo.verts[3 * fr[1] + d] - r0;
+    e2r[d] = sd * geo.verts[3 * fr[2] + d] - r0;
     nt[d] = geo.normal[3 * P.test + d];
-    nr[d] = geo.normal[3 * P.trial + d];
+    nr[d] = sd * geo.normal[3 * P.trial + d];
   }
   double acc[kStatic];
 #pragma unroll
@@ -567,15 +636,16 @@ __global__ void singular_dyn_kernel(SingularGeom geo, const SingularPair* __rest
   const int* fr = geo.faces + 3 * P.trial;
   R e1t[3], e2t[3], d0[3], e1r[3], e2r[3], nt[3], nr[3];
   for (int d = 0; d < 3; ++d) {
+    const double sd = d == 0 ? tr_sign_x(P.tr) : d == 1 ? tr_sign_y(P.tr) : 1.0;  // image pairs: S p
     const double t0 = geo.verts[3 * ft[0] + d];
-    const double r0 = geo.verts[3 * fr[0] + d];
+    const double r0 = sd * geo.verts[3 * fr[0] + d];
     e1t[d] = (R)(geo.verts[3 * ft[1] + d] - t0);
     e2t[d] = (R)(geo.verts[3 * ft[2] + d] - t0);
     d0[d] = (R)(r0 - t0);
-    e1r[d] = (R)(geo.verts[3 * fr[1] + d] - r0);
-    e2r[d] = (R)(geo.verts[3 * fr[2] + d] - r0);
+    e1r[d] = (R)(sd * geo.verts[3 * fr[1] + d] - r0);
+    e2r[d] = (R)(sd * geo.verts[3 * fr[2] + d] - r0);
     nt[d] = (R)geo.normal[3 * P.test + d];
-    nr[d] = (R)geo.normal[3 * P.trial + d];
+    nr[d] = (R)(sd * geo.normal[3 * P.trial + d]);
   }
   // accumulators: SR[3], IR[9], IDh[9], IKh[3] (complex) = 48 reals
   R acc[48];
@@ -679,9 +749,18 @@ __global__ void singular_dyn_kernel(SingularGeom geo, const SingularPair* __rest
   C2 S0 = cplx<R>::make((R)(M[0] + M[1] + M[2]), R(0));
   for (int a = 0; a < 3; ++a) S0 = cadd(S0, SR[a]);
   const double* ct = curls + 9 * (size_t)P.test;
-  const double* cr = curls + 9 * (size_t)P.trial;
+  const double* cr0 = curls + 9 * (size_t)P.trial;
+  double cr[9];  // image pairs: reflected curls det(S) S c
+  {
+    const double sx = tr_sign_x(P.tr), sy = tr_sign_y(P.tr), det = sx * sy;
+    for (int b = 0; b < 3; ++b) {
+      cr[3 * b] = det * sx * cr0[3 * b];
+      cr[3 * b + 1] = det * sy * cr0[3 * b + 1];
+      cr[3 * b + 2] = det * cr0[3 * b + 2];
+    }
+  }
   const R kk_nn = p.k2 * (R)P.nprod;
-  const bool coincident = P.kind == 1;
+  const bool coincident = P.kind == 1 && P.tr == 0;  // mass terms: the face with itself, never with an image
   const R a2 = (R)(2.0 * area[P.test]);
   C2* o = out + (size_t)kSingOut * warp;
   for (int a = 0; a < 3; ++a) {
@@ -729,7 +808,8 @@ __global__ void gather_columns_kernel(const C2* __restrict__ Rext, long long ldR
                                       const int* __restrict__ col_fb, const int* __restrict__ ext_row,
                                       const int* __restrict__ halo_slot_of_ext, const int* __restrict__ halo_row_ptr,
                                       const int* __restrict__ halo_row, int n_ext, int n_halo_rows,
-                                      C2* __restrict__ A, long long lda, C2* __restrict__ A2, int col0) {
+                                      C2* __restrict__ A, long long lda, C2* __restrict__ A2, int col0,
+                                      const double* __restrict__ row_weight) {
   extern __shared__ unsigned char smem_raw[];
   C2* hb = reinterpret_cast<C2*>(smem_raw);
   const int j = col0 + blockIdx.x;
@@ -743,6 +823,7 @@ __global__ void gather_columns_kernel(const C2* __restrict__ Rext, long long ldR
     for (int k = k0; k < k1; ++k) v = cadd(v, Rext[(size_t)col_fb[k] * ldR + e]);
     const int hs = halo_slot_of_ext[e];
     if (hs < 0) {
+      if (row_weight) v = cscale(v, (decltype(v.x))row_weight[ext_row[e]]);  // symmetry orbit weight of the row
       Aj[ext_row[e]] = v;
       if (A2j) A2j[ext_row[e]] = v;
     } else {
@@ -756,6 +837,7 @@ __global__ void gather_columns_kernel(const C2* __restrict__ Rext, long long ldR
     s.y = 0;
     for (int i = halo_row_ptr[h]; i < halo_row_ptr[h + 1]; ++i) s = cadd(s, hb[i]);
     const int r = halo_row[h];
+    if (row_weight) s = cscale(s, (decltype(s.x))row_weight[r]);
     Aj[r] = cadd(Aj[r], s);
     if (A2j) A2j[r] = cadd(A2j[r], s);
   }
@@ -785,9 +867,12 @@ template <> struct FaceRec<float> { typedef FaceF32 type; };
 template <> struct FaceRec<double> { typedef FaceF64 type; };
 
 template <int Q>
+// sx, sy: reflection of the trial face (symmetry images; 1, 1 for the face itself).
 __device__ __forceinline__ void rhs_pair_f32(const FaceF32& F, const FaceF32& Gf, const RhsParams<float>& p,
-                                             float2 S[3], float2 K[3]) {
-  PairF32 P = pair_setup_f32(Gf.anchor_hi, Gf.anchor_lo, F.anchor_hi, F.anchor_lo, p.kdf);
+                                             float2 S[3], float2 K[3], float sx = 1.f, float sy = 1.f) {
+  const float ghi[3] = {sx * Gf.anchor_hi[0], sy * Gf.anchor_hi[1], Gf.anchor_hi[2]};
+  const float glo[3] = {sx * Gf.anchor_lo[0], sy * Gf.anchor_lo[1], Gf.anchor_lo[2]};
+  PairF32 P = pair_setup_f32(ghi, glo, F.anchor_hi, F.anchor_lo, p.kdf);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     S[a] = make_float2(0.f, 0.f);
@@ -799,7 +884,7 @@ __device__ __forceinline__ void rhs_pair_f32(const FaceF32& F, const FaceF32& Gf
     float2 us = make_float2(0.f, 0.f), uk = make_float2(0.f, 0.f);
 #pragma unroll
     for (int n = 0; n < Q; ++n) {
-      float d[3] = {Gf.off[3 * n] - of[0], Gf.off[3 * n + 1] - of[1], Gf.off[3 * n + 2] - of[2]};
+      float d[3] = {sx * Gf.off[3 * n] - of[0], sy * Gf.off[3 * n + 1] - of[1], Gf.off[3 * n + 2] - of[2]};
       float rinv, rv[3];
       float2 G;
       green_f32(P, d, p.k, rinv, rv, G);
@@ -832,8 +917,9 @@ __device__ __forceinline__ void rhs_pair_f32(const FaceF32& F, const FaceF32& Gf
 
 template <int Q>
 __device__ __forceinline__ void rhs_pair_f64(const FaceF64& F, const FaceF64& Gf, const RhsParams<double>& p,
-                                             double2 S[3], double2 K[3]) {
-  const double C[3] = {Gf.anchor[0] - F.anchor[0], Gf.anchor[1] - F.anchor[1], Gf.anchor[2] - F.anchor[2]};
+                                             double2 S[3], double2 K[3], double sx = 1.0, double sy = 1.0) {
+  const double sg[3] = {sx, sy, 1.0};
+  const double C[3] = {sx * Gf.anchor[0] - F.anchor[0], sy * Gf.anchor[1] - F.anchor[1], Gf.anchor[2] - F.anchor[2]};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     S[a] = make_double2(0., 0.);
@@ -845,7 +931,7 @@ __device__ __forceinline__ void rhs_pair_f64(const FaceF64& F, const FaceF64& Gf
 #pragma unroll
     for (int n = 0; n < Q; ++n) {
       double rv[3];
-      for (int d = 0; d < 3; ++d) rv[d] = C[d] + (Gf.off[3 * n + d] - F.off[3 * m + d]);
+      for (int d = 0; d < 3; ++d) rv[d] = C[d] + (sg[d] * Gf.off[3 * n + d] - F.off[3 * m + d]);
       const double r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
       if (r2 == 0.0) continue;
       const double r = sqrt(r2), rinv = 1.0 / r;
@@ -884,7 +970,8 @@ __global__ void rhs_faces_kernel(const typename FaceRec<R>::type* __restrict__ f
                                  const typename cplx<R>::type* __restrict__ drive,  // NC x nf
                                  const SingularPair* __restrict__ pairs, const int* __restrict__ by_test_ptr,
                                  const int* __restrict__ by_test, const typename cplx<R>::type* __restrict__ sblocks,
-                                 RhsParams<R> p, typename cplx<R>::type* __restrict__ rb) {
+                                 RhsParams<R> p, typename cplx<R>::type* __restrict__ rb, int ntr, int4 trs,
+                                 const unsigned char* __restrict__ fix_mask) {
   typedef typename cplx<R>::type C2;
   const int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -895,15 +982,21 @@ __global__ void rhs_faces_kernel(const typename FaceRec<R>::type* __restrict__ f
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int c = 0; c < NC; ++c) acc[a][c] = cplx<R>::make(0, 0);
+  // driven faces and their symmetry images (touching pairs are in the singular blocks)
+  for (int ti = 0; ti < ntr; ++ti)
   for (int i = lane; i < ndriven; i += 32) {
+    const int tr = ti == 0 ? trs.x : ti == 1 ? trs.y : ti == 2 ? trs.z : trs.w;
     const int g = driven[i];
     const auto& Gf = faces[g];
-    if (share_vertex(F.verts, Gf.verts[0], Gf.verts[1], Gf.verts[2])) continue;
+    int sv[3];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) sv[b] = (tr == 0 || (fix_mask[Gf.verts[b]] & tr) == tr) ? Gf.verts[b] : -2;
+    if (share_vertex(F.verts, sv[0], sv[1], sv[2])) continue;
     C2 S[3], K[3];
     if constexpr (sizeof(R) == 4)
-      rhs_pair_f32<Q>(F, Gf, p, S, K);
+      rhs_pair_f32<Q>(F, Gf, p, S, K, (float)tr_sign_x(tr), (float)tr_sign_y(tr));
     else
-      rhs_pair_f64<Q>(F, Gf, p, S, K);
+      rhs_pair_f64<Q>(F, Gf, p, S, K, tr_sign_x(tr), tr_sign_y(tr));
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
       const C2 q = cmul(p.qscale, drive[(size_t)c * nf + g]);
@@ -941,7 +1034,7 @@ __global__ void rhs_faces_kernel(const typename FaceRec<R>::type* __restrict__ f
 template <typename C2>
 __global__ void rhs_gather_kernel(const C2* __restrict__ rb, int nf, int nc, const int* __restrict__ col_ptr,
                                   const int* __restrict__ col_fb, const int* __restrict__ vertex_row, int nv,
-                                  C2* __restrict__ b, long long ldb) {
+                                  C2* __restrict__ b, long long ldb, const double* __restrict__ row_weight) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nv) return;
   for (int c = 0; c < nc; ++c) {
@@ -949,6 +1042,7 @@ __global__ void rhs_gather_kernel(const C2* __restrict__ rb, int nf, int nc, con
     s.x = 0;
     s.y = 0;
     for (int k = col_ptr[j]; k < col_ptr[j + 1]; ++k) s = cadd(s, rb[(size_t)c * nf * 3 + col_fb[k]]);
+    if (row_weight) s = cscale(s, (decltype(s.x))row_weight[vertex_row[j]]);
     b[(size_t)c * ldb + vertex_row[j]] = s;
   }
 }
@@ -997,7 +1091,8 @@ cudaError_t launch_regular(const DeviceMesh& m, Precision prec, double k, double
     auto launch = [&](auto kern) {
       ensure_smem_limit((const void*)kern, sm);
       kern<<<grid, W * 32, sm, stream>>>(m.faces32, m.nf, m.tile_group_ptr, m.lane_slots, m.tile_row_base,
-                                         m.max_tile_rows, (float2*)Rext, ldR, p);
+                                         m.max_tile_rows, (float2*)Rext, ldR, p, m.ntr,
+                                         make_int4(m.tr[0], m.tr[1], m.tr[2], m.tr[3]), m.fix_mask);
     };
     if (m.Q == 6)
       launch(regular_f32_kernel<6, W>);
@@ -1016,7 +1111,8 @@ cudaError_t launch_regular(const DeviceMesh& m, Precision prec, double k, double
     auto launch = [&](auto kern) {
       ensure_smem_limit((const void*)kern, sm);
       kern<<<grid, W * 32, sm, stream>>>(m.faces64, m.nf, m.tile_group_ptr, m.lane_slots, m.tile_row_base,
-                                         m.max_tile_rows, (double2*)Rext, ldR, p);
+                                         m.max_tile_rows, (double2*)Rext, ldR, p, m.ntr,
+                                         make_int4(m.tr[0], m.tr[1], m.tr[2], m.tr[3]), m.fix_mask);
     };
     if (m.Q == 6)
       launch(regular_f64_kernel<6, W>);
@@ -1096,7 +1192,7 @@ cudaError_t launch_gather(const DeviceMesh& m, Precision prec, const void* Rext,
     if (sm > 48 * 1024) ensure_smem_limit((const void*)gather_columns_kernel<float2>, sm);
     gather_columns_kernel<float2><<<m.nv, threads, sm, stream>>>(
         (const float2*)Rext, ldR, m.col_ptr, m.col_fb, m.ext_row, m.halo_slot_of_ext, m.halo_row_ptr, m.halo_row,
-        m.n_ext, m.n_halo_rows, (float2*)A, lda, (float2*)A2, 0);
+        m.n_ext, m.n_halo_rows, (float2*)A, lda, (float2*)A2, 0, m.row_weight);
     if (m.n_isolated)
       isolated_identity_kernel<float2><<<(m.n_isolated + 127) / 128, 128, 0, stream>>>(
           m.isolated, m.n_isolated, m.vertex_row, (float2*)A, lda, (float2*)A2);
@@ -1105,7 +1201,7 @@ cudaError_t launch_gather(const DeviceMesh& m, Precision prec, const void* Rext,
     if (sm > 48 * 1024) ensure_smem_limit((const void*)gather_columns_kernel<double2>, sm);
     gather_columns_kernel<double2><<<m.nv, threads, sm, stream>>>(
         (const double2*)Rext, ldR, m.col_ptr, m.col_fb, m.ext_row, m.halo_slot_of_ext, m.halo_row_ptr,
-        m.halo_row, m.n_ext, m.n_halo_rows, (double2*)A, lda, (double2*)A2, 0);
+        m.halo_row, m.n_ext, m.n_halo_rows, (double2*)A, lda, (double2*)A2, 0, m.row_weight);
     if (m.n_isolated)
       isolated_identity_kernel<double2><<<(m.n_isolated + 127) / 128, 128, 0, stream>>>(
           m.isolated, m.n_isolated, m.vertex_row, (double2*)A, lda, (double2*)A2);
@@ -1130,7 +1226,9 @@ cudaError_t launch_rhs(const DeviceMesh& m, Precision prec, double k, const Oper
   rhs_faces_kernel<float, QQ, NCC><<<nblk, threads, 0, stream>>>(m.faces32, m.nf, m.driven, m.ndriven,        \
                                                                  (const float2*)drive, m.pairs,              \
                                                                  m.pairs_by_test_ptr, m.pairs_by_test,       \
-                                                                 (const float2*)sblocks, p, (float2*)rb)
+                                                                 (const float2*)sblocks, p, (float2*)rb,     \
+                                                                 m.ntr, make_int4(m.tr[0], m.tr[1], m.tr[2], \
+                                                                 m.tr[3]), m.fix_mask)
 #define BEM_RHS32_Q(NCC)        \
   if (m.Q == 6)                 \
     BEM_RHS32(6, NCC);          \
@@ -1147,7 +1245,7 @@ cudaError_t launch_rhs(const DeviceMesh& m, Precision prec, double k, const Oper
     }
     rhs_gather_kernel<float2><<<(m.nv + 127) / 128, 128, 0, stream>>>((const float2*)rb, m.nf, nc, m.col_ptr,
                                                                        m.col_fb, m.vertex_row, m.nv, (float2*)b,
-                                                                       ldb);
+                                                                       ldb, m.row_weight);
   } else {
     RhsParams<double> p;
     p.k = k;
@@ -1159,7 +1257,9 @@ cudaError_t launch_rhs(const DeviceMesh& m, Precision prec, double k, const Oper
   rhs_faces_kernel<double, QQ, NCC><<<nblk, threads, 0, stream>>>(m.faces64, m.nf, m.driven, m.ndriven,       \
                                                                   (const double2*)drive, m.pairs,            \
                                                                   m.pairs_by_test_ptr, m.pairs_by_test,      \
-                                                                  (const double2*)sblocks, p, (double2*)rb)
+                                                                  (const double2*)sblocks, p, (double2*)rb,  \
+                                                                  m.ntr, make_int4(m.tr[0], m.tr[1], m.tr[2], \
+                                                                  m.tr[3]), m.fix_mask)
 #define BEM_RHS64_Q(NCC)        \
   if (m.Q == 6)                 \
     BEM_RHS64(6, NCC);          \
@@ -1176,7 +1276,7 @@ cudaError_t launch_rhs(const DeviceMesh& m, Precision prec, double k, const Oper
     }
     rhs_gather_kernel<double2><<<(m.nv + 127) / 128, 128, 0, stream>>>((const double2*)rb, m.nf, nc, m.col_ptr,
                                                                         m.col_fb, m.vertex_row, m.nv,
-                                                                        (double2*)b, ldb);
+                                                                        (double2*)b, ldb, m.row_weight);
   }
   return cudaGetLastError();
 }

@@ -322,6 +322,12 @@ long long bem_context_scratch_bytes(const bem_context* ctx) {
 
 int bem_upload_mesh(bem_context* ctx, const double* vertices, int n_vertices, const int* faces, int n_faces,
                     int regular_order, int singular_order, bem_mesh** out) {
+  return bem_upload_mesh_symmetric(ctx, vertices, n_vertices, faces, n_faces, regular_order, singular_order,
+                                   BEM_SYMMETRY_OFF, out);
+}
+
+int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_vertices, const int* faces,
+                              int n_faces, int regular_order, int singular_order, int symmetry, bem_mesh** out) {
   if (!ctx) return BEM_ERR_INVALID_ARGUMENT;
   return guarded(ctx, [&]() -> int {
     if (!out || !vertices || !faces) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "null pointer argument");
@@ -332,7 +338,8 @@ int bem_upload_mesh(bem_context* ctx, const double* vertices, int n_vertices, co
       b->stream = ctx->stream;
       b->pool = ctx->pool;
     }
-    std::string e = bem::build_mesh_plan(vertices, n_vertices, faces, n_faces, regular_order, singular_order, 512, m->plan);
+    std::string e = bem::build_mesh_plan(vertices, n_vertices, faces, n_faces, regular_order, singular_order, 512, m->plan,
+                                         symmetry);
     if (!e.empty()) {
       delete m;
       return fail(ctx, BEM_ERR_INVALID_ARGUMENT, e);
@@ -349,6 +356,12 @@ int bem_upload_mesh(bem_context* ctx, const double* vertices, int n_vertices, co
       d.n_halo = (int)P.halo_ext.size();
       d.n_halo_rows = (int)P.halo_row.size();
       d.npairs = (int)P.pairs.size();
+      d.ntr = (int)P.transforms.size();
+      for (int i = 0; i < d.ntr && i < 4; ++i) d.tr[i] = P.transforms[i];
+      if (P.symmetry != 0) {
+        d.fix_mask = upload(m, P.fix_mask);
+        d.row_weight = upload(m, P.row_weight);
+      }
       d.faces32 = upload(m, P.faces32);
       d.faces64 = upload(m, P.faces64);
       d.tile_group_ptr = upload(m, P.tile_group_ptr);
@@ -721,7 +734,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       stats->max_rel_residual = max_res;
       stats->batches = batches;
       for (int i = 0; i < 8; ++i) stats->kernel_s[i] = kacc[i];
-      stats->regular_pairs = (long long)dm.nf * dm.nf - dm.npairs;
+      stats->regular_pairs = (long long)dm.ntr * dm.nf * dm.nf - dm.npairs;  // identity and image pairs
       stats->singular_pairs = dm.npairs;
       stats->singular_points = m->singular_points;
       stats->lu_gemm_used = gemm_used;

@@ -77,7 +77,8 @@ __global__ void __launch_bounds__(256) field_f32_kernel(const FaceF32* __restric
                                                         const float2* __restrict__ drive,  // NC x nf
                                                         const double* __restrict__ obs, int nobs,
                                                         const FieldParamsF32* __restrict__ prm,
-                                                        double2* __restrict__ out, FieldRule<float> fr) {
+                                                        double2* __restrict__ out, FieldRule<float> fr, int ntr,
+                                                        int4 trs) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int o = blockIdx.x * 32 + lane, bt = blockIdx.y;
   const bool live = o < nobs;
@@ -100,14 +101,19 @@ __global__ void __launch_bounds__(256) field_f32_kernel(const FaceF32* __restric
     br[c] = 0.f;
     bcmp[c] = 0.f;
   }
+  // sources: every face and, under symmetry, its images (BeatEngineCore.jl:1240-1280)
+  for (int ti = 0; ti < ntr; ++ti)
   for (int g = wid; g < nf; g += kFieldWarps) {
     const FaceF32& F = faces[g];
+    const int tr = ti == 0 ? trs.x : ti == 1 ? trs.y : ti == 2 ? trs.z : trs.w;
+    const float sg[3] = {(tr & 1) ? -1.f : 1.f, (tr & 2) ? -1.f : 1.f, 1.f};
+    const float nrm[3] = {sg[0] * F.normal[0], sg[1] * F.normal[1], F.normal[2]};
     // base phase k|c_g - x| in double-float
     df C[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      df s = two_sum(F.anchor_hi[d], -xhi[d]);
-      s.lo += F.anchor_lo[d] - xlo[d];
+      df s = two_sum(sg[d] * F.anchor_hi[d], -xhi[d]);
+      s.lo += sg[d] * F.anchor_lo[d] - xlo[d];
       C[d] = quick_two_sum(s.hi, s.lo);
     }
     df r2 = df_add(df_add(df_mul(C[0], C[0]), df_mul(C[1], C[1])), df_mul(C[2], C[2]));
@@ -115,7 +121,7 @@ __global__ void __launch_bounds__(256) field_f32_kernel(const FaceF32* __restric
     const float R0 = R.hi + R.lo;
     const float theta0 = df_reduce_two_pi(df_mul(kdf, R));
     const float Cf[3] = {C[0].hi + C[0].lo, C[1].hi + C[1].lo, C[2].hi + C[2].lo};
-    const float Cn = fmaf(Cf[0], F.normal[0], fmaf(Cf[1], F.normal[1], Cf[2] * F.normal[2]));
+    const float Cn = fmaf(Cf[0], nrm[0], fmaf(Cf[1], nrm[1], Cf[2] * nrm[2]));
     float2 qg[NC], fs[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
@@ -124,7 +130,7 @@ __global__ void __launch_bounds__(256) field_f32_kernel(const FaceF32* __restric
     }
 #pragma unroll
     for (int n = 0; n < Q; ++n) {
-      const float d[3] = {F.off[3 * n], F.off[3 * n + 1], F.off[3 * n + 2]};
+      const float d[3] = {sg[0] * F.off[3 * n], sg[1] * F.off[3 * n + 1], F.off[3 * n + 2]};
       const float rv[3] = {Cf[0] + d[0], Cf[1] + d[1], Cf[2] + d[2]};
       const float rr = fmaf(rv[0], rv[0], fmaf(rv[1], rv[1], rv[2] * rv[2]));
       const float rinv = rr > 1e-30f ? rsqrt_ftz(rr) : 0.f;
@@ -138,7 +144,7 @@ __global__ void __launch_bounds__(256) field_f32_kernel(const FaceF32* __restric
       const float sc = rinv * BEM_INV_FOUR_PI;
       const float2 G = make_float2(cs * sc, sn * sc);
       // (r . n_y) / r with r . n_y = C . n + d . n (d . n = 0 for points on the face plane, kept for generality)
-      const float t = (Cn + fmaf(d[0], F.normal[0], fmaf(d[1], F.normal[1], d[2] * F.normal[2]))) * rinv;
+      const float t = (Cn + fmaf(d[0], nrm[0], fmaf(d[1], nrm[1], d[2] * nrm[2]))) * rinv;
       const float2 Dk = make_float2(t * (-G.x * rinv - G.y * k), t * (G.x * k - G.y * rinv));
       const float wn = fr.w[n];
 #pragma unroll
@@ -183,7 +189,8 @@ __global__ void __launch_bounds__(256) field_f64_kernel(const FaceF64* __restric
                                                         const double2* __restrict__ drive,
                                                         const double* __restrict__ obs, int nobs,
                                                         const FieldParamsF64* __restrict__ prm,
-                                                        double2* __restrict__ out, FieldRule<double> fr) {
+                                                        double2* __restrict__ out, FieldRule<double> fr, int ntr,
+                                                        int4 trs) {
   const int o = blockIdx.x, bt = blockIdx.y;
   const double xo[3] = {obs[3 * o], obs[3 * o + 1], obs[3 * o + 2]};
   const double k = prm->k[bt];
@@ -191,8 +198,11 @@ __global__ void __launch_bounds__(256) field_f64_kernel(const FaceF64* __restric
   double2 acc[NC];
 #pragma unroll
   for (int c = 0; c < NC; ++c) acc[c] = make_double2(0., 0.);
+  for (int ti = 0; ti < ntr; ++ti)  // every face and its symmetry images
   for (int g = threadIdx.x; g < nf; g += blockDim.x) {
     const FaceF64& F = faces[g];
+    const int tr = ti == 0 ? trs.x : ti == 1 ? trs.y : ti == 2 ? trs.z : trs.w;
+    const double sg[3] = {(tr & 1) ? -1.0 : 1.0, (tr & 2) ? -1.0 : 1.0, 1.0};
     double2 qg[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) qg[c] = cscale(cmul(qs, drive[(size_t)c * nf + g]), F.area2);
@@ -200,7 +210,7 @@ __global__ void __launch_bounds__(256) field_f64_kernel(const FaceF64* __restric
     for (int n = 0; n < Q; ++n) {
       double rv[3];
 #pragma unroll
-      for (int d = 0; d < 3; ++d) rv[d] = (F.anchor[d] - xo[d]) + F.off[3 * n + d];
+      for (int d = 0; d < 3; ++d) rv[d] = (sg[d] * F.anchor[d] - xo[d]) + sg[d] * F.off[3 * n + d];
       const double rr = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
       if (rr == 0.0) continue;
       const double r = sqrt(rr), rinv = 1.0 / r;
@@ -208,7 +218,7 @@ __global__ void __launch_bounds__(256) field_f64_kernel(const FaceF64* __restric
       sincos(k * r, &sn, &cs);
       const double sc = rinv * (0.25 / CUDART_PI);
       const double2 G = make_double2(cs * sc, sn * sc);
-      const double t = (rv[0] * F.normal[0] + rv[1] * F.normal[1] + rv[2] * F.normal[2]) * rinv;
+      const double t = (rv[0] * sg[0] * F.normal[0] + rv[1] * sg[1] * F.normal[1] + rv[2] * F.normal[2]) * rinv;
       const double2 Dk = make_double2(t * (-G.x * rinv - G.y * k), t * (G.x * k - G.y * rinv));
       const double wn = fr.w[n];
 #pragma unroll
@@ -286,7 +296,8 @@ cudaError_t launch_field(const DeviceMesh& m, Precision prec, int batch, const d
     cudaMemcpyAsync(dp, &hp, sizeof(hp), cudaMemcpyHostToDevice, stream);
 #define BEM_F32(QQ, NCC)                                                                                   \
   field_f32_kernel<QQ, NCC><<<grid32, 256, 0, stream>>>(m.faces32, m.nf, (const float2*)sources,           \
-                                                      (const float2*)drive, obs, nobs, dp, out, fr32)
+                                                      (const float2*)drive, obs, nobs, dp, out, fr32, m.ntr, \
+                                                      make_int4(m.tr[0], m.tr[1], m.tr[2], m.tr[3]))
 #define BEM_F32_Q(NCC)    \
   if (m.Q == 6)           \
     BEM_F32(6, NCC);      \
@@ -313,7 +324,8 @@ cudaError_t launch_field(const DeviceMesh& m, Precision prec, int batch, const d
     cudaMemcpyAsync(dp, &hp, sizeof(hp), cudaMemcpyHostToDevice, stream);
 #define BEM_F64(QQ, NCC)                                                                                   \
   field_f64_kernel<QQ, NCC><<<grid, 256, 0, stream>>>(m.faces64, m.nf, (const double2*)sources,            \
-                                                      (const double2*)drive, obs, nobs, dp, out, fr64)
+                                                      (const double2*)drive, obs, nobs, dp, out, fr64, m.ntr, \
+                                                      make_int4(m.tr[0], m.tr[1], m.tr[2], m.tr[3]))
 #define BEM_F64_Q(NCC)    \
   if (m.Q == 6)           \
     BEM_F64(6, NCC);      \
@@ -375,11 +387,11 @@ cudaError_t launch_field_single(Precision prec, const void* faces, int nf, int Q
     const float2* s = (const float2*)sources;
     const float2* d = (const float2*)drive;
     if (Q == 6)
-      field_f32_kernel<6, 1><<<grid32, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32);
+      field_f32_kernel<6, 1><<<grid32, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32, 1, make_int4(0, 0, 0, 0));
     else if (Q == 3)
-      field_f32_kernel<3, 1><<<grid32, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32);
+      field_f32_kernel<3, 1><<<grid32, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32, 1, make_int4(0, 0, 0, 0));
     else
-      field_f32_kernel<1, 1><<<grid32, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32);
+      field_f32_kernel<1, 1><<<grid32, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr32, 1, make_int4(0, 0, 0, 0));
   } else {
     FieldParamsF64* dp = (FieldParamsF64*)params;
     write_field_params_f64<<<1, 1, 0, stream>>>(dp, k);
@@ -387,11 +399,11 @@ cudaError_t launch_field_single(Precision prec, const void* faces, int nf, int Q
     const double2* s = (const double2*)sources;
     const double2* d = (const double2*)drive;
     if (Q == 6)
-      field_f64_kernel<6, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr64);
+      field_f64_kernel<6, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr64, 1, make_int4(0, 0, 0, 0));
     else if (Q == 3)
-      field_f64_kernel<3, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr64);
+      field_f64_kernel<3, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr64, 1, make_int4(0, 0, 0, 0));
     else
-      field_f64_kernel<1, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr64);
+      field_f64_kernel<1, 1><<<grid, 256, 0, stream>>>(f, nf, s, d, obs, nobs, dp, out, fr64, 1, make_int4(0, 0, 0, 0));
   }
   return cudaGetLastError();
 }

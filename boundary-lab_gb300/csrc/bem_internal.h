@@ -51,12 +51,27 @@ struct alignas(16) LaneSlot {
 // Singular (vertex-sharing) pair.
 struct SingularPair {
   int test, trial, rule, kind;  // kind 1 coincident, 2 edge, 3 vertex
+  int tr;                       // symmetry transform of the trial face (0 identity, 1 x, 2 y, 3 xy)
+  int pad;
   double jac;                   // (2 A_test)(2 A_trial)
-  double nprod;                 // n_test . n_trial
+  double nprod;                 // n_test . (S n_trial)
 };
+
+// Symmetry transform tr (bit 0: x -> -x, bit 1: y -> -y): S = diag(sx, sy, 1),
+// reflected points and normals are S p, reflected surface curls det(S) S c
+// (BeatEngineCore.jl:323-355).  A vertex is fixed by tr when it lies on every
+// plane tr reflects across: (fix_mask & tr) == tr.
+inline int tr_sx(int tr) { return (tr & 1) ? -1 : 1; }
+inline int tr_sy(int tr) { return (tr & 2) ? -1 : 1; }
 
 struct MeshPlan {
   int nv = 0, nf = 0, Q = 0, regular_order = 4, singular_order = 4;
+  // symmetry: 0 off, 1 x (half model, x >= 0), 2 xy (quarter model, x, y >= 0)
+  int symmetry = 0;
+  std::vector<int> transforms;          // {0} | {0, 1} | {0, 1, 2, 3}
+  std::vector<unsigned char> fix_mask;  // per vertex: bit 0 on x = 0, bit 1 on y = 0
+  std::vector<double> row_weight;       // per matrix row: symmetry orbit weight of its vertex (1, 2, 4)
+  int image_pairs = 0;                  // singular pairs of a test face with a reflected trial face
   // regular rule on the reference triangle
   std::vector<double> rule_pts;  // Q x 2
   std::vector<double> rule_w;    // Q
@@ -106,6 +121,6 @@ struct MeshPlan {
 
 // Build the plan; returns an empty string on success, else an error message.
 std::string build_mesh_plan(const double* verts, int nv, const int* faces, int nf, int regular_order,
-                            int singular_order, int tile_faces, MeshPlan& plan);
+                            int singular_order, int tile_faces, MeshPlan& plan, int symmetry = 0);
 
 }  // namespace bem

@@ -61,6 +61,12 @@ struct DeviceMesh {
   double* area = nullptr;
   double* m11m10 = nullptr;  // 9 + 3 doubles
   int* driven = nullptr;
+  // symmetry: transforms applied to trial faces (0 identity, 1 x, 2 y, 3 xy),
+  // per-vertex plane masks, per-matrix-row orbit weights (null when off)
+  int ntr = 1;
+  int tr[4] = {0, 0, 0, 0};
+  unsigned char* fix_mask = nullptr;
+  double* row_weight = nullptr;
   // regular rule: weights w_q, basis values phi_a(xi_q) (a-major, 3 x Q) and
   // their products cw[a*Q + q] = phi_a(xi_q) w_q
   double rule_w[kMaxQ] = {0};

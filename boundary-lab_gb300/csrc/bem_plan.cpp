@@ -204,6 +204,73 @@ void rcb(std::vector<int>& ids, int lo, int hi, const std::vector<double>& cent,
 
 }  // namespace
 
+// Symmetry set-up (BeatEngineCore.jl:323-439): the mesh is the fundamental
+// domain (x >= 0, and y >= 0 for xy).  Vertices within the plane tolerance
+// (max(1e-9, 1e-6 x bounding-box diagonal)) of a symmetry plane are snapped onto
+// it, a vertex on the negative side of an active plane is an error, each
+// vertex's planes are recorded (fix_mask) and its orbit weight is 2 per plane.
+static std::string apply_symmetry(MeshPlan& P) {
+  const int nv = P.nv;
+  P.transforms = P.symmetry == 0 ? std::vector<int>{0} : P.symmetry == 1 ? std::vector<int>{0, 1}
+                                                                          : std::vector<int>{0, 1, 2, 3};
+  P.fix_mask.assign(nv, 0);
+  std::vector<double> w(nv, 1.0);
+  if (P.symmetry != 0) {
+    double lo[3] = {P.verts[0], P.verts[1], P.verts[2]}, hi[3] = {lo[0], lo[1], lo[2]};
+    for (int v = 1; v < nv; ++v)
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = std::min(lo[d], P.verts[3 * v + d]);
+        hi[d] = std::max(hi[d], P.verts[3 * v + d]);
+      }
+    const double diag = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                                  (hi[2] - lo[2]) * (hi[2] - lo[2]));
+    const double tol = std::max(1e-9, diag * 1e-6);
+    const int axes = P.symmetry == 1 ? 1 : 2;
+    for (int v = 0; v < nv; ++v)
+      for (int a = 0; a < axes; ++a) {
+        double& c = P.verts[3 * v + a];
+        if (c < -tol) {
+          const char* name = a == 0 ? "X" : "Y";
+          return std::string("Mesh is not in the positive ") + name + " fundamental domain for " +
+                 (P.symmetry == 1 ? "X" : "XY") + " symmetry. Vertex " + std::to_string(v + 1) + " has " +
+                 (a == 0 ? "x" : "y") + "=" + std::to_string(c) + " m.";
+        }
+        if (std::fabs(c) <= tol) {
+          c = 0.0;
+          P.fix_mask[v] |= (unsigned char)(1 << a);
+          w[v] *= 2.0;
+        }
+      }
+  }
+  P.row_weight = w;  // vertex order here; permuted to matrix rows once vertex_row is known
+  return std::string();
+}
+
+// Adjacency of a test face with the image of a trial face under tr: the shared
+// vertices are common indices fixed by tr (on the mesh, the image of a trial
+// vertex coincides with a test vertex exactly when it is that vertex and lies on
+// the planes tr reflects across).  Same result layout as classify().
+Adjacency classify_image(const int* fa, const int* fb, const std::vector<unsigned char>& fix, int tr) {
+  int sa[9], sb[9], n = 0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      if (fa[i] == fb[j] && (fix[fb[j]] & tr) == tr) {
+        sa[n] = i + 1;
+        sb[n] = j + 1;
+        ++n;
+      }
+  if (n >= 3) return {1, 0, 0, 0, 0};
+  if (n == 2) {
+    if (sb[1] < sb[0]) {
+      std::swap(sa[0], sa[1]);
+      std::swap(sb[0], sb[1]);
+    }
+    return {2, sa[0], sa[1], sb[0], sb[1]};
+  }
+  if (n == 1) return {3, sa[0], 0, sb[0], 0};
+  return {0, 0, 0, 0, 0};
+}
+
 // Pack faces (given by their three tile-local vertex rows) into groups of at
 // most kLanes faces in which no two faces share a vertex.  Target: the minimum
 // ceil(n / kLanes) groups.  Faces are dealt round-robin (consecutive faces of a
@@ -326,23 +393,30 @@ static std::vector<std::vector<int>> pack_lane_groups(const std::vector<std::arr
   return out;
 }
 
-std::string build_mesh_plan(const double* verts, int nv, const int* faces, int nf, int regular_order,
-                            int singular_order, int tile_faces, MeshPlan& P) {
+std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, int nf, int regular_order,
+                            int singular_order, int tile_faces, MeshPlan& P, int symmetry) {
   if (nv <= 0 || nf <= 0) return "mesh must have at least one vertex and one face";
   if (regular_order < 1 || regular_order > 4) return "regular quadrature order must be 1..4";
   if (singular_order < 1 || singular_order > 4) return "Duffy 1D Gauss order must be between 1 and 4";
+  if (symmetry < 0 || symmetry > 2) return "symmetry must be 0 (off), 1 (x) or 2 (xy)";
   if (tile_faces < 32) tile_faces = 32;
   P = MeshPlan();
   P.nv = nv;
   P.nf = nf;
   P.regular_order = regular_order;
   P.singular_order = singular_order;
-  P.verts.assign(verts, verts + 3 * (size_t)nv);
+  P.symmetry = symmetry;
+  P.verts.assign(verts_in, verts_in + 3 * (size_t)nv);
   P.faces.assign(faces, faces + 3 * (size_t)nf);
   for (int i = 0; i < 3 * nf; ++i)
     if (faces[i] < 0 || faces[i] >= nv) return "face references a vertex index out of range";
   for (int i = 0; i < 3 * nv; ++i)
-    if (!std::isfinite(verts[i])) return "vertex coordinates must be finite";
+    if (!std::isfinite(verts_in[i])) return "vertex coordinates must be finite";
+  {
+    std::string e = apply_symmetry(P);
+    if (!e.empty()) return e;
+  }
+  const double* verts = P.verts.data();  // snapped to the symmetry planes
 
   regular_rule(regular_order, P.rule_pts, P.rule_w);
   const int Q = (int)P.rule_w.size();
@@ -479,6 +553,11 @@ std::string build_mesh_plan(const double* verts, int nv, const int* faces, int n
       P.vertex_row[v] = (int)P.row_vertex.size();
       P.row_vertex.push_back(v);
     }
+  {  // orbit weights to matrix-row order
+    std::vector<double> rw(nv, 1.0);
+    for (int v = 0; v < nv; ++v) rw[P.vertex_row[v]] = P.row_weight[v];
+    P.row_weight.swap(rw);
+  }
   P.n_ext = P.tile_row_base[P.n_tiles];
   P.ext_row.resize(P.n_ext);
   P.ext_is_halo.resize(P.n_ext);
@@ -562,14 +641,19 @@ std::string build_mesh_plan(const double* verts, int nv, const int* faces, int n
   P.rule_ptr.assign(1, 0);
   P.duffy.clear();
   std::vector<SingularPair> pairs;
+  for (int tr : P.transforms)
   for (int t = 0; t < nf; ++t) {
     std::vector<int> cand;
     std::set<int> seen;
-    for (int a = 0; a < 3; ++a)
-      for (int r : v2f[faces[3 * t + a]])
+    for (int a = 0; a < 3; ++a) {
+      const int v = faces[3 * t + a];
+      if (tr != 0 && (P.fix_mask[v] & tr) != tr) continue;  // images touch the test face only on the planes
+      for (int r : v2f[v])
         if (seen.insert(r).second) cand.push_back(r);
+    }
     for (int r : cand) {
-      Adjacency adj = classify(&faces[3 * t], &faces[3 * r]);
+      Adjacency adj = tr == 0 ? classify(&faces[3 * t], &faces[3 * r])
+                              : classify_image(&faces[3 * t], &faces[3 * r], P.fix_mask, tr);
       if (adj.kind == 0) continue;
       auto key = adj.kind == 1 ? std::make_tuple(1, 0, 0, 0, 0)
                  : adj.kind == 2 ? std::make_tuple(2, adj.ta, adj.tb, adj.ra, adj.rb)
@@ -599,9 +683,12 @@ std::string build_mesh_plan(const double* verts, int nv, const int* faces, int n
       sp.trial = r;
       sp.rule = rule;
       sp.kind = adj.kind;
+      sp.tr = tr;
+      sp.pad = 0;
       sp.jac = (2.0 * P.area[t]) * (2.0 * P.area[r]);
-      sp.nprod = P.normal[3 * t] * P.normal[3 * r] + P.normal[3 * t + 1] * P.normal[3 * r + 1] +
+      sp.nprod = P.normal[3 * t] * tr_sx(tr) * P.normal[3 * r] + P.normal[3 * t + 1] * tr_sy(tr) * P.normal[3 * r + 1] +
                  P.normal[3 * t + 2] * P.normal[3 * r + 2];
+      if (tr != 0) ++P.image_pairs;
       pairs.push_back(sp);
     }
   }

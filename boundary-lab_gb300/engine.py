@@ -57,9 +57,10 @@ class CudaEngine:
         self.ctx, self.lock = shared_context(device)
         self.mesh: native.Mesh | None = None
 
-    def prepare(self, vertices, faces, drives, points, regular_order: int = 4, singular_order: int = 4) -> None:
+    def prepare(self, vertices, faces, drives, points, regular_order: int = 4, singular_order: int = 4,
+                symmetry: str = "off") -> None:
         with self.lock:
-            self.mesh = self.ctx.upload_mesh(vertices, faces, regular_order, singular_order)
+            self.mesh = self.ctx.upload_mesh(vertices, faces, regular_order, singular_order, symmetry=symmetry)
             self.mesh.set_excitation(drives)
             self.mesh.set_observation_points(points)
 

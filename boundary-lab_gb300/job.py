@@ -12,8 +12,11 @@ Differences from the reference, by design:
     request order, one event per frequency); cancellation is checked between
     batches and between emitted results;
   * every channel's excitation is solved against one LU factorisation per
-    frequency (the reference refactors per channel, solver.jl:889-909);
-  * symmetry modes x / xy are not implemented yet and are rejected.
+    frequency (the reference refactors per channel, solver.jl:889-909).
+Symmetry modes x / xy follow the reference: the combined mesh is snapped to
+the symmetry planes and validated as a fundamental domain (solver.jl:718-719),
+the operators, right-hand sides and field include the reflected images, and
+impedance is scaled by the symmetry reduction factor (solver.jl:607-631).
 """
 
 from __future__ import annotations
@@ -48,9 +51,6 @@ class ExteriorJob:
             raise rq.RequestError("Solve request must include config.")
         self.config = request["config"]
         self.symmetry = rq.symmetry_mode_from_config(self.config)
-        if self.symmetry != "off":
-            raise rq.RequestError(f"symmetry mode '{self.symmetry}' is not supported by the {BACKEND_ID} backend yet; "
-                                  "solve the full model with symmetry off.")
         self.frequencies = np.asarray(request.get("frequencies_hz", []), dtype=np.float32).reshape(-1)
         if self.frequencies.size == 0:
             raise rq.RequestError("frequencies_hz must contain at least one frequency.")
@@ -94,6 +94,11 @@ class ExteriorJob:
         self.status(f"GB300 BEM loading {len(self.mesh_inputs)} mesh{'' if len(self.mesh_inputs) == 1 else 'es'}")
         parts = [meshmod.read_gmsh22(m.path, m.scale) for m in self.mesh_inputs]
         self.mesh = meshmod.combine_meshes(parts, [m.translation for m in self.mesh_inputs])
+        self.mesh = meshmod.snap_symmetry_planes(self.mesh, self.symmetry)
+        try:
+            meshmod.validate_symmetry_fundamental_domain(self.mesh, self.symmetry)
+        except ValueError as exc:
+            raise rq.RequestError(str(exc)) from exc
         rq.validate_radiator_elements(self.radiators, self.mesh.tags, self.mesh.element_mesh_ids)
         drives = np.stack([
             rq.face_drive_pattern(self.radiators, rq.channel_unit_drives(self.radiators, name), self.mesh.n_faces,
@@ -108,7 +113,7 @@ class ExteriorJob:
             kwargs["batch"] = self.batch
         self.engine = self.engine_factory(**kwargs)
         self.engine.prepare(self.mesh.vertices, self.mesh.faces, drives, self.points, self.regular_order,
-                            self.singular_order)
+                            self.singular_order, symmetry=self.symmetry)
 
     def close(self) -> None:
         if self.engine is not None:

@@ -501,6 +501,116 @@ def horn_in_box(
     return BoundaryMesh(vertices, f, np.asarray(tags, dtype=np.int32))
 
 
+# ---------------------------------------------------------------------------
+# Symmetry (BeatEngineCore.jl:357-439)
+# ---------------------------------------------------------------------------
+
+SYMMETRY_AXES = {"off": (), "x": (0,), "xy": (0, 1)}
+
+
+def symmetry_plane_tolerance(vertices: np.ndarray) -> float:
+    """max(1e-9, 1e-6 x bounding-box diagonal) (symmetry_plane_tolerance)."""
+    v = np.asarray(vertices, dtype=np.float64)
+    if len(v) == 0:
+        return 1e-9
+    return max(1e-9, float(np.linalg.norm(v.max(axis=0) - v.min(axis=0))) * 1e-6)
+
+
+def snap_symmetry_planes(mesh: BoundaryMesh, mode: str) -> BoundaryMesh:
+    """Vertices within the plane tolerance of an active symmetry plane moved onto it
+    (snap_symmetry_planes); the same mesh object when nothing moves."""
+    axes = SYMMETRY_AXES[mode]
+    if not axes:
+        return mesh
+    tol = symmetry_plane_tolerance(mesh.vertices)
+    v = mesh.vertices.copy()
+    for a in axes:
+        v[np.abs(v[:, a]) <= tol, a] = 0.0
+    if np.array_equal(v, mesh.vertices):
+        return mesh
+    return BoundaryMesh(v, mesh.faces, mesh.tags, mesh.element_mesh_ids)
+
+
+def validate_symmetry_fundamental_domain(mesh: BoundaryMesh, mode: str) -> None:
+    """Raise when a vertex lies on the negative side of an active plane
+    (validate_symmetry_fundamental_domain!; same message)."""
+    tol = symmetry_plane_tolerance(mesh.vertices)
+    for a in SYMMETRY_AXES[mode]:
+        bad = np.nonzero(mesh.vertices[:, a] < -tol)[0]
+        if len(bad):
+            name = "XY" if mode == "xy" else "X"
+            axis = "X" if a == 0 else "Y"
+            raise ValueError(f"Mesh is not in the positive {axis} fundamental domain for {name} symmetry. "
+                             f"Vertex {int(bad[0]) + 1} has {axis.lower()}={mesh.vertices[bad[0], a]} m.")
+
+
+def p1_symmetry_orbit_weights(mesh: BoundaryMesh, mode: str) -> np.ndarray:
+    """2 per active symmetry plane the vertex lies on (p1_symmetry_orbit_weights)."""
+    tol = symmetry_plane_tolerance(mesh.vertices)
+    w = np.ones(mesh.n_vertices)
+    for a in SYMMETRY_AXES[mode]:
+        w[np.abs(mesh.vertices[:, a]) <= tol] *= 2.0
+    return w
+
+
+def fundamental_domain(mesh: BoundaryMesh, mode: str) -> BoundaryMesh:
+    """The faces of a mesh whose centroids lie in the positive domain of the active
+    planes, with unused vertices dropped (for building symmetric test models)."""
+    keep = np.ones(mesh.n_faces, dtype=bool)
+    for a in SYMMETRY_AXES[mode]:
+        keep &= mesh.centroids[:, a] > 0.0
+    faces = mesh.faces[keep]
+    used = np.unique(faces)
+    remap = -np.ones(mesh.n_vertices, dtype=np.int64)
+    remap[used] = np.arange(len(used))
+    part = snap_symmetry_planes(BoundaryMesh(mesh.vertices[used], remap[faces].astype(np.int32), mesh.tags[keep]), mode)
+    validate_symmetry_fundamental_domain(part, mode)  # faces must not straddle a plane
+    return part
+
+
+def mirror_to_full(mesh: BoundaryMesh, mode: str) -> tuple[BoundaryMesh, np.ndarray]:
+    """The full model of a fundamental-domain mesh: the mesh plus its reflections
+    (faces reversed so normals stay outward), vertices on the planes shared.
+    Returns (full mesh, index of each fundamental-domain vertex in the full mesh)."""
+    mesh = snap_symmetry_planes(mesh, mode)
+    verts = [mesh.vertices]
+    faces = [mesh.faces]
+    tags = [mesh.tags]
+    index = np.arange(mesh.n_vertices)
+    for signs in {"x": [(-1, 1)], "xy": [(-1, 1), (1, -1), (-1, -1)]}.get(mode, []):
+        s = np.array([signs[0], signs[1], 1.0])
+        base = sum(len(v) for v in verts)
+        ids = np.empty(mesh.n_vertices, dtype=np.int64)
+        new = []
+        for i, p in enumerate(mesh.vertices):
+            q = p * s
+            if np.array_equal(q, p):
+                ids[i] = i  # on every reflecting plane: shared with the original
+            else:
+                ids[i] = base + len(new)
+                new.append(q)
+        # vertices on one plane only: shared with the image across that plane
+        if len(new):
+            verts.append(np.array(new))
+        f = ids[mesh.faces]
+        faces.append(f[:, [0, 2, 1]] if signs[0] * signs[1] < 0 else f)
+        tags.append(mesh.tags)
+    full_v = np.concatenate(verts)
+    full_f = np.concatenate(faces).astype(np.int64)
+    # weld coincident vertices (a vertex on the x plane reflected in y lands on its y-image, etc.)
+    key = {}
+    remap = np.empty(len(full_v), dtype=np.int64)
+    out_v = []
+    for i, p in enumerate(full_v):
+        k = tuple(np.round(p, 12))
+        if k not in key:
+            key[k] = len(out_v)
+            out_v.append(p)
+        remap[i] = key[k]
+    full = BoundaryMesh(np.array(out_v), remap[full_f].astype(np.int32), np.concatenate(tags))
+    return full, remap[index]
+
+
 def config_mesh(name: str) -> BoundaryMesh:
     """The synthetic meshes of the benchmark workloads, by name."""
     if name == "sphere1280":

@@ -26,6 +26,8 @@ STATUS_NAMES = {
     4: "BEM_ERR_SINGULAR",
     5: "BEM_ERR_NOT_CONVERGED",
 }
+SYMMETRY_MODES = {"off": 0, "x": 1, "xy": 2}
+
 EXPORTED_SYMBOLS = (
     "bem_abi_version",
     "bem_create_context",
@@ -33,6 +35,7 @@ EXPORTED_SYMBOLS = (
     "bem_last_error",
     "bem_context_stream",
     "bem_upload_mesh",
+    "bem_upload_mesh_symmetric",
     "bem_release_mesh",
     "bem_mesh_info",
     "bem_set_excitation",
@@ -151,6 +154,9 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         lib.bem_context_stream.restype = vp
         lib.bem_upload_mesh.argtypes = [vp, dp, ip, ctypes.POINTER(ctypes.c_int), ip, ip, ip, ctypes.POINTER(vp)]
         lib.bem_upload_mesh.restype = ip
+        lib.bem_upload_mesh_symmetric.argtypes = [vp, dp, ip, ctypes.POINTER(ctypes.c_int), ip, ip, ip, ip,
+                                                  ctypes.POINTER(vp)]
+        lib.bem_upload_mesh_symmetric.restype = ip
         lib.bem_release_mesh.argtypes = [vp]
         lib.bem_release_mesh.restype = None
         lib.bem_mesh_info.argtypes = [vp, ctypes.POINTER(ip), ctypes.POINTER(ip), ctypes.POINTER(ip)]
@@ -230,12 +236,15 @@ class Context:
             pass
 
     def upload_mesh(self, vertices: np.ndarray, faces: np.ndarray, regular_order: int = 4,
-                    singular_order: int = 4) -> "Mesh":
+                    singular_order: int = 4, symmetry: str | int = "off") -> "Mesh":
+        """Upload a mesh; symmetry "off", "x" (half model, x >= 0) or "xy" (quarter model)."""
         v = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 3)
         f = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 3)
+        sym = SYMMETRY_MODES[symmetry] if isinstance(symmetry, str) else int(symmetry)
         handle = ctypes.c_void_p()
-        self._check(self._lib.bem_upload_mesh(self._h, _dptr(v), len(v), f.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
-                                              len(f), int(regular_order), int(singular_order), ctypes.byref(handle)))
+        self._check(self._lib.bem_upload_mesh_symmetric(
+            self._h, _dptr(v), len(v), f.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(f), int(regular_order),
+            int(singular_order), sym, ctypes.byref(handle)))
         return Mesh(self, handle, len(v), len(f))
 
     def lu_factor_dense(self, a: np.ndarray, precision: int = BEM_PRECISION_FP64, lu_gemm: int = 0):

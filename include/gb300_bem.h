@@ -82,6 +82,18 @@ long long bem_context_scratch_bytes(const bem_context* ctx);
  * regular_order: 1..4 (4 = the six-point rule); singular_order: 1..4. */
 int bem_upload_mesh(bem_context* ctx, const double* vertices, int n_vertices, const int* faces, int n_faces,
                     int regular_order, int singular_order, bem_mesh** out);
+/* Symmetric models (no separate reference entry point: symmetry_mode of
+ * solve_request_impl, solver.jl:685-736, with BeatEngineCore.jl:323-439): the
+ * mesh is the fundamental domain (x >= 0 for BEM_SYMMETRY_X; x, y >= 0 for
+ * BEM_SYMMETRY_XY), vertices within max(1e-9, 1e-6 x bounding-box diagonal) of a
+ * plane are snapped onto it (a vertex on the negative side is an error), and
+ * every operator, the right-hand side and the field include the reflected
+ * images of every face (BeatEngineCpuAssembly.jl:411-445, 571-634), with rows
+ * weighted by the vertex orbit weights.  Solutions are those of the full model
+ * restricted to the fundamental domain. */
+enum bem_symmetry { BEM_SYMMETRY_OFF = 0, BEM_SYMMETRY_X = 1, BEM_SYMMETRY_XY = 2 };
+int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_vertices, const int* faces,
+                              int n_faces, int regular_order, int singular_order, int symmetry, bem_mesh** out);
 void bem_release_mesh(bem_mesh* mesh);
 /* Sizes of an uploaded mesh (any output pointer may be NULL). */
 int bem_mesh_info(const bem_mesh* mesh, int* n_vertices, int* n_faces, int* n_singular_pairs);

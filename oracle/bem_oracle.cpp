@@ -26,6 +26,8 @@
 //   singular pair integral   src/BeatEngineCpuAssembly.jl:151-218, 447-486
 //   colored threading        src/BeatEngineCpuAssembly.jl:102-130, 636-803
 //   field evaluation         src/BeatEngineCpuField.jl:1-45, BeatEngineCore.jl:1240-1280
+//   symmetry                 src/BeatEngineCore.jl:323-439, 481-505, 917-943,
+//                            src/BeatEngineCpuAssembly.jl:411-445, 488-634
 //
 // The template parameter T is the working precision: float restates the
 // reference's production FP32 path ("BEAT CPU restated"); double is the FP64
@@ -251,6 +253,80 @@ template <typename T> std::vector<Elem<T>> build_elements(const double* verts, c
   return el;
 }
 
+// ------------------------------------------------------------- symmetry ----
+// BeatEngineCore.jl:323-439: transforms (x: S = diag(-1, 1, 1); y: diag(1, -1, 1);
+// xy: diag(-1, -1, 1)), reflected points / normals S p, curls det(S) S c, the
+// plane tolerance max(1e-9, 1e-6 x bounding-box diagonal), snapping of
+// near-plane vertices onto the planes, and the P1 orbit weights (2 per plane).
+struct SymTransform {
+  int sx, sy, det;
+};
+inline std::vector<SymTransform> image_transforms(int mode) {
+  if (mode == 1) return {{-1, 1, -1}};
+  if (mode == 2) return {{-1, 1, -1}, {1, -1, -1}, {-1, -1, 1}};
+  return {};
+}
+inline double symmetry_tolerance(const double* verts, int nv) {
+  if (nv <= 0) return 1e-9;
+  double lo[3] = {verts[0], verts[1], verts[2]}, hi[3] = {verts[0], verts[1], verts[2]};
+  for (int v = 1; v < nv; ++v)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::min(lo[d], verts[3 * v + d]);
+      hi[d] = std::max(hi[d], verts[3 * v + d]);
+    }
+  const double diag = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                                (hi[2] - lo[2]) * (hi[2] - lo[2]));
+  return std::max(1e-9, diag * 1e-6);
+}
+// snapped vertex copy and P1 orbit weights (p1_symmetry_orbit_weights)
+inline std::vector<double> snap_symmetry(const double* verts, int nv, int mode, std::vector<double>& weights) {
+  std::vector<double> out(verts, verts + 3 * (size_t)nv);
+  weights.assign(nv, 1.0);
+  if (mode == 0) return out;
+  const double tol = symmetry_tolerance(verts, nv);
+  const int axes = mode == 1 ? 1 : 2;
+  for (int v = 0; v < nv; ++v)
+    for (int a = 0; a < axes; ++a)
+      if (std::fabs(out[3 * v + a]) <= tol) {
+        out[3 * v + a] = 0.0;
+        weights[v] *= 2.0;
+      }
+  return out;
+}
+template <typename T> inline V3<T> reflect_point(const SymTransform& t, const V3<T>& p) {
+  return {T(t.sx) * p[0], T(t.sy) * p[1], p[2]};
+}
+template <typename T> Elem<T> reflect_element(const Elem<T>& e, const SymTransform& t) {
+  Elem<T> r = e;
+  for (int a = 0; a < 3; ++a) {
+    r.v[a] = reflect_point(t, e.v[a]);
+    r.curls[a] = {T(t.det * t.sx) * e.curls[a][0], T(t.det * t.sy) * e.curls[a][1], T(t.det) * e.curls[a][2]};
+  }
+  r.normal = reflect_point(t, e.normal);
+  return r;
+}
+// geometric_adjacency_info, BeatEngineCore.jl:481-505 (1-based local vertex ids)
+template <typename T> AdjInfo geometric_adjacency(const V3<T>* a, const V3<T>* b, T tol) {
+  int sa[9], sb[9], n = 0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      if (norm(sub(a[i], b[j])) <= tol) {
+        sa[n] = i + 1;
+        sb[n] = j + 1;
+        ++n;
+      }
+  if (n >= 3) return {1, sa[0], sa[1], sb[0], sb[1]};
+  if (n == 2) {
+    if (sb[1] < sb[0]) {
+      std::swap(sa[0], sa[1]);
+      std::swap(sb[0], sb[1]);
+    }
+    return {2, sa[0], sa[1], sb[0], sb[1]};
+  }
+  if (n == 1) return {3, sa[0], 0, sb[0], 0};
+  return {0, 0, 0, 0, 0};
+}
+
 template <typename T> inline V3<T> local_to_global(const V3<T>* v, const V2<T>& p) {
   T a = T(1) - p[0] - p[1];
   return {a * v[0][0] + p[0] * v[1][0] + p[1] * v[2][0], a * v[0][1] + p[0] * v[1][1] + p[1] * v[2][1],
@@ -375,19 +451,135 @@ template <typename T> inline C<T> green(T radius, T inv_radius, T k) {
 // ----------------------------------------------------------- C interface ----
 namespace {
 
+template <typename T> struct Assembler {
+  // Accumulates pair integrals into row-major S, Kp (nv x nf), D, H (nv x nv).
+  C<T>*S, *D, *Kp, *H;
+  int nv, nf;
+  T k, k2;
+  const TriRule<T>* rule;
+  std::vector<V3<T>> basis;
+
+  // _beat_cpu_accumulate_regular_pair_signed!, BeatEngineCpuAssembly.jl:278-373
+  // (sign -1 subtracts, for the image singular delta)
+  void regular_pair(const Elem<T>& te, const Elem<T>& re, const std::vector<V3<T>>& tq_pts,
+                    const std::vector<V3<T>>& rq_pts, T sign) {
+    const int Q = (int)rule->w.size();
+    C<T> sb[3] = {}, ab[3] = {}, db[3][3] = {}, hb[3][3] = {};
+    T cp[3][3];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) cp[a][b] = dot(te.curls[a], re.curls[b]);
+    const T nprod = dot(te.normal, re.normal);
+    const T jac = T(4.0) * te.area * re.area;
+    for (int tq = 0; tq < Q; ++tq) {
+      const V3<T>& x = tq_pts[tq];
+      const T tw = rule->w[tq];
+      for (int rq = 0; rq < Q; ++rq) {
+        V3<T> rv = sub(rq_pts[rq], x);
+        T radius = norm(rv);
+        if (radius == T(0)) continue;
+        T inv_r = T(1) / radius;
+        C<T> g = green(radius, inv_r, k);
+        C<T> gs = g * C<T>(-inv_r, k);
+        T trial_dot = dot(rv, re.normal) * inv_r;
+        T test_dot = -dot(rv, te.normal) * inv_r;
+        C<T> dv = gs * trial_dot, av = gs * test_dot;
+        T weight = tw * rule->w[rq] * jac;
+        C<T> wg = g * weight, wd = dv * weight, wa = av * weight;
+        for (int a = 0; a < 3; ++a) {
+          T tv = basis[tq][a];
+          sb[a] += tv * wg;
+          ab[a] += tv * wa;
+          for (int b = 0; b < 3; ++b) {
+            T bp = tv * basis[rq][b];
+            db[a][b] += bp * wd;
+            hb[a][b] += (cp[a][b] - k2 * bp * nprod) * wg;
+          }
+        }
+      }
+    }
+    for (int a = 0; a < 3; ++a) {
+      const size_t row = te.face[a];
+      S[row * nf + re_dp0] += sign * sb[a];
+      Kp[row * nf + re_dp0] += sign * ab[a];
+      for (int b = 0; b < 3; ++b) {
+        const size_t col = re.face[b];
+        D[row * nv + col] += sign * db[a][b];
+        H[row * nv + col] += sign * hb[a][b];
+      }
+    }
+  }
+  int re_dp0 = 0;  // DP0 dof (face index) of the trial element of the current pair
+
+  // _beat_cpu_accumulate_pair!, BeatEngineCpuAssembly.jl:151-218
+  void singular_pair(const Elem<T>& te, const Elem<T>& re, const DuffyRule<T>& du, T jac, T nprod) {
+    T cp[3][3];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) cp[a][b] = dot(te.curls[a], re.curls[b]);
+    for (size_t q = 0; q < du.w.size(); ++q) {
+      V3<T> tb = p1_values(du.test[q]), rb = p1_values(du.trial[q]);
+      V3<T> x = local_to_global(te.v, du.test[q]);
+      V3<T> y = local_to_global(re.v, du.trial[q]);
+      V3<T> rv = sub(y, x);
+      T radius = norm(rv);
+      if (radius == T(0)) continue;
+      T inv_r = T(1) / radius;
+      C<T> g = green(radius, inv_r, k);
+      C<T> gs = g * C<T>(-inv_r, k);
+      T trial_dot = dot(rv, re.normal) * inv_r;
+      T test_dot = -dot(rv, te.normal) * inv_r;
+      C<T> dv = gs * trial_dot, av = gs * test_dot;
+      T weight = du.w[q] * jac;
+      for (int a = 0; a < 3; ++a) {
+        const size_t row = te.face[a];
+        T tv = tb[a];
+        S[row * nf + re_dp0] += tv * g * weight;
+        Kp[row * nf + re_dp0] += tv * av * weight;
+        for (int b = 0; b < 3; ++b) {
+          const size_t col = re.face[b];
+          T bp = tv * rb[b];
+          D[row * nv + col] += bp * dv * weight;
+          H[row * nv + col] += (cp[a][b] - k2 * bp * nprod) * g * weight;
+        }
+      }
+    }
+  }
+};
+
+// A Duffy rule remapped to an adjacency orientation (BeatEngineCore.jl:633-655, 856-873)
+template <typename T> DuffyRule<T> remapped_rule(const DuffyRule<T>& b, const AdjInfo& info) {
+  DuffyRule<T> rr;
+  rr.w = b.w;
+  for (size_t q = 0; q < b.w.size(); ++q) {
+    if (info.kind == 1) {
+      rr.test.push_back(b.test[q]);
+      rr.trial.push_back(b.trial[q]);
+    } else if (info.kind == 2) {
+      rr.test.push_back(remap_edge(b.test[q], info.ta, info.tb));
+      rr.trial.push_back(remap_edge(b.trial[q], info.ra, info.rb));
+    } else {
+      rr.test.push_back(remap_vertex(b.test[q], info.ta));
+      rr.trial.push_back(remap_vertex(b.trial[q], info.ra));
+    }
+  }
+  return rr;
+}
+
+// assemble_regular_galerkin_operators_cpu, BeatEngineCpuAssembly.jl:636-870:
+// regular pairs, their symmetry images (all pairs, :675-735), singular pairs,
+// the image singular delta (Duffy minus regular for image pairs that touch,
+// :805-857), then the P1 orbit row weights (:627-634, :861).
 template <typename T>
-int assemble_impl(const double* verts, int nv, const int* faces, int nf, double kd, int reg_order, int sing_order,
-                  C<T>* S, C<T>* D, C<T>* Kp, C<T>* H, int nthreads) {
+int assemble_impl(const double* verts_in, int nv, const int* faces, int nf, double kd, int reg_order, int sing_order,
+                  int symmetry, C<T>* S, C<T>* D, C<T>* Kp, C<T>* H, int nthreads) {
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
-  const T k = T(kd);
-  std::vector<Elem<T>> el = build_elements<T>(verts, faces, nf);
+  std::vector<double> weights;
+  const std::vector<double> verts = snap_symmetry(verts_in, nv, symmetry, weights);
+  std::vector<Elem<T>> el = build_elements<T>(verts.data(), faces, nf);
   TriRule<T> rule = triangle_rule<T>(reg_order);
   const int Q = (int)rule.w.size();
   std::vector<std::vector<V3<T>>> qpts(nf, std::vector<V3<T>>(Q));
-  std::vector<V3<T>> basis(Q);
-  for (int q = 0; q < Q; ++q) basis[q] = p1_values(rule.pts[q]);
   for (int f = 0; f < nf; ++f)
     for (int q = 0; q < Q; ++q) qpts[f][q] = local_to_global(el[f].v, rule.pts[q]);
   std::memset((void*)S, 0, sizeof(C<T>) * (size_t)nv * nf);
@@ -395,115 +587,113 @@ int assemble_impl(const double* verts, int nv, const int* faces, int nf, double 
   std::memset((void*)D, 0, sizeof(C<T>) * (size_t)nv * nv);
   std::memset((void*)H, 0, sizeof(C<T>) * (size_t)nv * nv);
   std::vector<std::vector<int>> groups = color_groups(faces, nf, nv);
-  const T k2 = k * k;
+  Assembler<T> base;
+  base.S = S;
+  base.D = D;
+  base.Kp = Kp;
+  base.H = H;
+  base.nv = nv;
+  base.nf = nf;
+  base.k = T(kd);
+  base.k2 = base.k * base.k;
+  base.rule = &rule;
+  for (int q = 0; q < Q; ++q) base.basis.push_back(p1_values(rule.pts[q]));
+  const std::vector<SymTransform> images = image_transforms(symmetry);
 
-  // Regular pairs, BeatEngineCpuAssembly.jl:375-409, 682-713
-  for (const auto& group : groups) {
+  // Regular pairs, BeatEngineCpuAssembly.jl:375-409, 682-713; images :411-445, 715-735
+  for (int ti = -1; ti < (int)images.size(); ++ti) {
+    std::vector<Elem<T>> trial_el = el;
+    std::vector<std::vector<V3<T>>> trial_q = qpts;
+    if (ti >= 0)
+      for (int f = 0; f < nf; ++f) {
+        trial_el[f] = reflect_element(el[f], images[ti]);
+        for (int q = 0; q < Q; ++q) trial_q[f][q] = reflect_point(images[ti], qpts[f][q]);
+      }
+    for (const auto& group : groups) {
 #pragma omp parallel for schedule(dynamic, 1)
-    for (long gi = 0; gi < (long)group.size(); ++gi) {
-      const int t = group[gi];
-      const Elem<T>& te = el[t];
-      for (int r = 0; r < nf; ++r) {
-        const Elem<T>& re = el[r];
-        if (elements_adjacent(te.face, re.face)) continue;
-        C<T> sb[3] = {}, ab[3] = {}, db[3][3] = {}, hb[3][3] = {};
-        T cp[3][3];
-        for (int a = 0; a < 3; ++a)
-          for (int b = 0; b < 3; ++b) cp[a][b] = dot(te.curls[a], re.curls[b]);
-        const T nprod = dot(te.normal, re.normal);
-        const T jac = T(4.0) * te.area * re.area;
-        for (int tq = 0; tq < Q; ++tq) {
-          const V3<T>& x = qpts[t][tq];
-          const T tw = rule.w[tq];
-          for (int rq = 0; rq < Q; ++rq) {
-            V3<T> rv = sub(qpts[r][rq], x);
-            T radius = norm(rv);
-            if (radius == T(0)) continue;
-            T inv_r = T(1) / radius;
-            C<T> g = green(radius, inv_r, k);
-            C<T> gs = g * C<T>(-inv_r, k);
-            T trial_dot = dot(rv, re.normal) * inv_r;
-            T test_dot = -dot(rv, te.normal) * inv_r;
-            C<T> dv = gs * trial_dot, av = gs * test_dot;
-            T weight = tw * rule.w[rq] * jac;
-            C<T> wg = g * weight, wd = dv * weight, wa = av * weight;
-            for (int a = 0; a < 3; ++a) {
-              T tv = basis[tq][a];
-              sb[a] += tv * wg;
-              ab[a] += tv * wa;
-              for (int b = 0; b < 3; ++b) {
-                T bp = tv * basis[rq][b];
-                db[a][b] += bp * wd;
-                hb[a][b] += (cp[a][b] - k2 * bp * nprod) * wg;
-              }
-            }
-          }
-        }
-        for (int a = 0; a < 3; ++a) {
-          const size_t row = te.face[a];
-          S[row * nf + r] += sb[a];
-          Kp[row * nf + r] += ab[a];
-          for (int b = 0; b < 3; ++b) {
-            const size_t col = re.face[b];
-            D[row * nv + col] += db[a][b];
-            H[row * nv + col] += hb[a][b];
-          }
+      for (long gi = 0; gi < (long)group.size(); ++gi) {
+        Assembler<T> as = base;
+        const int t = group[gi];
+        for (int r = 0; r < nf; ++r) {
+          if (ti < 0 && elements_adjacent(el[t].face, el[r].face)) continue;
+          as.re_dp0 = r;
+          as.regular_pair(el[t], trial_el[r], qpts[t], trial_q[r], T(1));
         }
       }
     }
   }
 
-  // Singular pairs, BeatEngineCpuAssembly.jl:151-218, 447-486, 764-797
   if (sing_order > 0) {
+    // Singular pairs, BeatEngineCpuAssembly.jl:151-218, 447-486, 764-797
     SingularCache<T> sc = build_singular_cache<T>(el, faces, nf, nv, sing_order);
     for (const auto& group : groups) {
 #pragma omp parallel for schedule(dynamic, 1)
       for (long gi = 0; gi < (long)group.size(); ++gi) {
+        Assembler<T> as = base;
         const int t = group[gi];
         for (const auto& pr : sc.by_test[t]) {
-          const Elem<T>& te = el[pr.test];
-          const Elem<T>& re = el[pr.trial];
-          const DuffyRule<T>& du = sc.rules[pr.rule];
-          T cp[3][3];
-          for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) cp[a][b] = dot(te.curls[a], re.curls[b]);
-          for (size_t q = 0; q < du.w.size(); ++q) {
-            V3<T> tb = p1_values(du.test[q]), rb = p1_values(du.trial[q]);
-            V3<T> x = local_to_global(te.v, du.test[q]);
-            V3<T> y = local_to_global(re.v, du.trial[q]);
-            V3<T> rv = sub(y, x);
-            T radius = norm(rv);
-            if (radius == T(0)) continue;
-            T inv_r = T(1) / radius;
-            C<T> g = green(radius, inv_r, k);
-            C<T> gs = g * C<T>(-inv_r, k);
-            T trial_dot = dot(rv, re.normal) * inv_r;
-            T test_dot = -dot(rv, te.normal) * inv_r;
-            C<T> dv = gs * trial_dot, av = gs * test_dot;
-            T weight = du.w[q] * pr.jac;
-            for (int a = 0; a < 3; ++a) {
-              const size_t row = te.face[a];
-              T tv = tb[a];
-              S[row * nf + pr.trial] += tv * g * weight;
-              Kp[row * nf + pr.trial] += tv * av * weight;
-              for (int b = 0; b < 3; ++b) {
-                const size_t col = re.face[b];
-                T bp = tv * rb[b];
-                D[row * nv + col] += bp * dv * weight;
-                H[row * nv + col] += (cp[a][b] - k2 * bp * pr.nprod) * g * weight;
-              }
-            }
+          as.re_dp0 = pr.trial;
+          as.singular_pair(el[pr.test], el[pr.trial], sc.rules[pr.rule], pr.jac, pr.nprod);
+        }
+      }
+    }
+    // Image singular delta: image_singular_candidates / _beat_cpu_image_singular_cache
+    // (BeatEngineCore.jl:917-943, BeatEngineCpuAssembly.jl:488-527, 565-625)
+    DuffyRule<T> dbase[4] = {DuffyRule<T>(), duffy_rule<T>(sing_order, 1), duffy_rule<T>(sing_order, 2),
+                             duffy_rule<T>(sing_order, 3)};
+    const T tol = T(1e-8);
+    for (const SymTransform& tr : images) {
+      std::vector<Elem<T>> img(nf);
+      std::vector<std::vector<V3<T>>> img_q(nf, std::vector<V3<T>>(Q));
+      for (int f = 0; f < nf; ++f) {
+        img[f] = reflect_element(el[f], tr);
+        for (int q = 0; q < Q; ++q) img_q[f][q] = reflect_point(tr, qpts[f][q]);
+      }
+      std::vector<std::vector<std::pair<int, AdjInfo>>> by_test(nf);
+      for (int t = 0; t < nf; ++t)
+        for (int r = 0; r < nf; ++r) {
+          AdjInfo info = geometric_adjacency(el[t].v, img[r].v, tol);
+          if (info.kind != 0) by_test[t].push_back({r, info});
+        }
+      for (const auto& group : groups) {
+#pragma omp parallel for schedule(dynamic, 1)
+        for (long gi = 0; gi < (long)group.size(); ++gi) {
+          Assembler<T> as = base;
+          const int t = group[gi];
+          for (const auto& pr : by_test[t]) {
+            const int r = pr.first;
+            const DuffyRule<T> du = remapped_rule(dbase[pr.second.kind], pr.second);
+            const T jac = (T(2.0) * el[t].area) * (T(2.0) * el[r].area);
+            as.re_dp0 = r;
+            as.singular_pair(el[t], img[r], du, jac, dot(el[t].normal, img[r].normal));
+            as.regular_pair(el[t], img[r], qpts[t], img_q[r], T(-1));
           }
         }
       }
     }
   }
+  if (symmetry != 0)
+    for (int v = 0; v < nv; ++v) {
+      const T w = T(weights[v]);
+      for (int c = 0; c < nf; ++c) {
+        S[(size_t)v * nf + c] *= w;
+        Kp[(size_t)v * nf + c] *= w;
+      }
+      for (int c = 0; c < nv; ++c) {
+        D[(size_t)v * nv + c] *= w;
+        H[(size_t)v * nv + c] *= w;
+      }
+    }
   return 0;
 }
 
 // l2_identity_element_matrix + assemble_l2_identity_matrix, BeatEngineCore.jl:731-749, 952-979
-template <typename T> int mass_impl(const double* verts, int nv, const int* faces, int nf, int reg_order, T* M11, T* M10) {
-  std::vector<Elem<T>> el = build_elements<T>(verts, faces, nf);
+// (rows weighted by the P1 orbit weights under symmetry, BeatEngineCore.jl:974-977)
+template <typename T>
+int mass_impl(const double* verts_in, int nv, const int* faces, int nf, int reg_order, int symmetry, T* M11, T* M10) {
+  std::vector<double> weights;
+  const std::vector<double> verts = snap_symmetry(verts_in, nv, symmetry, weights);
+  std::vector<Elem<T>> el = build_elements<T>(verts.data(), faces, nf);
   TriRule<T> rule = triangle_rule<T>(reg_order);
   std::memset(M11, 0, sizeof(T) * (size_t)nv * nv);
   std::memset(M10, 0, sizeof(T) * (size_t)nv * nf);
@@ -523,36 +713,46 @@ template <typename T> int mass_impl(const double* verts, int nv, const int* face
       M10[row * nf + f] += blk10[i];
     }
   }
+  if (symmetry != 0)
+    for (int v = 0; v < nv; ++v) {
+      for (int c = 0; c < nv; ++c) M11[(size_t)v * nv + c] *= T(weights[v]);
+      for (int c = 0; c < nf; ++c) M10[(size_t)v * nf + c] *= T(weights[v]);
+    }
   return 0;
 }
 
 // evaluate_galerkin_field_cpu, BeatEngineCpuField.jl:1-45 (sources built as in
-// build_field_evaluation_cache, BeatEngineCore.jl:1240-1280, symmetry off)
+// build_field_evaluation_cache, BeatEngineCore.jl:1240-1280, including the
+// symmetry images of every face)
 template <typename T>
-int field_impl(const double* verts, int nv, const int* faces, int nf, int reg_order, double kd, const C<T>* pressure,
-               const C<T>* qn, const double* pts, int npts, C<T>* out, int nthreads) {
+int field_impl(const double* verts_in, int nv, const int* faces, int nf, int reg_order, int symmetry, double kd,
+               const C<T>* pressure, const C<T>* qn, const double* pts, int npts, C<T>* out, int nthreads) {
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
-  (void)nv;
   const T k = T(kd);
-  std::vector<Elem<T>> el = build_elements<T>(verts, faces, nf);
+  std::vector<double> weights;
+  const std::vector<double> verts = snap_symmetry(verts_in, nv, symmetry, weights);
+  std::vector<Elem<T>> el = build_elements<T>(verts.data(), faces, nf);
   TriRule<T> rule = triangle_rule<T>(reg_order);
   const int Q = (int)rule.w.size();
-  const size_t ns = (size_t)nf * Q;
+  std::vector<SymTransform> trs = {{1, 1, 1}};
+  for (const SymTransform& t : image_transforms(symmetry)) trs.push_back(t);
+  const size_t ns = (size_t)nf * Q * trs.size();
   std::vector<V3<T>> sp(ns), sn(ns), bv(ns);
   std::vector<T> sw(ns);
   std::vector<int> se(ns);
   size_t s = 0;
   for (int f = 0; f < nf; ++f) {
     T js = T(2.0) * el[f].area;
-    for (int q = 0; q < Q; ++q, ++s) {
-      sp[s] = local_to_global(el[f].v, rule.pts[q]);
-      sn[s] = el[f].normal;
-      sw[s] = rule.w[q] * js;
-      se[s] = f;
-      bv[s] = p1_values(rule.pts[q]);
-    }
+    for (const SymTransform& tr : trs)
+      for (int q = 0; q < Q; ++q, ++s) {
+        sp[s] = reflect_point(tr, local_to_global(el[f].v, rule.pts[q]));
+        sn[s] = reflect_point(tr, el[f].normal);
+        sw[s] = rule.w[q] * js;
+        se[s] = f;
+        bv[s] = p1_values(rule.pts[q]);
+      }
   }
 #pragma omp parallel for schedule(static)
   for (long p = 0; p < npts; ++p) {
@@ -583,31 +783,33 @@ extern "C" {
 
 // Operators, row-major complex interleaved: S, Kp (nv x nf); D, H (nv x nv).
 int oracle_assemble_f64(const double* verts, int nv, const int* faces, int nf, double k, int reg_order, int sing_order,
-                        double* S, double* D, double* Kp, double* H, int nthreads) {
-  return assemble_impl<double>(verts, nv, faces, nf, k, reg_order, sing_order, reinterpret_cast<C<double>*>(S),
+                        int symmetry, double* S, double* D, double* Kp, double* H, int nthreads) {
+  return assemble_impl<double>(verts, nv, faces, nf, k, reg_order, sing_order, symmetry, reinterpret_cast<C<double>*>(S),
                                reinterpret_cast<C<double>*>(D), reinterpret_cast<C<double>*>(Kp),
                                reinterpret_cast<C<double>*>(H), nthreads);
 }
 int oracle_assemble_f32(const double* verts, int nv, const int* faces, int nf, double k, int reg_order, int sing_order,
-                        float* S, float* D, float* Kp, float* H, int nthreads) {
-  return assemble_impl<float>(verts, nv, faces, nf, k, reg_order, sing_order, reinterpret_cast<C<float>*>(S),
+                        int symmetry, float* S, float* D, float* Kp, float* H, int nthreads) {
+  return assemble_impl<float>(verts, nv, faces, nf, k, reg_order, sing_order, symmetry, reinterpret_cast<C<float>*>(S),
                               reinterpret_cast<C<float>*>(D), reinterpret_cast<C<float>*>(Kp),
                               reinterpret_cast<C<float>*>(H), nthreads);
 }
-int oracle_mass_f64(const double* verts, int nv, const int* faces, int nf, int reg_order, double* M11, double* M10) {
-  return mass_impl<double>(verts, nv, faces, nf, reg_order, M11, M10);
+int oracle_mass_f64(const double* verts, int nv, const int* faces, int nf, int reg_order, int symmetry, double* M11,
+                    double* M10) {
+  return mass_impl<double>(verts, nv, faces, nf, reg_order, symmetry, M11, M10);
 }
-int oracle_mass_f32(const double* verts, int nv, const int* faces, int nf, int reg_order, float* M11, float* M10) {
-  return mass_impl<float>(verts, nv, faces, nf, reg_order, M11, M10);
+int oracle_mass_f32(const double* verts, int nv, const int* faces, int nf, int reg_order, int symmetry, float* M11,
+                    float* M10) {
+  return mass_impl<float>(verts, nv, faces, nf, reg_order, symmetry, M11, M10);
 }
-int oracle_field_f64(const double* verts, int nv, const int* faces, int nf, int reg_order, double k,
+int oracle_field_f64(const double* verts, int nv, const int* faces, int nf, int reg_order, int symmetry, double k,
                      const double* pressure, const double* qn, const double* pts, int npts, double* out, int nthreads) {
-  return field_impl<double>(verts, nv, faces, nf, reg_order, k, reinterpret_cast<const C<double>*>(pressure),
+  return field_impl<double>(verts, nv, faces, nf, reg_order, symmetry, k, reinterpret_cast<const C<double>*>(pressure),
                             reinterpret_cast<const C<double>*>(qn), pts, npts, reinterpret_cast<C<double>*>(out), nthreads);
 }
-int oracle_field_f32(const double* verts, int nv, const int* faces, int nf, int reg_order, double k,
+int oracle_field_f32(const double* verts, int nv, const int* faces, int nf, int reg_order, int symmetry, double k,
                      const float* pressure, const float* qn, const double* pts, int npts, float* out, int nthreads) {
-  return field_impl<float>(verts, nv, faces, nf, reg_order, k, reinterpret_cast<const C<float>*>(pressure),
+  return field_impl<float>(verts, nv, faces, nf, reg_order, symmetry, k, reinterpret_cast<const C<float>*>(pressure),
                            reinterpret_cast<const C<float>*>(qn), pts, npts, reinterpret_cast<C<float>*>(out), nthreads);
 }
 

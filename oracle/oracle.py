@@ -33,12 +33,12 @@ _ip = ctypes.POINTER(ctypes.c_int)
 def lib() -> ctypes.CDLL:
     handle = ctypes.CDLL(str(build_oracle()))
     i, d = ctypes.c_int, ctypes.c_double
-    handle.oracle_assemble_f64.argtypes = [_dp, i, _ip, i, d, i, i, _dp, _dp, _dp, _dp, i]
-    handle.oracle_assemble_f32.argtypes = [_dp, i, _ip, i, d, i, i, _fp, _fp, _fp, _fp, i]
-    handle.oracle_mass_f64.argtypes = [_dp, i, _ip, i, i, _dp, _dp]
-    handle.oracle_mass_f32.argtypes = [_dp, i, _ip, i, i, _fp, _fp]
-    handle.oracle_field_f64.argtypes = [_dp, i, _ip, i, i, d, _dp, _dp, _dp, i, _dp, i]
-    handle.oracle_field_f32.argtypes = [_dp, i, _ip, i, i, d, _fp, _fp, _dp, i, _fp, i]
+    handle.oracle_assemble_f64.argtypes = [_dp, i, _ip, i, d, i, i, i, _dp, _dp, _dp, _dp, i]
+    handle.oracle_assemble_f32.argtypes = [_dp, i, _ip, i, d, i, i, i, _fp, _fp, _fp, _fp, i]
+    handle.oracle_mass_f64.argtypes = [_dp, i, _ip, i, i, i, _dp, _dp]
+    handle.oracle_mass_f32.argtypes = [_dp, i, _ip, i, i, i, _fp, _fp]
+    handle.oracle_field_f64.argtypes = [_dp, i, _ip, i, i, i, d, _dp, _dp, _dp, i, _dp, i]
+    handle.oracle_field_f32.argtypes = [_dp, i, _ip, i, i, i, d, _fp, _fp, _dp, i, _fp, i]
     handle.oracle_triangle_rule.argtypes = [i, _dp, _dp, i]
     handle.oracle_duffy_rule.argtypes = [i, i, _dp, _dp, _dp, i]
     handle.oracle_singular_pair_count.argtypes = [_dp, i, _ip, i, i]
@@ -68,9 +68,13 @@ class Operators:
     hypersingular: np.ndarray  # (N_p, N_p)
 
 
+SYMMETRY = {"off": 0, "x": 1, "xy": 2}
+
+
 def assemble(mesh, k: float, *, precision: str = "f64", regular_order: int = 4, singular_order: int = 4,
-             threads: int = 0) -> Operators:
-    """Galerkin S, D, K', H operators (BeatEngineCpuAssembly.jl:636-886, symmetry off)."""
+             threads: int = 0, symmetry: str = "off") -> Operators:
+    """Galerkin S, D, K', H operators (BeatEngineCpuAssembly.jl:636-886); with symmetry
+    "x" / "xy" the mesh is the fundamental domain and the images are included."""
     v, f = _geom(mesh)
     nv, nf = len(v), len(f)
     ctype = np.complex128 if precision == "f64" else np.complex64
@@ -82,14 +86,14 @@ def assemble(mesh, k: float, *, precision: str = "f64", regular_order: int = 4, 
         fn, pt = lib().oracle_assemble_f64, _dp
     else:
         fn, pt = lib().oracle_assemble_f32, _fp
-    rc = fn(_ptr(v, _dp), nv, _ptr(f, _ip), nf, float(k), regular_order, singular_order,
+    rc = fn(_ptr(v, _dp), nv, _ptr(f, _ip), nf, float(k), regular_order, singular_order, SYMMETRY[symmetry],
             _ptr(S, pt), _ptr(D, pt), _ptr(Kp, pt), _ptr(H, pt), threads)
     if rc != 0:
         raise RuntimeError(f"oracle assembly failed ({rc})")
     return Operators(S, D, Kp, H)
 
 
-def mass(mesh, *, precision: str = "f64", regular_order: int = 4) -> tuple[np.ndarray, np.ndarray]:
+def mass(mesh, *, precision: str = "f64", regular_order: int = 4, symmetry: str = "off") -> tuple[np.ndarray, np.ndarray]:
     """Dense L2 identity matrices M11 (P1 x P1) and M10 (P1 x DP0) (BeatEngineCore.jl:952-979)."""
     v, f = _geom(mesh)
     nv, nf = len(v), len(f)
@@ -97,9 +101,11 @@ def mass(mesh, *, precision: str = "f64", regular_order: int = 4) -> tuple[np.nd
     M11 = np.zeros((nv, nv), rtype)
     M10 = np.zeros((nv, nf), rtype)
     if precision == "f64":
-        lib().oracle_mass_f64(_ptr(v, _dp), nv, _ptr(f, _ip), nf, regular_order, _ptr(M11, _dp), _ptr(M10, _dp))
+        lib().oracle_mass_f64(_ptr(v, _dp), nv, _ptr(f, _ip), nf, regular_order, SYMMETRY[symmetry], _ptr(M11, _dp),
+                              _ptr(M10, _dp))
     else:
-        lib().oracle_mass_f32(_ptr(v, _dp), nv, _ptr(f, _ip), nf, regular_order, _ptr(M11, _fp), _ptr(M10, _fp))
+        lib().oracle_mass_f32(_ptr(v, _dp), nv, _ptr(f, _ip), nf, regular_order, SYMMETRY[symmetry], _ptr(M11, _fp),
+                              _ptr(M10, _fp))
     return M11, M10
 
 
@@ -127,7 +133,7 @@ def neumann_data(mesh, radiator_faces: np.ndarray, drive: complex, rho: float, o
 
 
 def field(mesh, pressure: np.ndarray, q: np.ndarray, k: float, points: np.ndarray, *, precision: str = "f64",
-          regular_order: int = 4, threads: int = 0) -> np.ndarray:
+          regular_order: int = 4, threads: int = 0, symmetry: str = "off") -> np.ndarray:
     """Exterior potential u(x) = sum_s [dG/dn_y p(y_s) - G q_s] w_s (BeatEngineCpuField.jl:1-45)."""
     v, f = _geom(mesh)
     pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
@@ -135,13 +141,13 @@ def field(mesh, pressure: np.ndarray, q: np.ndarray, k: float, points: np.ndarra
         p = np.ascontiguousarray(pressure, np.complex128)
         qq = np.ascontiguousarray(q, np.complex128)
         out = np.zeros(len(pts), np.complex128)
-        rc = lib().oracle_field_f64(_ptr(v, _dp), len(v), _ptr(f, _ip), len(f), regular_order, float(k),
+        rc = lib().oracle_field_f64(_ptr(v, _dp), len(v), _ptr(f, _ip), len(f), regular_order, SYMMETRY[symmetry], float(k),
                                     _ptr(p, _dp), _ptr(qq, _dp), _ptr(pts, _dp), len(pts), _ptr(out, _dp), threads)
     else:
         p = np.ascontiguousarray(pressure, np.complex64)
         qq = np.ascontiguousarray(q, np.complex64)
         out = np.zeros(len(pts), np.complex64)
-        rc = lib().oracle_field_f32(_ptr(v, _dp), len(v), _ptr(f, _ip), len(f), regular_order, float(k),
+        rc = lib().oracle_field_f32(_ptr(v, _dp), len(v), _ptr(f, _ip), len(f), regular_order, SYMMETRY[symmetry], float(k),
                                     _ptr(p, _fp), _ptr(qq, _fp), _ptr(pts, _dp), len(pts), _ptr(out, _fp), threads)
     if rc != 0:
         raise RuntimeError(f"oracle field failed ({rc})")
@@ -181,17 +187,18 @@ class FrequencySolution:
 
 
 def solve_frequency(mesh, k: float, q_columns: np.ndarray, points: np.ndarray, *, precision: str = "f64",
-                    regular_order: int = 4, singular_order: int = 4, threads: int = 0) -> FrequencySolution:
+                    regular_order: int = 4, singular_order: int = 4, threads: int = 0,
+                    symmetry: str = "off") -> FrequencySolution:
     """One exterior BM frequency solve: assemble, factor once, solve every right-hand side, field."""
     ops = assemble(mesh, k, precision=precision, regular_order=regular_order, singular_order=singular_order,
-                   threads=threads)
-    M11, M10 = mass(mesh, precision=precision, regular_order=regular_order)
+                   threads=threads, symmetry=symmetry)
+    M11, M10 = mass(mesh, precision=precision, regular_order=regular_order, symmetry=symmetry)
     lhs, rhs_op = burton_miller_matrices(ops, M11, M10, k)
     q_columns = np.asarray(q_columns).reshape(len(mesh.faces), -1).astype(lhs.dtype)
     pressure = solve(lhs, rhs_op @ q_columns)
     fields = np.stack(
         [field(mesh, pressure[:, c], q_columns[:, c], k, points, precision=precision, regular_order=regular_order,
-               threads=threads) for c in range(q_columns.shape[1])],
+               threads=threads, symmetry=symmetry) for c in range(q_columns.shape[1])],
         axis=1,
     )
     return FrequencySolution(pressure, fields)

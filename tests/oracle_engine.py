@@ -31,7 +31,8 @@ class OracleEngine:
     def __init__(self, device: int = 0, precision: str = "mixed", batch: int = 0, **_):
         self.mesh = None
 
-    def prepare(self, vertices, faces, drives, points, regular_order=4, singular_order=4):
+    def prepare(self, vertices, faces, drives, points, regular_order=4, singular_order=4, symmetry="off"):
+        self.symmetry = symmetry
         self.vertices = np.asarray(vertices, float)
         self.faces = np.asarray(faces, np.int32)
         self.drives = np.asarray(drives, np.complex128).reshape(-1, len(self.faces))
@@ -50,7 +51,8 @@ class OracleEngine:
             omega = 2 * np.pi * f
             q = (self.drives * (1j * rho * omega)).T
             sol = oracle.solve_frequency(self.mesh, omega / sound_speed, q, self.points,
-                                         regular_order=self.orders[0], singular_order=self.orders[1])
+                                         regular_order=self.orders[0], singular_order=self.orders[1],
+                                         symmetry=self.symmetry)
             ps.append(sol.pressure.T)
             us.append(sol.field.T)
         stats = {"assembly_s": 0.0, "solve_s": 0.0, "field_s": 0.0, "max_refine_steps": 0, "max_rel_residual": 0.0}

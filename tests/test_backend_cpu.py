@@ -95,7 +95,12 @@ def test_job_pressure_matches_direct_oracle(mesh_file):
 
 def test_job_rejections(mesh_file):
     with pytest.raises(Exception, match="symmetry"):
-        job_mod.ExteriorJob({"config": base_config(mesh_file, symmetry="x"), "frequencies_hz": [100.0]})
+        job_mod.ExteriorJob({"config": base_config(mesh_file, symmetry="z"), "frequencies_hz": [100.0]})
+    # the whole sphere is not an x >= 0 fundamental domain (solver.jl:718-719)
+    sym_job = job_mod.ExteriorJob({"config": base_config(mesh_file, symmetry="x"), "frequencies_hz": [100.0]},
+                                  engine_factory=oracle_factory)
+    with pytest.raises(Exception, match="fundamental domain"):
+        sym_job.setup()
     with pytest.raises(Exception, match="at least one"):
         job_mod.ExteriorJob({"config": base_config(mesh_file), "frequencies_hz": []})
     job = job_mod.ExteriorJob({"config": base_config(mesh_file, radiators=[{"name": "x", "tag": 7}]),
@@ -238,3 +243,33 @@ def test_reference_job_server_runs_a_job(blab, monkeypatch, mesh_file, tmp_path)
         assert orch.get(job.job_id).result_npz.exists()
     finally:
         orch.shutdown()
+
+
+@pytest.fixture(scope="module")
+def half_and_full_files(tmp_path_factory):
+    box = meshes.box_with_piston((0.3, 0.2, 0.25), 600, 0.05, "+z")  # 8 x 6 cells: grid line on x = 0
+    half = meshes.fundamental_domain(box, "x")
+    full, _ = meshes.mirror_to_full(half, "x")
+    d = tmp_path_factory.mktemp("sym")
+    paths = []
+    for name, m in (("half.msh", half), ("full.msh", full)):
+        meshes.write_gmsh22(d / name, m.vertices * 1000.0, m.faces, m.tags)
+        paths.append(d / name)
+    return paths
+
+
+def test_symmetric_job_matches_full_model(half_and_full_files):
+    half_file, full_file = half_and_full_files
+    events = {}
+    for name, path, sym in (("half", half_file, "x"), ("full", full_file, "off")):
+        cfg = base_config(path, symmetry=sym, radiators=[{"name": "piston", "tag": 2, "channel": "main"}])
+        job = job_mod.ExteriorJob({"config": cfg, "frequencies_hz": [800.0]}, engine_factory=oracle_factory)
+        events[name] = next(job.results())["result"]
+    h, f = events["half"], events["full"]
+    assert h["diagnostics"]["symmetry"] == "x"
+    for key in ("horizontal_pressure", "vertical_pressure"):
+        a = np.asarray(h[key]["real"]) + 1j * np.asarray(h[key]["imag"])
+        b = np.asarray(f[key]["real"]) + 1j * np.asarray(f[key]["imag"])
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 5e-5
+    # impedance: the half model's radiator force times the reduction factor 2
+    assert np.allclose(h["impedance"], f["impedance"], rtol=5e-5)
