@@ -622,7 +622,8 @@ template <> struct SingParams<double> {
 constexpr int kSingOut = 12;
 
 template <typename R>
-__global__ void singular_dyn_kernel(SingularGeom geo, const SingularPair* __restrict__ pairs, int npairs,
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)  // FP32: two 256-thread CTAs per SM (<= 128 registers)
+    singular_dyn_kernel(SingularGeom geo, const SingularPair* __restrict__ pairs, int npairs,
                                     const int* __restrict__ rule_ptr, const R* __restrict__ duffy,
                                     const double* __restrict__ moments, const double* __restrict__ curls,
                                     const double* __restrict__ area, const double* __restrict__ m11m10,
