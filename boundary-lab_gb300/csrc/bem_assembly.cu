@@ -109,35 +109,73 @@ __device__ __forceinline__ void green_f32(const PairF32& P, const float* d, floa
   G = make_float2(c * sc, s * sc);
 }
 
-// cw[a*Q + q] = phi_a(xi_q) * w_q of the regular rule (kernel parameters, so
-// meshes with different rules can run concurrently on different streams).
-struct RegParamsF32 {
-  df kdf;      // wavenumber as double-float
-  float k, k2;
-  float kturn;  // k / 2pi (phase in turns)
-  float2 cD, cH;  // LHS coefficients of D and H
-  float2 cw2[3 * kMaxQ];  // (cw, cw): operand pairs of the packed FP32x2 FMAs
+// Frequency-independent part of the pair set-up: C = anchor_g - anchor_f in
+// double-float, Cf = C rounded to float, and |C| as double-float.
+struct PairGeomF32 {
+  float Cf[3];
+  df R;
 };
 
-template <int Q, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, 3) regular_f32_kernel(const FaceF32* __restrict__ faces, int nf,
-                                                                 const int* __restrict__ tile_group_ptr,
-                                                                 const LaneSlot* __restrict__ slots,
-                                                                 const int* __restrict__ tile_row_base,
-                                                                 int max_rows, float2* __restrict__ Rext,
-                                                                 long long ldR, RegParamsF32 p, int ntr, int4 trs,
-                                                                 const unsigned char* __restrict__ fix_mask) {
+__device__ __forceinline__ PairGeomF32 pair_geom_f32(const float* ahi_g, const float* alo_g, const float* ahi_f,
+                                                     const float* alo_f) {
+  PairGeomF32 P;
+  df C[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    df s = two_sum(ahi_g[d], -ahi_f[d]);
+    s.lo += alo_g[d] - alo_f[d];
+    C[d] = quick_two_sum(s.hi, s.lo);
+    P.Cf[d] = C[d].hi + C[d].lo;
+  }
+  P.R = df_sqrt(df_add(df_add(df_mul(C[0], C[0]), df_mul(C[1], C[1])), df_mul(C[2], C[2])));
+  return P;
+}
+
+// Parameters of one regular-assembly launch over NFQ frequencies (kernel
+// parameters, so meshes with different rules run concurrently on different
+// streams).  cw[a*Q + q] = phi_a(xi_q) * w_q of the regular rule; w_q = sum_a cw.
+template <int NFQ> struct RegParamsF32 {
+  float2 cw2[3 * kMaxQ];  // (cw, cw): operand pairs of the packed FP32x2 FMAs
+  float2 w2[kMaxQ];       // (w, w)
+  df kdf[NFQ];              // wavenumbers as double-float
+  float kturn[NFQ];         // k / 2pi (phase in turns)
+  float k2[NFQ];
+  float2 mcD[NFQ];   // -cD
+  float2 ikcD[NFQ];  // i k cD
+  float2 cH[NFQ];
+};
+
+// Regular face pairs for NFQ frequencies at once.  Per q-pair (test point m,
+// trial point n) the frequency-independent part (r, 1/r, the compensated
+// r - |C|, the normal factor t = (r . n_g) / r) is formed once, then per
+// frequency the phase e^{ikr} and
+//   H = G (cD t (ik - 1/r) + cnn),  G = e^{ikr} / r,  cnn = -k^2 (n_f . n_g) cH,
+// which is cD * (double-layer kernel) + the -k^2 nn cH part of the
+// hypersingular kernel in one complex weight.  Per test point the trial-basis
+// sums Hs[b] = sum_n cw[b][n] H and Gs = sum_n w_n G are folded into
+// W[a][b] += cw[a][m] Hs[b] and S0 += w_m Gs, and each pair adds
+//   jac * (W[a][b] + (curl_a . curl_b) cH S0)
+// (BeatEngineCpuAssembly.jl:278-373: the D and H regular integrals, with
+// S0 = sum_{a,b} of the single-layer integrals of the basis products, because
+// the P1 basis functions sum to one).
+template <int Q, int WARPS, int NFQ>
+__global__ void __launch_bounds__(WARPS * 32, 3)  // three CTAs per SM (<= 168 registers)
+    regular_f32_kernel(const FaceF32* __restrict__ faces, int nf, const int* __restrict__ tile_group_ptr,
+                       const LaneSlot* __restrict__ slots, const int* __restrict__ tile_row_base, int max_rows,
+                       float2* __restrict__ Rext, long long ldR, long long strideR, RegParamsF32<NFQ> p, int ntr,
+                       int4 trs, const unsigned char* __restrict__ fix_mask) {
   extern __shared__ float2 smem_acc32[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tile = blockIdx.y;
   const int g = blockIdx.x * WARPS + warp;
   const int base = tile_row_base[tile];
   const int rows = tile_row_base[tile + 1] - base;
-  float2* acc = smem_acc32 + (size_t)warp * 3 * max_rows;
+  float2* acc = smem_acc32 + (size_t)warp * NFQ * 3 * max_rows;  // [NFQ][3][max_rows]
   // rule coefficients of the (not unrolled) test-point loop, indexed at run time
-  __shared__ float2 s_cw2[3 * kMaxQ];
+  __shared__ float2 s_cw2[3 * kMaxQ], s_w2[kMaxQ];
   if (threadIdx.x < 3 * kMaxQ) s_cw2[threadIdx.x] = p.cw2[threadIdx.x];
-  for (int i = lane; i < 3 * max_rows; i += 32) acc[i] = make_float2(0.0f, 0.0f);
+  if (threadIdx.x < kMaxQ) s_w2[threadIdx.x] = p.w2[threadIdx.x];
+  for (int i = lane; i < NFQ * 3 * max_rows; i += 32) acc[i] = make_float2(0.0f, 0.0f);
   __syncthreads();
   if (g >= nf) return;
 
@@ -237,26 +275,31 @@ __global__ void __launch_bounds__(WARPS * 32, 3) regular_f32_kernel(const FaceF3
         //   2 C.d + d.d = Pg[n] + Pf[m] - 2 og[n].of[m],
         //   Pg[n] = 2 C.og[n] + og[n].og[n],  Pf[m] = of[m].of[m] - 2 C.of[m],
         // every term of size |C| h or h^2 (no cancellation against |C|^2).
-        const PairF32 P = pair_setup_f32(ahi_g, alo_g, ahi_f, alo_f, p.kdf);
-        const float R0 = fmaxf(P.R0, 1e-30f);
-        const float t0 = P.theta0 * BEM_INV_TWO_PI;  // k|C| in turns, |t0| <= 1/2
+        const PairGeomF32 P = pair_geom_f32(ahi_g, alo_g, ahi_f, alo_f);
+        const float R0 = fmaxf(P.R.hi + P.R.lo, 1e-30f);
         float Pg[Q];
 #pragma unroll
         for (int n = 0; n < Q; ++n)
           Pg[n] = fmaf(2.0f, fmaf(P.Cf[0], og[n][0], fmaf(P.Cf[1], og[n][1], P.Cf[2] * og[n][2])), gg[n]);
-        float2 IG[3][3], ID[3][3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int b = 0; b < 3; ++b) {
-            IG[a][b] = make_float2(0.f, 0.f);
-            ID[a][b] = make_float2(0.f, 0.f);
-          }
-        // The test-point loop is kept rolled: fully unrolling 6 x 6 Green
-        // evaluations overflowed the instruction cache (no_instruction stalls).
-        // test-face data used after the loop, loaded now
+        // test-face data
         const float nn = fmaf(F.normal[0], ng[0], fmaf(F.normal[1], ng[1], F.normal[2] * ng[2]));
         const float jac = F.area2 * a2g * BEM_INV_FOUR_PI;
+        float t0[NFQ];    // k|C| mod 2pi, in turns (|t0| <= 1/2)
+        float2 cnn[NFQ];  // -k^2 nn cH
+        float2 W[NFQ][3][3], S0[NFQ];
+#pragma unroll
+        for (int f = 0; f < NFQ; ++f) {
+          t0[f] = df_reduce_two_pi(df_mul(p.kdf[f], P.R)) * BEM_INV_TWO_PI;
+          const float s = -p.k2[f] * nn;
+          cnn[f] = make_float2(s * p.cH[f].x, s * p.cH[f].y);
+          S0[f] = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) W[f][a][b] = make_float2(0.f, 0.f);
+        }
+        // The test-point loop is kept rolled: fully unrolling 6 x 6 Green
+        // evaluations overflowed the instruction cache (no_instruction stalls).
         float nf0 = F.off[0], nf1 = F.off[1], nf2 = F.off[2];
 #pragma unroll 1
         for (int m = 0; m < Q; ++m) {
@@ -271,71 +314,65 @@ __global__ void __launch_bounds__(WARPS * 32, 3) regular_f32_kernel(const FaceF3
           const float Pf = fmaf(-2.0f, fmaf(P.Cf[0], f0, fmaf(P.Cf[1], f1, P.Cf[2] * f2)),
                                 fmaf(f0, f0, fmaf(f1, f1, f2 * f2)));
           const float cmn = fmaf(cm0, ng[0], fmaf(cm1, ng[1], cm2 * ng[2]));
-          float2 u[3], v[3];
+          float2 Hs[NFQ][3], Gs[NFQ];
 #pragma unroll
-          for (int b = 0; b < 3; ++b) {
-            u[b] = make_float2(0.f, 0.f);
-            v[b] = make_float2(0.f, 0.f);
+          for (int f = 0; f < NFQ; ++f) {
+            Gs[f] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int b = 0; b < 3; ++b) Hs[f][b] = make_float2(0.f, 0.f);
           }
 #pragma unroll
           for (int n = 0; n < Q; ++n) {
-            // r vector y_m -> x_n
+            // frequency-independent: r vector y_m -> x_n, 1/r, r - |C|, (r . n_g) / r
             const float r0 = cm0 + og[n][0], r1 = cm1 + og[n][1], r2v = cm2 + og[n][2];
             const float r2 = fmaxf(fmaf(r0, r0, fmaf(r1, r1, r2v * r2v)), 1e-30f);
             const float rinv = rsqrt_ftz(r2);
             const float num = fmaf(-2.0f, fmaf(og[n][0], f0, fmaf(og[n][1], f1, og[n][2] * f2)), Pg[n] + Pf);
             const float delta = num * rcp_ftz(fmaf(r2, rinv, R0));
-            float turn = fmaf(p.kturn, delta, t0);
-            turn -= round_nearest_small(turn);  // |turn| <= 1/2
-            float sn, cs;
-            sincos_ftz(turn * BEM_TWO_PI_HI, &sn, &cs);
-            // G * 4pi = e^{ikr} / r;  dG/dn_y * 4pi = G4 (ik - 1/r) (r . n_g) / r
-            const float Gx = cs * rinv, Gy = sn * rinv;
             const float t = (cmn + gn[n]) * rinv;
-            const float2 G2 = make_float2(Gx, Gy);
-            const float2 Dk = make_float2(t * fmaf(-Gx, rinv, -Gy * p.k), t * fmaf(Gx, p.k, -Gy * rinv));
-            // complex accumulations as packed FP32x2 FMAs (re and im in one instruction)
+            const float2 tt = make_float2(t, t), trr = make_float2(t * rinv, t * rinv);
 #pragma unroll
-            for (int b = 0; b < 3; ++b) {
-              const float2 c = p.cw2[b * Q + n];
-              u[b] = __ffma2_rn(c, G2, u[b]);
-              v[b] = __ffma2_rn(c, Dk, v[b]);
+            for (int f = 0; f < NFQ; ++f) {
+              float turn = fmaf(p.kturn[f], delta, t0[f]);
+              turn -= round_nearest_small(turn);  // |turn| <= 1/2
+              float sn, cs;
+              sincos_ftz(turn * BEM_TWO_PI_HI, &sn, &cs);
+              const float2 G = __fmul2_rn(make_float2(cs, sn), make_float2(rinv, rinv));  // e^{ikr} / r
+              // E = cD t (ik - 1/r) + cnn = (t/r)(-cD) + t (i k cD) + cnn
+              const float2 E = __ffma2_rn(trr, p.mcD[f], __ffma2_rn(tt, p.ikcD[f], cnn[f]));
+              const float2 H = make_float2(fmaf(G.x, E.x, -G.y * E.y), fmaf(G.x, E.y, G.y * E.x));
+#pragma unroll
+              for (int b = 0; b < 3; ++b) Hs[f][b] = __ffma2_rn(p.cw2[b * Q + n], H, Hs[f][b]);
+              Gs[f] = __ffma2_rn(p.w2[n], G, Gs[f]);
             }
           }
 #pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            const float2 c = s_cw2[a * Q + m];
+          for (int f = 0; f < NFQ; ++f) {
 #pragma unroll
-            for (int b = 0; b < 3; ++b) {
-              IG[a][b] = __ffma2_rn(c, u[b], IG[a][b]);
-              ID[a][b] = __ffma2_rn(c, v[b], ID[a][b]);
+            for (int a = 0; a < 3; ++a) {
+              const float2 c = s_cw2[a * Q + m];
+#pragma unroll
+              for (int b = 0; b < 3; ++b) W[f][a][b] = __ffma2_rn(c, Hs[f][b], W[f][a][b]);
             }
+            S0[f] = __ffma2_rn(s_w2[m], Gs[f], S0[f]);
           }
         }
-        // combine: L = jac/(4pi) * (cD * D + cH * (curl.curl S0 - k^2 nn IG))
-        //            = A1 * ID + A3 * IG + curl.curl * B
-        float2 S0 = make_float2(0.f, 0.f);
+        // L[a][b] = jac (W[a][b] + (curl_a . curl_b) cH S0)
+        float2 Bc[NFQ];
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int b = 0; b < 3; ++b) S0 = cadd(S0, IG[a][b]);
-        const float2 A1 = make_float2(jac * p.cD.x, jac * p.cD.y);
-        const float2 A2 = make_float2(jac * p.cH.x, jac * p.cH.y);
-        const float kk_nn = p.k2 * nn;
-        const float2 A3 = make_float2(-kk_nn * A2.x, -kk_nn * A2.y);
-        const float2 Bc = cmul(A2, S0);
+        for (int f = 0; f < NFQ; ++f) Bc[f] = cmul(p.cH[f], S0[f]);
+        const float2 jj = make_float2(jac, jac);
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
           const float cf0 = F.curls[3 * a], cf1 = F.curls[3 * a + 1], cf2 = F.curls[3 * a + 2];
 #pragma unroll
           for (int b = 0; b < 3; ++b) {
-            const float cc = fmaf(cf0, cg[3 * b], fmaf(cf1, cg[3 * b + 1], cf2 * cg[3 * b + 2]));
-            const float2 d = ID[a][b], i = IG[a][b];
-            float2* dst = &acc[b * max_rows + s.loc[a]];
-            float2 o = *dst;
-            o.x += fmaf(A1.x, d.x, fmaf(-A1.y, d.y, fmaf(A3.x, i.x, fmaf(-A3.y, i.y, cc * Bc.x))));
-            o.y += fmaf(A1.x, d.y, fmaf(A1.y, d.x, fmaf(A3.x, i.y, fmaf(A3.y, i.x, cc * Bc.y))));
-            *dst = o;
+            const float cc = jac * fmaf(cf0, cg[3 * b], fmaf(cf1, cg[3 * b + 1], cf2 * cg[3 * b + 2]));
+#pragma unroll
+            for (int f = 0; f < NFQ; ++f) {
+              float2* dst = &acc[(f * 3 + b) * max_rows + s.loc[a]];
+              *dst = __fadd2_rn(*dst, __ffma2_rn(jj, W[f][a][b], __fmul2_rn(make_float2(cc, cc), Bc[f])));
+            }
           }
         }
       }
@@ -343,10 +380,11 @@ __global__ void __launch_bounds__(WARPS * 32, 3) regular_f32_kernel(const FaceF3
     __syncwarp();
   }
   }  // symmetry transforms
-  // write this warp's three extended-row segments
-  for (int i = lane; i < 3 * rows; i += 32) {
-    const int b = i / rows, loc = i - b * rows;
-    Rext[(size_t)(3 * g + b) * ldR + base + loc] = acc[b * max_rows + loc];
+  // write this warp's extended-row segments: three per frequency
+  for (int i = lane; i < NFQ * 3 * rows; i += 32) {
+    const int fb = i / rows, loc = i - fb * rows;
+    const int f = fb / 3, b = fb - 3 * f;
+    Rext[(size_t)f * strideR + (size_t)(3 * g + b) * ldR + base + loc] = acc[fb * max_rows + loc];
   }
 }
 
@@ -1075,33 +1113,72 @@ static df make_df(double x) {
   return r;
 }
 
-cudaError_t launch_regular(const DeviceMesh& m, Precision prec, double k, double2 cD, double2 cH, void* Rext,
-                           long long ldR, cudaStream_t stream) {
+namespace {
+template <int NFQ>
+cudaError_t launch_regular_f32(const DeviceMesh& m, const double* k, const double2* cD, const double2* cH,
+                               float2* Rext, long long ldR, long long strideR, cudaStream_t stream) {
+  constexpr int W = 4;
+  dim3 grid((m.nf + W - 1) / W, m.n_tiles);
+  RegParamsF32<NFQ> p;
+  for (int i = 0; i < 3 * kMaxQ; ++i) p.cw2[i] = make_float2((float)m.rule_cw[i], (float)m.rule_cw[i]);
+  for (int q = 0; q < kMaxQ; ++q) {  // w_q = sum_a phi_a(xi_q) w_q (the basis sums to one)
+    const float w = q < m.Q ? (float)(m.rule_cw[q] + m.rule_cw[m.Q + q] + m.rule_cw[2 * m.Q + q]) : 0.0f;
+    p.w2[q] = make_float2(w, w);
+  }
+  for (int f = 0; f < NFQ; ++f) {
+    p.kdf[f] = make_df(k[f]);
+    p.kturn[f] = (float)(k[f] / (2.0 * M_PI));
+    p.k2[f] = (float)(k[f] * k[f]);
+    p.mcD[f] = make_float2((float)-cD[f].x, (float)-cD[f].y);
+    p.ikcD[f] = make_float2((float)(-k[f] * cD[f].y), (float)(k[f] * cD[f].x));
+    p.cH[f] = f2(cH[f]);
+  }
+  const size_t sm = (size_t)W * NFQ * 3 * m.max_tile_rows * sizeof(float2);
+  auto launch = [&](auto kern) {
+    ensure_smem_limit((const void*)kern, sm);
+    kern<<<grid, W * 32, sm, stream>>>(m.faces32, m.nf, m.tile_group_ptr, m.lane_slots, m.tile_row_base,
+                                       m.max_tile_rows, Rext, ldR, strideR, p, m.ntr,
+                                       make_int4(m.tr[0], m.tr[1], m.tr[2], m.tr[3]), m.fix_mask);
+  };
+  if (m.Q == 6)
+    launch(regular_f32_kernel<6, W, NFQ>);
+  else if (m.Q == 3)
+    launch(regular_f32_kernel<3, W, NFQ>);
+  else
+    launch(regular_f32_kernel<1, W, NFQ>);
+  return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_regular(const DeviceMesh& m, Precision prec, int nfreq, const double* k, const double2* cD,
+                           const double2* cH, void* Rext, long long ldR, long long strideR, cudaStream_t stream) {
+  if (prec == Precision::Mixed) {
+    // two frequencies per launch share the frequency-independent geometry
+    int f = 0;
+    for (; f + 2 <= nfreq; f += 2) {
+      cudaError_t e = launch_regular_f32<2>(m, k + f, cD + f, cH + f, (float2*)Rext + (size_t)f * strideR, ldR,
+                                            strideR, stream);
+      if (e != cudaSuccess) return e;
+    }
+    if (f < nfreq)
+      return launch_regular_f32<1>(m, k + f, cD + f, cH + f, (float2*)Rext + (size_t)f * strideR, ldR, strideR,
+                                   stream);
+    return cudaSuccess;
+  }
+  for (int f = 0; f < nfreq; ++f) {
+    cudaError_t e = launch_regular_f64(m, k[f], cD[f], cH[f], (double2*)Rext + (size_t)f * strideR, ldR, stream);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+int regular_launches(Precision prec, int nfreq) { return prec == Precision::Mixed ? (nfreq + 1) / 2 : nfreq; }
+
+cudaError_t launch_regular_f64(const DeviceMesh& m, double k, double2 cD, double2 cH, double2* Rext, long long ldR,
+                               cudaStream_t stream) {
   const int W = 4;
   dim3 grid((m.nf + W - 1) / W, m.n_tiles);
-  if (prec == Precision::Mixed) {
-    RegParamsF32 p;
-    p.kdf = make_df(k);
-    p.k = (float)k;
-    p.k2 = (float)(k * k);
-    p.kturn = (float)(k / (2.0 * M_PI));
-    p.cD = f2(cD);
-    p.cH = f2(cH);
-    for (int i = 0; i < 3 * kMaxQ; ++i) p.cw2[i] = make_float2((float)m.rule_cw[i], (float)m.rule_cw[i]);
-    size_t sm = (size_t)W * 3 * m.max_tile_rows * sizeof(float2);
-    auto launch = [&](auto kern) {
-      ensure_smem_limit((const void*)kern, sm);
-      kern<<<grid, W * 32, sm, stream>>>(m.faces32, m.nf, m.tile_group_ptr, m.lane_slots, m.tile_row_base,
-                                         m.max_tile_rows, (float2*)Rext, ldR, p, m.ntr,
-                                         make_int4(m.tr[0], m.tr[1], m.tr[2], m.tr[3]), m.fix_mask);
-    };
-    if (m.Q == 6)
-      launch(regular_f32_kernel<6, W>);
-    else if (m.Q == 3)
-      launch(regular_f32_kernel<3, W>);
-    else
-      launch(regular_f32_kernel<1, W>);
-  } else {
+  {
     RegParamsF64 p;
     p.k = k;
     p.k2 = k * k;

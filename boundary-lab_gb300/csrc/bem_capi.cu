@@ -203,32 +203,68 @@ Layout layout_for(const bem::DeviceMesh& dm, bem::Precision prec) {
   return L;
 }
 
-// Assemble the LHS (cD, cH, cM) into A (and A2 if given) and, if nc > 0, the RHS
-// into b (nc columns, leading dimension ldb, permuted rows) for one frequency.
-void assemble_one(bem_mesh* m, bem::Precision prec, double k, const bem::OperatorCoeffs& c, void* A, void* A2,
-                  double2 qscale, int nc, const void* drive, void* b) {
+// Frequencies assembled together: the mixed form evaluates the regular pairs of
+// two frequencies in one launch (shared geometry), each into its own
+// extended-row buffer.
+int assembly_group(bem::Precision prec) { return prec == bem::Precision::Mixed ? 2 : 1; }
+
+// Assemble the LHS (c[i].cD, cH, cM) of cnt frequencies into A[i] (and A2[i] if
+// given) and, if nc > 0, the RHS into b[i] (nc columns, leading dimension ldb,
+// permuted rows).  Returns the number of kernels launched.
+long long assemble_frequencies(bem_mesh* m, bem::Precision prec, int cnt, const double* k,
+                               const bem::OperatorCoeffs* c, void* const* A, void* const* A2, const double2* qscale,
+                               int nc, const void* drive, void* const* b) {
   bem_context* ctx = m->ctx;
   const bem::DeviceMesh& dm = m->dm;
   Layout L = layout_for(dm, prec);
-  ck(ctx->rext.ensure((size_t)L.ldR * 3 * dm.nf * L.esz), "alloc extended rows");
-  ck(ctx->sblocks.ensure((size_t)std::max(dm.npairs, 1) * 12 * L.esz), "alloc singular blocks");
-  ck(bem::launch_singular_dyn(dm, prec, k, c, ctx->sblocks.p, ctx->stream), "singular kernel");
-  prof_mark(ctx, BEM_K_SINGULAR);
-  ck(bem::launch_regular(dm, prec, k, c.cD, c.cH, ctx->rext.p, L.ldR, ctx->stream), "regular kernel");
-  prof_mark(ctx, BEM_K_REGULAR);
-  ck(bem::launch_singular_scatter(dm, prec, ctx->sblocks.p, ctx->rext.p, L.ldR, ctx->stream), "singular scatter");
-  if (dm.n_isolated) {
-    ck(cudaMemsetAsync(A, 0, (size_t)L.lda * dm.nv * L.esz, ctx->stream), "memset");
-    if (A2) ck(cudaMemsetAsync(A2, 0, (size_t)L.lda * dm.nv * L.esz, ctx->stream), "memset");
+  const int G = std::min(assembly_group(prec), cnt);
+  const size_t rext_n = (size_t)L.ldR * 3 * dm.nf;         // elements per extended-row buffer
+  const size_t sblk_n = (size_t)std::max(dm.npairs, 1) * 12;  // elements per singular-block buffer
+  ck(ctx->rext.ensure(rext_n * L.esz * G), "alloc extended rows");
+  ck(ctx->sblocks.ensure(sblk_n * L.esz * G), "alloc singular blocks");
+  if (nc > 0) ck(ctx->rb.ensure((size_t)nc * dm.nf * 3 * L.esz), "alloc rhs faces");
+  auto rext = [&](int i) { return (void*)((char*)ctx->rext.p + rext_n * L.esz * i); };
+  auto sblk = [&](int i) { return (void*)((char*)ctx->sblocks.p + sblk_n * L.esz * i); };
+  long long launches = 0;
+  for (int f0 = 0; f0 < cnt; f0 += G) {
+    const int g = std::min(G, cnt - f0);
+    double2 cD[2], cH[2];
+    for (int i = 0; i < g; ++i) {
+      ck(bem::launch_singular_dyn(dm, prec, k[f0 + i], c[f0 + i], sblk(i), ctx->stream), "singular kernel");
+      cD[i] = c[f0 + i].cD;
+      cH[i] = c[f0 + i].cH;
+    }
+    prof_mark(ctx, BEM_K_SINGULAR);
+    ck(bem::launch_regular(dm, prec, g, k + f0, cD, cH, rext(0), L.ldR, (long long)rext_n, ctx->stream),
+       "regular kernel");
+    prof_mark(ctx, BEM_K_REGULAR);
+    for (int i = 0; i < g; ++i) {
+      void* Ai = A[f0 + i];
+      void* A2i = A2 ? A2[f0 + i] : nullptr;
+      ck(bem::launch_singular_scatter(dm, prec, sblk(i), rext(i), L.ldR, ctx->stream), "singular scatter");
+      if (dm.n_isolated) {
+        ck(cudaMemsetAsync(Ai, 0, (size_t)L.lda * dm.nv * L.esz, ctx->stream), "memset");
+        if (A2i) ck(cudaMemsetAsync(A2i, 0, (size_t)L.lda * dm.nv * L.esz, ctx->stream), "memset");
+      }
+      ck(bem::launch_gather(dm, prec, rext(i), L.ldR, Ai, L.lda, A2i, ctx->stream), "gather kernel");
+    }
+    prof_mark(ctx, BEM_K_GATHER);
+    if (nc > 0) {
+      for (int i = 0; i < g; ++i)
+        ck(bem::launch_rhs(dm, prec, k[f0 + i], c[f0 + i], qscale[f0 + i], drive, nc, sblk(i), ctx->rb.p, b[f0 + i],
+                           L.ldb, ctx->stream),
+           "rhs kernel");
+      prof_mark(ctx, BEM_K_RHS);
+    }
+    // per frequency: singular, scatter, gather (+ isolated rows), right-hand side (2)
+    launches += (long long)g * (3 + (dm.n_isolated ? 1 : 0) + (nc > 0 ? 2 : 0)) + bem::regular_launches(prec, g);
   }
-  ck(bem::launch_gather(dm, prec, ctx->rext.p, L.ldR, A, L.lda, A2, ctx->stream), "gather kernel");
-  prof_mark(ctx, BEM_K_GATHER);
-  if (nc > 0) {
-    ck(ctx->rb.ensure((size_t)nc * dm.nf * 3 * L.esz), "alloc rhs faces");
-    ck(bem::launch_rhs(dm, prec, k, c, qscale, drive, nc, ctx->sblocks.p, ctx->rb.p, b, L.ldb, ctx->stream),
-       "rhs kernel");
-    prof_mark(ctx, BEM_K_RHS);
-  }
+  return launches;
+}
+
+void assemble_one(bem_mesh* m, bem::Precision prec, double k, const bem::OperatorCoeffs& c, void* A, void* A2,
+                  double2 qscale, int nc, const void* drive, void* b) {
+  assemble_frequencies(m, prec, 1, &k, &c, &A, A2 ? &A2 : nullptr, &qscale, nc, drive, &b);
 }
 
 void free_mesh_device(bem_mesh* m) {
@@ -515,9 +551,10 @@ long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int np
   const long long lda = round_up(nv, 32);
   const long long n_ext = (long long)(nv * 1.3) + 64;
   long long bytes = 0;
-  bytes += round_up(n_ext, 32) * 3LL * nf * esz;                            // extended rows
+  const long long group = precision == BEM_PRECISION_MIXED ? 2 : 1;        // frequencies assembled together
+  bytes += round_up(n_ext, 32) * 3LL * nf * esz * group;                    // extended rows
   bytes += (long long)batch * lda * nv * esz * (precision == BEM_PRECISION_MIXED ? 2 : 1);  // matrices (+copy)
-  bytes += (long long)npairs * (12 * esz + 24 * 8 + 48);                    // singular blocks, moments, pairs
+  bytes += (long long)npairs * (12 * esz * group + 24 * 8 + 48);            // singular blocks, moments, pairs
   bytes += (long long)batch * nrhs * lda * (esz + 3 * 16 + 16);             // rhs, x, r, b64, d
   bytes += (long long)batch * nrhs * ((long long)nf * 6 * esz + (long long)npts * 16);  // field sources + out
   bytes += (long long)nf * (160 + 288 + 64);                                // face records and maps
@@ -595,16 +632,20 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       std::vector<double2> qs(bt);
       cudaEventRecord(ctx->ev[0], ctx->stream);
       prof_begin(ctx);
+      std::vector<bem::OperatorCoeffs> cs(bt);
+      std::vector<void*> As(bt), A2s(bt), bs(bt);
       for (int i = 0; i < bt; ++i) {
         const double omega = 2.0 * M_PI * freqs_hz[f0 + i];
         const double k = omega / o.sound_speed;
         ks[i] = k;
         qs[i] = make_double2(0.0, o.rho * omega);
-        char* A = (char*)ctx->mats.p + matsz * i;
-        char* A2 = mixed ? (char*)ctx->mats2.p + matsz * i : nullptr;
-        char* b = (char*)ctx->b32.p + (size_t)i * nc * L.ldb * L.esz;
-        assemble_one(m, prec, k, bm_coeffs(k), A, A2, qs[i], nc, drive, b);
+        cs[i] = bm_coeffs(k);
+        As[i] = (char*)ctx->mats.p + matsz * i;
+        A2s[i] = mixed ? (char*)ctx->mats2.p + matsz * i : nullptr;
+        bs[i] = (char*)ctx->b32.p + (size_t)i * nc * L.ldb * L.esz;
       }
+      launches += assemble_frequencies(m, prec, bt, ks.data(), cs.data(), As.data(), mixed ? A2s.data() : nullptr,
+                                       qs.data(), nc, drive, bs.data());
       cudaEventRecord(ctx->ev[1], ctx->stream);
       ck(cudaMemsetAsync(ctx->info.p, 0, (size_t)bt * sizeof(int), ctx->stream), "memset info");
       bool used_tensor = false;
@@ -619,9 +660,9 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
                                 ctx->cublas, ctx->stream, (bem::LuGemm)o.lu_gemm, tcws, &used_tensor, &tc_err,
                                 (int*)ctx->rowmap.p, &lu_launches),
          "LU factorisation");
-      // kernels of this batch: 6 per frequency in assembly (+1 with isolated vertices), the
-      // LU, the permutation, the solves (mixed: 5 + 5 per refinement step), the field (2, +1 mixed)
-      launches += (long long)bt * (6 + (dm.n_isolated ? 1 : 0)) + lu_launches + 1;
+      // kernels of this batch besides the assembly: the LU, the permutation, the solves
+      // (mixed: 5 + 5 per refinement step), the field (2, +1 mixed)
+      launches += lu_launches + 1;
       gemm_used = mixed ? (used_tensor ? 2 : 1) : 0;
       ck(bem::lu_perm_batched((const int*)ctx->ipiv.p, nv, bt, (int*)ctx->perm.p, ctx->stream), "pivot permutation");
       prof_mark(ctx, BEM_K_LU);

@@ -75,8 +75,13 @@ struct DeviceMesh {
 };
 
 // assembly (bem_assembly.cu)
-cudaError_t launch_regular(const DeviceMesh& m, Precision prec, double k, double2 cD, double2 cH, void* Rext,
-                           long long ldR, cudaStream_t stream);
+// Regular pairs of nfreq frequencies into nfreq extended-row buffers (Rext +
+// f * strideR elements); the mixed form evaluates two frequencies per launch.
+cudaError_t launch_regular(const DeviceMesh& m, Precision prec, int nfreq, const double* k, const double2* cD,
+                           const double2* cH, void* Rext, long long ldR, long long strideR, cudaStream_t stream);
+int regular_launches(Precision prec, int nfreq);
+cudaError_t launch_regular_f64(const DeviceMesh& m, double k, double2 cD, double2 cH, double2* Rext, long long ldR,
+                               cudaStream_t stream);
 cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, cudaStream_t stream);
 cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, double k, const OperatorCoeffs& c, void* blocks,
                                 cudaStream_t stream);
