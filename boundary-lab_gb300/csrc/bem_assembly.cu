@@ -134,35 +134,44 @@ __device__ __forceinline__ PairGeomF32 pair_geom_f32(const float* ahi_g, const f
 // Parameters of one regular-assembly launch over NFQ frequencies (kernel
 // parameters, so meshes with different rules run concurrently on different
 // streams).  cw[a*Q + q] = phi_a(xi_q) * w_q of the regular rule; w_q = sum_a cw.
-template <int NFQ> struct RegParamsF32 {
-  float2 cw2[3 * kMaxQ];  // (cw, cw): operand pairs of the packed FP32x2 FMAs
+template <int NFQ, bool DT> struct RegParamsF32 {
+  float2 cw2[3 * kMaxQ];  // (cw, cw) at [a*Q + q]: operand pairs of the packed FP32x2 FMAs
   float2 w2[kMaxQ];       // (w, w)
-  df kdf[NFQ];              // wavenumbers as double-float
-  float kturn[NFQ];         // k / 2pi (phase in turns)
-  float k2[NFQ];
-  float2 mcD[NFQ];   // -cD
-  float2 ikcD[NFQ];  // i k cD
+  float2 cwp[3][kMaxQ];   // (cw, cw) at [b][n], zero for the padding point of an odd rule
+  float2 wp[kMaxQ];       // (w, w) at [n], zero for the padding point
+  df kdf[NFQ];     // wavenumbers as double-float
+  float k[NFQ], k2[NFQ];
+  float2 cHn[NFQ];  // cH / cD (cH when the launch has no double-layer term)
+  float2 cDn[NFQ];  // cD (1 when the launch has no double-layer term)
   float2 cH[NFQ];
 };
 
 // Regular face pairs for NFQ frequencies at once.  Per q-pair (test point m,
 // trial point n) the frequency-independent part (r, 1/r, the compensated
-// r - |C|, the normal factor t = (r . n_g) / r) is formed once, then per
-// frequency the phase e^{ikr} and
-//   H = G (cD t (ik - 1/r) + cnn),  G = e^{ikr} / r,  cnn = -k^2 (n_f . n_g) cH,
-// which is cD * (double-layer kernel) + the -k^2 nn cH part of the
-// hypersingular kernel in one complex weight.  Per test point the trial-basis
-// sums Hs[b] = sum_n cw[b][n] H and Gs = sum_n w_n G are folded into
+// r - |C|, t = (r . n_g) / r, t / r, t / r^2) is formed once, then per
+// frequency the phase kr and
+//   H = e^{ikr} E'',  E'' = (1/r) (t (ik - 1/r) + cnn'),  cnn' = -k^2 (n_f . n_g) cH / cD,
+// so that cD H = G (cD t (ik - 1/r) - k^2 nn cH), G = e^{ikr} / r: the
+// double-layer kernel times cD plus the -k^2 nn cH part of the hypersingular
+// kernel in one complex weight.  Per test point the trial-basis sums
+// Hs[b] = sum_n cw[b][n] H and Gs = sum_n w_n G are folded into
 // W[a][b] += cw[a][m] Hs[b] and S0 += w_m Gs, and each pair adds
-//   jac * (W[a][b] + (curl_a . curl_b) cH S0)
+//   jac * (cD W[a][b] + (curl_a . curl_b) cH S0)
 // (BeatEngineCpuAssembly.jl:278-373: the D and H regular integrals, with
 // S0 = sum_{a,b} of the single-layer integrals of the basis products, because
-// the P1 basis functions sum to one).
-template <int Q, int WARPS, int NFQ>
+// the P1 basis functions sum to one).  DT = false (cD = 0) drops the
+// double-layer term: E'' = cnn / r, with cH in place of cH / cD.
+//
+// The phase kr = k|C| + k(r - |C|) is taken in radians without a per-q-pair
+// reduction: k|C| is reduced mod 2pi per pair in double-float and
+// |k(r - |C|)| <= k h (h the element size), so |kr| stays a few pi at most
+// for any mesh that resolves the wavelength.
+template <int Q, int WARPS, int NFQ, bool DT>
 __global__ void __launch_bounds__(WARPS * 32, 3)  // three CTAs per SM (<= 168 registers)
     regular_f32_kernel(const FaceF32* __restrict__ faces, int nf, const int* __restrict__ tile_group_ptr,
-                       const LaneSlot* __restrict__ slots, const int* __restrict__ tile_row_base, int max_rows,
-                       float2* __restrict__ Rext, long long ldR, long long strideR, RegParamsF32<NFQ> p, int ntr,
+                       const LaneSlot* __restrict__ slots, const float* __restrict__ group_faces,
+                       const int* __restrict__ tile_row_base, int max_rows,
+                       float2* __restrict__ Rext, long long ldR, long long strideR, RegParamsF32<NFQ, DT> p, int ntr,
                        int4 trs, const unsigned char* __restrict__ fix_mask) {
   extern __shared__ float2 smem_acc32[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -181,7 +190,12 @@ __global__ void __launch_bounds__(WARPS * 32, 3)  // three CTAs per SM (<= 168 r
 
   // trial face (warp-uniform): quadrature offsets og[n] with og.og and og.n_g
   const FaceF32& T = faces[g];
-  float ahi_g[3], alo_g[3], ng[3], og[Q][3], cg[9], gg[Q], gn[Q];
+  // Trial points are taken two at a time (n = 2j, 2j + 1) in the lanes of
+  // packed FP32x2 registers; an odd rule is padded with the centroid at zero
+  // weight.
+  constexpr int NP = (Q + 1) / 2;
+  float ahi_g[3], alo_g[3], ng[3], cg[9];
+  float2 ogp[NP][3], ggp[NP], ngnp[NP];  // offsets, og.og, -og.n_g
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     ahi_g[d] = T.anchor_hi[d];
@@ -191,11 +205,20 @@ __global__ void __launch_bounds__(WARPS * 32, 3)  // three CTAs per SM (<= 168 r
 #pragma unroll
   for (int i = 0; i < 9; ++i) cg[i] = T.curls[i];
 #pragma unroll
-  for (int n = 0; n < Q; ++n) {
+  for (int j = 0; j < NP; ++j) {
+    float o[2][3], gg[2], gn[2];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) og[n][d] = T.off[3 * n + d];
-    gg[n] = fmaf(og[n][0], og[n][0], fmaf(og[n][1], og[n][1], og[n][2] * og[n][2]));
-    gn[n] = fmaf(og[n][0], ng[0], fmaf(og[n][1], ng[1], og[n][2] * ng[2]));
+    for (int e = 0; e < 2; ++e) {
+      const int n = 2 * j + e;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) o[e][d] = n < Q ? T.off[3 * n + d] : 0.0f;
+      gg[e] = fmaf(o[e][0], o[e][0], fmaf(o[e][1], o[e][1], o[e][2] * o[e][2]));
+      gn[e] = fmaf(o[e][0], ng[0], fmaf(o[e][1], ng[1], o[e][2] * ng[2]));
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) ogp[j][d] = make_float2(o[0][d], o[1][d]);
+    ggp[j] = make_float2(gg[0], gg[1]);
+    ngnp[j] = make_float2(-gn[0], -gn[1]);
   }
   const float a2g = T.area2;
   const int gv0 = T.verts[0], gv1 = T.verts[1], gv2 = T.verts[2];
@@ -218,9 +241,9 @@ __global__ void __launch_bounds__(WARPS * 32, 3)  // three CTAs per SM (<= 168 r
       ng[0] *= fx;
       ng[1] *= fy;
 #pragma unroll
-      for (int n = 0; n < Q; ++n) {
-        og[n][0] *= fx;
-        og[n][1] *= fy;
+      for (int j = 0; j < NP; ++j) {  // og.og and og.n_g are unchanged by a reflection
+        ogp[j][0] = __fmul2_rn(ogp[j][0], make_float2(fx, fx));
+        ogp[j][1] = __fmul2_rn(ogp[j][1], make_float2(fy, fy));
       }
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
@@ -236,25 +259,25 @@ __global__ void __launch_bounds__(WARPS * 32, 3)  // three CTAs per SM (<= 168 r
 
   // Software pipeline over the lane groups: the slot of group grp + 2 and the
   // face header (vertices, anchor) of group grp + 1 are loaded while group grp
-  // is integrated, so the pair set-up never waits on a global load.
+  // is integrated, so the pair set-up never waits on a global load.  The test
+  // faces of a group are stored field-major (group_faces[grp][word][lane], the
+  // words of FaceF32), so every field load of the warp is one 128-byte line.
   const int g0 = tile_group_ptr[tile], g1 = tile_group_ptr[tile + 1];
   LaneSlot s_next{-1, {0, 0, 0}}, s_cur{-1, {0, 0, 0}};
   int hv[3] = {-1, -1, -1};
   float hhi[3] = {0.f, 0.f, 0.f}, hlo[3] = {0.f, 0.f, 0.f};
-  auto load_head = [&](const LaneSlot& sl) {
-    if (sl.face >= 0) {
-      const FaceF32& H = faces[sl.face];
+  auto load_head = [&](int grp) {
+    const float* H = group_faces + (size_t)grp * kFaceWords * 32 + lane;
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        hv[d] = H.verts[d];
-        hhi[d] = H.anchor_hi[d];
-        hlo[d] = H.anchor_lo[d];
-      }
+    for (int d = 0; d < 3; ++d) {
+      hv[d] = __float_as_int(H[(kFwVerts + d) * 32]);
+      hhi[d] = H[(kFwAnchorHi + d) * 32];
+      hlo[d] = H[(kFwAnchorLo + d) * 32];
     }
   };
   if (g0 < g1) {
     s_cur = slots[(size_t)g0 * 32 + lane];
-    load_head(s_cur);
+    load_head(g0);
   }
   if (g0 + 1 < g1) s_next = slots[(size_t)(g0 + 1) * 32 + lane];
   for (int grp = g0; grp < g1; ++grp) {
@@ -263,11 +286,11 @@ __global__ void __launch_bounds__(WARPS * 32, 3)  // three CTAs per SM (<= 168 r
     const float ahi_f[3] = {hhi[0], hhi[1], hhi[2]}, alo_f[3] = {hlo[0], hlo[1], hlo[2]};
     if (grp + 1 < g1) {
       s_cur = s_next;
-      load_head(s_cur);
+      load_head(grp + 1);
     }
     if (grp + 2 < g1) s_next = slots[(size_t)(grp + 2) * 32 + lane];
     if (s.face >= 0) {
-      const FaceF32& F = faces[s.face];
+      const float* F = group_faces + (size_t)grp * kFaceWords * 32 + lane;  // this lane's test face: word w at F[32 w]
       if (!share_vertex(fv, sv0, sv1, sv2)) {
         // With C = anchor_g - anchor_f, x_n = anchor_g + og[n], y_m = anchor_f + of[m]
         // and d = og[n] - of[m]:  r = |C + d|, and
@@ -277,21 +300,30 @@ __global__ void __launch_bounds__(WARPS * 32, 3)  // three CTAs per SM (<= 168 r
         // every term of size |C| h or h^2 (no cancellation against |C|^2).
         const PairGeomF32 P = pair_geom_f32(ahi_g, alo_g, ahi_f, alo_f);
         const float R0 = fmaxf(P.R.hi + P.R.lo, 1e-30f);
-        float Pg[Q];
+        float2 Pgp[NP];  // 2 C.og + og.og
+        {
+          const float2 c0 = make_float2(2.0f * P.Cf[0], 2.0f * P.Cf[0]);
+          const float2 c1 = make_float2(2.0f * P.Cf[1], 2.0f * P.Cf[1]);
+          const float2 c2 = make_float2(2.0f * P.Cf[2], 2.0f * P.Cf[2]);
 #pragma unroll
-        for (int n = 0; n < Q; ++n)
-          Pg[n] = fmaf(2.0f, fmaf(P.Cf[0], og[n][0], fmaf(P.Cf[1], og[n][1], P.Cf[2] * og[n][2])), gg[n]);
+          for (int j = 0; j < NP; ++j)
+            Pgp[j] = __ffma2_rn(c0, ogp[j][0], __ffma2_rn(c1, ogp[j][1], __ffma2_rn(c2, ogp[j][2], ggp[j])));
+        }
+        const float2 R0p = make_float2(R0, R0);
         // test-face data
-        const float nn = fmaf(F.normal[0], ng[0], fmaf(F.normal[1], ng[1], F.normal[2] * ng[2]));
-        const float jac = F.area2 * a2g * BEM_INV_FOUR_PI;
-        float t0[NFQ];    // k|C| mod 2pi, in turns (|t0| <= 1/2)
-        float2 cnn[NFQ];  // -k^2 nn cH
+        const float nn =
+            fmaf(F[32 * kFwNormal], ng[0], fmaf(F[32 * (kFwNormal + 1)], ng[1], F[32 * (kFwNormal + 2)] * ng[2]));
+        const float jac = F[32 * kFwArea2] * a2g * BEM_INV_FOUR_PI;
+        float2 th0[NFQ];            // k|C| mod 2pi in [-pi, pi], both lanes
+        float2 cnnx[NFQ], cnny[NFQ];  // cnn' = -k^2 nn cHn, each part in both lanes
         float2 W[NFQ][3][3], S0[NFQ];
 #pragma unroll
         for (int f = 0; f < NFQ; ++f) {
-          t0[f] = df_reduce_two_pi(df_mul(p.kdf[f], P.R)) * BEM_INV_TWO_PI;
+          const float th = df_reduce_two_pi(df_mul(p.kdf[f], P.R));
+          th0[f] = make_float2(th, th);
           const float s = -p.k2[f] * nn;
-          cnn[f] = make_float2(s * p.cH[f].x, s * p.cH[f].y);
+          cnnx[f] = make_float2(s * p.cHn[f].x, s * p.cHn[f].x);
+          cnny[f] = make_float2(s * p.cHn[f].y, s * p.cHn[f].y);
           S0[f] = make_float2(0.f, 0.f);
 #pragma unroll
           for (int a = 0; a < 3; ++a)
@@ -300,20 +332,25 @@ __global__ void __launch_bounds__(WARPS * 32, 3)  // three CTAs per SM (<= 168 r
         }
         // The test-point loop is kept rolled: fully unrolling 6 x 6 Green
         // evaluations overflowed the instruction cache (no_instruction stalls).
-        float nf0 = F.off[0], nf1 = F.off[1], nf2 = F.off[2];
+        const float* Foff = F + 32 * kFwOff;
+        float nf0 = Foff[0], nf1 = Foff[32], nf2 = Foff[64];
 #pragma unroll 1
         for (int m = 0; m < Q; ++m) {
           const float f0 = nf0, f1 = nf1, f2 = nf2;
           {  // offsets of test point m + 1, consumed in the next iteration
             const int mn = m + 1 < Q ? m + 1 : m;
-            nf0 = F.off[3 * mn];
-            nf1 = F.off[3 * mn + 1];
-            nf2 = F.off[3 * mn + 2];
+            nf0 = Foff[96 * mn];
+            nf1 = Foff[96 * mn + 32];
+            nf2 = Foff[96 * mn + 64];
           }
           const float cm0 = P.Cf[0] - f0, cm1 = P.Cf[1] - f1, cm2 = P.Cf[2] - f2;
           const float Pf = fmaf(-2.0f, fmaf(P.Cf[0], f0, fmaf(P.Cf[1], f1, P.Cf[2] * f2)),
                                 fmaf(f0, f0, fmaf(f1, f1, f2 * f2)));
-          const float cmn = fmaf(cm0, ng[0], fmaf(cm1, ng[1], cm2 * ng[2]));
+          const float ncmn = -fmaf(cm0, ng[0], fmaf(cm1, ng[1], cm2 * ng[2]));
+          const float2 cm0p = make_float2(cm0, cm0), cm1p = make_float2(cm1, cm1), cm2p = make_float2(cm2, cm2);
+          const float2 m2f0 = make_float2(-2.0f * f0, -2.0f * f0), m2f1 = make_float2(-2.0f * f1, -2.0f * f1),
+                       m2f2 = make_float2(-2.0f * f2, -2.0f * f2);
+          const float2 Pfp = make_float2(Pf, Pf), ncmnp = make_float2(ncmn, ncmn);
           float2 Hs[NFQ][3], Gs[NFQ];
 #pragma unroll
           for (int f = 0; f < NFQ; ++f) {
@@ -322,28 +359,45 @@ __global__ void __launch_bounds__(WARPS * 32, 3)  // three CTAs per SM (<= 168 r
             for (int b = 0; b < 3; ++b) Hs[f][b] = make_float2(0.f, 0.f);
           }
 #pragma unroll
-          for (int n = 0; n < Q; ++n) {
-            // frequency-independent: r vector y_m -> x_n, 1/r, r - |C|, (r . n_g) / r
-            const float r0 = cm0 + og[n][0], r1 = cm1 + og[n][1], r2v = cm2 + og[n][2];
-            const float r2 = fmaxf(fmaf(r0, r0, fmaf(r1, r1, r2v * r2v)), 1e-30f);
-            const float rinv = rsqrt_ftz(r2);
-            const float num = fmaf(-2.0f, fmaf(og[n][0], f0, fmaf(og[n][1], f1, og[n][2] * f2)), Pg[n] + Pf);
-            const float delta = num * rcp_ftz(fmaf(r2, rinv, R0));
-            const float t = (cmn + gn[n]) * rinv;
-            const float2 tt = make_float2(t, t), trr = make_float2(t * rinv, t * rinv);
+          for (int j = 0; j < NP; ++j) {
+            // frequency-independent, two trial points per instruction: r vector
+            // y_m -> x_n, 1/r, r - |C|, -t = -(r . n_g) / r, -t / r, -t / r^2, w / r
+            const float2 r0 = __fadd2_rn(cm0p, ogp[j][0]), r1 = __fadd2_rn(cm1p, ogp[j][1]),
+                         r2v = __fadd2_rn(cm2p, ogp[j][2]);
+            float2 r2 = __ffma2_rn(r0, r0, __ffma2_rn(r1, r1, __fmul2_rn(r2v, r2v)));
+            r2 = make_float2(fmaxf(r2.x, 1e-30f), fmaxf(r2.y, 1e-30f));
+            const float2 rinv = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+            const float2 num =
+                __ffma2_rn(ogp[j][0], m2f0, __ffma2_rn(ogp[j][1], m2f1, __ffma2_rn(ogp[j][2], m2f2, __fadd2_rn(Pgp[j], Pfp))));
+            const float2 den = __ffma2_rn(r2, rinv, R0p);
+            const float2 delta = __fmul2_rn(num, make_float2(rcp_ftz(den.x), rcp_ftz(den.y)));
+            const float2 nt = __fmul2_rn(__fadd2_rn(ncmnp, ngnp[j]), rinv);
+            const float2 ntr = __fmul2_rn(nt, rinv);
+            const float2 ntrr = __fmul2_rn(ntr, rinv);
+            const float2 wr = __fmul2_rn(make_float2(p.wp[2 * j].x, p.wp[2 * j + 1].x), rinv);
 #pragma unroll
             for (int f = 0; f < NFQ; ++f) {
-              float turn = fmaf(p.kturn[f], delta, t0[f]);
-              turn -= round_nearest_small(turn);  // |turn| <= 1/2
-              float sn, cs;
-              sincos_ftz(turn * BEM_TWO_PI_HI, &sn, &cs);
-              const float2 G = __fmul2_rn(make_float2(cs, sn), make_float2(rinv, rinv));  // e^{ikr} / r
-              // E = cD t (ik - 1/r) + cnn = (t/r)(-cD) + t (i k cD) + cnn
-              const float2 E = __ffma2_rn(trr, p.mcD[f], __ffma2_rn(tt, p.ikcD[f], cnn[f]));
-              const float2 H = make_float2(fmaf(G.x, E.x, -G.y * E.y), fmaf(G.x, E.y, G.y * E.x));
+              const float2 th = __ffma2_rn(make_float2(p.k[f], p.k[f]), delta, th0[f]);  // kr - 2 pi n
+              // E'' = (-t/r^2 + cnn'.x / r, k t / r + cnn'.y / r)
+              float2 Ex, Ey;
+              if (DT) {
+                Ex = __ffma2_rn(rinv, cnnx[f], ntrr);
+                Ey = __ffma2_rn(rinv, cnny[f], __fmul2_rn(make_float2(-p.k[f], -p.k[f]), ntr));
+              } else {
+                Ex = __fmul2_rn(rinv, cnnx[f]);
+                Ey = __fmul2_rn(rinv, cnny[f]);
+              }
 #pragma unroll
-              for (int b = 0; b < 3; ++b) Hs[f][b] = __ffma2_rn(p.cw2[b * Q + n], H, Hs[f][b]);
-              Gs[f] = __ffma2_rn(p.w2[n], G, Gs[f]);
+              for (int e = 0; e < 2; ++e) {
+                const int n = 2 * j + e;
+                const float ex = e ? Ex.y : Ex.x, ey = e ? Ey.y : Ey.x, w = e ? wr.y : wr.x;
+                float sn, cs;
+                sincos_ftz(e ? th.y : th.x, &sn, &cs);
+                const float2 H = make_float2(fmaf(cs, ex, -sn * ey), fmaf(cs, ey, sn * ex));  // e^{ikr} E''
+#pragma unroll
+                for (int b = 0; b < 3; ++b) Hs[f][b] = __ffma2_rn(p.cwp[b][n], H, Hs[f][b]);
+                Gs[f] = __ffma2_rn(make_float2(w, w), make_float2(cs, sn), Gs[f]);  // w e^{ikr} / r
+              }
             }
           }
 #pragma unroll
@@ -357,14 +411,21 @@ __global__ void __launch_bounds__(WARPS * 32, 3)  // three CTAs per SM (<= 168 r
             S0[f] = __ffma2_rn(s_w2[m], Gs[f], S0[f]);
           }
         }
-        // L[a][b] = jac (W[a][b] + (curl_a . curl_b) cH S0)
+        // L[a][b] = jac (cD W[a][b] + (curl_a . curl_b) cH S0)
         float2 Bc[NFQ];
 #pragma unroll
-        for (int f = 0; f < NFQ; ++f) Bc[f] = cmul(p.cH[f], S0[f]);
+        for (int f = 0; f < NFQ; ++f) {
+          Bc[f] = cmul(p.cH[f], S0[f]);
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) W[f][a][b] = cmul(p.cDn[f], W[f][a][b]);
+        }
         const float2 jj = make_float2(jac, jac);
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-          const float cf0 = F.curls[3 * a], cf1 = F.curls[3 * a + 1], cf2 = F.curls[3 * a + 2];
+          const float cf0 = F[32 * (kFwCurls + 3 * a)], cf1 = F[32 * (kFwCurls + 3 * a + 1)],
+                      cf2 = F[32 * (kFwCurls + 3 * a + 2)];
 #pragma unroll
           for (int b = 0; b < 3; ++b) {
             const float cc = jac * fmaf(cf0, cg[3 * b], fmaf(cf1, cg[3 * b + 1], cf2 * cg[3 * b + 2]));
@@ -1114,38 +1175,50 @@ static df make_df(double x) {
 }
 
 namespace {
-template <int NFQ>
+template <int NFQ, bool DT>
 cudaError_t launch_regular_f32(const DeviceMesh& m, const double* k, const double2* cD, const double2* cH,
                                float2* Rext, long long ldR, long long strideR, cudaStream_t stream) {
   constexpr int W = 4;
   dim3 grid((m.nf + W - 1) / W, m.n_tiles);
-  RegParamsF32<NFQ> p;
+  RegParamsF32<NFQ, DT> p;
   for (int i = 0; i < 3 * kMaxQ; ++i) p.cw2[i] = make_float2((float)m.rule_cw[i], (float)m.rule_cw[i]);
   for (int q = 0; q < kMaxQ; ++q) {  // w_q = sum_a phi_a(xi_q) w_q (the basis sums to one)
     const float w = q < m.Q ? (float)(m.rule_cw[q] + m.rule_cw[m.Q + q] + m.rule_cw[2 * m.Q + q]) : 0.0f;
     p.w2[q] = make_float2(w, w);
+    p.wp[q] = make_float2(w, w);
+    for (int b = 0; b < 3; ++b) {
+      const float c = q < m.Q ? (float)m.rule_cw[b * m.Q + q] : 0.0f;
+      p.cwp[b][q] = make_float2(c, c);
+    }
   }
   for (int f = 0; f < NFQ; ++f) {
     p.kdf[f] = make_df(k[f]);
-    p.kturn[f] = (float)(k[f] / (2.0 * M_PI));
+    p.k[f] = (float)k[f];
     p.k2[f] = (float)(k[f] * k[f]);
-    p.mcD[f] = make_float2((float)-cD[f].x, (float)-cD[f].y);
-    p.ikcD[f] = make_float2((float)(-k[f] * cD[f].y), (float)(k[f] * cD[f].x));
     p.cH[f] = f2(cH[f]);
+    if (DT) {
+      const double d = cD[f].x * cD[f].x + cD[f].y * cD[f].y;  // cH / cD
+      p.cHn[f] = make_float2((float)((cH[f].x * cD[f].x + cH[f].y * cD[f].y) / d),
+                             (float)((cH[f].y * cD[f].x - cH[f].x * cD[f].y) / d));
+      p.cDn[f] = f2(cD[f]);
+    } else {
+      p.cHn[f] = f2(cH[f]);
+      p.cDn[f] = make_float2(1.0f, 0.0f);
+    }
   }
   const size_t sm = (size_t)W * NFQ * 3 * m.max_tile_rows * sizeof(float2);
   auto launch = [&](auto kern) {
     ensure_smem_limit((const void*)kern, sm);
-    kern<<<grid, W * 32, sm, stream>>>(m.faces32, m.nf, m.tile_group_ptr, m.lane_slots, m.tile_row_base,
-                                       m.max_tile_rows, Rext, ldR, strideR, p, m.ntr,
+    kern<<<grid, W * 32, sm, stream>>>(m.faces32, m.nf, m.tile_group_ptr, m.lane_slots, m.group_faces32,
+                                       m.tile_row_base, m.max_tile_rows, Rext, ldR, strideR, p, m.ntr,
                                        make_int4(m.tr[0], m.tr[1], m.tr[2], m.tr[3]), m.fix_mask);
   };
   if (m.Q == 6)
-    launch(regular_f32_kernel<6, W, NFQ>);
+    launch(regular_f32_kernel<6, W, NFQ, DT>);
   else if (m.Q == 3)
-    launch(regular_f32_kernel<3, W, NFQ>);
+    launch(regular_f32_kernel<3, W, NFQ, DT>);
   else
-    launch(regular_f32_kernel<1, W, NFQ>);
+    launch(regular_f32_kernel<1, W, NFQ, DT>);
   return cudaGetLastError();
 }
 }  // namespace
@@ -1153,16 +1226,19 @@ cudaError_t launch_regular_f32(const DeviceMesh& m, const double* k, const doubl
 cudaError_t launch_regular(const DeviceMesh& m, Precision prec, int nfreq, const double* k, const double2* cD,
                            const double2* cH, void* Rext, long long ldR, long long strideR, cudaStream_t stream) {
   if (prec == Precision::Mixed) {
-    // two frequencies per launch share the frequency-independent geometry
+    // two frequencies per launch share the frequency-independent geometry; an
+    // operator without the double-layer term (cD = 0) runs one per launch
     int f = 0;
-    for (; f + 2 <= nfreq; f += 2) {
-      cudaError_t e = launch_regular_f32<2>(m, k + f, cD + f, cH + f, (float2*)Rext + (size_t)f * strideR, ldR,
-                                            strideR, stream);
+    while (f < nfreq) {
+      float2* R = (float2*)Rext + (size_t)f * strideR;
+      const bool dt = cD[f].x != 0.0 || cD[f].y != 0.0;
+      const bool two = f + 1 < nfreq && dt && (cD[f + 1].x != 0.0 || cD[f + 1].y != 0.0);
+      cudaError_t e = two  ? launch_regular_f32<2, true>(m, k + f, cD + f, cH + f, R, ldR, strideR, stream)
+                      : dt ? launch_regular_f32<1, true>(m, k + f, cD + f, cH + f, R, ldR, strideR, stream)
+                           : launch_regular_f32<1, false>(m, k + f, cD + f, cH + f, R, ldR, strideR, stream);
       if (e != cudaSuccess) return e;
+      f += two ? 2 : 1;
     }
-    if (f < nfreq)
-      return launch_regular_f32<1>(m, k + f, cD + f, cH + f, (float2*)Rext + (size_t)f * strideR, ldR, strideR,
-                                   stream);
     return cudaSuccess;
   }
   for (int f = 0; f < nfreq; ++f) {

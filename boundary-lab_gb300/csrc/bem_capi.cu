@@ -402,6 +402,7 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
       d.faces64 = upload(m, P.faces64);
       d.tile_group_ptr = upload(m, P.tile_group_ptr);
       d.lane_slots = upload(m, P.lane_slots);
+      d.group_faces32 = upload(m, P.group_faces32);
       d.tile_row_base = upload(m, P.tile_row_base);
       d.ext_row = upload(m, P.ext_row);
       d.halo_slot_of_ext = upload(m, P.halo_slot_of_ext);
@@ -557,7 +558,7 @@ long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int np
   bytes += (long long)npairs * (12 * esz * group + 24 * 8 + 48);            // singular blocks, moments, pairs
   bytes += (long long)batch * nrhs * lda * (esz + 3 * 16 + 16);             // rhs, x, r, b64, d
   bytes += (long long)batch * nrhs * ((long long)nf * 6 * esz + (long long)npts * 16);  // field sources + out
-  bytes += (long long)nf * (160 + 288 + 64);                                // face records and maps
+  bytes += (long long)nf * (2 * 160 + 288 + 64);                            // face records (+ lane-group copy), maps
   if (precision == BEM_PRECISION_MIXED)                                      // tensor-core update operands
     bytes += (long long)batch * (2 * round_up(2LL * nv, 128) + 2 * round_up(nv, 256)) * 256 * 4;
   bytes += 64LL << 20;                                                      // cuBLAS workspace and slack

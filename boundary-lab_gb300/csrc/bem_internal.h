@@ -28,6 +28,9 @@ struct alignas(16) FaceF32 {
   int verts[3];
 };
 static_assert(sizeof(FaceF32) == 160, "FaceF32 layout");
+// FaceF32 as 40 four-byte words (the field-major copy of the lane groups)
+constexpr int kFaceWords = 40;
+constexpr int kFwAnchorHi = 0, kFwAnchorLo = 3, kFwNormal = 6, kFwArea2 = 9, kFwCurls = 10, kFwOff = 19, kFwVerts = 37;
 
 // FP64 face record (288 B).
 struct alignas(16) FaceF64 {
@@ -89,6 +92,7 @@ struct MeshPlan {
   int max_tile_rows = 0;              // max distinct vertices in one tile
   std::vector<int> tile_group_ptr;    // n_tiles + 1, in units of groups
   std::vector<LaneSlot> lane_slots;   // n_groups x 32
+  std::vector<float> group_faces32;   // n_groups x kFaceWords x 32: the test face of each lane slot, field-major
   std::vector<int> tile_row_base;     // n_tiles + 1: extended-row offset of each tile
   int n_ext = 0;                      // total extended rows
   std::vector<int> ext_row;           // n_ext: matrix row (permuted order) of each extended row

@@ -36,6 +36,7 @@ struct DeviceMesh {
   FaceF64* faces64 = nullptr;
   int* tile_group_ptr = nullptr;
   LaneSlot* lane_slots = nullptr;
+  float* group_faces32 = nullptr;  // lane groups' test faces, field-major
   int* tile_row_base = nullptr;
   int* ext_row = nullptr;
   int* halo_slot_of_ext = nullptr;

@@ -23,6 +23,8 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstddef>
+#include <cstring>
 #include <map>
 #include <numeric>
 #include <set>
@@ -619,6 +621,29 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
       }
     }
     P.tile_group_ptr.push_back(P.tile_group_ptr.back() + (int)groups.size());
+  }
+  // the same groups, field-major: word w of lane l's face record at [grp][w][l]
+  static_assert(offsetof(FaceF32, anchor_lo) == 4 * kFwAnchorLo && offsetof(FaceF32, normal) == 4 * kFwNormal &&
+                    offsetof(FaceF32, area2) == 4 * kFwArea2 && offsetof(FaceF32, curls) == 4 * kFwCurls &&
+                    offsetof(FaceF32, off) == 4 * kFwOff && offsetof(FaceF32, verts) == 4 * kFwVerts &&
+                    sizeof(FaceF32) == 4 * kFaceWords,
+                "FaceF32 word offsets");
+  {
+    const size_t ng = P.lane_slots.size() / kLanes;
+    P.group_faces32.assign(ng * kFaceWords * kLanes, 0.0f);
+    for (size_t g = 0; g < ng; ++g)
+      for (int l = 0; l < kLanes; ++l) {
+        const int f = P.lane_slots[g * kLanes + l].face;
+        float w[kFaceWords];
+        if (f >= 0) {
+          std::memcpy(w, &P.faces32[f], sizeof(w));
+        } else {
+          std::memset(w, 0, sizeof(w));
+          const int none = -1;
+          for (int a = 0; a < 3; ++a) std::memcpy(&w[kFwVerts + a], &none, sizeof(int));
+        }
+        for (int i = 0; i < kFaceWords; ++i) P.group_faces32[(g * kFaceWords + i) * kLanes + l] = w[i];
+      }
   }
   // column gather CSR: vertex j <- (g, b)
   P.col_ptr.assign(nv + 1, 0);

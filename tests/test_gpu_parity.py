@@ -68,6 +68,23 @@ def test_single_operators_fp64(gpu_ctx, native, box_small, which):
     assert rel(A, ref) < 1e-11
 
 
+@pytest.mark.parametrize("which", ["D", "H", "DH"])
+def test_single_operators_mixed(gpu_ctx, native, box_small, which):
+    """Mixed form with one operator at a time: D alone (cH = 0), H alone (cD = 0:
+    the regular kernel without the double-layer term), and a complex cD."""
+    O = _oracle()
+    k = 2 * np.pi * 4000.0 / 343.0
+    coeffs = {"D": (1.0, 0.0, 0.0), "H": (0.0, 1.0, 0.0), "DH": (0.3 - 0.7j, 0.2 + 0.4j, 0.0)}[which]
+    m = gpu_ctx.upload_mesh(box_small.vertices, box_small.faces)
+    try:
+        A = m.assemble_lhs(k, coeffs=coeffs, precision=native.BEM_PRECISION_MIXED)
+    finally:
+        m.release()
+    ops = O.assemble(box_small, k)
+    ref = coeffs[0] * ops.double_layer + coeffs[1] * ops.hypersingular
+    assert rel(A, ref) < 2e-6
+
+
 def test_bm_lhs_mixed_matches_oracle(gpu_ctx, native, box_small):
     O = _oracle()
     freq = 6000.0
