@@ -39,6 +39,8 @@ METRIC = "frequency solves/s @10k tris (mixed vs FP64, ≤1e-5 err); p50/p99 lat
 UNIT = "frequency-solves/s"
 SOUND_SPEED = 343.0
 RHO = 1.205
+# regular_f32_kernel DRAM bytes per frequency on box10k (ncu, profiles/regular_f32_kernel_box10k.md)
+REGULAR_DRAM_BYTES_PER_FREQ = 1.3804e9  # (70.4 MB read + 2,690.4 MB written) / 2 frequencies
 
 
 def pkg(name: str):
@@ -358,8 +360,12 @@ def main() -> None:
     # dominant kernel roofline: regular-pair assembly, FP32 pipe (mixed form)
     st0 = stats_list[0]
     regular_qpairs = st0["regular_pairs"] * 36
-    flops_per_qpair = 101  # counted from the regular_f32_kernel source (FMA = 2 flop)
-    reg_s = kernel_s["regular"] / (args.steps * B)
+    # per q-pair and frequency, counted from the regular_f32_kernel source (FMA = 2 flop):
+    # half of the q-pair geometry shared by the launch's two frequencies (23 flop), the
+    # phase and weight (7), e^{ikr} E'' and the basis sums (22), and per test point the
+    # W and S0 updates and its geometry (8.6, per q-pair)
+    flops_per_qpair = 49
+    reg_s = kernel_s["regular"] / (args.steps * B)  # seconds per frequency
     achieved = regular_qpairs * flops_per_qpair / reg_s / 1e12 if reg_s > 0 else None
     clock = result["clocks"]["sm_mhz"] or 1920.0
     fp32_peak = 152 * 128 * 2 * clock * 1e6 / 1e12
@@ -370,13 +376,14 @@ def main() -> None:
         "peak": fp32_peak,
         "unit": "TFLOP/s",
         "frac": (achieved / fp32_peak) if achieved else None,
-        # DRAM bytes per launch from one ncu capture of this kernel at this workload
-        # (dram__bytes_read.sum + dram__bytes_write.sum, current source); the
-        # algorithmic bytes are the extended-row output, 3 x N_f x ldR x 8 B = 1.360e9
-        "traffic": 1.3146e9 if args.workload == "box10k" and args.faces in (None, 10000) else None,
+        # DRAM bytes per frequency (half of one two-frequency launch) from one ncu capture
+        # of this kernel at this workload (dram__bytes_read.sum + dram__bytes_write.sum,
+        # current source); the algorithmic bytes are the extended-row output,
+        # 3 x N_f x ldR x 8 B = 1.360e9 per frequency
+        "traffic": REGULAR_DRAM_BYTES_PER_FREQ if args.workload == "box10k" and args.faces in (None, 10000) else None,
         "peak_source": "152 SMs x 128 FP32 lanes x 2 flop x median SM clock sampled during the run "
                        "(MEASURED_PEAKS.json has no FP32 figure)",
-        "work_per_launch": f"{regular_qpairs:.4g} q-pairs x {flops_per_qpair} flop",
+        "work_per_frequency": f"{regular_qpairs:.4g} q-pairs x {flops_per_qpair} flop",
     }
 
     if fp64_workload:
