@@ -200,6 +200,56 @@ __global__ void prep_b_kernel(const float2* __restrict__ A, long long lda, long 
   blo[o] = v - hi;
 }
 
+// Both operand splits of one update in one launch.  Blocks [0, nta) split A:
+// each takes 32 rows x 8 columns of L21 (complex), loaded along the rows
+// (coalesced, through shared memory) and written as the 64 x 16 real-embedded
+// hi / lo tile with the K index fastest (float4 stores).  The remaining blocks
+// split B, 128 complex entries each (K fastest on both sides).  Entries beyond
+// M rows / N columns / K depth are written as zero.
+__global__ void __launch_bounds__(256) prep_ab_kernel(const float2* __restrict__ A, long long lda, long long strideA,
+                                                      int row0, int col0, int kcol0, int M, int N, int K, int rows_pad,
+                                                      int cols_pad, int rows_used, int cols_used, int kp, int nta,
+                                                      float* __restrict__ ahi, float* __restrict__ alo,
+                                                      float* __restrict__ bhi, float* __restrict__ blo) {
+  const int b = blockIdx.y;
+  const float2* Ab = A + (size_t)b * strideA;
+  const int t = threadIdx.x;
+  if ((int)blockIdx.x < nta) {
+    __shared__ float2 tile[8][33];
+    const int tiles_k = kp / 16;
+    const int ti = blockIdx.x / tiles_k, tk = blockIdx.x - ti * tiles_k;
+    const int i0 = ti * 32, k0 = tk * 8;
+    {
+      const int i = t & 31, k = t >> 5;
+      float2 a = make_float2(0.f, 0.f);
+      if (i0 + i < M && k0 + k < K) a = Ab[(size_t)(kcol0 + k0 + k) * lda + row0 + i0 + i];
+      tile[k][i] = a;
+    }
+    __syncthreads();
+    const int rr = t >> 2, q = t & 3;  // embedded row 2 i + e, k pair (2q, 2q + 1)
+    const int i = rr >> 1, e = rr & 1;
+    const float2 a0 = tile[2 * q][i], a1 = tile[2 * q + 1][i];
+    // row 2i: (re, -im) per k; row 2i + 1: (im, re)
+    const float4 v = e == 0 ? make_float4(a0.x, -a0.y, a1.x, -a1.y) : make_float4(a0.y, a0.x, a1.y, a1.x);
+    const float4 hi = make_float4(round_tf32(v.x), round_tf32(v.y), round_tf32(v.z), round_tf32(v.w));
+    const float4 lo = make_float4(v.x - hi.x, v.y - hi.y, v.z - hi.z, v.w - hi.w);
+    const size_t o = ((size_t)b * rows_pad + 2 * i0 + rr) * KP_MAX + 2 * k0 + 4 * q;
+    *reinterpret_cast<float4*>(ahi + o) = hi;
+    *reinterpret_cast<float4*>(alo + o) = lo;
+    return;
+  }
+  const long long idx = (long long)(blockIdx.x - nta) * blockDim.x + t;  // (column j, complex k)
+  const int kc = kp / 2;
+  if (idx >= (long long)cols_used * kc) return;
+  const int j = (int)(idx / kc), k = (int)(idx - (long long)j * kc);
+  float2 u = make_float2(0.f, 0.f);
+  if (j < N && k < K) u = Ab[(size_t)(col0 + j) * lda + kcol0 + k];
+  const float2 hi = make_float2(round_tf32(u.x), round_tf32(u.y));
+  const size_t o = ((size_t)b * cols_pad + j) * KP_MAX + 2 * k;
+  *reinterpret_cast<float2*>(bhi + o) = hi;
+  *reinterpret_cast<float2*>(blo + o) = make_float2(u.x - hi.x, u.y - hi.y);
+}
+
 __global__ void __launch_bounds__(128, 2)
     trailing_update_tf32x3(const __grid_constant__ CUtensorMap map_ahi, const __grid_constant__ CUtensorMap map_alo,
                            const __grid_constant__ CUtensorMap map_bhi, const __grid_constant__ CUtensorMap map_blo,
@@ -425,16 +475,11 @@ cudaError_t tc_update(TcGemmPlan* p, float2* A, long long lda, long long strideA
   if (rows_used > p->rows_pad || cols_used > p->cols_pad) return cudaErrorInvalidValue;
   const int kp = (2 * K + TK - 1) / TK * TK;
   {
-    const long long total = (long long)rows_used * kp;
-    dim3 g((unsigned)((total + 255) / 256), p->batch);
-    prep_a_kernel<<<g, 256, 0, stream>>>(A, lda, strideA, row0, kcol0, M, K, p->rows_pad, rows_used, kp, p->ahi,
-                                         p->alo);
-  }
-  {
-    const long long total = (long long)cols_used * kp;
-    dim3 g((unsigned)((total + 255) / 256), p->batch);
-    prep_b_kernel<<<g, 256, 0, stream>>>(A, lda, strideA, kcol0, col0, N, K, p->cols_pad, cols_used, kp, p->bhi,
-                                         p->blo);
+    const int nta = (rows_used / 64) * (kp / 16);  // A tiles: 64 embedded rows x 16
+    const long long nb_b = ((long long)cols_used * (kp / 2) + 255) / 256;
+    dim3 g((unsigned)(nta + nb_b), p->batch);
+    prep_ab_kernel<<<g, 256, 0, stream>>>(A, lda, strideA, row0, col0, kcol0, M, N, K, p->rows_pad, p->cols_pad,
+                                          rows_used, cols_used, kp, nta, p->ahi, p->alo, p->bhi, p->blo);
   }
   const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024;
   if (!ensure_smem_limit((const void*)trailing_update_tf32x3, smem)) return cudaErrorInvalidValue;

@@ -553,7 +553,7 @@ cudaError_t lu_two_level(const LuJob& j, int NB) {
 }  // namespace
 
 int lu_launch_count(int n, int nb, int NB, bool tensor) {
-  const int per_update = tensor ? 3 : 0;  // operand split x2 + tcgen05 kernel (cuBLAS kernels are not counted)
+  const int per_update = tensor ? 2 : 0;  // operand split + tcgen05 kernel (cuBLAS kernels are not counted)
   int count = 0;
   for (int k0 = 0; k0 < n; k0 += NB) {
     const int KB = std::min(NB, n - k0);
@@ -608,7 +608,7 @@ cudaError_t lu_factor_batched(Precision prec, void* A, long long lda, int n, int
   if (n_launches) *n_launches = 0;
   for (int k = 0; k < n; k += nb) {
     const int kb = std::min(nb, n - k);
-    if (n_launches) *n_launches += 2 + (n - k - kb > 0 ? 1 + (plan ? 3 : 0) : 0);
+    if (n_launches) *n_launches += 2 + (n - k - kb > 0 ? 1 + (plan ? 2 : 0) : 0);
     if (cluster_panel) {
       cudaError_t e = lu_panel_cluster(prec, A, lda, strideA, n, k, kb, nb, ccl, batch, ipiv, info, stream, rowmap);
       if (e != cudaSuccess) return e;
