@@ -233,7 +233,9 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--batch", type=int, default=0,
+                    help="frequencies per step; 0: the library's largest batch (bem_auto_batch: the LU's "
+                         "cluster panels resident in one wave)")
     ap.add_argument("--workload", default="box10k", choices=sorted(WORKLOADS),
                     help="synthetic workload (box10k: the headline mixed-form configuration)")
     ap.add_argument("--faces", type=int, default=None, help="re-mesh the box workloads to about this many triangles")
@@ -272,16 +274,16 @@ def main() -> None:
     if args.form:
         spec = {**spec, "form": args.form}
     fp64_workload = spec["form"] == "fp64"
-    B = min(args.batch, len(freqs))
     ctx = native.Context(local_rank)
     m = ctx.upload_mesh(mesh.vertices, mesh.faces)
     m.set_excitation(drive)
     m.set_observation_points(points)
+    form = native.BEM_PRECISION_FP64 if fp64_workload else native.BEM_PRECISION_MIXED
+    B = min(args.batch if args.batch > 0 else m.auto_batch(0, form), len(freqs))
     stream = torch.cuda.ExternalStream(ctx.stream_handle, device=f"cuda:{local_rank}")
     p_dev = torch.empty((B, 1, mesh.n_vertices), dtype=torch.complex128, device="cuda")
     u_dev = torch.empty((B, 1, len(points)), dtype=torch.complex128, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    form = native.BEM_PRECISION_FP64 if fp64_workload else native.BEM_PRECISION_MIXED
     opts = dict(precision=form, sound_speed=SOUND_SPEED, rho=RHO, batch=B, refine_tol=1e-10,
                 max_refine=8, lu_gemm=args.lu_gemm, lu_block=args.lu_block)
 

@@ -547,6 +547,32 @@ void bem_default_options(bem_solve_options* opt) {
   opt->lu_gemm = 0;
 }
 
+}  // extern "C"
+
+namespace {
+// Automatic batch: the matrices of a batch within ~16 GiB, at most 32, and at
+// most as many as the LU's cluster panels keep resident at once (a larger batch
+// runs every panel in two waves); the sweep is then split into equal batches.
+int auto_batch(const bem_mesh* m, bem::Precision prec, int n_freq) {
+  const Layout L = layout_for(m->dm, prec);
+  const double per = (double)L.lda * m->dm.nv * L.esz * (prec == bem::Precision::Mixed ? 2 : 1);
+  int cap = (int)std::max(1.0, std::min(32.0, std::floor(16.0 * (1ull << 30) / per)));
+  cap = std::max(1, std::min(cap, bem::lu_resident_batch(prec, m->dm.nv)));
+  if (n_freq <= 0) return cap;  // the largest batch
+  const int nbatch = (n_freq + cap - 1) / cap;
+  return (n_freq + nbatch - 1) / nbatch;
+}
+}  // namespace
+
+extern "C" {
+
+int bem_auto_batch(bem_mesh* m, int precision, int n_freq) {
+  if (!m) return 0;
+  return guarded(m->ctx, [&]() -> int {
+    return auto_batch(m, precision == BEM_PRECISION_FP64 ? bem::Precision::FP64 : bem::Precision::Mixed, n_freq);
+  });
+}
+
 long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int npts, int batch, int precision) {
   const long long esz = precision == BEM_PRECISION_MIXED ? 8 : 16;
   const long long lda = round_up(nv, 32);
@@ -587,12 +613,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
     const bem::DeviceMesh& dm = m->dm;
     const int nv = dm.nv, nc = m->nc;
     Layout L = layout_for(dm, prec);
-    int B = o.batch > 0 ? std::min(o.batch, 64) : 0;
-    if (B == 0) {
-      // automatic: matrices of one batch within ~8 GiB, at most 16 frequencies
-      const double per = (double)L.lda * nv * L.esz * (mixed ? 2 : 1);
-      B = (int)std::max(1.0, std::min(32.0, std::floor(16.0 * (1ull << 30) / per)));
-    }
+    int B = o.batch > 0 ? std::min(o.batch, 64) : auto_batch(m, prec, n_freq);
     B = std::min(B, n_freq);
     const int nb = o.lu_block > 0 ? std::min(o.lu_block, 64) : 0;  // 0: the LU chooses
     const size_t matsz = (size_t)L.lda * nv * L.esz;

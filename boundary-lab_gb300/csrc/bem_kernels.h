@@ -131,6 +131,7 @@ cudaError_t norms_batched(const double2* r, const double2* b, long long ldb, int
 // width (64 or 32) and cluster size for an n x n matrix; false when no cluster
 // configuration fits (then the single-CTA panel is used).
 bool lu_cluster_plan(Precision prec, int n, int want_nb, int batch, int* nb, int* cl);
+int lu_resident_batch(Precision prec, int n);
 // rowmap: if not null, receives per matrix [count, (dst row, src row) x count]:
 // the net effect of the panel's kb interchanges on any column (at most 2 kb rows).
 cudaError_t lu_panel_cluster(Precision prec, void* A, long long lda, long long strideA, int n, int k, int kb, int nb,

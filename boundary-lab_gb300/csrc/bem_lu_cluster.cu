@@ -309,6 +309,186 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_cluster_kernel(typenam
   cluster.sync();  // no CTA leaves while others may still read its shared memory
 }
 
+// Register-resident panel (mixed form, 32 columns): one thread per panel row.
+// The thread keeps the part of its row right of the current column in
+// registers, shifted so that the current column is always a[0] (every register
+// index is a constant, and the step loop stays rolled); the multipliers it
+// produces go to shared memory (Lb[column][thread]).  Interchanges are virtual:
+// each thread carries the logical row index lg of its physical row, the pivot
+// search compares logical indices (LAPACK's first maximum of |re| + |im|), and
+// every row is written once, at the end, to its logical position.  A step:
+//  1. this CTA's candidate row (the smallest lg among the largest) is copied
+//     into slot j & 1, and the row with lg = j into the row-j slot; the
+//     candidate (value, lg) and a row-j flag are pushed into every CTA;
+//  2. cluster barrier;
+//  3. every warp takes the pivot; warp 0 fetches the pivot row from its CTA
+//     (the pivot's U row j: columns j.. as u[0..]); rank 0 stores it; CTA barrier;
+//  4. the pivot row leaves (lg = j), the row with lg = j takes the pivot's old
+//     lg; every other active row stores l = a[0] / pivot, subtracts l u and
+//     shifts; the next candidate is reduced per warp; CTA barrier.
+// Requires a full panel (kb = 32) and chunk <= kRegPanelThreads.
+constexpr int kRegPanelThreads = 640;
+constexpr int kRegPanelWarps = kRegPanelThreads / 32;
+
+// first maximum over (value, logical row), also returning the lane that held it
+__device__ __forceinline__ void warp_argmax_at(float& b, int& x, int& at) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ov = __shfl_xor_sync(0xffffffffu, b, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, x, o), oa = __shfl_xor_sync(0xffffffffu, at, o);
+    if (ov > b || (ov == b && oi < x)) {
+      b = ov;
+      x = oi;
+      at = oa;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float2* A, long long lda, long long strideA,
+                                                                           int n, int k, int kb, int chunk, int* ipiv,
+                                                                           int* info, int* rowmap) {
+  constexpr int NB = 32;
+  constexpr int NW = kRegPanelWarps;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int CL = (int)cluster.num_blocks();
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* Lb = reinterpret_cast<float2*>(smem_raw);  // [NB][kRegPanelThreads] multipliers by column, thread
+  __shared__ float2 pub[2][NB], dg[2][NB], urow[NB + 1];
+  __shared__ float cval[2][16];
+  __shared__ int cidx[2][16], chasj[2][16];
+  __shared__ float wval[NW];
+  __shared__ int widx[NW], wlane[NW];
+  __shared__ int s_pivs[NB];
+  float2* M = A + (size_t)blockIdx.y * strideA;
+  int* piv = ipiv + (size_t)blockIdx.y * n;
+  const int m = n - k;
+  const int r0 = rank * chunk;
+  const int rows = max(0, min(chunk, m - r0));
+  const bool mine = tid < rows;
+  int lg = r0 + tid;         // logical row of this thread's physical row
+  int done_at = -1;          // step at which this row became the pivot row
+  float2 a[NB];
+  {
+    const float2* src = M + (size_t)k * lda + k + r0 + tid;
+#pragma unroll
+    for (int c = 0; c < NB; ++c) a[c] = mine ? src[(size_t)c * lda] : make_float2(0.f, 0.f);
+  }
+  if (tid == 0) urow[NB] = make_float2(0.f, 0.f);  // zero beyond the panel for the shifted update
+  auto candidate = [&](float& best, int& bi, int& bt) {  // this thread's candidate for the current column
+    best = -1.0f;
+    bi = INT_MAX;
+    bt = tid;
+    if (mine && done_at < 0) argmax_merge(best, bi, abs1(a[0]), lg);
+    warp_argmax_at(best, bi, bt);
+  };
+  {
+    float best;
+    int bi, bt;
+    candidate(best, bi, bt);
+    if (lane == 0) {
+      wval[wid] = best;
+      widx[wid] = bi;
+      wlane[wid] = bt;
+    }
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int j = 0; j < NB; ++j) {
+    const int s = j & 1;
+    {  // 1. publish and push
+      float bv = lane < NW ? wval[lane] : -1.0f;
+      int bi = lane < NW ? widx[lane] : INT_MAX;
+      int bt = lane < NW ? wlane[lane] : 0;
+      warp_argmax_at(bv, bi, bt);
+      if (bi != INT_MAX && tid == bt) {
+#pragma unroll
+        for (int c = 0; c < NB; ++c) pub[s][c] = a[c];
+      }
+      const bool hasj = mine && done_at < 0 && lg == j;
+      if (hasj) {
+#pragma unroll
+        for (int c = 0; c < NB; ++c) dg[s][c] = a[c];
+      }
+      const int cnt = __syncthreads_or(hasj);
+      if (tid < CL) {
+        *cluster.map_shared_rank(&cval[s][rank], tid) = bi != INT_MAX ? bv : -1.0f;
+        *cluster.map_shared_rank(&cidx[s][rank], tid) = bi;
+        *cluster.map_shared_rank(&chasj[s][rank], tid) = cnt;
+      }
+    }
+    cluster.sync();  // 2.
+    // 3. pivot (logical row p, held by CTA pr), in every warp
+    float b = lane < CL ? cval[s][lane] : -1.0f;
+    int x = lane < CL ? cidx[s][lane] : INT_MAX;
+    int pr = lane;
+    warp_argmax_at(b, x, pr);
+    const bool fallback = x == INT_MAX;  // no comparable candidate (all NaN): keep row j
+    const int p = fallback ? j : x;
+    if (wid == 0) {
+      int jr = 0;  // CTA holding logical row j
+      const unsigned hb = __ballot_sync(0xffffffffu, lane < CL && chasj[s][lane] != 0);
+      if (hb) jr = __ffs(hb) - 1;
+      const float2* su = fallback ? cluster.map_shared_rank(&dg[s][0], jr) : cluster.map_shared_rank(&pub[s][0], pr);
+      const float2 u = lane < NB - j ? su[lane] : make_float2(0.f, 0.f);  // U(j, j + lane)
+      urow[lane] = u;
+      if (rank == 0 && lane < NB - j) M[(size_t)(k + j + lane) * lda + k + j] = u;  // row j of U, columns j..31
+    }
+    if (rank == 0 && tid == 0) {
+      piv[k + j] = k + p;
+      s_pivs[j] = p;
+    }
+    __syncthreads();
+    const float2 d = urow[0];
+    float2 inv;
+    if (d.x == 0.f && d.y == 0.f) {
+      inv = make_float2(0.f, 0.f);
+      if (rank == 0 && tid == 0 && info[blockIdx.y] == 0) info[blockIdx.y] = k + j + 1;
+    } else {
+      inv = inverse(d);
+    }
+    // 4. this thread's row
+    if (mine && done_at < 0) {
+      if (lg == p) {  // the pivot row: it is logical row j now, finished
+        lg = j;
+        done_at = j;
+      } else {
+        if (lg == j) lg = p;  // the old row j moves to the pivot's place
+        const float2 l = cmul(a[0], inv);
+        Lb[(size_t)j * kRegPanelThreads + tid] = l;
+#pragma unroll
+        for (int c = 1; c < NB; ++c) {
+          const float2 u = urow[c];
+          a[c - 1].x = fmaf(-l.x, u.x, fmaf(l.y, u.y, a[c].x));
+          a[c - 1].y = fmaf(-l.x, u.y, fmaf(-l.y, u.x, a[c].y));
+        }
+        a[NB - 1] = make_float2(0.f, 0.f);
+      }
+    }
+    {
+      float best;
+      int bi, bt;
+      candidate(best, bi, bt);
+      if (lane == 0) {  // every thread read wval / widx in this step's push, before the cluster barrier
+        wval[wid] = best;
+        widx[wid] = bi;
+        wlane[wid] = bt;
+      }
+    }
+    __syncthreads();
+  }
+  // every row to its logical position: the multipliers left of its pivot column
+  // (all 32 for rows that never became the pivot)
+  if (mine) {
+    const int ncol = done_at < 0 ? NB : done_at;
+    float2* dst = M + (size_t)k * lda + k + lg;
+    for (int c = 0; c < ncol; ++c) dst[(size_t)c * lda] = Lb[(size_t)c * kRegPanelThreads + tid];
+  }
+  if (rank == 0 && wid == 0 && rowmap != nullptr) net_row_map<NB>(s_pivs, NB, k, rowmap + (size_t)blockIdx.y * kRowmapStride);
+  cluster.sync();  // no CTA leaves while others may still read its shared memory
+}
+
 // perm[i] such that (P b)[i] = b[perm[i]], from LAPACK-style interchanges.
 __global__ void lu_perm_kernel(const int* __restrict__ ipiv, int n, int* __restrict__ perm) {
   extern __shared__ int sp[];
@@ -545,6 +725,26 @@ template <typename K> int active_clusters(K kern, int threads, size_t smem, int 
 template <typename R> bool choose_panel(int n, int want_nb, int batch, int& nb, int& cl) {
   bool found = false;
   int best_waves = 0;
+  if (sizeof(R) == 4 && (want_nb == 0 || want_nb == 32)) {
+    // the register-resident panel (32 wide) where a cluster of at most 16 CTAs
+    // holds the rows at one per thread: the fewest waves, then the smallest cluster
+    for (int c : {1, 2, 4, 8, 16}) {
+      if ((n + c - 1) / c > kRegPanelThreads) continue;
+      const size_t sm = (size_t)32 * kRegPanelThreads * sizeof(float2);
+      if (c > 1 && max_cluster(lu_panel_reg_kernel, kRegPanelThreads, sm) < c) continue;
+      if (c == 1 && !ensure_smem_limit((const void*)lu_panel_reg_kernel, sm)) continue;
+      const int act = active_clusters(lu_panel_reg_kernel, kRegPanelThreads, sm, c);
+      if (act < 1) continue;
+      const int waves = (std::max(batch, 1) + act - 1) / act;
+      if (!found || waves < best_waves) {
+        found = true;
+        best_waves = waves;
+        nb = 32;
+        cl = c;
+      }
+    }
+    if (found) return true;
+  }
   for (int w : {64, 32}) {
     if (want_nb > 0 && w != want_nb) continue;
     for (int c : {4, 8, 16}) {
@@ -594,12 +794,37 @@ bool lu_cluster_plan(Precision prec, int n, int want_nb, int batch, int* nb, int
   return last_ok[pi];
 }
 
+// Matrices whose cluster panels are resident at once (one wave) for an n x n
+// factorisation with the panel plan of a large batch: a batch beyond this
+// runs every panel in two waves.
+int lu_resident_batch(Precision prec, int n) {
+  int nb = 0, cl = 0;
+  if (!lu_cluster_plan(prec, n, 0, 64, &nb, &cl)) return 64;
+  const int chunk = (n + cl - 1) / cl;
+  int act = 0;
+  if (prec == Precision::Mixed && nb == 32 && chunk <= kRegPanelThreads)
+    act = active_clusters(lu_panel_reg_kernel, kRegPanelThreads, (size_t)32 * kRegPanelThreads * sizeof(float2), cl);
+  else if (prec == Precision::Mixed)
+    act = nb == 64 ? active_clusters(lu_panel_cluster_kernel<float, 64>, kPanelThreads, panel_smem<float, 64>(chunk), cl)
+                   : active_clusters(lu_panel_cluster_kernel<float, 32>, kPanelThreads, panel_smem<float, 32>(chunk), cl);
+  else
+    act = nb == 64 ? active_clusters(lu_panel_cluster_kernel<double, 64>, kPanelThreads, panel_smem<double, 64>(chunk), cl)
+                   : active_clusters(lu_panel_cluster_kernel<double, 32>, kPanelThreads, panel_smem<double, 32>(chunk), cl);
+  return std::max(1, act);
+}
+
 cudaError_t lu_panel_cluster(Precision prec, void* A, long long lda, long long strideA, int n, int k, int kb, int nb,
                              int cl, int batch, int* ipiv, int* info, cudaStream_t stream, int* rowmap) {
   const int m = n - k;
   const int chunk = (m + cl - 1) / cl;
   void* args[] = {&A, &lda, &strideA, &n, &k, &kb, (void*)&chunk, &ipiv, &info, &rowmap};
   dim3 grid(cl, batch);
+  if (prec == Precision::Mixed && nb == 32 && chunk <= kRegPanelThreads && kb == 32) {
+    const size_t sm = (size_t)32 * kRegPanelThreads * sizeof(float2);
+    ensure_smem_limit((const void*)lu_panel_reg_kernel, sm);
+    cudaFuncSetAttribute(lu_panel_reg_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return launch_cluster(lu_panel_reg_kernel, grid, kRegPanelThreads, sm, cl, stream, args);
+  }
   if (prec == Precision::Mixed) {
     if (nb == 64) {
       const size_t sm = panel_smem<float, 64>(chunk);

@@ -45,6 +45,7 @@ EXPORTED_SYMBOLS = (
     "bem_assemble_lhs",
     "bem_apply_rhs_operator",
     "bem_estimate_device_bytes",
+    "bem_auto_batch",
     "bem_evaluate_field_noalloc",
     "bem_lu_factor_dense",
     "bem_trim_context",
@@ -178,6 +179,8 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         lib.bem_lu_factor_dense.restype = ip
         lib.bem_estimate_device_bytes.argtypes = [ip, ip, ip, ip, ip, ip, ip]
         lib.bem_estimate_device_bytes.restype = ctypes.c_longlong
+        lib.bem_auto_batch.argtypes = [vp, ip, ip]
+        lib.bem_auto_batch.restype = ip
         lib.bem_trim_context.argtypes = [vp]
         lib.bem_trim_context.restype = ip
         lib.bem_context_scratch_bytes.argtypes = [vp]
@@ -288,6 +291,14 @@ class Mesh:
         if self._h is not None and self.ctx._h is not None:
             self.ctx._lib.bem_release_mesh(self._h)
         self._h = None
+
+    def auto_batch(self, n_freq: int, precision: int = BEM_PRECISION_MIXED) -> int:
+        """The batch the solve uses with batch=0 for a sweep of n_freq frequencies;
+        n_freq <= 0: the largest batch (the LU's cluster panels in one wave)."""
+        b = int(self.ctx._lib.bem_auto_batch(self._h, precision, int(n_freq)))
+        if b < 1:
+            raise BemError(1, self.ctx._lib.bem_last_error(self.ctx._h).decode())
+        return b
 
     def set_excitation(self, unit_drive: np.ndarray) -> None:
         d = np.asarray(unit_drive, dtype=np.complex128).reshape(-1, self.n_faces)

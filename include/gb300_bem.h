@@ -112,7 +112,7 @@ typedef struct bem_solve_options {
   double rho;            /* kg/m^3 */
   double refine_tol;     /* mixed form: stop when ||b - A x|| / ||b|| <= refine_tol (FP64 residual) */
   int max_refine;        /* mixed form: maximum refinement steps */
-  int batch;             /* frequencies factored together (<= 64); 0 = automatic */
+  int batch;             /* frequencies factored together (<= 64); 0 = automatic (bem_auto_batch) */
   int lu_block;          /* LU panel width, 32 or 64 (trailing updates are 128 deep);
                             0 = automatic (the width whose panels run in the fewest waves) */
   int outputs_on_device; /* 1: pressure_out / field_out are device pointers of the context's device */
@@ -161,6 +161,13 @@ void bem_default_options(bem_solve_options* opt);
  * stats may be NULL. */
 int bem_solve_frequencies(bem_mesh* mesh, const double* freqs_hz, int n_freq, const bem_solve_options* opt,
                           double* pressure_out, double* field_out, bem_solve_stats* stats);
+
+/* The batch bem_solve_frequencies uses for options.batch = 0 on a sweep of
+ * n_freq frequencies (returned; 0 on a bad argument): at most B_max, the sweep
+ * split into equal batches.  B_max (returned for n_freq <= 0): matrices within
+ * ~16 GiB, at most 32, and at most as many as the LU's cluster panels keep
+ * resident on this GPU at once (a larger batch runs every panel in two waves). */
+int bem_auto_batch(bem_mesh* mesh, int precision, int n_freq);
 
 /* Parity entry point: the dense P1 x P1 operator cD*D + cH*H + cM*M11 at
  * wavenumber k, written column-major [n_vertices][n_vertices] complex (row i
