@@ -23,6 +23,8 @@
 #include <cooperative_groups.h>
 #include <limits.h>
 
+#include <type_traits>
+
 #include "bem_common.cuh"
 #include "bem_kernels.h"
 
@@ -317,12 +319,14 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_cluster_kernel(typenam
 // each thread carries the logical row index lg of its physical row, the pivot
 // search compares logical indices (LAPACK's first maximum of |re| + |im|), and
 // every row is written once, at the end, to its logical position.  A step:
-//  1. this CTA's candidate row (the smallest lg among the largest) is copied
-//     into slot j & 1, and the row with lg = j into the row-j slot; the
-//     candidate (value, lg) and a row-j flag are pushed into every CTA;
-//  2. cluster barrier;
-//  3. every warp takes the pivot; warp 0 fetches the pivot row from its CTA
-//     (the pivot's U row j: columns j.. as u[0..]); rank 0 stores it; CTA barrier;
+//  1. this CTA's candidate row (the smallest lg among the largest) and the
+//     candidate (value, lg) are pushed into slot j & 1 of every CTA (DSMEM
+//     stores), and the row with lg = j is copied into the local row-j slot;
+//     the writers fence (acq_rel, cluster scope);
+//  2. cluster barrier (relaxed arrive, acquiring wait);
+//  3. every warp takes the pivot and reads the pivot row from its own shared
+//     memory (the pivot's U row j: columns j.. as u[0..]); rank 0 stores it;
+//     only if every candidate is NaN is row j fetched from its CTA instead;
 //  4. the pivot row leaves (lg = j), the row with lg = j takes the pivot's old
 //     lg; every other active row stores l = a[0] / pivot, subtracts l u and
 //     shifts; the next candidate is reduced per warp; CTA barrier.
@@ -355,7 +359,8 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* Lb = reinterpret_cast<float2*>(smem_raw);  // [NB][kRegPanelThreads] multipliers by column, thread
-  __shared__ float2 pub[2][NB], dg[2][NB], urow[NB + 1];
+  __shared__ float2 rowsC[2][16][NB];  // pushed candidate rows, by source CTA
+  __shared__ float2 pub[NB], dg[2][NB], urow[NB];
   __shared__ float cval[2][16];
   __shared__ int cidx[2][16], chasj[2][16];
   __shared__ float wval[NW];
@@ -375,7 +380,6 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
 #pragma unroll
     for (int c = 0; c < NB; ++c) a[c] = mine ? src[(size_t)c * lda] : make_float2(0.f, 0.f);
   }
-  if (tid == 0) urow[NB] = make_float2(0.f, 0.f);  // zero beyond the panel for the shifted update
   auto candidate = [&](float& best, int& bi, int& bt) {  // this thread's candidate for the current column
     best = -1.0f;
     bi = INT_MAX;
@@ -404,7 +408,7 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
       warp_argmax_at(bv, bi, bt);
       if (bi != INT_MAX && tid == bt) {
 #pragma unroll
-        for (int c = 0; c < NB; ++c) pub[s][c] = a[c];
+        for (int c = 0; c < NB; ++c) pub[c] = a[c];
       }
       const bool hasj = mine && done_at < 0 && lg == j;
       if (hasj) {
@@ -412,13 +416,22 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
         for (int c = 0; c < NB; ++c) dg[s][c] = a[c];
       }
       const int cnt = __syncthreads_or(hasj);
+      bool wrote = hasj;
+      if (bi != INT_MAX && tid < CL * NB) {  // the candidate row into every CTA
+        *cluster.map_shared_rank(&rowsC[s][rank][tid & (NB - 1)], tid / NB) = pub[tid & (NB - 1)];
+        wrote = true;
+      }
       if (tid < CL) {
         *cluster.map_shared_rank(&cval[s][rank], tid) = bi != INT_MAX ? bv : -1.0f;
         *cluster.map_shared_rank(&cidx[s][rank], tid) = bi;
         *cluster.map_shared_rank(&chasj[s][rank], tid) = cnt;
+        wrote = true;
       }
+      if (wrote) asm volatile("fence.acq_rel.cluster;" ::: "memory");
     }
-    cluster.sync();  // 2.
+    // 2. the writes above were fenced by their writers; the wait acquires them
+    asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.aligned;" ::: "memory");
     // 3. pivot (logical row p, held by CTA pr), in every warp
     float b = lane < CL ? cval[s][lane] : -1.0f;
     int x = lane < CL ? cidx[s][lane] : INT_MAX;
@@ -426,21 +439,23 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
     warp_argmax_at(b, x, pr);
     const bool fallback = x == INT_MAX;  // no comparable candidate (all NaN): keep row j
     const int p = fallback ? j : x;
-    if (wid == 0) {
-      int jr = 0;  // CTA holding logical row j
-      const unsigned hb = __ballot_sync(0xffffffffu, lane < CL && chasj[s][lane] != 0);
-      if (hb) jr = __ffs(hb) - 1;
-      const float2* su = fallback ? cluster.map_shared_rank(&dg[s][0], jr) : cluster.map_shared_rank(&pub[s][0], pr);
-      const float2 u = lane < NB - j ? su[lane] : make_float2(0.f, 0.f);  // U(j, j + lane)
-      urow[lane] = u;
-      if (rank == 0 && lane < NB - j) M[(size_t)(k + j + lane) * lda + k + j] = u;  // row j of U, columns j..31
+    const float2* U = &rowsC[s][pr][0];  // the pivot row, u[c] = U(j, j + c) (zero beyond the panel)
+    if (fallback) {  // every CTA takes this branch together
+      if (wid == 0) {
+        int jr = 0;  // CTA holding logical row j
+        const unsigned hb = __ballot_sync(0xffffffffu, lane < CL && chasj[s][lane] != 0);
+        if (hb) jr = __ffs(hb) - 1;
+        urow[lane] = *cluster.map_shared_rank(&dg[s][lane], jr);
+      }
+      __syncthreads();
+      U = urow;
     }
+    if (rank == 0 && wid == 0 && lane < NB - j) M[(size_t)(k + j + lane) * lda + k + j] = U[lane];  // U row j
     if (rank == 0 && tid == 0) {
       piv[k + j] = k + p;
       s_pivs[j] = p;
     }
-    __syncthreads();
-    const float2 d = urow[0];
+    const float2 d = U[0];
     float2 inv;
     if (d.x == 0.f && d.y == 0.f) {
       inv = make_float2(0.f, 0.f);
@@ -457,13 +472,21 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
         if (lg == j) lg = p;  // the old row j moves to the pivot's place
         const float2 l = cmul(a[0], inv);
         Lb[(size_t)j * kRegPanelThreads + tid] = l;
+        // a[c - 1] = a[c] - l u[c]: columns j + 1.. (from step 16 on, the upper half of the window is zero)
+        auto update = [&](auto width) {
+          constexpr int W = decltype(width)::value;
 #pragma unroll
-        for (int c = 1; c < NB; ++c) {
-          const float2 u = urow[c];
-          a[c - 1].x = fmaf(-l.x, u.x, fmaf(l.y, u.y, a[c].x));
-          a[c - 1].y = fmaf(-l.x, u.y, fmaf(-l.y, u.x, a[c].y));
-        }
-        a[NB - 1] = make_float2(0.f, 0.f);
+          for (int c = 1; c < W; ++c) {
+            const float2 u = U[c];
+            a[c - 1].x = fmaf(-l.x, u.x, fmaf(l.y, u.y, a[c].x));
+            a[c - 1].y = fmaf(-l.x, u.y, fmaf(-l.y, u.x, a[c].y));
+          }
+          a[W - 1] = make_float2(0.f, 0.f);
+        };
+        if (j < NB / 2)
+          update(std::integral_constant<int, NB>{});
+        else
+          update(std::integral_constant<int, NB / 2>{});
       }
     }
     {
