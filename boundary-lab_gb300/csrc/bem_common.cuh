@@ -116,9 +116,11 @@ BEM_D void sincos_ftz(float x, float* s, float* c) {
 }
 // Nearest integer of |x| < 2^22 on the FMA pipe: adding 1.5 * 2^23 rounds away
 // every fraction bit (round to nearest even); subtracting it back is exact.
+// __fadd_rn / __fsub_rn are never contracted with a multiply that produced x, so
+// the result is that of the rounded x in every inlined context.
 BEM_D float round_nearest_small(float x) {
   const float kMagic = 12582912.0f;
-  return (x + kMagic) - kMagic;
+  return __fsub_rn(__fadd_rn(x, kMagic), kMagic);
 }
 
 // sin x and cos x with RELATIVE accuracy for small |x| (sin(z/2) feeds
