@@ -184,6 +184,27 @@ def test_batch_equals_single(gpu_ctx, native, sphere320):
         m.release()
 
 
+def test_auto_batch(gpu_ctx, native, sphere320):
+    """bem_auto_batch: the largest batch is within [1, 32]; a sweep is split into equal
+    batches of at most that; batch = 0 solves exactly like the batch it reports."""
+    drives = (sphere320.tags == meshes.RADIATOR_TAG).astype(np.complex128)[None, :]
+    m = gpu_ctx.upload_mesh(sphere320.vertices, sphere320.faces)
+    try:
+        m.set_excitation(drives)
+        m.set_observation_points(np.array([[0, 0, 2.0]]))
+        bmax = m.auto_batch(0)
+        assert 1 <= bmax <= 32
+        for n in (1, 7, 40, 64):
+            nb = -(-n // bmax)
+            assert m.auto_batch(n) == -(-n // nb)
+        freqs = np.linspace(300.0, 3000.0, 7)
+        pa, ua, _ = m.solve(freqs, batch=0)
+        pe, ue, _ = m.solve(freqs, batch=m.auto_batch(len(freqs)))
+        assert rel(pa, pe) == 0.0 and rel(ua, ue) == 0.0
+    finally:
+        m.release()
+
+
 def test_isolated_vertex_gets_zero_pressure(gpu_ctx, native, sphere320):
     v = np.vstack([sphere320.vertices, [[5.0, 5.0, 5.0]]])
     mesh = meshes.BoundaryMesh(v, sphere320.faces, sphere320.tags)
