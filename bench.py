@@ -474,6 +474,9 @@ def main() -> None:
         # serving stream: seeded Poisson arrivals of mixed-size jobs, latency per job
         if args.serving_jobs > 0 and args.workload == "box10k":
             result["serving"] = serving_run(args, local_rank)
+        # retained-trace field (the bem_field operation): one request per call, host traces
+        if args.workload == "box10k":
+            result["retained_field"] = retained_field_run(mesh, local_rank)
     # gpu_launches: this library's kernels launched in the timed region, counted by
     # the library itself per call (bem_solve_stats.kernel_launches)
     result["gpu_launches"] = int(sum(st["kernel_launches"] for st in stats_list))
@@ -483,6 +486,36 @@ def main() -> None:
         print(json.dumps(result))
     if dist:
         dist.destroy_process_group()
+
+
+def retained_field_run(mesh, device: int, n_points: int = 5000, calls: int = 8) -> dict:
+    """The exterior field of retained boundary traces (coupled_field.evaluate_bem_field,
+    the reference's bem_field operation) on this mesh: 5,000 Fibonacci points at 2 m,
+    seeded complex64 traces, 2,500 Hz; the first call uploads the domain (excluded)."""
+    cf = pkg("coupled_field")
+    rng = np.random.default_rng(11)
+    p = (rng.normal(size=mesh.n_vertices) + 1j * rng.normal(size=mesh.n_vertices)).astype(np.complex64)
+    q = (rng.normal(size=mesh.n_faces) + 1j * rng.normal(size=mesh.n_faces)).astype(np.complex64)
+    i = np.arange(n_points)
+    z = 1.0 - (2.0 * i + 1.0) / n_points
+    phi = i * np.pi * (3.0 - np.sqrt(5.0))
+    rr = np.sqrt(1.0 - z * z)
+    pts = 2.0 * np.stack([rr * np.cos(phi), rr * np.sin(phi), z], axis=1)
+    ev = cf.FieldEvaluator(device)
+    req = cf.BemFieldEvaluationRequest("bench", pts, mesh.vertices, mesh.faces, p, q, 2500.0, SOUND_SPEED)
+    try:
+        cf.evaluate_bem_field(req, evaluator=ev)  # domain upload + warm-up
+        t0 = time.perf_counter()
+        for _ in range(calls):
+            cf.evaluate_bem_field(req, evaluator=ev)
+        dt = (time.perf_counter() - t0) / calls
+    finally:
+        ev.release()
+    pairs = n_points * mesh.n_faces * 3  # (point, source) Green evaluations, 3-point rule
+    return {"what": "coupled_field.evaluate_bem_field per request (host traces in, host field out, "
+                    "C ABI bem_evaluate_field), 3-point rule, mixed form, 2,500 Hz, 5,000 points at 2 m",
+            "ms_per_request": dt * 1e3, "points": n_points, "faces": int(mesh.n_faces),
+            "green_evaluations_per_s": pairs / dt}
 
 
 def serving_run(args, device: int) -> dict:

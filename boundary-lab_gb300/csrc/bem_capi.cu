@@ -84,9 +84,10 @@ struct bem_context {
   std::string err;
   cudaMemPool_t pool = nullptr;
   DevBuf rext, mats, mats2, ipiv, perm, info, sblocks, rb, b32, b64, x64, r64, d32, fsrc, fout, norms, pout, tcws, rowmap;
+  DevBuf ftrace_p, ftrace_q, fpoints;  // bem_evaluate_field: boundary traces and points
   std::vector<DevBuf*> scratch() {
     return {&rext, &mats, &mats2, &ipiv, &perm, &info, &sblocks, &rb, &b32, &b64, &x64, &r64, &d32, &fsrc, &fout, &norms,
-            &pout, &tcws, &rowmap};
+            &pout, &tcws, &rowmap, &ftrace_p, &ftrace_q, &fpoints};
   }
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<bem_mesh*> meshes;
@@ -529,6 +530,63 @@ int bem_set_observation_points(bem_mesh* m, const double* points, int n_points) 
        "copy points");
     ck(cudaStreamSynchronize(ctx->stream), "copy points");
     m->nobs = n_points;
+    return BEM_OK;
+  });
+}
+
+int bem_evaluate_field(bem_mesh* m, double k, int precision, const double* pressure, const double* neumann,
+                       const double* points, int n_points, double* field_out) {
+  if (!m) return BEM_ERR_INVALID_ARGUMENT;
+  bem_context* ctx = m->ctx;
+  return guarded(ctx, [&]() -> int {
+    if (!pressure || !neumann || !points || !field_out || n_points < 1)
+      return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (!(k > 0) || !std::isfinite(k)) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "wavenumber must be finite and > 0");
+    if (precision != BEM_PRECISION_FP64 && precision != BEM_PRECISION_MIXED)
+      return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "unknown precision");
+    const bem::DeviceMesh& dm = m->dm;
+    const int nv = dm.nv, nf = dm.nf;
+    for (long long i = 0; i < 3LL * n_points; ++i)
+      if (!std::isfinite(points[i])) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "points must be finite");
+    for (long long i = 0; i < 2LL * nv; ++i)
+      if (!std::isfinite(pressure[i])) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "boundary pressure must be finite");
+    for (long long i = 0; i < 2LL * nf; ++i)
+      if (!std::isfinite(neumann[i])) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "boundary normal derivative must be finite");
+    const bem::Precision prec = precision == BEM_PRECISION_MIXED ? bem::Precision::Mixed : bem::Precision::FP64;
+    const bool mixed = prec == bem::Precision::Mixed;
+    const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
+    const long long ldp = round_up(nv, 32);
+    // traces in the working precision: pressure [ldp] (vertex order), normal derivative [nf]
+    std::vector<char> hp((size_t)ldp * esz, 0), hq((size_t)nf * esz);
+    for (int i = 0; i < nv; ++i) {
+      if (mixed)
+        ((float2*)hp.data())[i] = make_float2((float)pressure[2 * i], (float)pressure[2 * i + 1]);
+      else
+        ((double2*)hp.data())[i] = make_double2(pressure[2 * i], pressure[2 * i + 1]);
+    }
+    for (int i = 0; i < nf; ++i) {
+      if (mixed)
+        ((float2*)hq.data())[i] = make_float2((float)neumann[2 * i], (float)neumann[2 * i + 1]);
+      else
+        ((double2*)hq.data())[i] = make_double2(neumann[2 * i], neumann[2 * i + 1]);
+    }
+    ck(ctx->ftrace_p.ensure(hp.size()), "alloc boundary pressure");
+    ck(ctx->ftrace_q.ensure(hq.size()), "alloc boundary normal derivative");
+    ck(ctx->fpoints.ensure((size_t)n_points * 3 * sizeof(double)), "alloc points");
+    const size_t srcb = (size_t)nf * dm.Q * esz;
+    ck(ctx->fsrc.ensure(round_up(srcb, 256) + 4096), "alloc field sources");
+    ck(ctx->fout.ensure((size_t)n_points * sizeof(double2)), "alloc field out");
+    ck(cudaMemcpyAsync(ctx->ftrace_p.p, hp.data(), hp.size(), cudaMemcpyHostToDevice, ctx->stream), "copy pressure");
+    ck(cudaMemcpyAsync(ctx->ftrace_q.p, hq.data(), hq.size(), cudaMemcpyHostToDevice, ctx->stream), "copy normal derivative");
+    ck(cudaMemcpyAsync(ctx->fpoints.p, points, (size_t)n_points * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream),
+       "copy points");
+    const double2 one = make_double2(1.0, 0.0);
+    ck(bem::launch_field(dm, prec, 1, &k, &one, ctx->ftrace_p.p, ldp, 1, ctx->ftrace_q.p, (const double*)ctx->fpoints.p,
+                         n_points, ctx->fsrc.p, (double2*)ctx->fout.p, ctx->stream),
+       "field kernel");
+    ck(cudaMemcpyAsync(field_out, ctx->fout.p, (size_t)n_points * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream),
+       "copy field");
+    ck(cudaStreamSynchronize(ctx->stream), "field sync");
     return BEM_OK;
   });
 }

@@ -46,6 +46,7 @@ EXPORTED_SYMBOLS = (
     "bem_apply_rhs_operator",
     "bem_estimate_device_bytes",
     "bem_auto_batch",
+    "bem_evaluate_field",
     "bem_evaluate_field_noalloc",
     "bem_lu_factor_dense",
     "bem_trim_context",
@@ -181,6 +182,8 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         lib.bem_estimate_device_bytes.restype = ctypes.c_longlong
         lib.bem_auto_batch.argtypes = [vp, ip, ip]
         lib.bem_auto_batch.restype = ip
+        lib.bem_evaluate_field.argtypes = [vp, ctypes.c_double, ip, dp, dp, dp, ip, dp]
+        lib.bem_evaluate_field.restype = ip
         lib.bem_trim_context.argtypes = [vp]
         lib.bem_trim_context.restype = ip
         lib.bem_context_scratch_bytes.argtypes = [vp]
@@ -299,6 +302,19 @@ class Mesh:
         if b < 1:
             raise BemError(1, self.ctx._lib.bem_last_error(self.ctx._h).decode())
         return b
+
+    def evaluate_field(self, k: float, pressure: np.ndarray, neumann: np.ndarray, points: np.ndarray,
+                       precision: int = BEM_PRECISION_MIXED) -> np.ndarray:
+        """Exterior field u(x) of retained boundary traces (pressure per vertex, normal
+        derivative per face) at points [n][3]; returns complex128 [n]."""
+        p = np.ascontiguousarray(pressure, dtype=np.complex128).reshape(self.n_vertices)
+        q = np.ascontiguousarray(neumann, dtype=np.complex128).reshape(self.n_faces)
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(len(pts), np.complex128)
+        self.ctx._check(self.ctx._lib.bem_evaluate_field(self._h, float(k), int(precision), _dptr(_cplx_view(p)),
+                                                         _dptr(_cplx_view(q)), _dptr(pts), len(pts),
+                                                         _dptr(_cplx_view(out))))
+        return out
 
     def set_excitation(self, unit_drive: np.ndarray) -> None:
         d = np.asarray(unit_drive, dtype=np.complex128).reshape(-1, self.n_faces)

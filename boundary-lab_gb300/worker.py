@@ -6,6 +6,10 @@ Same command line and events as src/blab/solvers/julia_local/solver.jl:
                                             {"request": "<path>", "operation": "solve"}
 Events (one JSON object per stdout line): ready, initialized, status, result,
 cancelled, completed, failed (solver.jl:12-24, 703-715, 807, 957-996, 1019-1036).
+The coupled worker's `bem_field` operation (coupled_solver.jl:2516-2546) is served
+too: the field of retained boundary traces, read from the request's binary arrays,
+answered by a `field_result` event with a `values_binary` descriptor and `completed`
+(the protocol of src/blab/solvers/coupled_field.py).
 The cancel file named by the request's `cancel_path` is honoured between
 frequencies.  Because the command line matches, the reference's own adapter
 runs this worker unchanged:
@@ -65,7 +69,24 @@ def solve_request(request: dict) -> None:
     emit("completed", solved_count=len(job.frequencies))
 
 
+_field_evaluator = None
+
+
+def field_request(request: dict, request_path: str) -> None:
+    """The `bem_field` operation: the exterior field of retained boundary traces."""
+    global _field_evaluator
+    _package()
+    cf = importlib.import_module("boundary-lab_gb300.coupled_field")
+    if _field_evaluator is None:
+        _field_evaluator = cf.FieldEvaluator(device=int(os.environ.get("GB300_BEM_DEVICE", "0")))
+    scalars, arrays = cf.request_from_wire(request, Path(request_path))
+    values = _field_evaluator.evaluate(scalars, arrays)
+    emit("field_result", values_binary=cf.write_binary_result(request, Path(request_path), values))
+    emit("completed")
+
+
 def worker_loop() -> None:
+    global _field_evaluator
     emit("ready", protocol="boundary_lab_julia_worker", pid=os.getpid())
     for line in sys.stdin:
         text = line.strip()
@@ -73,9 +94,19 @@ def worker_loop() -> None:
             continue
         try:
             message = json.loads(text)
-            with open(str(message["request"]), encoding="utf-8") as fh:
+            request_path = str(message["request"])
+            with open(request_path, encoding="utf-8") as fh:
                 request = json.load(fh)
-            solve_request(request)
+            operation = str(message.get("operation", "solve"))
+            if operation == "bem_field":
+                field_request(request, request_path)
+            elif operation == "solve":
+                if _field_evaluator is not None:  # a solve releases the retained field caches
+                    _field_evaluator.release()
+                    _field_evaluator = None
+                solve_request(request)
+            else:
+                raise ValueError(f"Unsupported worker operation: {operation}")
         except Exception as exc:  # noqa: BLE001 - every failure becomes a `failed` event
             emit("failed", error=f"{type(exc).__name__}: {exc}")
 

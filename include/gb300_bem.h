@@ -186,6 +186,17 @@ int bem_assemble_lhs(bem_mesh* mesh, double k, int precision, const double* coef
 int bem_apply_rhs_operator(bem_mesh* mesh, double k, int precision, const double* coeffs, const double* q, int n_rhs,
                            double* out);
 
+/* Exterior field of retained boundary traces on an uploaded mesh: the
+ * reference's bem_field operation (evaluate_bem_field_request,
+ * coupled_solver.jl:2438-2497, evaluate_galerkin_field_*), used after a
+ * physical-system solve.  u(x) = sum over the mesh's quadrature sources of
+ * [dG/dn_y p(y) - G q] w, with the mesh's regular rule and symmetry images.
+ * pressure: [n_vertices] complex (P1); neumann: [n_faces] complex (DP0 normal
+ * derivative); points: [n_points][3]; field_out: [n_points] complex.  Host
+ * buffers; the mesh's excitation and observation points are not touched. */
+int bem_evaluate_field(bem_mesh* mesh, double k, int precision, const double* pressure, const double* neumann,
+                       const double* points, int n_points, double* field_out);
+
 /* Exterior field for callers that cannot allocate device memory (no
  * counterpart in the reference).  Some callers cannot call cudaMalloc where they
  * need a field, e.g. a real-time audio callback, a host framework that owns all
