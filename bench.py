@@ -477,6 +477,7 @@ def main() -> None:
         # retained-trace field (the bem_field operation): one request per call, host traces
         if args.workload == "box10k":
             result["retained_field"] = retained_field_run(mesh, local_rank)
+            result["job_server"] = job_server_run(local_rank)
     # gpu_launches: this library's kernels launched in the timed region, counted by
     # the library itself per call (bem_solve_stats.kernel_launches)
     result["gpu_launches"] = int(sum(st["kernel_launches"] for st in stats_list))
@@ -516,6 +517,85 @@ def retained_field_run(mesh, device: int, n_points: int = 5000, calls: int = 8) 
                     "C ABI bem_evaluate_field), 3-point rule, mixed form, 2,500 Hz, 5,000 points at 2 m",
             "ms_per_request": dt * 1e3, "points": n_points, "faces": int(mesh.n_faces),
             "green_evaluations_per_s": pairs / dt}
+
+
+def job_server_run(device: int, n_jobs: int = 6, n_freq: int = 16, faces: int = 5000) -> dict:
+    """Whole requests through the HTTP job server (job_server.py): each job uploads its
+    mesh as an asset, is parsed, planned, solved and post-processed, and a client per
+    job reads its event windows.  Run with four jobs on the GPU at once and with one
+    (the reference server's default); event latency = client receipt - event time."""
+    import base64
+    import shutil
+    import tempfile
+    import urllib.request
+
+    js = pkg("job_server")
+    meshes = pkg("meshes")
+    mesh = meshes.box_with_piston((0.3, 0.2, 0.25), faces, 0.05, "+z")
+    tmp = Path(tempfile.mkdtemp(prefix="bench-jobs-"))
+    meshes.write_gmsh22(tmp / "box.msh", mesh.vertices * 1000.0, mesh.faces, mesh.tags)
+    body = {"schema_version": 2,
+            "config": {"mesh_file": "box.msh", "scale_factor": 0.001, "rho": RHO, "sound_speed": SOUND_SPEED,
+                       "step_size": 5.0, "distance": 2.0,
+                       "radiators": [{"name": "piston", "tag": int(meshes.RADIATOR_TAG), "channel": "main"}],
+                       "channels": [{"name": "main"}], "spherical_sampling_enabled": True,
+                       "spherical_sampling_points": 500},
+            "frequencies_hz": np.geomspace(200.0, 6000.0, n_freq).tolist(),
+            "assets": [{"original_path": "box.msh", "filename": "box.msh",
+                        "content_base64": base64.b64encode((tmp / "box.msh").read_bytes()).decode()}]}
+    payload = json.dumps(body).encode()
+    out = {"what": f"{n_jobs} jobs x {n_freq} freqs (200 Hz-6 kHz) on a {mesh.n_faces}-triangle box, mesh uploaded "
+                   "as a base64 asset, 2x73 polar + 500 sphere points, mixed form; POST /jobs to the last "
+                   "completed event, events read through GET /jobs/{id}/events windows"}
+    for name, running in (("concurrent_jobs", 4), ("one_job_at_a_time", 1)):
+        orch = js.JobOrchestrator(max_running_jobs=running, max_queued_jobs=n_jobs, artifact_root=tmp / name,
+                                  solver_factory=js.gb300_solver_factory(device=device))
+        srv = js.JobHTTPServer(("127.0.0.1", 0), orch)
+        threading.Thread(target=srv.serve_forever, daemon=True).start()
+        url = f"http://127.0.0.1:{srv.server_address[1]}"
+        lat: list[float] = []
+        failures: list[str] = []
+
+        def read(job_id):
+            since = 0
+            while True:
+                with urllib.request.urlopen(f"{url}/jobs/{job_id}/events?since={since}", timeout=600) as resp:
+                    for line in resp:
+                        now = time.time()
+                        ev = json.loads(line)
+                        since = ev["index"] + 1
+                        if ev["type"] == "result":
+                            lat.append(now - ev["timestamp"])
+                        if ev["type"] in js.TERMINAL_STATES:
+                            if ev["type"] != "completed":
+                                failures.append(str(ev.get("error", ev["type"])))
+                            return
+
+        try:
+            t0 = time.perf_counter()
+            ids = []
+            for _ in range(n_jobs):
+                req = urllib.request.Request(url + "/jobs", data=payload, method="POST",
+                                             headers={"Content-Type": "application/json"})
+                with urllib.request.urlopen(req, timeout=60) as resp:
+                    ids.append(json.loads(resp.read())["job_id"])
+            readers = [threading.Thread(target=read, args=(j,)) for j in ids]
+            for t in readers:
+                t.start()
+            for t in readers:
+                t.join(900)
+            wall = time.perf_counter() - t0
+        finally:
+            srv.shutdown()
+            srv.server_close()
+            orch.shutdown()
+        lat_ms = np.asarray(lat) * 1e3
+        out[name] = {"max_running_jobs": running, "wall_s": wall, "failed": failures[:3],
+                     "frequency_solves_per_s": n_jobs * n_freq / wall,
+                     "result_event_latency_ms_p50": float(np.percentile(lat_ms, 50)) if lat else None,
+                     "result_event_latency_ms_p99": float(np.percentile(lat_ms, 99)) if lat else None}
+    shutil.rmtree(tmp, ignore_errors=True)
+    return out
 
 
 def serving_run(args, device: int) -> dict:

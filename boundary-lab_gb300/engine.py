@@ -1,8 +1,11 @@
 """Numerical engine behind a solve session.
 
-``CudaEngine`` drives the C ABI (one context per process and device, shared by
-sessions; a lock serialises calls on it, like the reference's per-worker lock,
-src/blab/solvers/beat_engine_backend.py:314-334).  Any object with the same
+``CudaEngine`` drives the C ABI.  By default it uses one context per process
+and device, shared by sessions, with a lock that serialises calls on it (like
+the reference's per-worker lock, src/blab/solvers/beat_engine_backend.py:314-334).
+With ``context="thread"`` each calling thread gets its own context (its own
+CUDA stream and scratch), so the worker threads of a job server run their jobs
+on the GPU at the same time.  Any object with the same
 three methods can stand in for it (``engine_factory`` arguments and the
 ``GB300_BEM_ENGINE=module:callable`` environment variable), which is how the
 CPU tests drive the session and worker logic without a GPU.
@@ -32,6 +35,7 @@ class EngineResult:
 _contexts: dict[int, native.Context] = {}
 _context_locks: dict[int, threading.Lock] = {}
 _pool_lock = threading.Lock()
+_per_thread = threading.local()
 
 
 def shared_context(device: int) -> tuple[native.Context, threading.Lock]:
@@ -42,19 +46,32 @@ def shared_context(device: int) -> tuple[native.Context, threading.Lock]:
         return _contexts[device], _context_locks[device]
 
 
+def thread_context(device: int) -> tuple[native.Context, threading.Lock]:
+    """The calling thread's own context on ``device`` (created on first use, kept for the thread's life)."""
+    contexts = getattr(_per_thread, "contexts", None)
+    if contexts is None:
+        contexts = _per_thread.contexts = {}
+    if device not in contexts:
+        contexts[device] = (native.Context(device), threading.Lock())
+    return contexts[device]
+
+
 class CudaEngine:
     """One uploaded mesh on one GPU."""
 
     name = "gb300_cuda"
 
-    def __init__(self, device: int = 0, precision: str = "mixed", batch: int = 0, refine_tol: float = 1e-10):
+    def __init__(self, device: int = 0, precision: str = "mixed", batch: int = 0, refine_tol: float = 1e-10,
+                 context: str = "shared"):
         if precision not in PRECISIONS:
             raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
+        if context not in ("shared", "thread"):
+            raise ValueError("context must be 'shared' or 'thread'")
         self.device = device
         self.precision = precision
         self.batch = batch
         self.refine_tol = refine_tol
-        self.ctx, self.lock = shared_context(device)
+        self.ctx, self.lock = shared_context(device) if context == "shared" else thread_context(device)
         self.mesh: native.Mesh | None = None
 
     def prepare(self, vertices, faces, drives, points, regular_order: int = 4, singular_order: int = 4,
