@@ -10,6 +10,12 @@ The coupled worker's `bem_field` operation (coupled_solver.jl:2516-2546) is serv
 too: the field of retained boundary traces, read from the request's binary arrays,
 answered by a `field_result` event with a `values_binary` descriptor and `completed`
 (the protocol of src/blab/solvers/coupled_field.py).
+A `solve` request that carries a `compiled_system` (the physical-system contract,
+src/blab/system_contract.py) runs the coupled worker's exterior BEM branch
+(coupled_solver.jl:267-569, system_exterior.py): `result` events carry
+`{"result": {schema_version, freq_hz, excitation_port_ids, quantities,
+diagnostics}}`.  As the coupled solver, the worker started without arguments
+reads one such request from stdin and prints one result object per line.
 The cancel file named by the request's `cancel_path` is honoured between
 frequencies.  Because the command line matches, the reference's own adapter
 runs this worker unchanged:
@@ -69,6 +75,36 @@ def solve_request(request: dict) -> None:
     emit("completed", solved_count=len(job.frequencies))
 
 
+def system_request(request: dict, *, event_mode: bool = True) -> None:
+    """A physical-system solve (exterior BEM branch): `result` events, then `completed` or
+    `cancelled` (coupled_solver.jl:2531-2534); plain result lines when not in event mode."""
+    _package()
+    se = importlib.import_module("boundary-lab_gb300.system_exterior")
+    job = se.ExteriorSystemJob(request, device=int(os.environ.get("GB300_BEM_DEVICE", "0")))
+    try:
+        for result in job.results():
+            if event_mode:
+                emit("result", result=result)
+            else:
+                sys.stdout.write(json.dumps(_clean(result), separators=(",", ":")) + "\n")
+                sys.stdout.flush()
+    except se.SystemJobCancelled as exc:
+        if event_mode:
+            emit("cancelled", solved_count=exc.solved_count)
+        return
+    finally:
+        job.close()
+    if event_mode:
+        emit("completed", solved_count=len(job.frequencies))
+
+
+def dispatch_solve(request: dict) -> None:
+    if "compiled_system" in request:
+        system_request(request)
+    else:
+        solve_request(request)
+
+
 _field_evaluator = None
 
 
@@ -104,7 +140,7 @@ def worker_loop() -> None:
                 if _field_evaluator is not None:  # a solve releases the retained field caches
                     _field_evaluator.release()
                     _field_evaluator = None
-                solve_request(request)
+                dispatch_solve(request)
             else:
                 raise ValueError(f"Unsupported worker operation: {operation}")
         except Exception as exc:  # noqa: BLE001 - every failure becomes a `failed` event
@@ -125,6 +161,19 @@ def main(argv: list[str]) -> int:
         else:
             emit("failed", error=f"Unknown argument: {argv[i]}")
             return 1
+    if not worker and request_path is None and not sys.stdin.isatty():
+        # the coupled solver's one-shot form: a system request on stdin, plain result lines out,
+        # errors on stderr with exit status 1 (coupled_solver.jl:2561-2575)
+        try:
+            request = json.loads(sys.stdin.read() or "null")
+            if not isinstance(request, dict) or "compiled_system" not in request:
+                emit("failed", error="Missing --request path.")
+                return 1
+            system_request(request, event_mode=False)
+            return 0
+        except Exception as exc:  # noqa: BLE001
+            sys.stderr.write(f"{type(exc).__name__}: {exc}\n")
+            return 1
     try:
         if worker:
             worker_loop()
@@ -133,7 +182,7 @@ def main(argv: list[str]) -> int:
             emit("failed", error="Missing --request path.")
             return 1
         with open(request_path, encoding="utf-8") as fh:
-            solve_request(json.load(fh))
+            dispatch_solve(json.load(fh))
         return 0
     except Exception as exc:  # noqa: BLE001
         emit("failed", error=f"{type(exc).__name__}: {exc}")
