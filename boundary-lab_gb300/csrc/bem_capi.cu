@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstring>
 #include <exception>
+#include <functional>
 #include <string>
 #include <mutex>
 #include <vector>
@@ -80,6 +81,7 @@ inline void ck(cudaError_t e, const char* what) {
 struct bem_context {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // once-per-mesh FP64 singular moments, overlapped with the first assembly
   cublasHandle_t cublas = nullptr;
   std::string err;
   cudaMemPool_t pool = nullptr;
@@ -90,6 +92,8 @@ struct bem_context {
             &pout, &tcws, &rowmap, &ftrace_p, &ftrace_q, &fpoints};
   }
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  void* stage = nullptr;  // pinned host staging of mesh uploads (grown on demand)
+  size_t stage_bytes = 0;
   std::vector<bem_mesh*> meshes;
   // optional per-kernel-family timing (options.profile)
   bool prof = false;
@@ -107,6 +111,7 @@ struct bem_mesh {
   DevBuf drive32, drive64, obs;
   int nobs = 0;
   DevBuf driven;
+  cudaEvent_t moments_ready = nullptr;  // recorded on ctx->side after the singular moments kernel
   long long singular_points = 0;
 };
 
@@ -119,12 +124,48 @@ void* mesh_alloc(bem_mesh* m, size_t bytes, const char* what) {
   return p;
 }
 
-template <typename T> T* upload(bem_mesh* m, const std::vector<T>& v) {
-  if (v.empty()) return nullptr;
-  void* p = mesh_alloc(m, v.size() * sizeof(T), "allocate mesh data");
-  ck(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, m->ctx->stream), "upload");
-  return (T*)p;
-}
+// The arrays of one mesh upload, packed at 256-byte offsets into one device
+// allocation and sent in one copy from the context's pinned staging buffer
+// (instead of one pageable copy and one allocation per array).
+struct UploadPack {
+  struct Part {
+    size_t off, bytes;
+    const void* src;
+    std::function<void(char*)> bind;
+  };
+  std::vector<Part> parts;
+  size_t total = 0;
+  template <typename T> void add(T*& dst, const std::vector<T>& v) {
+    dst = nullptr;
+    if (v.empty()) return;
+    const size_t off = (total + 255) & ~(size_t)255;
+    const size_t bytes = v.size() * sizeof(T);
+    T** d = &dst;
+    parts.push_back({off, bytes, v.data(), [d, off](char* base) { *d = (T*)(base + off); }});
+    total = off + bytes;
+  }
+  void commit(bem_mesh* m) {
+    if (total == 0) return;
+    bem_context* ctx = m->ctx;
+    if (ctx->stage_bytes < total) {
+      if (ctx->stage) {
+        ck(cudaStreamSynchronize(ctx->stream), "upload staging");
+        cudaFreeHost(ctx->stage);
+        ctx->stage = nullptr;
+        ctx->stage_bytes = 0;
+      }
+      const size_t want = total + total / 4;
+      ck(cudaHostAlloc(&ctx->stage, want, cudaHostAllocDefault), "allocate upload staging");
+      ctx->stage_bytes = want;
+    }
+    char* base = (char*)mesh_alloc(m, total, "allocate mesh data");
+    for (const Part& p : parts) {
+      std::memcpy((char*)ctx->stage + p.off, p.src, p.bytes);
+      p.bind(base);
+    }
+    ck(cudaMemcpyAsync(base, ctx->stage, total, cudaMemcpyHostToDevice, ctx->stream), "upload");
+  }
+};
 
 // Profiling marks: the time between two consecutive marks is charged to the
 // slot of the later mark.
@@ -231,14 +272,18 @@ long long assemble_frequencies(bem_mesh* m, bem::Precision prec, int cnt, const 
     const int g = std::min(G, cnt - f0);
     double2 cD[2], cH[2];
     for (int i = 0; i < g; ++i) {
-      ck(bem::launch_singular_dyn(dm, prec, k[f0 + i], c[f0 + i], sblk(i), ctx->stream), "singular kernel");
       cD[i] = c[f0 + i].cD;
       cH[i] = c[f0 + i].cH;
     }
-    prof_mark(ctx, BEM_K_SINGULAR);
+    // regular pairs first: on a freshly uploaded mesh they run while the side stream
+    // still integrates the FP64 singular moments that the singular kernel reads
     ck(bem::launch_regular(dm, prec, g, k + f0, cD, cH, rext(0), L.ldR, (long long)rext_n, ctx->stream),
        "regular kernel");
     prof_mark(ctx, BEM_K_REGULAR);
+    if (m->moments_ready) ck(cudaStreamWaitEvent(ctx->stream, m->moments_ready, 0), "wait for singular moments");
+    for (int i = 0; i < g; ++i)
+      ck(bem::launch_singular_dyn(dm, prec, k[f0 + i], c[f0 + i], sblk(i), ctx->stream), "singular kernel");
+    prof_mark(ctx, BEM_K_SINGULAR);
     for (int i = 0; i < g; ++i) {
       void* Ai = A[f0 + i];
       void* A2i = A2 ? A2[f0 + i] : nullptr;
@@ -269,6 +314,11 @@ void assemble_one(bem_mesh* m, bem::Precision prec, double k, const bem::Operato
 }
 
 void free_mesh_device(bem_mesh* m) {
+  if (m->moments_ready) {  // the side stream may still read the mesh data
+    cudaStreamWaitEvent(m->ctx->stream, m->moments_ready, 0);
+    cudaEventDestroy(m->moments_ready);
+    m->moments_ready = nullptr;
+  }
   for (void* p : m->allocs) cudaFreeAsync(p, m->ctx->stream);
   m->allocs.clear();
   m->drive32.release();
@@ -299,7 +349,13 @@ int bem_create_context(int device, bem_context** out) {
     delete ctx;
     return BEM_ERR_CUDA;
   }
+  if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return BEM_ERR_CUDA;
+  }
   if (cublasCreate(&ctx->cublas) != CUBLAS_STATUS_SUCCESS) {
+    cudaStreamDestroy(ctx->side);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return BEM_ERR_CUDA;
@@ -308,6 +364,7 @@ int bem_create_context(int device, bem_context** out) {
   ctx->pool = device_pool(device);
   if (!ctx->pool) {
     cublasDestroy(ctx->cublas);
+    cudaStreamDestroy(ctx->side);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return BEM_ERR_CUDA;
@@ -335,7 +392,12 @@ void bem_destroy_context(bem_context* ctx) {
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : ctx->pev) cudaEventDestroy(e);
+  if (ctx->stage) cudaFreeHost(ctx->stage);
   if (ctx->cublas) cublasDestroy(ctx->cublas);
+  if (ctx->side) {
+    cudaStreamSynchronize(ctx->side);
+    cudaStreamDestroy(ctx->side);
+  }
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -395,45 +457,48 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
       d.npairs = (int)P.pairs.size();
       d.ntr = (int)P.transforms.size();
       for (int i = 0; i < d.ntr && i < 4; ++i) d.tr[i] = P.transforms[i];
-      if (P.symmetry != 0) {
-        d.fix_mask = upload(m, P.fix_mask);
-        d.row_weight = upload(m, P.row_weight);
-      }
-      d.faces32 = upload(m, P.faces32);
-      d.faces64 = upload(m, P.faces64);
-      d.tile_group_ptr = upload(m, P.tile_group_ptr);
-      d.lane_slots = upload(m, P.lane_slots);
-      d.group_faces32 = upload(m, P.group_faces32);
-      d.tile_row_base = upload(m, P.tile_row_base);
-      d.ext_row = upload(m, P.ext_row);
-      d.halo_slot_of_ext = upload(m, P.halo_slot_of_ext);
-      d.halo_row_ptr = upload(m, P.halo_row_ptr);
-      d.halo_row = upload(m, P.halo_row);
-      d.col_ptr = upload(m, P.col_ptr);
-      d.col_fb = upload(m, P.col_fb);
-      d.face_ext = upload(m, P.face_ext);
-      d.vertex_row = upload(m, P.vertex_row);
       std::vector<int> iso;
       for (int v = 0; v < P.nv; ++v)
         if (P.col_ptr[v] == P.col_ptr[v + 1]) iso.push_back(v);
       d.n_isolated = (int)iso.size();
-      d.isolated = upload(m, iso);
-      d.pairs = upload(m, P.pairs);
-      d.pairs_by_trial_ptr = upload(m, P.pairs_by_trial_ptr);
-      d.pairs_by_test_ptr = upload(m, P.pairs_by_test_ptr);
-      d.pairs_by_test = upload(m, P.pairs_by_test);
-      d.rule_ptr = upload(m, P.rule_ptr);
-      d.duffy = upload(m, P.duffy);
-      d.duffy32 = upload(m, std::vector<float>(P.duffy.begin(), P.duffy.end()));
-      d.verts = upload(m, P.verts);
-      d.faces = upload(m, P.faces);
-      d.normal = upload(m, P.normal);
-      d.curls = upload(m, P.curls);
-      d.area = upload(m, P.area);
+      const std::vector<float> duffy32(P.duffy.begin(), P.duffy.end());
       std::vector<double> mm(12);
       for (int i = 0; i < 9; ++i) mm[i] = P.m11[i];
       for (int i = 0; i < 3; ++i) mm[9 + i] = P.m10[i];
-      d.m11m10 = upload(m, mm);
+      UploadPack pack;
+      if (P.symmetry != 0) {
+        pack.add(d.fix_mask, P.fix_mask);
+        pack.add(d.row_weight, P.row_weight);
+      }
+      pack.add(d.faces32, P.faces32);
+      pack.add(d.faces64, P.faces64);
+      pack.add(d.tile_group_ptr, P.tile_group_ptr);
+      pack.add(d.lane_slots, P.lane_slots);
+      pack.add(d.group_faces32, P.group_faces32);
+      pack.add(d.tile_row_base, P.tile_row_base);
+      pack.add(d.ext_row, P.ext_row);
+      pack.add(d.halo_slot_of_ext, P.halo_slot_of_ext);
+      pack.add(d.halo_row_ptr, P.halo_row_ptr);
+      pack.add(d.halo_row, P.halo_row);
+      pack.add(d.col_ptr, P.col_ptr);
+      pack.add(d.col_fb, P.col_fb);
+      pack.add(d.face_ext, P.face_ext);
+      pack.add(d.vertex_row, P.vertex_row);
+      pack.add(d.isolated, iso);
+      pack.add(d.pairs, P.pairs);
+      pack.add(d.pairs_by_trial_ptr, P.pairs_by_trial_ptr);
+      pack.add(d.pairs_by_test_ptr, P.pairs_by_test_ptr);
+      pack.add(d.pairs_by_test, P.pairs_by_test);
+      pack.add(d.rule_ptr, P.rule_ptr);
+      pack.add(d.duffy, P.duffy);
+      pack.add(d.duffy32, duffy32);
+      pack.add(d.verts, P.verts);
+      pack.add(d.faces, P.faces);
+      pack.add(d.normal, P.normal);
+      pack.add(d.curls, P.curls);
+      pack.add(d.area, P.area);
+      pack.add(d.m11m10, mm);
+      pack.commit(m);
       for (int q = 0; q < P.Q; ++q) {
         const double u = P.rule_pts[2 * q], v = P.rule_pts[2 * q + 1];
         const double phi[3] = {1.0 - u - v, u, v};
@@ -444,11 +509,16 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
         }
       }
       for (const auto& sp : P.pairs) m->singular_points += P.rule_ptr[sp.rule + 1] - P.rule_ptr[sp.rule];
-      if (d.npairs > 0) {
+      if (d.npairs > 0)
         d.moments = (double*)mesh_alloc(m, (size_t)d.npairs * 24 * sizeof(double), "allocate singular moments");
-        ck(bem::launch_singular_static(d, d.moments, ctx->stream), "singular moments kernel");
-      }
       ck(cudaStreamSynchronize(ctx->stream), "mesh upload");
+      if (d.npairs > 0) {
+        // the k-independent moments (FP64) on the side stream; the first singular kernel
+        // of a solve waits for them, the regular assembly before it does not
+        ck(bem::launch_singular_static(d, d.moments, ctx->side), "singular moments kernel");
+        ck(cudaEventCreateWithFlags(&m->moments_ready, cudaEventDisableTiming), "create event");
+        ck(cudaEventRecord(m->moments_ready, ctx->side), "record event");
+      }
     } catch (...) {
       free_mesh_device(m);
       delete m;

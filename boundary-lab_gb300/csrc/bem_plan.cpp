@@ -25,10 +25,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstring>
-#include <map>
 #include <numeric>
-#include <set>
-#include <tuple>
 
 namespace bem {
 namespace {
@@ -530,25 +527,35 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
   P.vertex_row.assign(nv, -1);
   P.row_vertex.clear();
   std::vector<std::vector<int>> tile_rows(P.n_tiles);
-  std::vector<std::map<int, int>> tile_loc(P.n_tiles);
-  for (int t = 0; t < P.n_tiles; ++t) {
+  std::vector<int> face_loc(3 * (size_t)nf, -1);  // tile-local row of each face vertex
+  {
+    std::vector<int> loc(nv, -1);  // tile-local row of a vertex while its tile is built
     std::vector<int> prim, halo;
-    std::set<int> seen;
-    for (int f : tile_face_list[t])
-      for (int a = 0; a < 3; ++a) {
-        int v = faces[3 * f + a];
-        if (seen.insert(v).second) (primary[v] == t ? prim : halo).push_back(v);
+    for (int t = 0; t < P.n_tiles; ++t) {
+      prim.clear();
+      halo.clear();
+      for (int f : tile_face_list[t])
+        for (int a = 0; a < 3; ++a) {
+          const int v = faces[3 * f + a];
+          if (loc[v] == -1) {
+            loc[v] = -2;  // seen; the row index is assigned below
+            (primary[v] == t ? prim : halo).push_back(v);
+          }
+        }
+      for (int v : prim) {
+        P.vertex_row[v] = (int)P.row_vertex.size();
+        P.row_vertex.push_back(v);
       }
-    for (int v : prim) {
-      P.vertex_row[v] = (int)P.row_vertex.size();
-      P.row_vertex.push_back(v);
+      std::vector<int>& rows = tile_rows[t];
+      rows = prim;
+      rows.insert(rows.end(), halo.begin(), halo.end());
+      for (size_t i = 0; i < rows.size(); ++i) loc[rows[i]] = (int)i;
+      for (int f : tile_face_list[t])
+        for (int a = 0; a < 3; ++a) face_loc[3 * f + a] = loc[faces[3 * f + a]];
+      for (int v : rows) loc[v] = -1;
+      P.tile_row_base[t + 1] = P.tile_row_base[t] + (int)rows.size();
+      P.max_tile_rows = std::max(P.max_tile_rows, (int)rows.size());
     }
-    std::vector<int>& rows = tile_rows[t];
-    rows = prim;
-    rows.insert(rows.end(), halo.begin(), halo.end());
-    for (size_t i = 0; i < rows.size(); ++i) tile_loc[t][rows[i]] = (int)i;
-    P.tile_row_base[t + 1] = P.tile_row_base[t] + (int)rows.size();
-    P.max_tile_rows = std::max(P.max_tile_rows, (int)rows.size());
   }
   for (int v = 0; v < nv; ++v)
     if (P.vertex_row[v] < 0) {  // vertex used by no face: identity-free zero row
@@ -571,7 +578,7 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
     }
   for (int f = 0; f < nf; ++f) {
     int t = face_tile[f];
-    for (int a = 0; a < 3; ++a) P.face_ext[3 * f + a] = P.tile_row_base[t] + tile_loc[t][faces[3 * f + a]];
+    for (int a = 0; a < 3; ++a) P.face_ext[3 * f + a] = P.tile_row_base[t] + face_loc[3 * f + a];
   }
   // halo gather lists, grouped by target row (ascending ext id within a row)
   {
@@ -601,9 +608,8 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
   for (int t = 0; t < P.n_tiles; ++t) {
     std::vector<std::array<int, 3>> fl;
     fl.reserve(tile_face_list[t].size());
-    for (int f : tile_face_list[t])
-      fl.push_back({tile_loc[t][faces[3 * f]], tile_loc[t][faces[3 * f + 1]], tile_loc[t][faces[3 * f + 2]]});
-    std::vector<std::vector<int>> groups = pack_lane_groups(fl, (int)tile_loc[t].size());
+    for (int f : tile_face_list[t]) fl.push_back({face_loc[3 * f], face_loc[3 * f + 1], face_loc[3 * f + 2]});
+    std::vector<std::vector<int>> groups = pack_lane_groups(fl, (int)tile_rows[t].size());
     for (auto& g : groups)
       for (int& i : g) i = tile_face_list[t][i];
     for (auto& g : groups) {
@@ -612,7 +618,7 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
         if (l < (int)g.size()) {
           int f = g[l];
           s.face = f;
-          for (int a = 0; a < 3; ++a) s.loc[a] = tile_loc[t][faces[3 * f + a]];
+          for (int a = 0; a < 3; ++a) s.loc[a] = face_loc[3 * f + a];
         } else {
           s.face = -1;
           s.loc[0] = s.loc[1] = s.loc[2] = 0;
@@ -662,32 +668,39 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
     for (int a = 0; a < 3; ++a) v2f[faces[3 * f + a]].push_back(f);
   std::vector<DPoint> base[4];
   for (int k = 1; k <= 3; ++k) base[k] = duffy_base(singular_order, k);
-  std::map<std::tuple<int, int, int, int, int>, int> rule_of_key;
+  // rule id of an adjacency key (kind, ta, tb, ra, rb; every field < 4), numbered in
+  // order of first appearance; -1 until seen
+  std::vector<int> rule_of_key(4 * 256, -1);
+  int n_rules = 0;
   P.rule_ptr.assign(1, 0);
   P.duffy.clear();
   std::vector<SingularPair> pairs;
+  pairs.reserve(16 * (size_t)nf * P.transforms.size());
+  std::vector<int> seen(nf, -1);  // candidate stamp: the (transform, test face) that last listed the face
+  std::vector<int> cand;
+  int stamp = 0;
   for (int tr : P.transforms)
-  for (int t = 0; t < nf; ++t) {
-    std::vector<int> cand;
-    std::set<int> seen;
+  for (int t = 0; t < nf; ++t, ++stamp) {
+    cand.clear();
     for (int a = 0; a < 3; ++a) {
       const int v = faces[3 * t + a];
       if (tr != 0 && (P.fix_mask[v] & tr) != tr) continue;  // images touch the test face only on the planes
       for (int r : v2f[v])
-        if (seen.insert(r).second) cand.push_back(r);
+        if (seen[r] != stamp) {
+          seen[r] = stamp;
+          cand.push_back(r);
+        }
     }
     for (int r : cand) {
       Adjacency adj = tr == 0 ? classify(&faces[3 * t], &faces[3 * r])
                               : classify_image(&faces[3 * t], &faces[3 * r], P.fix_mask, tr);
       if (adj.kind == 0) continue;
-      auto key = adj.kind == 1 ? std::make_tuple(1, 0, 0, 0, 0)
-                 : adj.kind == 2 ? std::make_tuple(2, adj.ta, adj.tb, adj.ra, adj.rb)
-                                 : std::make_tuple(3, adj.ta, 0, adj.ra, 0);
-      auto it = rule_of_key.find(key);
-      int rule;
-      if (it == rule_of_key.end()) {
-        rule = (int)rule_of_key.size();
-        rule_of_key[key] = rule;
+      const int key = adj.kind == 1 ? 256
+                      : adj.kind == 2 ? 512 + 64 * adj.ta + 16 * adj.tb + 4 * adj.ra + adj.rb
+                                      : 768 + 64 * adj.ta + 4 * adj.ra;
+      int rule = rule_of_key[key];
+      if (rule < 0) {
+        rule = rule_of_key[key] = n_rules++;
         for (const DPoint& p : base[adj.kind]) {
           double tu = p[0], tv = p[1], ru = p[2], rv = p[3];
           if (adj.kind == 2) {
@@ -700,8 +713,6 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
           P.duffy.insert(P.duffy.end(), {tu, tv, ru, rv, p[4]});
         }
         P.rule_ptr.push_back((int)(P.duffy.size() / 5));
-      } else {
-        rule = it->second;
       }
       SingularPair sp;
       sp.test = t;
@@ -717,14 +728,15 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
       pairs.push_back(sp);
     }
   }
-  std::vector<int> idx(pairs.size());
-  std::iota(idx.begin(), idx.end(), 0);
-  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return pairs[a].trial < pairs[b].trial; });
-  P.pairs.resize(pairs.size());
-  for (size_t i = 0; i < idx.size(); ++i) P.pairs[i] = pairs[idx[i]];
+  // pairs grouped by trial face, generation order kept within a face (a stable counting sort)
   P.pairs_by_trial_ptr.assign(nf + 1, 0);
-  for (const auto& sp : P.pairs) P.pairs_by_trial_ptr[sp.trial + 1]++;
+  for (const auto& sp : pairs) P.pairs_by_trial_ptr[sp.trial + 1]++;
   for (int f = 0; f < nf; ++f) P.pairs_by_trial_ptr[f + 1] += P.pairs_by_trial_ptr[f];
+  P.pairs.resize(pairs.size());
+  {
+    std::vector<int> fill(P.pairs_by_trial_ptr.begin(), P.pairs_by_trial_ptr.end() - 1);
+    for (const auto& sp : pairs) P.pairs[fill[sp.trial]++] = sp;
+  }
   P.pairs_by_test_ptr.assign(nf + 1, 0);
   for (const auto& sp : P.pairs) P.pairs_by_test_ptr[sp.test + 1]++;
   for (int f = 0; f < nf; ++f) P.pairs_by_test_ptr[f + 1] += P.pairs_by_test_ptr[f];
