@@ -648,9 +648,21 @@ struct SingularGeom {
   const double* normal;
 };
 
+// Per-pair record of the mixed form (kPairRec floats), written once per mesh by
+// the moments kernel below so that the per-frequency FP32 singular kernel runs
+// no FP64 instruction (on this part the FP64 pipe, not FP32, limited it):
+//   [0..20]  e1t, e2t, d0, e1r, e2r, n_test, n_trial (3 each; the trial side
+//            reflected for image pairs), each rounded from its FP64 value
+//   [21] jac   [22] n_test . (S n_trial)   [23] 2 A_test
+//   [24..32] curl_a(test) . curl_b(trial image), a-major, summed in FP64
+//   [33] SG0[0] + SG0[1] + SG0[2] (FP64 sum)   [34..57] the 24 static moments
+constexpr int kRecGeom = 0, kRecJac = 21, kRecNprod = 22, kRecA2 = 23, kRecCurl = 24, kRecS0 = 33, kRecMom = 34;
+static_assert(kRecMom + kStatic <= kPairRec, "pair record layout");
+
 __global__ void singular_static_kernel(SingularGeom geo, const SingularPair* __restrict__ pairs, int npairs,
                                        const int* __restrict__ rule_ptr, const double* __restrict__ duffy,
-                                       double* __restrict__ moments) {
+                                       const double* __restrict__ curls, const double* __restrict__ area,
+                                       double* __restrict__ moments, float* __restrict__ rec) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= npairs) return;
@@ -700,11 +712,40 @@ __global__ void singular_static_kernel(SingularGeom geo, const SingularPair* __r
       }
     }
   }
+  double mom[kStatic];
 #pragma unroll
-  for (int i = 0; i < kStatic; ++i) {
-    const double v = warp_sum(acc[i]);
-    if (lane == 0) moments[(size_t)kStatic * warp + i] = v * P.jac;
+  for (int i = 0; i < kStatic; ++i) mom[i] = warp_sum(acc[i]) * P.jac;
+  if (lane != 0) return;
+  for (int i = 0; i < kStatic; ++i) moments[(size_t)kStatic * warp + i] = mom[i];
+  float* o = rec + (size_t)kPairRec * warp;
+  for (int d = 0; d < 3; ++d) {
+    o[kRecGeom + d] = (float)e1t[d];
+    o[kRecGeom + 3 + d] = (float)e2t[d];
+    o[kRecGeom + 6 + d] = (float)d0[d];
+    o[kRecGeom + 9 + d] = (float)e1r[d];
+    o[kRecGeom + 12 + d] = (float)e2r[d];
+    o[kRecGeom + 15 + d] = (float)nt[d];
+    o[kRecGeom + 18 + d] = (float)nr[d];
   }
+  o[kRecJac] = (float)P.jac;
+  o[kRecNprod] = (float)P.nprod;
+  o[kRecA2] = (float)(2.0 * area[P.test]);
+  const double* ct = curls + 9 * (size_t)P.test;
+  const double* cr0 = curls + 9 * (size_t)P.trial;
+  const double sx = tr_sign_x(P.tr), sy = tr_sign_y(P.tr), det = sx * sy;
+  double cr[9];  // reflected trial curls det(S) S c
+  for (int b = 0; b < 3; ++b) {
+    cr[3 * b] = det * sx * cr0[3 * b];
+    cr[3 * b + 1] = det * sy * cr0[3 * b + 1];
+    cr[3 * b + 2] = det * cr0[3 * b + 2];
+  }
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b)
+      o[kRecCurl + 3 * a + b] =
+          (float)(ct[3 * a] * cr[3 * b] + ct[3 * a + 1] * cr[3 * b + 1] + ct[3 * a + 2] * cr[3 * b + 2]);
+  o[kRecS0] = (float)(mom[0] + mom[1] + mom[2]);
+  for (int i = 0; i < kStatic; ++i) o[kRecMom + i] = (float)mom[i];
+  for (int i = kRecMom + kStatic; i < kPairRec; ++i) o[i] = 0.0f;
 }
 
 template <typename R> struct SingParams;
@@ -878,6 +919,131 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)  // FP32: two 256
     C2 K = cplx<R>::make((R)M[21 + a] + IKh[a].x, IKh[a].y);
     C2 rhs = cadd(cmul(p.cS, S), cmul(p.cK, K));
     if (coincident) rhs = cadd(rhs, cscale(p.cM10, a2 * (R)m11m10[9 + a]));
+    o[9 + a] = rhs;
+  }
+}
+
+// The mixed form's singular kernel: the same Duffy remainder as
+// singular_dyn_kernel<float>, with every per-pair FP64 quantity (geometry,
+// curl products, static moments) read from the pair record instead of being
+// formed from FP64 data per frequency.  One warp per pair, lanes over the
+// Duffy points; after the warp reduction (every lane holds every sum) lanes
+// 0-8 form the nine LHS entries and lanes 9-11 the three RHS-operator entries.
+struct SingParamsF32 {
+  float k, k2;
+  float2 cD, cH, cM, cS, cK, cM10;
+  float m11m10[12];
+};
+
+__global__ void __launch_bounds__(256, 2)
+    singular_dyn_f32_kernel(const SingularPair* __restrict__ pairs, int npairs, const int* __restrict__ rule_ptr,
+                            const float* __restrict__ duffy, const float* __restrict__ rec, SingParamsF32 p,
+                            float2* __restrict__ out) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= npairs) return;
+  const SingularPair P = pairs[warp];
+  const float* G = rec + (size_t)kPairRec * warp;
+  float g[24];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(G) + i);
+    g[4 * i] = v.x;
+    g[4 * i + 1] = v.y;
+    g[4 * i + 2] = v.z;
+    g[4 * i + 3] = v.w;
+  }
+  const float* e1t = g + kRecGeom;
+  const float* e2t = g + kRecGeom + 3;
+  const float* d0 = g + kRecGeom + 6;
+  const float* e1r = g + kRecGeom + 9;
+  const float* e2r = g + kRecGeom + 12;
+  const float* nt = g + kRecGeom + 15;
+  const float* nr = g + kRecGeom + 18;
+  float2 acc2[24];  // SR[3], IR[9], IDh[9], IKh[3] as (re, im)
+#pragma unroll
+  for (int i = 0; i < 24; ++i) acc2[i] = make_float2(0.f, 0.f);
+  const float inv4pi = (float)(0.25 / CUDART_PI);
+  const int q0 = rule_ptr[P.rule], q1 = rule_ptr[P.rule + 1];
+  for (int q = q0 + lane; q < q1; q += 32) {
+    const float* pt = duffy + 5 * (size_t)q;
+    const float tu = pt[0], tv = pt[1], ru = pt[2], rvv = pt[3], w = pt[4];
+    const float px[3] = {1.f - tu - tv, tu, tv};
+    const float py[3] = {1.f - ru - rvv, ru, rvv};
+    float rv[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) rv[d] = (d0[d] + ru * e1r[d] + rvv * e2r[d]) - (tu * e1t[d] + tv * e2t[d]);
+    const float r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+    if (r2 == 0.f) continue;
+    float sh, ch;
+    const float rinv = rsqrt_ftz(r2);
+    const float r = r2 * rinv;
+    sincos_taylor(0.5f * p.k * r, &sh, &ch);
+    const float z = p.k * r;
+    const float s = rinv * inv4pi;
+    const float sinz = 2.f * sh * ch;
+    const float omc = 2.f * sh * sh;  // 1 - cos z
+    const float cosz = 1.f - omc;
+    const float Rr = -s * omc, Ri = s * sinz;
+    const float hr = omc - z * sinz, hi = z * cosz - sinz;
+    const float fy = (rv[0] * nr[0] + rv[1] * nr[1] + rv[2] * nr[2]) * s * rinv * rinv;
+    const float fx = -(rv[0] * nt[0] + rv[1] * nt[1] + rv[2] * nt[2]) * s * rinv * rinv;
+    const float2 G2 = make_float2(Rr, Ri), Hy = make_float2(hr * fy, hi * fy), Hx = make_float2(hr * fx, hi * fx);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float wa = w * px[a];
+      const float2 wa2 = make_float2(wa, wa);
+      acc2[a] = __ffma2_rn(wa2, G2, acc2[a]);
+      acc2[21 + a] = __ffma2_rn(wa2, Hx, acc2[21 + a]);
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const float2 wab = __fmul2_rn(wa2, make_float2(py[b], py[b]));
+        acc2[3 + 3 * a + b] = __ffma2_rn(wab, G2, acc2[3 + 3 * a + b]);
+        acc2[12 + 3 * a + b] = __ffma2_rn(wab, Hy, acc2[12 + 3 * a + b]);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 24; ++i) acc2[i] = make_float2(warp_sum(acc2[i].x), warp_sum(acc2[i].y));
+  if (lane >= 12) return;
+  const float jac = g[kRecJac];
+  const bool coincident = P.kind == 1 && P.tr == 0;  // mass terms: the face with itself, never with an image
+  const float a2 = g[kRecA2];
+  float2* o = out + (size_t)kSingOut * warp;
+  if (lane < 9) {
+    const int i = lane;
+    // S0 = sum w G (static + dynamic)
+    float2 S0 = make_float2(G[kRecS0], 0.f);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) S0 = cadd(S0, make_float2(acc2[a].x * jac, acc2[a].y * jac));
+    float2 IR = make_float2(0.f, 0.f), IDh = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < 9; ++j)
+      if (j == i) {
+        IR = make_float2(acc2[3 + j].x * jac, acc2[3 + j].y * jac);
+        IDh = make_float2(acc2[12 + j].x * jac, acc2[12 + j].y * jac);
+      }
+    const float kk_nn = p.k2 * g[kRecNprod];
+    const float cc = G[kRecCurl + i];
+    const float2 D = make_float2(G[kRecMom + 12 + i] + IDh.x, IDh.y);
+    const float2 IGt = make_float2(G[kRecMom + 3 + i] + IR.x, IR.y);
+    const float2 H = make_float2(cc * S0.x - kk_nn * IGt.x, cc * S0.y - kk_nn * IGt.y);
+    float2 L = cadd(cmul(p.cD, D), cmul(p.cH, H));
+    if (coincident) L = cadd(L, cscale(p.cM, a2 * p.m11m10[i]));
+    o[i] = L;
+  } else {
+    const int a = lane - 9;
+    float2 SR = make_float2(0.f, 0.f), IKh = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (j == a) {
+        SR = make_float2(acc2[j].x * jac, acc2[j].y * jac);
+        IKh = make_float2(acc2[21 + j].x * jac, acc2[21 + j].y * jac);
+      }
+    const float2 S = make_float2(G[kRecMom + a] + SR.x, SR.y);
+    const float2 K = make_float2(G[kRecMom + 21 + a] + IKh.x, IKh.y);
+    float2 rhs = cadd(cmul(p.cS, S), cmul(p.cK, K));
+    if (coincident) rhs = cadd(rhs, cscale(p.cM10, a2 * p.m11m10[9 + a]));
     o[9 + a] = rhs;
   }
 }
@@ -1278,12 +1444,13 @@ cudaError_t launch_regular_f64(const DeviceMesh& m, double k, double2 cD, double
   return cudaGetLastError();
 }
 
-cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, cudaStream_t stream) {
+cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, float* pairrec, cudaStream_t stream) {
   if (m.npairs == 0) return cudaSuccess;
   SingularGeom geo{m.verts, m.faces, m.normal};
   const int threads = 256;
   const int blocks = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
-  singular_static_kernel<<<blocks, threads, 0, stream>>>(geo, m.pairs, m.npairs, m.rule_ptr, m.duffy, moments);
+  singular_static_kernel<<<blocks, threads, 0, stream>>>(geo, m.pairs, m.npairs, m.rule_ptr, m.duffy, m.curls, m.area,
+                                                         moments, pairrec);
   return cudaGetLastError();
 }
 
@@ -1294,7 +1461,7 @@ cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, double k, c
   const int threads = 256;
   const int nblk = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
   if (prec == Precision::Mixed) {
-    SingParams<float> p;
+    SingParamsF32 p;
     p.k = (float)k;
     p.k2 = (float)(k * k);
     p.cD = f2(c.cD);
@@ -1303,9 +1470,9 @@ cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, double k, c
     p.cS = f2(c.cS);
     p.cK = f2(c.cK);
     p.cM10 = f2(c.cM10);
-    singular_dyn_kernel<float><<<nblk, threads, 0, stream>>>(geo, m.pairs, m.npairs, m.rule_ptr, m.duffy32,
-                                                             m.moments, m.curls, m.area, m.m11m10, p,
-                                                             (float2*)blocks);
+    for (int i = 0; i < 12; ++i) p.m11m10[i] = m.m11m10f[i];
+    singular_dyn_f32_kernel<<<nblk, threads, 0, stream>>>(m.pairs, m.npairs, m.rule_ptr, m.duffy32, m.pairrec, p,
+                                                          (float2*)blocks);
   } else {
     SingParams<double> p;
     p.k = k;

@@ -509,13 +509,16 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
         }
       }
       for (const auto& sp : P.pairs) m->singular_points += P.rule_ptr[sp.rule + 1] - P.rule_ptr[sp.rule];
-      if (d.npairs > 0)
+      for (int i = 0; i < 12; ++i) d.m11m10f[i] = (float)mm[i];
+      if (d.npairs > 0) {
         d.moments = (double*)mesh_alloc(m, (size_t)d.npairs * 24 * sizeof(double), "allocate singular moments");
+        d.pairrec = (float*)mesh_alloc(m, (size_t)d.npairs * bem::kPairRec * sizeof(float), "allocate pair records");
+      }
       ck(cudaStreamSynchronize(ctx->stream), "mesh upload");
       if (d.npairs > 0) {
         // the k-independent moments (FP64) on the side stream; the first singular kernel
         // of a solve waits for them, the regular assembly before it does not
-        ck(bem::launch_singular_static(d, d.moments, ctx->side), "singular moments kernel");
+        ck(bem::launch_singular_static(d, d.moments, d.pairrec, ctx->side), "singular moments kernel");
         ck(cudaEventCreateWithFlags(&m->moments_ready, cudaEventDisableTiming), "create event");
         ck(cudaEventRecord(m->moments_ready, ctx->side), "record event");
       }
@@ -709,7 +712,7 @@ long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int np
   const long long group = precision == BEM_PRECISION_MIXED ? 2 : 1;        // frequencies assembled together
   bytes += round_up(n_ext, 32) * 3LL * nf * esz * group;                    // extended rows
   bytes += (long long)batch * lda * nv * esz * (precision == BEM_PRECISION_MIXED ? 2 : 1);  // matrices (+copy)
-  bytes += (long long)npairs * (12 * esz * group + 24 * 8 + 48);            // singular blocks, moments, pairs
+  bytes += (long long)npairs * (12 * esz * group + 24 * 8 + 48 + bem::kPairRec * 4);  // singular blocks, moments, pairs, records
   bytes += (long long)batch * nrhs * lda * (esz + 3 * 16 + 16);             // rhs, x, r, b64, d
   bytes += (long long)batch * nrhs * ((long long)nf * 6 * esz + (long long)npts * 16);  // field sources + out
   bytes += (long long)nf * (2 * 160 + 288 + 64);                            // face records (+ lane-group copy), maps

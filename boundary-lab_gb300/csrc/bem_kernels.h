@@ -55,12 +55,14 @@ struct DeviceMesh {
   double* duffy = nullptr;
   float* duffy32 = nullptr;  // the same table rounded to float (mixed form)
   double* moments = nullptr;
+  float* pairrec = nullptr;  // npairs x kPairRec: FP32 record of each pair for the mixed-form singular kernel
   double* verts = nullptr;
   int* faces = nullptr;
   double* normal = nullptr;
   double* curls = nullptr;
   double* area = nullptr;
   double* m11m10 = nullptr;  // 9 + 3 doubles
+  float m11m10f[12] = {0};   // the same, rounded to float (host copy, passed as a kernel parameter)
   int* driven = nullptr;
   // symmetry: transforms applied to trial faces (0 identity, 1 x, 2 y, 3 xy),
   // per-vertex plane masks, per-matrix-row orbit weights (null when off)
@@ -83,7 +85,9 @@ cudaError_t launch_regular(const DeviceMesh& m, Precision prec, int nfreq, const
 int regular_launches(Precision prec, int nfreq);
 cudaError_t launch_regular_f64(const DeviceMesh& m, double k, double2 cD, double2 cH, double2* Rext, long long ldR,
                                cudaStream_t stream);
-cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, cudaStream_t stream);
+// Per-pair FP32 record written by the FP64 moments kernel (see bem_assembly.cu).
+constexpr int kPairRec = 64;
+cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, float* pairrec, cudaStream_t stream);
 cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, double k, const OperatorCoeffs& c, void* blocks,
                                 cudaStream_t stream);
 cudaError_t launch_singular_scatter(const DeviceMesh& m, Precision prec, const void* blocks, void* Rext,
