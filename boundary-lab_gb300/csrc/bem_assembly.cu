@@ -965,9 +965,18 @@ __global__ void __launch_bounds__(256, 2)
   for (int i = 0; i < 24; ++i) acc2[i] = make_float2(0.f, 0.f);
   const float inv4pi = (float)(0.25 / CUDART_PI);
   const int q0 = rule_ptr[P.rule], q1 = rule_ptr[P.rule + 1];
+  // the next point's five values are loaded one iteration ahead
+  float nx[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  if (q0 + lane < q1) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) nx[i] = __ldg(duffy + 5 * (size_t)(q0 + lane) + i);
+  }
   for (int q = q0 + lane; q < q1; q += 32) {
-    const float* pt = duffy + 5 * (size_t)q;
-    const float tu = pt[0], tv = pt[1], ru = pt[2], rvv = pt[3], w = pt[4];
+    const float tu = nx[0], tv = nx[1], ru = nx[2], rvv = nx[3], w = nx[4];
+    if (q + 32 < q1) {
+#pragma unroll
+      for (int i = 0; i < 5; ++i) nx[i] = __ldg(duffy + 5 * (size_t)(q + 32) + i);
+    }
     const float px[3] = {1.f - tu - tv, tu, tv};
     const float py[3] = {1.f - ru - rvv, ru, rvv};
     float rv[3];
