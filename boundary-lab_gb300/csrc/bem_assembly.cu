@@ -761,8 +761,9 @@ template <> struct SingParams<double> {
 // Per pair output: 9 LHS block entries then 3 RHS-operator entries (complex).
 constexpr int kSingOut = 12;
 
+// The plain FP64 form's singular kernel (the mixed form uses singular_dyn_f32_kernel below).
 template <typename R>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)  // FP32: two 256-thread CTAs per SM (<= 128 registers)
+__global__ void __launch_bounds__(256, 1)
     singular_dyn_kernel(SingularGeom geo, const SingularPair* __restrict__ pairs, int npairs,
                                     const int* __restrict__ rule_ptr, const R* __restrict__ duffy,
                                     const double* __restrict__ moments, const double* __restrict__ curls,
@@ -792,14 +793,9 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)  // FP32: two 256
   R acc[48];
 #pragma unroll
   for (int i = 0; i < 48; ++i) acc[i] = R(0);
-  float2 acc2[24];  // the same accumulators as (re, im) pairs (FP32 form)
-#pragma unroll
-  for (int i = 0; i < 24; ++i) acc2[i] = make_float2(0.f, 0.f);
   const R inv4pi = R(0.25 / CUDART_PI);
   const int q0 = rule_ptr[P.rule], q1 = rule_ptr[P.rule + 1];
   for (int q = q0 + lane; q < q1; q += 32) {
-    // Duffy points in the working precision (a float copy of the table for the
-    // mixed form: FP64->FP32 conversions run at the FP64 rate on this part)
     const R* pt = duffy + 5 * (size_t)q;
     const R tu = pt[0], tv = pt[1], ru = pt[2], rvv = pt[3], w = pt[4];
     const R px[3] = {R(1) - tu - tv, tu, tv};
@@ -809,16 +805,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)  // FP32: two 256
     for (int d = 0; d < 3; ++d) rv[d] = (d0[d] + ru * e1r[d] + rvv * e2r[d]) - (tu * e1t[d] + tv * e2t[d]);
     const R r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
     if (r2 == R(0)) continue;
-    R rinv, r, sh, ch;
-    if constexpr (sizeof(R) == 4) {
-      rinv = rsqrt_ftz(r2);
-      r = r2 * rinv;
-      sincos_taylor(R(0.5) * p.k * r, &sh, &ch);
-    } else {
-      rinv = rsqrt(r2);
-      r = r2 * rinv;
-      sincos(R(0.5) * p.k * r, &sh, &ch);
-    }
+    R sh, ch;
+    const R rinv = rsqrt(r2);
+    const R r = r2 * rinv;
+    sincos(R(0.5) * p.k * r, &sh, &ch);
     const R z = p.k * r;
     const R s = rinv * inv4pi;
     const R sinz = R(2) * sh * ch;
@@ -830,46 +820,21 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)  // FP32: two 256
     const R hr = omc - z * sinz, hi = z * cosz - sinz;
     const R fy = (rv[0] * nr[0] + rv[1] * nr[1] + rv[2] * nr[2]) * s * rinv * rinv;
     const R fx = -(rv[0] * nt[0] + rv[1] * nt[1] + rv[2] * nt[2]) * s * rinv * rinv;
-    if constexpr (sizeof(R) == 4) {
-      // complex accumulations as packed FP32x2 FMAs
-      const float2 G2 = make_float2(Rr, Ri), Hy = make_float2(hr * fy, hi * fy), Hx = make_float2(hr * fx, hi * fx);
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const float wa = w * px[a];
-        const float2 wa2 = make_float2(wa, wa);
-        acc2[a] = __ffma2_rn(wa2, G2, acc2[a]);
-        acc2[21 + a] = __ffma2_rn(wa2, Hx, acc2[21 + a]);
+    for (int a = 0; a < 3; ++a) {
+      const R wa = w * px[a];
+      acc[2 * a] += wa * Rr;
+      acc[2 * a + 1] += wa * Ri;
+      acc[42 + 2 * a] += wa * hr * fx;
+      acc[42 + 2 * a + 1] += wa * hi * fx;
 #pragma unroll
-        for (int b = 0; b < 3; ++b) {
-          const float2 wab = __fmul2_rn(wa2, make_float2(py[b], py[b]));
-          acc2[3 + 3 * a + b] = __ffma2_rn(wab, G2, acc2[3 + 3 * a + b]);
-          acc2[12 + 3 * a + b] = __ffma2_rn(wab, Hy, acc2[12 + 3 * a + b]);
-        }
+      for (int b = 0; b < 3; ++b) {
+        const R wab = wa * py[b];
+        acc[6 + 2 * (3 * a + b)] += wab * Rr;
+        acc[6 + 2 * (3 * a + b) + 1] += wab * Ri;
+        acc[24 + 2 * (3 * a + b)] += wab * hr * fy;
+        acc[24 + 2 * (3 * a + b) + 1] += wab * hi * fy;
       }
-    } else {
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const R wa = w * px[a];
-        acc[2 * a] += wa * Rr;
-        acc[2 * a + 1] += wa * Ri;
-        acc[42 + 2 * a] += wa * hr * fx;
-        acc[42 + 2 * a + 1] += wa * hi * fx;
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-          const R wab = wa * py[b];
-          acc[6 + 2 * (3 * a + b)] += wab * Rr;
-          acc[6 + 2 * (3 * a + b) + 1] += wab * Ri;
-          acc[24 + 2 * (3 * a + b)] += wab * hr * fy;
-          acc[24 + 2 * (3 * a + b) + 1] += wab * hi * fy;
-        }
-      }
-    }
-  }
-  if constexpr (sizeof(R) == 4) {
-#pragma unroll
-    for (int i = 0; i < 24; ++i) {
-      acc[2 * i] = acc2[i].x;
-      acc[2 * i + 1] = acc2[i].y;
     }
   }
 #pragma unroll

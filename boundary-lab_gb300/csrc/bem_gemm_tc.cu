@@ -13,16 +13,18 @@
 // about 2^-21 relative error per product (FP32 LU quality), so the FP64
 // refinement still converges in one or two steps.
 //
-// Kernel: one CTA (4 warps, two CTAs per SM) per 128 x 256 tile of C'.  A prep kernel writes
-// A'hi, A'lo, B'hi, B'lo as K-major (K contiguous) buffers; TMA brings 16-wide
-// K blocks into 64-byte-swizzled shared memory through a 2-stage mbarrier
-// pipeline; one thread issues tcgen05.mma (kind::tf32, M=128, N=256, K=8)
-// into a TMEM accumulator; all four warps read it back with tcgen05.ld, stage
-// -D in shared memory 32 columns at a time (double buffered per warp) and
-// TMA reduce-add it into C (cp.reduce.async.bulk.tensor .add.f32), so C is
-// never read by the SM: the read-modify-write happens in L2, asynchronously.
-// Every wait is bounded: on timeout the kernel records an error, waits
-// (bounded) for its own copies, frees its TMEM and returns.
+// Kernel: persistent, one CTA per SM, tiles of 128 x 256 of C'.  A prep kernel
+// writes A'hi, A'lo, B'hi, B'lo as K-major (K contiguous) buffers; a producer
+// warp brings 16-wide K blocks by TMA into 64-byte-swizzled shared memory
+// through a 4-stage mbarrier pipeline; one thread issues tcgen05.mma
+// (kind::tf32, M=128, N=256, K=8) into one of two TMEM accumulators; four
+// epilogue warps read the other accumulator back with tcgen05.ld, stage -D in
+// shared memory 32 columns at a time (double buffered per warp) and TMA
+// reduce-add it into C (cp.reduce.async.bulk.tensor .add.f32), so C is never
+// read by the SM: the read-modify-write happens in L2, asynchronously, while
+// the next tile's MMAs run.  Every wait is bounded: on timeout the kernel
+// records an error, waits (bounded) for its own copies and MMAs, frees its
+// TMEM and returns.
 //
 // General block update (tc_update): C[row0:row0+M, col0:col0+N] -= L U with
 // L = A[row0:, kcol0:kcol0+K] and U = A[kcol0:kcol0+K, col0:], K <= 128, so one
@@ -40,6 +42,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "bem_common.cuh"
 #include "bem_kernels.h"
 
@@ -50,13 +54,9 @@ constexpr int TM = 128;       // tile rows of C' (real rows)
 constexpr int TN = 256;       // tile columns of C'
 constexpr int TK = 16;        // K block per stage (16 fp32 = 64 B rows, 64-byte swizzle)
 constexpr int KP_MAX = 256;   // K' = 2 K <= 256 (K <= 128 complex), row stride of the split operands
-constexpr int STAGES = 2;
 constexpr int A_BYTES = TM * TK * 4;   // 8 KB
 constexpr int B_BYTES = TN * TK * 4;   // 16 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi + lo of A and B: 48 KB
-// Two stages (96 KB) per CTA and 256 TMEM columns: two CTAs share an SM, so one
-// CTA's epilogue (TMA reduce-adds into C) overlaps the other's loads and MMAs.
-constexpr int TMEM_COLS = 256;
 // mbarrier waits give up after kWaitLimit polls with a 1 us suspend hint each
 // (about one second), far above any healthy wait (microseconds).
 constexpr long long kWaitLimit = 1LL << 20;
@@ -155,51 +155,6 @@ __device__ __forceinline__ float round_tf32(float x) {
   return __uint_as_float(u);
 }
 
-// A'hi / A'lo [batch][rows_pad][KP_MAX] from L (rows row0.., columns col0..col0+kb of
-// each matrix); rows_used x kp entries are written (zero beyond M rows / 2 kb).
-__global__ void prep_a_kernel(const float2* __restrict__ A, long long lda, long long strideA, int row0, int col0, int M,
-                              int kb, int rows_pad, int rows_used, int kp, float* __restrict__ ahi,
-                              float* __restrict__ alo) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)rows_used * kp) return;
-  const int b = blockIdx.y;
-  const int rr = (int)(idx / kp), kk = (int)(idx % kp);
-  float v = 0.f;
-  const int i = rr >> 1, k = kk >> 1;
-  if (i < M && k < kb) {
-    const float2 a = A[(size_t)b * strideA + (size_t)(col0 + k) * lda + row0 + i];
-    if ((rr & 1) == 0)
-      v = (kk & 1) == 0 ? a.x : -a.y;
-    else
-      v = (kk & 1) == 0 ? a.y : a.x;
-  }
-  const float hi = round_tf32(v);
-  const size_t o = ((size_t)b * rows_pad + rr) * KP_MAX + kk;
-  ahi[o] = hi;
-  alo[o] = v - hi;
-}
-
-// B'hi / B'lo [batch][cols_pad][KP_MAX] from U (rows row0..row0+kb, columns col0.. of
-// each matrix); cols_used x kp entries are written (zero beyond N columns / 2 kb).
-__global__ void prep_b_kernel(const float2* __restrict__ A, long long lda, long long strideA, int row0, int col0, int N,
-                              int kb, int cols_pad, int cols_used, int kp, float* __restrict__ bhi,
-                              float* __restrict__ blo) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)cols_used * kp) return;
-  const int b = blockIdx.y;
-  const int j = (int)(idx / kp), kk = (int)(idx % kp);
-  float v = 0.f;
-  const int k = kk >> 1;
-  if (j < N && k < kb) {
-    const float2 u = A[(size_t)b * strideA + (size_t)(col0 + j) * lda + row0 + k];
-    v = (kk & 1) == 0 ? u.x : u.y;
-  }
-  const float hi = round_tf32(v);
-  const size_t o = ((size_t)b * cols_pad + j) * KP_MAX + kk;
-  bhi[o] = hi;
-  blo[o] = v - hi;
-}
-
 // Both operand splits of one update in one launch.  Blocks [0, nta) split A:
 // each takes 32 rows x 8 columns of L21 (complex), loaded along the rows
 // (coalesced, through shared memory) and written as the 64 x 16 real-embedded
@@ -250,121 +205,196 @@ __global__ void __launch_bounds__(256) prep_ab_kernel(const float2* __restrict__
   *reinterpret_cast<float2*>(blo + o) = make_float2(u.x - hi.x, u.y - hi.y);
 }
 
-__global__ void __launch_bounds__(128, 2)
-    trailing_update_tf32x3(const __grid_constant__ CUtensorMap map_ahi, const __grid_constant__ CUtensorMap map_alo,
-                           const __grid_constant__ CUtensorMap map_bhi, const __grid_constant__ CUtensorMap map_blo,
-                           const __grid_constant__ CUtensorMap map_c, int x0, int y0, int M2, int N, int KB,
-                           int* err) {
+// One CTA per SM walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ... (rows
+// of C' fastest, then columns, then matrices).  Warp 0 is the TMA producer,
+// warp 1 issues the MMAs, warps 2-5 are the epilogue.  Operands flow through a
+// 4-stage pipeline (192 KB) and the accumulator is double-buffered in TMEM
+// (2 x 256 columns), so the epilogue of one tile runs while the MMAs of the
+// next tile proceed.  A warp reads only its own TMEM lane quarter (warp % 4),
+// so epilogue warp w handles rows 32 (w % 4) of a tile.  (The one-tile-per-CTA
+// kernel with two CTAs per SM that this replaced was 2-3% slower on the LU.)
+constexpr int P_STAGES = 4;
+constexpr int P_EPI_WARPS = 4;
+constexpr int P_THREADS = 64 + 32 * P_EPI_WARPS;
+constexpr int P_TMEM_COLS = 2 * TN;
+constexpr size_t P_STAGE_AREA = (size_t)P_STAGES * STAGE_BYTES;  // 192 KB
+constexpr size_t P_EPI_BYTES = (size_t)P_EPI_WARPS * 8192;        // two 4 KB buffers per epilogue warp
+constexpr size_t P_SMEM = P_STAGE_AREA + P_EPI_BYTES + 1024;
+
+__global__ void __launch_bounds__(P_THREADS, 1)
+    trailing_update_tf32x3_persistent(const __grid_constant__ CUtensorMap map_ahi,
+                                      const __grid_constant__ CUtensorMap map_alo,
+                                      const __grid_constant__ CUtensorMap map_bhi,
+                                      const __grid_constant__ CUtensorMap map_blo,
+                                      const __grid_constant__ CUtensorMap map_c, int x0, int y0, int M2, int N, int KB,
+                                      int tiles_m, int tiles_n, int n_tiles, int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  // 1024-byte alignment for the swizzled tiles
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  __shared__ __align__(8) uint64_t full_bar[STAGES];
-  __shared__ __align__(8) uint64_t empty_bar[STAGES];
+  __shared__ __align__(8) uint64_t full_bar[P_STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[P_STAGES];
+  __shared__ __align__(8) uint64_t acc_full[2];
+  __shared__ __align__(8) uint64_t acc_empty[2];
   __shared__ __align__(8) uint64_t done_bar;
   __shared__ uint32_t tmem_slot;
-  __shared__ int s_fail;
+  __shared__ volatile int s_fail;
+  __shared__ int s_consumed;  // K blocks the MMA warp has taken from the pipeline
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * TM, n0 = blockIdx.y * TN, bz = blockIdx.z;
-
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; ++s) {
+    for (int s = 0; s < P_STAGES; ++s) {
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], P_EPI_WARPS);
+    }
     mbar_init(&done_bar, 1);
     s_fail = 0;
+    s_consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
-                 "r"(TMEM_COLS));
+                 "r"(P_TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
+  const int per_matrix = tiles_m * tiles_n;
+  int issued = 0;  // producer: K blocks whose loads were started
 
   if (warp == 0 && lane == 0) {
     // TMA producer
-    for (int kb = 0; kb < KB; ++kb) {
-      const int s = kb % STAGES;
-      if (kb >= STAGES && !mbar_wait(&empty_bar[s], ((kb / STAGES) - 1) & 1, err, 1)) {
-        s_fail = 1;
-        break;
+    int it = 0;
+    for (int t = blockIdx.x; t < n_tiles && !s_fail; t += gridDim.x) {
+      const int bz = t / per_matrix, rem = t - bz * per_matrix;
+      const int m0 = (rem % tiles_m) * TM, n0 = (rem / tiles_m) * TN;
+      for (int kb = 0; kb < KB; ++kb, ++it) {
+        const int s = it % P_STAGES;
+        if (it >= P_STAGES && !mbar_wait(&empty_bar[s], ((it / P_STAGES) - 1) & 1, err, 1)) {
+          s_fail = 1;
+          break;
+        }
+        unsigned char* st = base + (size_t)s * STAGE_BYTES;
+        mbar_expect_tx(&full_bar[s], STAGE_BYTES);
+        tma_load_3d(st, &map_ahi, &full_bar[s], kb * TK, m0, bz);
+        tma_load_3d(st + A_BYTES, &map_alo, &full_bar[s], kb * TK, m0, bz);
+        tma_load_3d(st + 2 * A_BYTES, &map_bhi, &full_bar[s], kb * TK, n0, bz);
+        tma_load_3d(st + 2 * A_BYTES + B_BYTES, &map_blo, &full_bar[s], kb * TK, n0, bz);
+        issued = it + 1;
       }
-      unsigned char* st = base + (size_t)s * STAGE_BYTES;
-      mbar_expect_tx(&full_bar[s], STAGE_BYTES);
-      tma_load_3d(st, &map_ahi, &full_bar[s], kb * TK, m0, bz);
-      tma_load_3d(st + A_BYTES, &map_alo, &full_bar[s], kb * TK, m0, bz);
-      tma_load_3d(st + 2 * A_BYTES, &map_bhi, &full_bar[s], kb * TK, n0, bz);
-      tma_load_3d(st + 2 * A_BYTES + B_BYTES, &map_blo, &full_bar[s], kb * TK, n0, bz);
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
-    bool ok = true;
-    for (int kb = 0; kb < KB && ok; ++kb) {
-      const int s = kb % STAGES;
-      if (!mbar_wait(&full_bar[s], (kb / STAGES) & 1, err, 2)) {
-        ok = false;
+    int it = 0, local = 0;
+    for (int t = blockIdx.x; t < n_tiles && !s_fail; t += gridDim.x, ++local) {
+      const int buf = local & 1;
+      if (local >= 2 && !mbar_wait(&acc_empty[buf], ((local >> 1) - 1) & 1, err, 5)) {
+        s_fail = 1;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      unsigned char* st = base + (size_t)s * STAGE_BYTES;
-      const uint32_t a_hi = smem_u32(st), a_lo = smem_u32(st + A_BYTES);
-      const uint32_t b_hi = smem_u32(st + 2 * A_BYTES), b_lo = smem_u32(st + 2 * A_BYTES + B_BYTES);
+      const uint32_t acc_addr = tmem + (uint32_t)(buf * TN);
+      bool ok = true;
+      for (int kb = 0; kb < KB; ++kb, ++it) {
+        const int s = it % P_STAGES;
+        if (!mbar_wait(&full_bar[s], (it / P_STAGES) & 1, err, 2)) {
+          ok = false;
+          break;
+        }
+        s_consumed = it + 1;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        unsigned char* st = base + (size_t)s * STAGE_BYTES;
+        const uint32_t a_hi = smem_u32(st), a_lo = smem_u32(st + A_BYTES);
+        const uint32_t b_hi = smem_u32(st + 2 * A_BYTES), b_lo = smem_u32(st + 2 * A_BYTES + B_BYTES);
 #pragma unroll
-      for (int ks = 0; ks < TK / 8; ++ks) {
-        const uint32_t off = ks * 32;  // 8 fp32 = 32 bytes along K inside the swizzled row
-        const uint32_t acc = (kb > 0 || ks > 0) ? 1u : 0u;
-        mma_tf32(tmem, smem_desc_sw64(a_hi + off), smem_desc_sw64(b_hi + off), acc);
-        mma_tf32(tmem, smem_desc_sw64(a_hi + off), smem_desc_sw64(b_lo + off), 1u);
-        mma_tf32(tmem, smem_desc_sw64(a_lo + off), smem_desc_sw64(b_hi + off), 1u);
+        for (int ks = 0; ks < TK / 8; ++ks) {
+          const uint32_t off = ks * 32;
+          const uint32_t acc = (kb > 0 || ks > 0) ? 1u : 0u;
+          mma_tf32(acc_addr, smem_desc_sw64(a_hi + off), smem_desc_sw64(b_hi + off), acc);
+          mma_tf32(acc_addr, smem_desc_sw64(a_hi + off), smem_desc_sw64(b_lo + off), 1u);
+          mma_tf32(acc_addr, smem_desc_sw64(a_lo + off), smem_desc_sw64(b_hi + off), 1u);
+        }
+        mma_commit(&empty_bar[s]);
       }
-      mma_commit(&empty_bar[s]);
+      if (!ok) {
+        s_fail = 1;
+        break;
+      }
+      mma_commit(&acc_full[buf]);  // arrives when this tile's MMAs have completed
     }
-    if (!ok) s_fail = 1;
     mma_commit(&done_bar);  // arrives once every MMA issued above has completed
-  }
-  __syncwarp();
-  // epilogue: warp w owns TMEM lanes [32w, 32w+32) = rows m0 + 32w + lane
-  const bool done = mbar_wait(&done_bar, 0, err, 3);
-  if (!done) s_fail = 1;  // make the epilogue decision uniform across the CTA
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (s_fail == 0) {
-    // Every MMA has completed, so the stage buffers are free: warp w stages its
-    // -D chunks in two 4 KB buffers at base + 8 KB * w.
-    float* stg = (float*)(base + (size_t)warp * 8192);
-    const bool rows_live = m0 + warp * 32 < M2;
-    for (int cc = 0; cc < TN / 32; ++cc) {
-      float v[32];
-      tmem_ld_32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cc * 32), v);
-      const int col = n0 + cc * 32;
-      if (!rows_live || col >= N) continue;  // warp-uniform; columns only grow with cc
-      float* buf = stg + (cc & 1) * 1024;
-      // the group that last read this buffer (chunk cc - 2) must be done reading
-      if (lane == 0) bulk_wait_read<1>();
-      __syncwarp();
-#pragma unroll
-      for (int j = 0; j < 32; ++j) buf[j * 32 + lane] = -v[j];
-      fence_async_smem();
-      __syncwarp();
-      if (lane == 0) {
-        tma_reduce_add_3d(&map_c, buf, x0 + m0 + warp * 32, y0 + col, bz);
-        bulk_commit();
+  } else if (warp >= 2) {
+    // epilogue: TMEM lane quarter q = warp % 4 holds rows m0 + 32 q .. + 31
+    const int q = warp & 3;
+    float* stg = (float*)(base + P_STAGE_AREA + (size_t)(warp - 2) * 8192);
+    int chunk = 0, local = 0;
+    for (int t = blockIdx.x; t < n_tiles && !s_fail; t += gridDim.x, ++local) {
+      const int buf = local & 1;
+      if (!mbar_wait(&acc_full[buf], (local >> 1) & 1, err, 3)) {
+        s_fail = 1;
+        break;
       }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int bz = t / per_matrix, rem = t - bz * per_matrix;
+      const int m0 = (rem % tiles_m) * TM, n0 = (rem / tiles_m) * TN;
+      const bool rows_live = m0 + q * 32 < M2;
+      for (int cc = 0; cc < TN / 32; ++cc) {
+        float v[32];
+        tmem_ld_32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * TN + cc * 32), v);
+        const int col = n0 + cc * 32;
+        if (!rows_live || col >= N) continue;  // warp-uniform
+        float* sb = stg + (chunk & 1) * 1024;
+        // the group that last read this buffer (two chunks ago) must be done reading
+        if (lane == 0) bulk_wait_read<1>();
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < 32; ++j) sb[j * 32 + lane] = -v[j];
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+          tma_reduce_add_3d(&map_c, sb, x0 + m0 + q * 32, y0 + col, bz);
+          bulk_commit();
+        }
+        ++chunk;
+      }
+      // this warp has read its quarter of the accumulator: the MMA warp may reuse it
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[buf])) : "memory");
     }
     if (lane == 0) bulk_wait_read<0>();
     __syncwarp();
-  } else if (threadIdx.x == 0) {
-    // drain: wait (bounded) for any TMA copies this CTA started
-    for (int s = 0; s < STAGES; ++s) mbar_wait(&full_bar[s], 0, err, 4);
+  }
+  __syncwarp();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // every MMA this CTA issued has completed before TMEM is released
+    mbar_wait(&done_bar, 0, err, 6);
+    // loads started but never consumed (only after a failure): wait for them (bounded)
+    for (int j = max(s_consumed, issued - P_STAGES); j < issued; ++j)
+      mbar_wait(&full_bar[j % P_STAGES], (j / P_STAGES) & 1, err, 4);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(P_TMEM_COLS));
+}
+
+// Number of SMs of the current device (the persistent grid), cached per device.
+int sm_count() {
+  static int cached[16] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 16) dev = 0;
+  if (cached[dev] == 0) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cached[dev] = n > 0 ? n : 1;
+  }
+  return cached[dev];
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -481,11 +511,13 @@ cudaError_t tc_update(TcGemmPlan* p, float2* A, long long lda, long long strideA
     prep_ab_kernel<<<g, 256, 0, stream>>>(A, lda, strideA, row0, col0, kcol0, M, N, K, p->rows_pad, p->cols_pad,
                                           rows_used, cols_used, kp, nta, p->ahi, p->alo, p->bhi, p->blo);
   }
-  const size_t smem = (size_t)STAGES * STAGE_BYTES + 1024;
-  if (!ensure_smem_limit((const void*)trailing_update_tf32x3, smem)) return cudaErrorInvalidValue;
-  dim3 grid(rows_used / TM, cols_used / TN, p->batch);
-  trailing_update_tf32x3<<<grid, 128, smem, stream>>>(p->mahi, p->malo, p->mbhi, p->mblo, p->mc, 2 * row0, col0, M2, N,
-                                                     kp / TK, p->err);
+  const int tiles_m = rows_used / TM, tiles_n = cols_used / TN;
+  const long long n_tiles = (long long)tiles_m * tiles_n * p->batch;
+  if (!ensure_smem_limit((const void*)trailing_update_tf32x3_persistent, P_SMEM)) return cudaErrorInvalidValue;
+  const int grid = (int)std::min<long long>(n_tiles, sm_count());
+  trailing_update_tf32x3_persistent<<<grid, P_THREADS, P_SMEM, stream>>>(
+      p->mahi, p->malo, p->mbhi, p->mblo, p->mc, 2 * row0, col0, M2, N, kp / TK, tiles_m, tiles_n, (int)n_tiles,
+      p->err);
   return cudaGetLastError();
 }
 
