@@ -87,9 +87,10 @@ struct bem_context {
   cudaMemPool_t pool = nullptr;
   DevBuf rext, mats, mats2, ipiv, perm, info, sblocks, rb, b32, b64, x64, r64, d32, fsrc, fout, norms, pout, tcws, rowmap;
   DevBuf ftrace_p, ftrace_q, fpoints;  // bem_evaluate_field: boundary traces and points
+  DevBuf xsplit;                       // the refinement's x as float hi / lo pairs
   std::vector<DevBuf*> scratch() {
     return {&rext, &mats, &mats2, &ipiv, &perm, &info, &sblocks, &rb, &b32, &b64, &x64, &r64, &d32, &fsrc, &fout, &norms,
-            &pout, &tcws, &rowmap, &ftrace_p, &ftrace_q, &fpoints};
+            &pout, &tcws, &rowmap, &ftrace_p, &ftrace_q, &fpoints, &xsplit};
   }
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   void* stage = nullptr;  // pinned host staging of mesh uploads (grown on demand)
@@ -761,6 +762,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       ck(ctx->x64.ensure(vecn * sizeof(double2)), "alloc x");
       ck(ctx->r64.ensure(vecn * sizeof(double2)), "alloc r");
       ck(ctx->d32.ensure(vecn * sizeof(float2)), "alloc d");
+      ck(ctx->xsplit.ensure(vecn * sizeof(float4)), "alloc x split");
       ck(ctx->norms.ensure((size_t)B * nc * 2 * sizeof(double)), "alloc norms");
     }
     if (field_out) {
@@ -840,7 +842,8 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
         int steps = 0;
         double worst = 0;
         for (;;) {
-          ck(bem::residual_batched(prec, ctx->mats2.p, L.lda, nv, bt, x, b64, L.ldb, nc, r, ctx->stream), "residual");
+          ck(bem::residual_batched(prec, ctx->mats2.p, L.lda, nv, bt, x, b64, L.ldb, nc, r, ctx->xsplit.p, ctx->stream),
+             "residual");
           ck(bem::norms_batched(r, b64, L.ldb, nv, bt * nc, (double*)ctx->norms.p, ctx->stream), "norms");
           ck(cudaMemcpyAsync(norms.data(), ctx->norms.p, (size_t)bt * nc * 2 * sizeof(double), cudaMemcpyDeviceToHost,
                              ctx->stream),
@@ -861,7 +864,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
         }
         max_steps = std::max(max_steps, steps);
         max_res = std::max(max_res, worst);
-        launches += 5 + 5LL * steps;
+        launches += 6 + 6LL * steps;  // 3 + (x split, residual, norms) per check + (convert, solve, axpy) per step
       }
       prof_mark(ctx, BEM_K_SOLVE);
       cudaEventRecord(ctx->ev[2], ctx->stream);

@@ -127,7 +127,7 @@ cudaError_t lu_solve_batched(Precision prec, const void* LU, long long lda, int 
                              void* B, long long ldb, int nrhs, int nb, cudaStream_t stream);
 // r = b - A x in FP64 arithmetic: A (complex64 or complex128), x, b, r complex128.
 cudaError_t residual_batched(Precision prec, const void* A, long long lda, int n, int batch, const double2* x,
-                             const double2* b, long long ldb, int nrhs, double2* r, cudaStream_t stream);
+                             const double2* b, long long ldb, int nrhs, double2* r, void* xsplit, cudaStream_t stream);
 // Per (matrix, rhs): out[2*i] = ||r_i||^2 and out[2*i+1] = ||b_i||^2.
 cudaError_t norms_batched(const double2* r, const double2* b, long long ldb, int n, int count, double* out,
                           cudaStream_t stream);

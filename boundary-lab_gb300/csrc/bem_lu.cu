@@ -390,47 +390,80 @@ __device__ __forceinline__ void acc_exact_prod(float& sh, float& sl, float& e, f
   e = fmaf(a, xl, e + pe);
 }
 
+// x (FP64) as float hi / lo pairs (re hi, im hi, re lo, im lo), once per residual,
+// so the residual kernel below runs no FP64 instruction in its inner loop.
+__global__ void split_x_kernel(const double2* __restrict__ x, float4* __restrict__ xs, long long count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const double2 v = x[i];
+  const float hr = (float)v.x, hi = (float)v.y;
+  xs[i] = make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
+}
+
+// r = b - A x with A in FP32 and x in FP64: every product a * (x_hi + x_lo) is
+// formed exactly (two FMAs) and summed in double-float, so r carries the
+// accuracy of an FP64 product with the FP32 matrix.  A CTA covers 64 rows; its
+// four groups of 64 threads take interleaved 64-column slices of each
+// 256-column block of x staged in shared memory, each thread keeping two
+// independent double-float sums (even / odd columns).  The four partial sums of
+// a row are added in a fixed order at the end (deterministic).
 __global__ void __launch_bounds__(256) residual_f32a_kernel(const float2* __restrict__ A, long long lda,
-                                                            long long strideA, int n, const double2* __restrict__ x,
+                                                            long long strideA, int n, const float4* __restrict__ xs,
                                                             const double2* __restrict__ b, long long ldb, int nrhs,
                                                             double2* __restrict__ r) {
-  __shared__ float4 xs[256];
-  const int row = blockIdx.x * 256 + threadIdx.x;
+  __shared__ float4 xsh[256];
+  __shared__ double part[2][4][64];
+  const int rl = threadIdx.x & 63, cg = threadIdx.x >> 6;
+  const int row = blockIdx.x * 64 + rl;
   const int mat = blockIdx.y / nrhs, rhs = blockIdx.y % nrhs;
   const float2* M = A + (size_t)mat * strideA;
   const size_t off = ((size_t)mat * nrhs + rhs) * ldb;
-  const double2* xv = x + off;
-  double accr = 0.0, acci = 0.0;
+  const float4* xv = xs + off;
+  float srh = 0.f, srl = 0.f, er = 0.f, sih = 0.f, sil = 0.f, ei = 0.f;      // even columns
+  float trh = 0.f, trl = 0.f, fr = 0.f, tih = 0.f, til = 0.f, fi = 0.f;      // odd columns
   for (int j0 = 0; j0 < n; j0 += 256) {
     __syncthreads();
     {
       const int j = j0 + threadIdx.x;
-      if (j < n) {
-        const double2 v = xv[j];
-        const float hr = (float)v.x, hi = (float)v.y;
-        xs[threadIdx.x] = make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
-      }
+      xsh[threadIdx.x] = j < n ? xv[j] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
-    if (row < n) {
-      const int jn = min(256, n - j0);
-      const float2* col = M + (size_t)j0 * lda + row;
-      float srh = 0.f, srl = 0.f, er = 0.f, sih = 0.f, sil = 0.f, ei = 0.f;
-#pragma unroll 8
-      for (int t = 0; t < jn; ++t) {
-        const float2 a = col[(size_t)t * lda];
-        const float4 xt = xs[t];
+    const int cb = j0 + cg * 64;
+    const int jn = min(64, n - cb);
+    if (row < n && jn > 0) {
+      const float2* col = M + (size_t)cb * lda + row;
+      const float4* xg = xsh + cg * 64;
+      int t = 0;
+#pragma unroll 4
+      for (; t + 1 < jn; t += 2) {
+        const float2 a0 = col[(size_t)t * lda], a1 = col[(size_t)(t + 1) * lda];
+        const float4 x0 = xg[t], x1 = xg[t + 1];
         // re += a.x xr - a.y xi ; im += a.x xi + a.y xr
-        acc_exact_prod(srh, srl, er, a.x, xt.x, xt.z);
-        acc_exact_prod(srh, srl, er, -a.y, xt.y, xt.w);
-        acc_exact_prod(sih, sil, ei, a.x, xt.y, xt.w);
-        acc_exact_prod(sih, sil, ei, a.y, xt.x, xt.z);
+        acc_exact_prod(srh, srl, er, a0.x, x0.x, x0.z);
+        acc_exact_prod(srh, srl, er, -a0.y, x0.y, x0.w);
+        acc_exact_prod(sih, sil, ei, a0.x, x0.y, x0.w);
+        acc_exact_prod(sih, sil, ei, a0.y, x0.x, x0.z);
+        acc_exact_prod(trh, trl, fr, a1.x, x1.x, x1.z);
+        acc_exact_prod(trh, trl, fr, -a1.y, x1.y, x1.w);
+        acc_exact_prod(tih, til, fi, a1.x, x1.y, x1.w);
+        acc_exact_prod(tih, til, fi, a1.y, x1.x, x1.z);
       }
-      accr += (double)srh + ((double)srl + (double)er);
-      acci += (double)sih + ((double)sil + (double)ei);
+      if (t < jn) {
+        const float2 a0 = col[(size_t)t * lda];
+        const float4 x0 = xg[t];
+        acc_exact_prod(srh, srl, er, a0.x, x0.x, x0.z);
+        acc_exact_prod(srh, srl, er, -a0.y, x0.y, x0.w);
+        acc_exact_prod(sih, sil, ei, a0.x, x0.y, x0.w);
+        acc_exact_prod(sih, sil, ei, a0.y, x0.x, x0.z);
+      }
     }
   }
-  if (row < n) {
+  part[0][cg][rl] = ((double)srh + ((double)srl + (double)er)) + ((double)trh + ((double)trl + (double)fr));
+  part[1][cg][rl] = ((double)sih + ((double)sil + (double)ei)) + ((double)tih + ((double)til + (double)fi));
+  __syncthreads();
+  if (cg == 0 && row < n) {
+    const double accr = ((part[0][0][rl] + part[0][1][rl]) + part[0][2][rl]) + part[0][3][rl];
+    const double acci = ((part[1][0][rl] + part[1][1][rl]) + part[1][2][rl]) + part[1][3][rl];
     const double2 bb = b[off + row];
     r[off + row] = make_double2(bb.x - accr, bb.y - acci);
   }
@@ -719,13 +752,18 @@ cudaError_t lu_solve_batched(Precision prec, const void* LU, long long lda, int 
 }
 
 cudaError_t residual_batched(Precision prec, const void* A, long long lda, int n, int batch, const double2* x,
-                             const double2* b, long long ldb, int nrhs, double2* r, cudaStream_t stream) {
+                             const double2* b, long long ldb, int nrhs, double2* r, void* xsplit, cudaStream_t stream) {
   const long long strideA = lda * (long long)n;
-  dim3 g((n + 255) / 256, batch * nrhs);
-  if (prec == Precision::Mixed)
-    residual_f32a_kernel<<<g, 256, 0, stream>>>((const float2*)A, lda, strideA, n, x, b, ldb, nrhs, r);
-  else
+  if (prec == Precision::Mixed) {
+    const long long count = (long long)batch * nrhs * ldb;
+    split_x_kernel<<<(unsigned)((count + 255) / 256), 256, 0, stream>>>(x, (float4*)xsplit, count);
+    dim3 g((n + 63) / 64, batch * nrhs);
+    residual_f32a_kernel<<<g, 256, 0, stream>>>((const float2*)A, lda, strideA, n, (const float4*)xsplit, b, ldb,
+                                                 nrhs, r);
+  } else {
+    dim3 g((n + 255) / 256, batch * nrhs);
     residual_kernel<double2><<<g, 256, 0, stream>>>((const double2*)A, lda, strideA, n, x, b, ldb, nrhs, r);
+  }
   return cudaGetLastError();
 }
 
