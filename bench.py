@@ -455,7 +455,7 @@ def main() -> None:
             e2e_times.append(time.perf_counter() - t0)
         result["e2e"] = {"value": B / statistics.median(e2e_times), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                          "d2h_bytes_per_step": int(d2h),
-                         "what": "per step: bem_upload_mesh (plan + FP64 singular moments) + excitation + points from "
+                         "what": "per step: bem_upload_mesh (plan + singular moments) + excitation + points from "
                                  "host arrays, bem_solve_frequencies of one batch with host output buffers"}
         # CPU baseline: the reference algorithm (FP32 restatement) on the host cores, bounded sample
         if args.cpu_baseline > 0:

@@ -659,74 +659,61 @@ struct SingularGeom {
 constexpr int kRecGeom = 0, kRecJac = 21, kRecNprod = 22, kRecA2 = 23, kRecCurl = 24, kRecS0 = 33, kRecMom = 34;
 static_assert(kRecMom + kStatic <= kPairRec, "pair record layout");
 
-__global__ void singular_static_kernel(SingularGeom geo, const SingularPair* __restrict__ pairs, int npairs,
-                                       const int* __restrict__ rule_ptr, const double* __restrict__ duffy,
-                                       const double* __restrict__ curls, const double* __restrict__ area,
-                                       double* __restrict__ moments, float* __restrict__ rec) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= npairs) return;
-  const SingularPair P = pairs[warp];
+// Double-float helpers of the moments kernel.
+__device__ __forceinline__ df to_df(double x) {
+  const float hi = (float)x;
+  return {hi, (float)(x - (double)hi)};
+}
+__device__ __forceinline__ double df_to_double(df a) { return (double)a.hi + (double)a.lo; }
+// 1 / sqrt(a) for a > 0: one Newton step in double-float on the FP32 approximate
+// reciprocal root (relative error about 2^-44).
+__device__ __forceinline__ df df_rsqrt(df a) {
+  const float y = rsqrt_ftz(a.hi);
+  const df y2 = two_prod(y, y);
+  const df ay2 = df_mul(a, y2);
+  const df res = df_sub(df{1.0f, 0.0f}, ay2);  // about 2^-22
+  return quick_two_sum(y, 0.5f * y * res.hi);
+}
+
+// Pair setup (one thread per pair, FP64): the pair's geometry as double-float
+// for the moments kernel, and the FP32 record fields that do not depend on the
+// moments (geometry, jac, n_t . S n_r, 2 A_test, curl products).
+//   pairgeo_df[p]: e1t e2t d0 e1r e2r n_test n_trial (21 double-floats = 42
+//   floats), jac (2 floats), padding.
+__global__ void pair_setup_kernel(SingularGeom geo, const SingularPair* __restrict__ pairs, int npairs,
+                                  const double* __restrict__ curls, const double* __restrict__ area,
+                                  float* __restrict__ geo_df, float* __restrict__ rec) {
+  const int pid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pid >= npairs) return;
+  const SingularPair P = pairs[pid];
   const int* ft = geo.faces + 3 * P.test;
   const int* fr = geo.faces + 3 * P.trial;
-  double t0[3], e1t[3], e2t[3], d0[3], e1r[3], e2r[3], nt[3], nr[3];
+  double g[21];
   for (int d = 0; d < 3; ++d) {
     // image pairs: the trial face reflected by P.tr (points and normal S p)
     const double sd = d == 0 ? tr_sign_x(P.tr) : d == 1 ? tr_sign_y(P.tr) : 1.0;
-    t0[d] = geo.verts[3 * ft[0] + d];
-    e1t[d] = geo.verts[3 * ft[1] + d] - t0[d];
-    e2t[d] = geo.verts[3 * ft[2] + d] - t0[d];
+    const double t0 = geo.verts[3 * ft[0] + d];
     const double r0 = sd * geo.verts[3 * fr[0] + d];
-    d0[d] = r0 - t0[d];
-    e1r[d] = sd * geo.verts[3 * fr[1] + d] - r0;
-    e2r[d] = sd * geo.verts[3 * fr[2] + d] - r0;
-    nt[d] = geo.normal[3 * P.test + d];
-    nr[d] = sd * geo.normal[3 * P.trial + d];
+    g[d] = geo.verts[3 * ft[1] + d] - t0;            // e1t
+    g[3 + d] = geo.verts[3 * ft[2] + d] - t0;        // e2t
+    g[6 + d] = r0 - t0;                               // d0
+    g[9 + d] = sd * geo.verts[3 * fr[1] + d] - r0;    // e1r
+    g[12 + d] = sd * geo.verts[3 * fr[2] + d] - r0;   // e2r
+    g[15 + d] = geo.normal[3 * P.test + d];           // n_test
+    g[18 + d] = sd * geo.normal[3 * P.trial + d];     // n_trial (reflected)
   }
-  double acc[kStatic];
-#pragma unroll
-  for (int i = 0; i < kStatic; ++i) acc[i] = 0.0;
-  const int q0 = rule_ptr[P.rule], q1 = rule_ptr[P.rule + 1];
-  for (int q = q0 + lane; q < q1; q += 32) {
-    const double* pt = duffy + 5 * (size_t)q;
-    const double tu = pt[0], tv = pt[1], ru = pt[2], rvv = pt[3], w = pt[4];
-    const double px[3] = {1.0 - tu - tv, tu, tv};
-    const double py[3] = {1.0 - ru - rvv, ru, rvv};
-    double rv[3];
-    for (int d = 0; d < 3; ++d) rv[d] = (d0[d] + ru * e1r[d] + rvv * e2r[d]) - (tu * e1t[d] + tv * e2t[d]);
-    const double r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
-    if (r2 == 0.0) continue;
-    const double rinv = rsqrt(r2);
-    const double s = rinv * (0.25 / CUDART_PI);
-    const double dny = -(rv[0] * nr[0] + rv[1] * nr[1] + rv[2] * nr[2]) * s * rinv * rinv;
-    const double dnx = (rv[0] * nt[0] + rv[1] * nt[1] + rv[2] * nt[2]) * s * rinv * rinv;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const double wa = w * px[a];
-      acc[a] += wa * s;
-      acc[21 + a] += wa * dnx;
-#pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        acc[3 + 3 * a + b] += wa * py[b] * s;
-        acc[12 + 3 * a + b] += wa * py[b] * dny;
-      }
-    }
+  float* G = geo_df + (size_t)kPairGeoDf * pid;
+  float* o = rec + (size_t)kPairRec * pid;
+  for (int i = 0; i < 21; ++i) {
+    const df v = to_df(g[i]);
+    G[2 * i] = v.hi;
+    G[2 * i + 1] = v.lo;
+    o[kRecGeom + i] = v.hi;
   }
-  double mom[kStatic];
-#pragma unroll
-  for (int i = 0; i < kStatic; ++i) mom[i] = warp_sum(acc[i]) * P.jac;
-  if (lane != 0) return;
-  for (int i = 0; i < kStatic; ++i) moments[(size_t)kStatic * warp + i] = mom[i];
-  float* o = rec + (size_t)kPairRec * warp;
-  for (int d = 0; d < 3; ++d) {
-    o[kRecGeom + d] = (float)e1t[d];
-    o[kRecGeom + 3 + d] = (float)e2t[d];
-    o[kRecGeom + 6 + d] = (float)d0[d];
-    o[kRecGeom + 9 + d] = (float)e1r[d];
-    o[kRecGeom + 12 + d] = (float)e2r[d];
-    o[kRecGeom + 15 + d] = (float)nt[d];
-    o[kRecGeom + 18 + d] = (float)nr[d];
-  }
+  const df jd = to_df(P.jac);
+  G[42] = jd.hi;
+  G[43] = jd.lo;
+  for (int i = 44; i < kPairGeoDf; ++i) G[i] = 0.0f;
   o[kRecJac] = (float)P.jac;
   o[kRecNprod] = (float)P.nprod;
   o[kRecA2] = (float)(2.0 * area[P.test]);
@@ -743,9 +730,98 @@ __global__ void singular_static_kernel(SingularGeom geo, const SingularPair* __r
     for (int b = 0; b < 3; ++b)
       o[kRecCurl + 3 * a + b] =
           (float)(ct[3 * a] * cr[3 * b] + ct[3 * a + 1] * cr[3 * b + 1] + ct[3 * a + 2] * cr[3 * b + 2]);
-  o[kRecS0] = (float)(mom[0] + mom[1] + mom[2]);
-  for (int i = 0; i < kStatic; ++i) o[kRecMom + i] = (float)mom[i];
   for (int i = kRecMom + kStatic; i < kPairRec; ++i) o[i] = 0.0f;
+}
+
+// The 24 k-independent moments of a pair (one warp per pair, lanes over the
+// Duffy points), in double-float arithmetic on the FP32 pipe: every product,
+// sum, the reciprocal root and the accumulation carry about 44 bits, which is
+// FP64 accuracy for these sums at the FP32 rate (this part's FP64 rate is
+// 1/64 of it).  Lane i < 24 then writes moment i = jac * sum_i in FP64 and its
+// float copy into the pair record; lane 0 also writes the record's S0 term.
+__global__ void __launch_bounds__(256)
+    singular_moments_df_kernel(const SingularPair* __restrict__ pairs, int npairs, const int* __restrict__ rule_ptr,
+                               const float* __restrict__ duffy_df, const float* __restrict__ geo_df,
+                               double* __restrict__ moments, float* __restrict__ rec) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= npairs) return;
+  const SingularPair P = pairs[warp];
+  const float* G = geo_df + (size_t)kPairGeoDf * warp;
+  df g[21];
+#pragma unroll
+  for (int i = 0; i < 21; ++i) g[i] = df{__ldg(G + 2 * i), __ldg(G + 2 * i + 1)};
+  const df* e1t = g;
+  const df* e2t = g + 3;
+  const df* d0 = g + 6;
+  const df* e1r = g + 9;
+  const df* e2r = g + 12;
+  const df* nt = g + 15;
+  const df* nr = g + 18;
+  const df inv4pi = {7.95774683356285095215e-02f, 3.21031911247035257e-09f};  // 1/(4 pi) as hi + lo
+  df acc[kStatic];
+#pragma unroll
+  for (int i = 0; i < kStatic; ++i) acc[i] = df{0.0f, 0.0f};
+  const df one = {1.0f, 0.0f};
+  const int q0 = rule_ptr[P.rule], q1 = rule_ptr[P.rule + 1];
+  for (int q = q0 + lane; q < q1; q += 32) {
+    const float* pt = duffy_df + 10 * (size_t)q;
+    const df tu = {pt[0], pt[1]}, tv = {pt[2], pt[3]}, ru = {pt[4], pt[5]}, rvv = {pt[6], pt[7]}, w = {pt[8], pt[9]};
+    const df px[3] = {df_sub(df_sub(one, tu), tv), tu, tv};
+    const df py[3] = {df_sub(df_sub(one, ru), rvv), ru, rvv};
+    df rv[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const df yr = df_add(df_add(d0[d], df_mul(ru, e1r[d])), df_mul(rvv, e2r[d]));
+      const df xt = df_add(df_mul(tu, e1t[d]), df_mul(tv, e2t[d]));
+      rv[d] = df_sub(yr, xt);
+    }
+    const df r2 = df_add(df_add(df_mul(rv[0], rv[0]), df_mul(rv[1], rv[1])), df_mul(rv[2], rv[2]));
+    if (r2.hi == 0.0f) continue;
+    const df rinv = df_rsqrt(r2);
+    const df s = df_mul(rinv, inv4pi);
+    const df srr = df_mul(s, df_mul(rinv, rinv));
+    const df dotn_r = df_add(df_add(df_mul(rv[0], nr[0]), df_mul(rv[1], nr[1])), df_mul(rv[2], nr[2]));
+    const df dotn_t = df_add(df_add(df_mul(rv[0], nt[0]), df_mul(rv[1], nt[1])), df_mul(rv[2], nt[2]));
+    const df ws = df_mul(w, s);
+    const df wd = df_neg(df_mul(w, df_mul(dotn_r, srr)));  // w dG0/dn_y
+    const df wn = df_mul(w, df_mul(dotn_t, srr));           // w dG0/dn_x
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const df was = df_mul(ws, px[a]);
+      const df wad = df_mul(wd, px[a]);
+      acc[a] = df_add(acc[a], was);
+      acc[21 + a] = df_add(acc[21 + a], df_mul(wn, px[a]));
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        acc[3 + 3 * a + b] = df_add(acc[3 + 3 * a + b], df_mul(was, py[b]));
+        acc[12 + 3 * a + b] = df_add(acc[12 + 3 * a + b], df_mul(wad, py[b]));
+      }
+    }
+  }
+  // butterfly reduction: every lane ends with every sum
+#pragma unroll
+  for (int i = 0; i < kStatic; ++i) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const df other = {__shfl_xor_sync(0xffffffffu, acc[i].hi, o), __shfl_xor_sync(0xffffffffu, acc[i].lo, o)};
+      acc[i] = df_add(acc[i], other);
+    }
+  }
+  double mine = 0.0;
+#pragma unroll
+  for (int i = 0; i < kStatic; ++i)
+    if (lane == i) mine = df_to_double(acc[i]) * P.jac;
+  float* o = rec + (size_t)kPairRec * warp;
+  if (lane < kStatic) {
+    moments[(size_t)kStatic * warp + lane] = mine;
+    o[kRecMom + lane] = (float)mine;
+  }
+  if (lane == 0) {
+    const double m0 = df_to_double(acc[0]) * P.jac, m1 = df_to_double(acc[1]) * P.jac,
+                 m2 = df_to_double(acc[2]) * P.jac;
+    o[kRecS0] = (float)(m0 + m1 + m2);
+  }
 }
 
 template <typename R> struct SingParams;
@@ -1421,10 +1497,12 @@ cudaError_t launch_regular_f64(const DeviceMesh& m, double k, double2 cD, double
 cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, float* pairrec, cudaStream_t stream) {
   if (m.npairs == 0) return cudaSuccess;
   SingularGeom geo{m.verts, m.faces, m.normal};
+  pair_setup_kernel<<<(m.npairs + 127) / 128, 128, 0, stream>>>(geo, m.pairs, m.npairs, m.curls, m.area, m.pairgeo_df,
+                                                                pairrec);
   const int threads = 256;
   const int blocks = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
-  singular_static_kernel<<<blocks, threads, 0, stream>>>(geo, m.pairs, m.npairs, m.rule_ptr, m.duffy, m.curls, m.area,
-                                                         moments, pairrec);
+  singular_moments_df_kernel<<<blocks, threads, 0, stream>>>(m.pairs, m.npairs, m.rule_ptr, m.duffy_df, m.pairgeo_df,
+                                                             moments, pairrec);
   return cudaGetLastError();
 }
 

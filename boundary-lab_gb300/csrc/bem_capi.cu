@@ -463,6 +463,12 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
         if (P.col_ptr[v] == P.col_ptr[v + 1]) iso.push_back(v);
       d.n_isolated = (int)iso.size();
       const std::vector<float> duffy32(P.duffy.begin(), P.duffy.end());
+      std::vector<float> duffy_df(2 * P.duffy.size());
+      for (size_t i = 0; i < P.duffy.size(); ++i) {
+        const float hi = (float)P.duffy[i];
+        duffy_df[2 * i] = hi;
+        duffy_df[2 * i + 1] = (float)(P.duffy[i] - (double)hi);
+      }
       std::vector<double> mm(12);
       for (int i = 0; i < 9; ++i) mm[i] = P.m11[i];
       for (int i = 0; i < 3; ++i) mm[9 + i] = P.m10[i];
@@ -493,6 +499,7 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
       pack.add(d.rule_ptr, P.rule_ptr);
       pack.add(d.duffy, P.duffy);
       pack.add(d.duffy32, duffy32);
+      pack.add(d.duffy_df, duffy_df);
       pack.add(d.verts, P.verts);
       pack.add(d.faces, P.faces);
       pack.add(d.normal, P.normal);
@@ -514,6 +521,7 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
       if (d.npairs > 0) {
         d.moments = (double*)mesh_alloc(m, (size_t)d.npairs * 24 * sizeof(double), "allocate singular moments");
         d.pairrec = (float*)mesh_alloc(m, (size_t)d.npairs * bem::kPairRec * sizeof(float), "allocate pair records");
+        d.pairgeo_df = (float*)mesh_alloc(m, (size_t)d.npairs * bem::kPairGeoDf * sizeof(float), "allocate pair geometry");
       }
       ck(cudaStreamSynchronize(ctx->stream), "mesh upload");
       if (d.npairs > 0) {
@@ -713,7 +721,7 @@ long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int np
   const long long group = precision == BEM_PRECISION_MIXED ? 2 : 1;        // frequencies assembled together
   bytes += round_up(n_ext, 32) * 3LL * nf * esz * group;                    // extended rows
   bytes += (long long)batch * lda * nv * esz * (precision == BEM_PRECISION_MIXED ? 2 : 1);  // matrices (+copy)
-  bytes += (long long)npairs * (12 * esz * group + 24 * 8 + 48 + bem::kPairRec * 4);  // singular blocks, moments, pairs, records
+  bytes += (long long)npairs * (12 * esz * group + 24 * 8 + 48 + (bem::kPairRec + bem::kPairGeoDf) * 4);  // singular blocks, moments, pairs, records
   bytes += (long long)batch * nrhs * lda * (esz + 3 * 16 + 16);             // rhs, x, r, b64, d
   bytes += (long long)batch * nrhs * ((long long)nf * 6 * esz + (long long)npts * 16);  // field sources + out
   bytes += (long long)nf * (2 * 160 + 288 + 64);                            // face records (+ lane-group copy), maps

@@ -54,6 +54,8 @@ struct DeviceMesh {
   int* rule_ptr = nullptr;
   double* duffy = nullptr;
   float* duffy32 = nullptr;  // the same table rounded to float (mixed form)
+  float* duffy_df = nullptr;  // the same table as double-float (hi, lo) pairs: 10 floats per point
+  float* pairgeo_df = nullptr;  // npairs x kPairGeoDf: per-pair geometry as double-float (moments kernel)
   double* moments = nullptr;
   float* pairrec = nullptr;  // npairs x kPairRec: FP32 record of each pair for the mixed-form singular kernel
   double* verts = nullptr;
@@ -85,8 +87,9 @@ cudaError_t launch_regular(const DeviceMesh& m, Precision prec, int nfreq, const
 int regular_launches(Precision prec, int nfreq);
 cudaError_t launch_regular_f64(const DeviceMesh& m, double k, double2 cD, double2 cH, double2* Rext, long long ldR,
                                cudaStream_t stream);
-// Per-pair FP32 record written by the FP64 moments kernel (see bem_assembly.cu).
+// Per-pair FP32 record written at upload by the pair setup and moments kernels (see bem_assembly.cu).
 constexpr int kPairRec = 64;
+constexpr int kPairGeoDf = 48;
 cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, float* pairrec, cudaStream_t stream);
 cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, double k, const OperatorCoeffs& c, void* blocks,
                                 cudaStream_t stream);
