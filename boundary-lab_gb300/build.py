@@ -58,7 +58,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
         obj = BUILD / (Path(src).stem + ".o")
         objects.append(obj)
         if force or _stale(obj, [CSRC / src, *headers]):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-c", str(CSRC / src), "-o", str(obj)])
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-c", str(CSRC / src), "-o", str(obj)])
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as pool:
             results = list(pool.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs))
@@ -69,7 +69,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
                 raise RuntimeError(f"build step failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
     if force or jobs or _stale(LIBRARY, objects):
         tmp = LIBRARY.with_suffix(f".so.tmp{os.getpid()}")
-        cmd = [nvcc, "-shared", *ARCH, "-o", str(tmp), *map(str, objects), "-lcublas"]
+        cmd = [nvcc, "-shared", *ARCH, "-o", str(tmp), *map(str, objects), "-lcublas", "-lpthread"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")

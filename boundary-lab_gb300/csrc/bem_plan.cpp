@@ -26,6 +26,7 @@
 #include <cstddef>
 #include <cstring>
 #include <numeric>
+#include <thread>
 
 namespace bem {
 namespace {
@@ -170,6 +171,29 @@ Adjacency classify(const int* fa, const int* fb) {
   }
   if (n == 1) return {3, sa[0], 0, sb[0], 0};
   return {0, 0, 0, 0, 0};
+}
+
+// Worker threads of the planner's parallel loops: the hardware threads, at most
+// 8; one for meshes too small to gain from it.
+int plan_threads(int nf) {
+  const unsigned hc = std::thread::hardware_concurrency();
+  if (nf < 2000) return 1;
+  return (int)std::max(1u, std::min(hc ? hc : 1u, 8u));
+}
+
+// f(begin, end, slice) over T contiguous slices of [0, n), on T threads (the
+// calling thread takes the first slice).
+template <class F>
+void parallel_slices(long long n, int T, F&& f) {
+  if (T <= 1) {
+    f(0, n, 0);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(T - 1);
+  for (int i = 1; i < T; ++i) th.emplace_back([&f, n, T, i]() { f(n * i / T, n * (i + 1) / T, i); });
+  f(0, n / T, 0);
+  for (auto& x : th) x.join();
 }
 
 // Recursive coordinate bisection of face centroids into leaves of <= cap faces.
@@ -436,67 +460,76 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
   std::vector<double> cent(3 * (size_t)nf);
   P.faces32.resize(nf);
   P.faces64.resize(nf);
-  for (int f = 0; f < nf; ++f) {
-    V3 v[3];
-    for (int a = 0; a < 3; ++a)
-      for (int d = 0; d < 3; ++d) v[a][d] = verts[3 * faces[3 * f + a] + d];
-    V3 e1 = sub(v[1], v[0]), e2 = sub(v[2], v[0]);
-    V3 cp = cross(e1, e2);
-    double nn = std::sqrt(dot(cp, cp));
-    if (!(nn > 0.0)) return "mesh contains a degenerate (zero-area) triangle";
-    V3 n = {cp[0] / nn, cp[1] / nn, cp[2] / nn};
-    P.area[f] = nn / 2.0;
-    double g11 = dot(e1, e1), g12 = dot(e1, e2), g22 = dot(e2, e2);
-    double det = g11 * g22 - g12 * g12;
-    double i11 = g22 / det, i12 = -g12 / det, i22 = g11 / det;
-    const double rg[3][2] = {{-1.0, -1.0}, {1.0, 0.0}, {0.0, 1.0}};
-    V3 curl[3];
-    for (int a = 0; a < 3; ++a) {
-      double c1 = i11 * rg[a][0] + i12 * rg[a][1], c2 = i12 * rg[a][0] + i22 * rg[a][1];
-      V3 g = {e1[0] * c1 + e2[0] * c2, e1[1] * c1 + e2[1] * c2, e1[2] * c1 + e2[2] * c2};
-      curl[a] = cross(n, g);
-    }
-    V3 c = {(v[0][0] + v[1][0] + v[2][0]) / 3.0, (v[0][1] + v[1][1] + v[2][1]) / 3.0,
-            (v[0][2] + v[1][2] + v[2][2]) / 3.0};
-    for (int d = 0; d < 3; ++d) {
-      cent[3 * f + d] = c[d];
-      P.normal[3 * f + d] = n[d];
-    }
-    for (int a = 0; a < 3; ++a)
-      for (int d = 0; d < 3; ++d) P.curls[9 * f + 3 * a + d] = curl[a][d];
+  const int Tg = plan_threads(nf);
+  std::vector<char> degenerate(Tg, 0);
+  parallel_slices(nf, Tg, [&](long long fb, long long fe, int ti) {
+    for (int f = (int)fb; f < (int)fe; ++f) {
+      V3 v[3];
+      for (int a = 0; a < 3; ++a)
+        for (int d = 0; d < 3; ++d) v[a][d] = verts[3 * faces[3 * f + a] + d];
+      V3 e1 = sub(v[1], v[0]), e2 = sub(v[2], v[0]);
+      V3 cp = cross(e1, e2);
+      double nn = std::sqrt(dot(cp, cp));
+      if (!(nn > 0.0)) {
+        degenerate[ti] = 1;
+        return;
+      }
+      V3 n = {cp[0] / nn, cp[1] / nn, cp[2] / nn};
+      P.area[f] = nn / 2.0;
+      double g11 = dot(e1, e1), g12 = dot(e1, e2), g22 = dot(e2, e2);
+      double det = g11 * g22 - g12 * g12;
+      double i11 = g22 / det, i12 = -g12 / det, i22 = g11 / det;
+      const double rg[3][2] = {{-1.0, -1.0}, {1.0, 0.0}, {0.0, 1.0}};
+      V3 curl[3];
+      for (int a = 0; a < 3; ++a) {
+        double c1 = i11 * rg[a][0] + i12 * rg[a][1], c2 = i12 * rg[a][0] + i22 * rg[a][1];
+        V3 g = {e1[0] * c1 + e2[0] * c2, e1[1] * c1 + e2[1] * c2, e1[2] * c1 + e2[2] * c2};
+        curl[a] = cross(n, g);
+      }
+      V3 c = {(v[0][0] + v[1][0] + v[2][0]) / 3.0, (v[0][1] + v[1][1] + v[2][1]) / 3.0,
+              (v[0][2] + v[1][2] + v[2][2]) / 3.0};
+      for (int d = 0; d < 3; ++d) {
+        cent[3 * f + d] = c[d];
+        P.normal[3 * f + d] = n[d];
+      }
+      for (int a = 0; a < 3; ++a)
+        for (int d = 0; d < 3; ++d) P.curls[9 * f + 3 * a + d] = curl[a][d];
 
-    FaceF32& F = P.faces32[f];
-    FaceF64& G = P.faces64[f];
-    std::fill((float*)&F, (float*)&F + 40, 0.0f);
-    std::fill((double*)&G, (double*)&G + sizeof(FaceF64) / 8, 0.0);
-    for (int d = 0; d < 3; ++d) {
-      F.anchor_hi[d] = (float)c[d];
-      F.anchor_lo[d] = (float)(c[d] - (double)F.anchor_hi[d]);
-      F.normal[d] = (float)n[d];
-      G.anchor[d] = c[d];
-      G.normal[d] = n[d];
-    }
-    F.area2 = (float)nn;
-    G.area2 = nn;
-    for (int a = 0; a < 3; ++a)
+      FaceF32& F = P.faces32[f];
+      FaceF64& G = P.faces64[f];
+      std::fill((float*)&F, (float*)&F + 40, 0.0f);
+      std::fill((double*)&G, (double*)&G + sizeof(FaceF64) / 8, 0.0);
       for (int d = 0; d < 3; ++d) {
-        F.curls[3 * a + d] = (float)curl[a][d];
-        G.curls[3 * a + d] = curl[a][d];
+        F.anchor_hi[d] = (float)c[d];
+        F.anchor_lo[d] = (float)(c[d] - (double)F.anchor_hi[d]);
+        F.normal[d] = (float)n[d];
+        G.anchor[d] = c[d];
+        G.normal[d] = n[d];
       }
-    for (int q = 0; q < Q; ++q) {
-      double u = P.rule_pts[2 * q], w2 = P.rule_pts[2 * q + 1];
-      for (int d = 0; d < 3; ++d) {
-        // quadrature point as in local_to_global (BeatEngineCore.jl:678-681)
-        double x = (1.0 - u - w2) * v[0][d] + u * v[1][d] + w2 * v[2][d];
-        F.off[3 * q + d] = (float)(x - c[d]);
-        G.off[3 * q + d] = x - c[d];
+      F.area2 = (float)nn;
+      G.area2 = nn;
+      for (int a = 0; a < 3; ++a)
+        for (int d = 0; d < 3; ++d) {
+          F.curls[3 * a + d] = (float)curl[a][d];
+          G.curls[3 * a + d] = curl[a][d];
+        }
+      for (int q = 0; q < Q; ++q) {
+        double u = P.rule_pts[2 * q], w2 = P.rule_pts[2 * q + 1];
+        for (int d = 0; d < 3; ++d) {
+          // quadrature point as in local_to_global (BeatEngineCore.jl:678-681)
+          double x = (1.0 - u - w2) * v[0][d] + u * v[1][d] + w2 * v[2][d];
+          F.off[3 * q + d] = (float)(x - c[d]);
+          G.off[3 * q + d] = x - c[d];
+        }
+      }
+      for (int a = 0; a < 3; ++a) {
+        F.verts[a] = faces[3 * f + a];
+        G.verts[a] = faces[3 * f + a];
       }
     }
-    for (int a = 0; a < 3; ++a) {
-      F.verts[a] = faces[3 * f + a];
-      G.verts[a] = faces[3 * f + a];
-    }
-  }
+  });
+  for (char d : degenerate)
+    if (d) return "mesh contains a degenerate (zero-area) triangle";
 
   // ---- test-face tiles by recursive coordinate bisection
   std::vector<int> order(nf);
@@ -668,74 +701,117 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
     for (int a = 0; a < 3; ++a) v2f[faces[3 * f + a]].push_back(f);
   std::vector<DPoint> base[4];
   for (int k = 1; k <= 3; ++k) base[k] = duffy_base(singular_order, k);
-  // rule id of an adjacency key (kind, ta, tb, ra, rb; every field < 4), numbered in
-  // order of first appearance; -1 until seen
+  // Candidate pairs, enumerated over (transform, test face) in order.  The index
+  // range is cut into contiguous slices enumerated by worker threads; each slice
+  // keeps its pairs in order with their adjacency keys (kind, ta, tb, ra, rb;
+  // every field < 4), and the rules are then numbered in order of first
+  // appearance over the slices in order, so the result does not depend on the
+  // number of threads.
+  const int ntr = (int)P.transforms.size();
+  const long long n_idx = (long long)ntr * nf;
+  const int T = plan_threads(nf);
+  struct Slice {
+    std::vector<SingularPair> pairs;
+    std::vector<short> keys;
+    int image_pairs = 0;
+  };
+  std::vector<Slice> slices(T);
+  parallel_slices(n_idx, T, [&](long long b, long long e, int ti) {
+    Slice& sl = slices[ti];
+    sl.pairs.reserve((size_t)(16 * (e - b)));
+    sl.keys.reserve((size_t)(16 * (e - b)));
+    std::vector<long long> seen(nf, -1);  // candidate stamp: the index that last listed the face
+    std::vector<int> cand;
+    for (long long idx = b; idx < e; ++idx) {
+      const int tr = P.transforms[(int)(idx / nf)];
+      const int t = (int)(idx % nf);
+      cand.clear();
+      for (int a = 0; a < 3; ++a) {
+        const int v = faces[3 * t + a];
+        if (tr != 0 && (P.fix_mask[v] & tr) != tr) continue;  // images touch the test face only on the planes
+        for (int r : v2f[v])
+          if (seen[r] != idx) {
+            seen[r] = idx;
+            cand.push_back(r);
+          }
+      }
+      for (int r : cand) {
+        Adjacency adj = tr == 0 ? classify(&faces[3 * t], &faces[3 * r])
+                                : classify_image(&faces[3 * t], &faces[3 * r], P.fix_mask, tr);
+        if (adj.kind == 0) continue;
+        const int key = adj.kind == 1 ? 256
+                        : adj.kind == 2 ? 512 + 64 * adj.ta + 16 * adj.tb + 4 * adj.ra + adj.rb
+                                        : 768 + 64 * adj.ta + 4 * adj.ra;
+        SingularPair sp;
+        sp.test = t;
+        sp.trial = r;
+        sp.rule = -1;
+        sp.kind = adj.kind;
+        sp.tr = tr;
+        sp.pad = 0;
+        sp.jac = (2.0 * P.area[t]) * (2.0 * P.area[r]);
+        sp.nprod = P.normal[3 * t] * tr_sx(tr) * P.normal[3 * r] +
+                   P.normal[3 * t + 1] * tr_sy(tr) * P.normal[3 * r + 1] + P.normal[3 * t + 2] * P.normal[3 * r + 2];
+        if (tr != 0) ++sl.image_pairs;
+        sl.pairs.push_back(sp);
+        sl.keys.push_back((short)key);
+      }
+    }
+  });
+  // rules in order of first appearance; rule_of_key is -1 until a key is seen
   std::vector<int> rule_of_key(4 * 256, -1);
   int n_rules = 0;
   P.rule_ptr.assign(1, 0);
   P.duffy.clear();
-  std::vector<SingularPair> pairs;
-  pairs.reserve(16 * (size_t)nf * P.transforms.size());
-  std::vector<int> seen(nf, -1);  // candidate stamp: the (transform, test face) that last listed the face
-  std::vector<int> cand;
-  int stamp = 0;
-  for (int tr : P.transforms)
-  for (int t = 0; t < nf; ++t, ++stamp) {
-    cand.clear();
-    for (int a = 0; a < 3; ++a) {
-      const int v = faces[3 * t + a];
-      if (tr != 0 && (P.fix_mask[v] & tr) != tr) continue;  // images touch the test face only on the planes
-      for (int r : v2f[v])
-        if (seen[r] != stamp) {
-          seen[r] = stamp;
-          cand.push_back(r);
-        }
-    }
-    for (int r : cand) {
-      Adjacency adj = tr == 0 ? classify(&faces[3 * t], &faces[3 * r])
-                              : classify_image(&faces[3 * t], &faces[3 * r], P.fix_mask, tr);
-      if (adj.kind == 0) continue;
-      const int key = adj.kind == 1 ? 256
-                      : adj.kind == 2 ? 512 + 64 * adj.ta + 16 * adj.tb + 4 * adj.ra + adj.rb
-                                      : 768 + 64 * adj.ta + 4 * adj.ra;
+  size_t n_pairs = 0;
+  for (Slice& sl : slices) {
+    P.image_pairs += sl.image_pairs;
+    n_pairs += sl.pairs.size();
+    for (size_t i = 0; i < sl.pairs.size(); ++i) {
+      const int key = sl.keys[i];
       int rule = rule_of_key[key];
       if (rule < 0) {
         rule = rule_of_key[key] = n_rules++;
-        for (const DPoint& p : base[adj.kind]) {
-          double tu = p[0], tv = p[1], ru = p[2], rv = p[3];
-          if (adj.kind == 2) {
-            remap_edge(tu, tv, adj.ta, adj.tb);
-            remap_edge(ru, rv, adj.ra, adj.rb);
-          } else if (adj.kind == 3) {
-            remap_vertex(tu, tv, adj.ta);
-            remap_vertex(ru, rv, adj.ra);
+        const int kind = key >> 8, ta = (key >> 6) & 3, tb = (key >> 4) & 3, ra = (key >> 2) & 3, rb = key & 3;
+        for (const DPoint& q : base[kind]) {
+          double tu = q[0], tv = q[1], ru = q[2], rv = q[3];
+          if (kind == 2) {
+            remap_edge(tu, tv, ta, tb);
+            remap_edge(ru, rv, ra, rb);
+          } else if (kind == 3) {
+            remap_vertex(tu, tv, ta);
+            remap_vertex(ru, rv, ra);
           }
-          P.duffy.insert(P.duffy.end(), {tu, tv, ru, rv, p[4]});
+          P.duffy.insert(P.duffy.end(), {tu, tv, ru, rv, q[4]});
         }
         P.rule_ptr.push_back((int)(P.duffy.size() / 5));
       }
-      SingularPair sp;
-      sp.test = t;
-      sp.trial = r;
-      sp.rule = rule;
-      sp.kind = adj.kind;
-      sp.tr = tr;
-      sp.pad = 0;
-      sp.jac = (2.0 * P.area[t]) * (2.0 * P.area[r]);
-      sp.nprod = P.normal[3 * t] * tr_sx(tr) * P.normal[3 * r] + P.normal[3 * t + 1] * tr_sy(tr) * P.normal[3 * r + 1] +
-                 P.normal[3 * t + 2] * P.normal[3 * r + 2];
-      if (tr != 0) ++P.image_pairs;
-      pairs.push_back(sp);
+      sl.pairs[i].rule = rule;
     }
   }
-  // pairs grouped by trial face, generation order kept within a face (a stable counting sort)
-  P.pairs_by_trial_ptr.assign(nf + 1, 0);
-  for (const auto& sp : pairs) P.pairs_by_trial_ptr[sp.trial + 1]++;
-  for (int f = 0; f < nf; ++f) P.pairs_by_trial_ptr[f + 1] += P.pairs_by_trial_ptr[f];
-  P.pairs.resize(pairs.size());
+  // pairs grouped by trial face, generation order kept within a face (a stable
+  // counting sort; each slice scatters its own pairs after the slices before it)
   {
-    std::vector<int> fill(P.pairs_by_trial_ptr.begin(), P.pairs_by_trial_ptr.end() - 1);
-    for (const auto& sp : pairs) P.pairs[fill[sp.trial]++] = sp;
+    std::vector<std::vector<int>> cnt(T, std::vector<int>(nf, 0));
+    parallel_slices(T, T, [&](long long b, long long e, int) {
+      for (long long ti = b; ti < e; ++ti)
+        for (const auto& sp : slices[ti].pairs) cnt[ti][sp.trial]++;
+    });
+    P.pairs_by_trial_ptr.assign(nf + 1, 0);
+    for (int f = 0; f < nf; ++f) {
+      int run = P.pairs_by_trial_ptr[f];
+      for (int ti = 0; ti < T; ++ti) {
+        const int c = cnt[ti][f];
+        cnt[ti][f] = run;  // this slice's first position for trial face f
+        run += c;
+      }
+      P.pairs_by_trial_ptr[f + 1] = run;
+    }
+    P.pairs.resize(n_pairs);
+    parallel_slices(T, T, [&](long long b, long long e, int) {
+      for (long long ti = b; ti < e; ++ti)
+        for (const auto& sp : slices[ti].pairs) P.pairs[cnt[ti][sp.trial]++] = sp;
+    });
   }
   P.pairs_by_test_ptr.assign(nf + 1, 0);
   for (const auto& sp : P.pairs) P.pairs_by_test_ptr[sp.test + 1]++;

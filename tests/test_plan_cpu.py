@@ -31,7 +31,7 @@ def plan_tool(tmp_path_factory):
     if shutil.which("g++") is None:
         pytest.skip("g++ not available")
     exe = tmp_path_factory.mktemp("plan") / "plan_check"
-    subprocess.run(["g++", "-O2", "-std=c++17", f"-I{CSRC}", str(ROOT / "tests" / "plan_check.cpp"),
+    subprocess.run(["g++", "-O2", "-std=c++17", "-pthread", f"-I{CSRC}", str(ROOT / "tests" / "plan_check.cpp"),
                     str(CSRC / "bem_plan.cpp"), "-o", str(exe)], check=True, capture_output=True)
     return exe
 
