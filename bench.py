@@ -166,7 +166,7 @@ def measured_peaks() -> dict:
     return {}
 
 
-def cpu_oracle_step(mesh, points, freq, drive, threads: int, precision: str = "f32"):
+def cpu_oracle_step(mesh, points, freq, drive, threads: int, precision: str = "f32", regular_order: int = 4):
     """One frequency of the reference algorithm on the host (assembly, BM system, LU,
     field): FP32 as the reference's engine computes, or FP64.  Returns (seconds, solution)."""
     from oracle import oracle
@@ -176,7 +176,8 @@ def cpu_oracle_step(mesh, points, freq, drive, threads: int, precision: str = "f
     q = drive[0] * (1j * RHO * omega)
     if precision == "f32":
         q = q.astype(np.complex64)
-    sol = oracle.solve_frequency(mesh, omega / SOUND_SPEED, q, points, precision=precision, threads=threads)
+    sol = oracle.solve_frequency(mesh, omega / SOUND_SPEED, q, points, precision=precision, threads=threads,
+                                 regular_order=regular_order)
     return time.perf_counter() - t0, sol
 
 
@@ -470,6 +471,18 @@ def main() -> None:
                 "value": len(ts) / sum(ts), "unit": UNIT, "cores": threads, "kind": "port",
                 "sample": f"{len(ts)} frequency of the same workload: {cpu_prec.upper()} restatement of BEAT CPU "
                           "assembly (colored OpenMP), BM system, LAPACK getrf/getrs, field",
+            }
+            # the reference CPU backend's own default rule: wavelength-driven regular order
+            # (kh = k sqrt(p90 face area): order 1 up to kh 0, order 2 up to kh 2, else 4)
+            se = pkg("system_exterior")
+            f_w = freqs[len(freqs) // 2]
+            sel = se.exterior_quadrature_selection({}, mesh, float(f_w), SOUND_SPEED, 4, "cpu")
+            tw = cpu_oracle_step(mesh, points, f_w, drive, threads, cpu_prec, regular_order=sel.order)[0]
+            result["cpu_baseline_wavelength_rule"] = {
+                "value": 1.0 / tw, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": f"1 frequency ({f_w:.0f} Hz) with the reference CPU default regular rule "
+                          f"(wavelength mode, order {sel.order}; the GPU path and cpu_baseline use the fixed "
+                          "order-4 rule of the CUDA backend)",
             }
         # serving stream: seeded Poisson arrivals of mixed-size jobs, latency per job
         if args.serving_jobs > 0 and args.workload == "box10k":
