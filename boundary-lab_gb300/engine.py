@@ -23,6 +23,7 @@ import numpy as np
 from . import native
 
 PRECISIONS = {"fp64": native.BEM_PRECISION_FP64, "mixed": native.BEM_PRECISION_MIXED}
+TRIM_ABOVE_BYTES = 8 << 30  # per-thread contexts keep at most this much scratch between jobs
 
 
 @dataclass
@@ -72,6 +73,7 @@ class CudaEngine:
         self.batch = batch
         self.refine_tol = refine_tol
         self.ctx, self.lock = shared_context(device) if context == "shared" else thread_context(device)
+        self.context = context
         self.mesh: native.Mesh | None = None
 
     def prepare(self, vertices, faces, drives, points, regular_order: int = 4, singular_order: int = 4,
@@ -94,6 +96,10 @@ class CudaEngine:
             if self.mesh is not None:
                 self.mesh.release()
                 self.mesh = None
+            # a worker thread's own context keeps its solve scratch between jobs; a large
+            # job's scratch (matrices of a whole batch) is returned to the pool afterwards
+            if self.context == "thread" and self.ctx.scratch_bytes > TRIM_ABOVE_BYTES:
+                self.ctx.trim()
 
 
 def engine_from_env(**kwargs):
