@@ -93,3 +93,39 @@ def test_system_request_matches_oracle(native, box_file, precision, tol):
             assert err < tol, (precision, g["freq_hz"], key, err)
         assert g["diagnostics"]["engine_form"] == ("mixed" if precision == "float32" else "fp64")
         assert g["quantities"][0]["values"]["dtype"] == ("complex64" if precision == "float32" else "complex128")
+
+
+def test_system_path_matches_legacy_path_on_the_gpu(native, box_file):
+    """The reference's own cross-check (tests/test_physical_compiler.py:786-868) on the CUDA
+    engine: the system path's field on the axis and its piston impedance equal the legacy
+    exterior job's on the same mesh and drive (float32 wire of the legacy result)."""
+    job_mod = pkg_module("job")
+    req = request(box_file, "float64")
+    sysreq = dict(req)
+    sysreq["excitation_port_ids"] = ["port:piston"]
+    sysreq["compiled_system"] = dict(req["compiled_system"])
+    sysreq["compiled_system"]["components"] = [c for c in req["compiled_system"]["components"]
+                                               if c["id"] == "component:piston"]
+    sysreq["compiled_system"]["excitation_ports"] = [p for p in req["compiled_system"]["excitation_ports"]
+                                                     if p["id"] == "port:piston"]
+    sysreq["outputs"] = [{"id": "far", "quantity": "exterior_pressure", "options": {"points_m": [[0.0, 0.0, 2.05]]}},
+                         {"id": "z", "quantity": "radiation_impedance"}]
+    job = se.ExteriorSystemJob(sysreq)
+    try:
+        got = list(job.results())
+    finally:
+        job.close()
+    # legacy: the mesh without the system's 5 cm translation, so its on-axis point at 2 m is the
+    # system's (0, 0, 2.05)
+    cfg = {"mesh_file": str(box_file), "scale_factor": 0.001, "rho": 1.205, "sound_speed": 343.0,
+           "step_size": 90.0, "distance": 2.0,
+           "radiators": [{"name": "piston", "tag": 2, "channel": "main"}], "channels": [{"name": "main"}],
+           "flat_target_normalization_enabled": False}
+    legacy = list(job_mod.ExteriorJob({"config": cfg, "frequencies_hz": req["frequencies_hz"]}).results())
+    for g, leg in zip(got, legacy):
+        v = values(g)
+        hp = leg["result"]["horizontal_pressure"]
+        h0 = complex(hp["real"][0][2], hp["imag"][0][2])  # 0 degrees
+        assert abs(v["far"][0, 0] - h0) / abs(h0) < 1e-5
+        zl = complex(*leg["result"]["impedance"][0])
+        assert abs(v["z"][0] - zl) / abs(zl) < 1e-5
