@@ -107,7 +107,7 @@ class ExteriorJob:
         ])
         parts_pts = [self.horizontal, self.vertical] + ([self.sphere[0]] if self.sphere is not None else [])
         self.points = np.vstack(parts_pts)
-        self.status("Initializing GB300 BEM (mesh plan, FP64 singular moments)")
+        self.status("Initializing GB300 BEM (mesh plan, singular moments)")
         kwargs = {"device": self.device, "precision": self.precision}
         if self.batch:
             kwargs["batch"] = self.batch

@@ -45,7 +45,7 @@ enum bem_status {
 enum bem_precision {
   BEM_PRECISION_FP64 = 0,  /* FP64 assembly, FP64 LU, FP64 field ("plain FP64 GPU form") */
   BEM_PRECISION_MIXED = 1  /* compensated FP32 assembly, FP32 LU, FP64 iterative refinement,
-                              FP64 singular moments, compensated FP32 field */
+                              FP64-accurate singular moments, compensated FP32 field */
 };
 
 /* Library ABI version (GB300_BEM_ABI_VERSION). */
@@ -74,7 +74,8 @@ long long bem_context_scratch_bytes(const bem_context* ctx);
 
 /* Upload a triangle mesh and build every frequency-independent cache: face
  * geometry and surface curls, the regular rule, singular (vertex-sharing) pair
- * list with remapped Duffy rules, and the FP64 k-independent singular moments.
+ * list with remapped Duffy rules, and the k-independent singular moments (FP64
+ * accuracy, computed in double-float on a second stream; the first solve waits for them).
  * Replaces load_combined_mesh + build_p1/dp0_space + triangle_rule +
  * build_singular_correction_cache + build_cuda_regular_assembly_cache +
  * build_cuda_singular_correction_cache (solver.jl:717-767,
