@@ -415,6 +415,14 @@ class JobRecord:
         }
 
 
+def _config_value(config, key: str, default):
+    """A field of a request config: a dict (the wire form) or an object with attributes (the
+    reference's SimulationConfig)."""
+    if isinstance(config, dict):
+        return config.get(key, default)
+    return getattr(config, key, default)
+
+
 def _safe_asset_filename(filename: str, index: int) -> str:
     cleaned = ASSET_NAME_UNSAFE.sub("_", Path(filename).name).strip("._")
     return cleaned or f"asset_{index}.msh"
@@ -621,10 +629,11 @@ class JobOrchestrator:
             if job is None:
                 return
             if job.cancel_event.is_set():
-                if job.status != "cancelled":
-                    job.status = "cancelled"
-                    job.finished_at = time.time()
-                    self._add_event_locked(job, "cancelled")
+                # as the reference: a job cancelled while queued gets a second "cancelled"
+                # event when its worker picks it up (server.py:369-374)
+                job.status = "cancelled"
+                job.finished_at = time.time()
+                self._add_event_locked(job, "cancelled")
                 return
             job.status = "running"
             job.started_at = time.time()
@@ -642,9 +651,9 @@ class JobOrchestrator:
             dataset = ResultDataset(
                 polar_angle_deg=np.asarray(solver.polar_angle_deg, dtype=np.float32),
                 radiator_names=np.asarray(solver.radiator_names),
-                polar_observation_distance_m=abs(float(config.get("distance", 2.0))
-                                                 + float(config.get("axial_offset", 0.0))),
-                exterior_sound_speed_m_per_s=float(config.get("sound_speed", 343.0)),
+                polar_observation_distance_m=abs(float(_config_value(config, "distance", 2.0))
+                                                 + float(_config_value(config, "axial_offset", 0.0))),
+                exterior_sound_speed_m_per_s=float(_config_value(config, "sound_speed", 343.0)),
                 sphere_r_distance_m=sphere.get("r_distance_m"),
                 sphere_theta_polar_rad=sphere.get("theta_polar_rad"),
                 sphere_phi_azimuth_rad=sphere.get("phi_azimuth_rad"),

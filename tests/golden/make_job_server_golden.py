@@ -11,7 +11,8 @@ Scenarios: two channels with sphere pressures on a full circle of angles
 (wrap-around reference interpolation) streamed out of frequency order; SPL-only
 results (no channel basis, a missing raw level, sphere levels); a silent
 channel (flat-target correction falls back to 1) with a repeated frequency and
-no sphere; a job cancelled after two results; a solver that fails.
+no sphere; a job cancelled after two results; a solver that fails; a job cancelled while
+queued behind a running one.
 Usage: python tests/golden/make_job_server_golden.py /path/to/boundary-lab
 """
 
@@ -170,6 +171,36 @@ def run(orch_cls, terminal, solver, cancel_after=None, timeout=30.0):
         shutil.rmtree(tmp, ignore_errors=True)
 
 
+def run_queued_cancel(orch_cls, terminal, scenario, from_dict, timeout=30.0):
+    """One worker: job A runs (held before its first result) while job B waits in the queue and
+    is cancelled there; then A is released.  Returns B's events."""
+    tmp = Path(tempfile.mkdtemp(prefix="golden-jobs-"))
+    first = ScriptedSolver(scenario, from_dict, pause_after=0)
+    made = []
+
+    def factory(cfg):
+        made.append(cfg)
+        return first if len(made) == 1 else ScriptedSolver(scenario, from_dict)
+
+    orch = orch_cls(max_running_jobs=1, max_queued_jobs=1, solver_factory=factory, artifact_root=tmp)
+    try:
+        config = SimpleNamespace(distance=2.0, axial_offset=0.0, sound_speed=343.0)
+        a = orch.submit(config, np.asarray([100.0], np.float32))
+        deadline = time.time() + timeout
+        while time.time() < deadline and orch.get(a.job_id).status != "running":
+            time.sleep(0.01)
+        b = orch.submit(config, np.asarray([100.0], np.float32))
+        orch.cancel(b.job_id)
+        first.release.set()
+        while time.time() < deadline and (orch.get(a.job_id).status not in terminal
+                                          or len(orch.events_since(b.job_id, 0)[0]) < 3):
+            time.sleep(0.01)
+        return normalise(orch.events_since(b.job_id, 0)[0], b.job_id)
+    finally:
+        orch.shutdown()
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
 def main(checkout: Path) -> None:
     sys.path.insert(0, str(checkout / "src"))
     from blab import server  # noqa: PLC0415
@@ -195,6 +226,11 @@ def main(checkout: Path) -> None:
                        ScriptedSolver(scenarios["spl_only"], frequency_result_from_dict, fail="mesh file not found"))
     golden["scenarios"]["failed"] = {**scenarios["spl_only"], "fail": "mesh file not found", "events": events,
                                      "artifact": None}
+    # a job cancelled while queued: the reference stores "cancelled" at the cancel and again
+    # when its worker later picks the job up (server.py:339-342, 369-374)
+    golden["scenarios"]["queued_cancel"] = {
+        "events": run_queued_cancel(server.JobOrchestrator, server.TERMINAL_STATES, scenarios["spl_only"],
+                                    frequency_result_from_dict)}
     (HERE / "job_server_reference.json").write_text(json.dumps(golden, separators=(",", ":")))
 
 

@@ -93,6 +93,13 @@ def test_events_and_artifact_match_reference(tmp_path, name):
         assert_npz_equal(artifact, GOLDEN / golden["artifact"])
 
 
+def test_queued_cancel_matches_reference(tmp_path):
+    """A job cancelled while queued behind a running one: the same events as the reference's store
+    (including its second "cancelled" when the worker picks the job up)."""
+    events = scripted.run_queued_cancel(js.JobOrchestrator, js.TERMINAL_STATES, REFERENCE["spl_only"], from_wire)
+    assert events == REFERENCE["queued_cancel"]["events"]
+
+
 def test_writer_alone_matches_reference(tmp_path):
     """ResultDataset + write_result_artifact, no job loop: results added in stream order."""
     sc = REFERENCE["channels"]
@@ -190,8 +197,8 @@ def test_submit_validation_and_capacity(tmp_path):
         wait_terminal(orch, a.job_id)
         wait_terminal(orch, c.job_id)
         assert orch.get(a.job_id).status == "completed" and orch.get(c.job_id).status == "completed"
-        assert orch.get(b.job_id).status == "cancelled"  # the pool skips a cancelled job
-        assert [e["type"] for e in orch.events_since(b.job_id, 0)[0]] == ["queued", "cancelled"]
+        assert orch.get(b.job_id).status == "cancelled"  # the pool does not run a cancelled job
+        assert [e["type"] for e in orch.events_since(b.job_id, 0)[0]] == ["queued", "cancelled", "cancelled"]
         assert not orch.cancel("nope")
         with pytest.raises(KeyError):
             orch.events_since("nope", 0)
