@@ -34,6 +34,7 @@ from __future__ import annotations
 
 import argparse
 import base64
+import dataclasses
 import hmac
 import json
 import logging
@@ -428,8 +429,12 @@ def _safe_asset_filename(filename: str, index: int) -> str:
     return cleaned or f"asset_{index}.msh"
 
 
-def _rewrite_mesh_paths(config: dict, staged: dict[str, str]) -> dict:
-    """The config with every uploaded mesh path replaced by its staged copy (server.py:847-850)."""
+def _rewrite_mesh_paths(config, staged: dict[str, str]):
+    """The config with every uploaded mesh path replaced by its staged copy (server.py:847-850);
+    a dict config gives a dict, a dataclass config (the reference's SimulationConfig) a copy."""
+    if dataclasses.is_dataclass(config) and not isinstance(config, type):
+        meshes = tuple(dataclasses.replace(m, file=staged.get(m.file, m.file)) for m in getattr(config, "meshes", ()))
+        return dataclasses.replace(config, mesh_file=staged.get(config.mesh_file, config.mesh_file), meshes=meshes)
     out = dict(config)
     if out.get("mesh_file") in staged:
         out["mesh_file"] = staged[out["mesh_file"]]

@@ -550,3 +550,39 @@ def test_scenario_helpers_are_self_consistent():
     solver = scripted.ScriptedSolver(sc, from_wire)
     got = [js.frequency_result_to_wire(r) for r in solver.solve_stream(None)]
     assert json.loads(json.dumps(got)) == sc["results"]
+
+
+def test_dataclass_config_assets_are_staged(tmp_path):
+    """A config object with mesh_file / meshes[].file attributes (the reference's SimulationConfig)
+    gets its uploaded mesh paths rewritten like a dict config."""
+    from dataclasses import dataclass
+
+    @dataclass(frozen=True)
+    class Mesh:
+        name: str
+        file: str
+
+    @dataclass(frozen=True)
+    class Config:
+        mesh_file: str
+        meshes: tuple
+        distance: float = 2.0
+
+    seen = {}
+
+    def factory(cfg):
+        seen["cfg"] = cfg
+        return GatedSolver(n=1)
+
+    orch = js.JobOrchestrator(artifact_root=tmp_path, solver_factory=factory)
+    try:
+        cfg = Config(mesh_file="/c/a.msh", meshes=(Mesh("m", "/c/a.msh"), Mesh("n", "/c/other.msh")))
+        asset = {"original_path": "/c/a.msh", "filename": "a.msh", "content_base64": base64.b64encode(b"x").decode()}
+        job = orch.submit(cfg, [100.0], [asset])
+        wait_terminal(orch, job.job_id)
+        got = seen["cfg"]
+        assert isinstance(got, Config) and Path(got.mesh_file).read_bytes() == b"x"
+        assert got.meshes[0].file == got.mesh_file and got.meshes[1].file == "/c/other.msh"
+        assert orch.get(job.job_id).status == "completed"
+    finally:
+        orch.shutdown()
