@@ -561,8 +561,9 @@ def job_server_run(device: int, n_jobs: int = 6, n_freq: int = 16, faces: int = 
                    "as a base64 asset, 2x73 polar + 500 sphere points, mixed form; POST /jobs to the last "
                    "completed event, events read through GET /jobs/{id}/events windows"}
     for name, running in (("concurrent_jobs", 4), ("one_job_at_a_time", 1)):
+        budget = js.default_memory_budget(device) if running > 1 else None
         orch = js.JobOrchestrator(max_running_jobs=running, max_queued_jobs=n_jobs, artifact_root=tmp / name,
-                                  solver_factory=js.gb300_solver_factory(device=device))
+                                  solver_factory=js.gb300_solver_factory(device=device, memory_budget_bytes=budget))
         srv = js.JobHTTPServer(("127.0.0.1", 0), orch)
         threading.Thread(target=srv.serve_forever, daemon=True).start()
         url = f"http://127.0.0.1:{srv.server_address[1]}"

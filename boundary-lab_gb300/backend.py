@@ -51,13 +51,13 @@ def request_dict(request) -> dict:
 
 class Gb300BemSession:
     def __init__(self, request, *, engine_factory: Callable | None = None, precision: str = "mixed",
-                 device: int = 0, batch: int = 0):
+                 device: int = 0, batch: int = 0, admission=None):
         self._request = request
         self._stop = threading.Event()
         self._status = getattr(request, "status_callback", None)
         try:
             self._job = ExteriorJob(request_dict(request), engine_factory=engine_factory, status=self._emit,
-                                    precision=precision, device=device, batch=batch)
+                                    precision=precision, device=device, batch=batch, admission=admission)
             meta = self._job.initialized_payload()
             sphere = meta["sphere_metadata"]
             self._metadata = contract.SolveMetadata(

@@ -82,6 +82,19 @@ class CudaEngine:
             self.mesh = self.ctx.upload_mesh(vertices, faces, regular_order, singular_order, symmetry=symmetry)
             self.mesh.set_excitation(drives)
             self.mesh.set_observation_points(points)
+            self.n_rhs = int(np.asarray(drives).reshape(-1, len(faces)).shape[0])
+            self.n_points = int(len(points))
+
+    def device_bytes(self, n_freq: int) -> int:
+        """Device memory of a solve of n_freq frequencies on this mesh: the mesh caches plus the
+        scratch of the batch the solve will use (bem_estimate_device_bytes)."""
+        if self.mesh is None:
+            raise RuntimeError("engine.prepare() must run before device_bytes()")
+        prec = PRECISIONS[self.precision]
+        with self.lock:
+            batch = self.batch or self.mesh.auto_batch(n_freq, prec)
+            return self.ctx.estimate_device_bytes(self.mesh.n_vertices, self.mesh.n_faces,
+                                                  self.mesh.n_singular_pairs, self.n_rhs, self.n_points, batch, prec)
 
     def solve(self, freqs_hz, sound_speed: float, rho: float) -> EngineResult:
         if self.mesh is None:

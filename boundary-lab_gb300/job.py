@@ -43,7 +43,7 @@ class JobCancelled(Exception):
 class ExteriorJob:
     def __init__(self, request: dict, *, engine_factory: Callable | None = None,
                  status: Callable[[str], None] | None = None, precision: str = "mixed", device: int = 0,
-                 batch: int = 0):
+                 batch: int = 0, admission=None):
         schema = int(rq.get_value(request, "schema_version", 1))
         if schema not in (1, 2):
             raise rq.RequestError(f"Unsupported solve request schema_version {schema}.")
@@ -78,6 +78,10 @@ class ExteriorJob:
         self.batch = batch
         self.engine = None
         self.mesh = None
+        # optional device-memory admission shared by concurrent jobs: acquire(bytes) -> token,
+        # release(token); the job holds its footprint from setup to close
+        self.admission = admission
+        self._admitted = None
 
     # ------------------------------------------------------------ metadata --
     def initialized_payload(self) -> dict:
@@ -114,11 +118,20 @@ class ExteriorJob:
         self.engine = self.engine_factory(**kwargs)
         self.engine.prepare(self.mesh.vertices, self.mesh.faces, drives, self.points, self.regular_order,
                             self.singular_order, symmetry=self.symmetry)
+        if self.admission is not None:
+            footprint = getattr(self.engine, "device_bytes", None)
+            need = int(footprint(min(16, len(self.frequencies)))) if callable(footprint) else 0
+            if need > self.admission.free_bytes():
+                self.status("Waiting for GPU memory")
+            self._admitted = self.admission.acquire(need)
 
     def close(self) -> None:
         if self.engine is not None:
             self.engine.close()
             self.engine = None
+        if self._admitted is not None:
+            self.admission.release(self._admitted)
+            self._admitted = None
 
     def _cancel_requested(self, stop: Callable[[], bool] | None) -> bool:
         if stop is not None and stop():

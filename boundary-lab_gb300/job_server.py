@@ -317,17 +317,63 @@ def _server_engine_factory(**kwargs):
     return engine_from_env(context="thread", **kwargs)
 
 
+class MemoryAdmission:
+    """Device-memory admission shared by the jobs of one server: a job holds its estimated
+    footprint (mesh caches plus one frequency batch) from mesh upload to the end of its solve,
+    and waits while it does not fit beside the running jobs.  A job larger than the whole
+    budget runs when nothing else holds memory."""
+
+    def __init__(self, budget_bytes: int):
+        if budget_bytes <= 0:
+            raise ValueError("budget_bytes must be > 0")
+        self.budget = int(budget_bytes)
+        self.used = 0
+        self.holders = 0
+        self._cond = threading.Condition()
+
+    def free_bytes(self) -> int:
+        with self._cond:
+            return self.budget - self.used
+
+    def acquire(self, nbytes: int) -> int:
+        nbytes = max(0, int(nbytes))
+        with self._cond:
+            while self.holders > 0 and self.used + nbytes > self.budget:
+                self._cond.wait()
+            self.used += nbytes
+            self.holders += 1
+        return nbytes
+
+    def release(self, token: int) -> None:
+        with self._cond:
+            self.used -= int(token)
+            self.holders -= 1
+            self._cond.notify_all()
+
+
+def default_memory_budget(device: int) -> int:
+    """85% of the device memory free now (torch's view of the device); 64 GiB without one."""
+    try:
+        import torch  # noqa: PLC0415
+
+        free, _total = torch.cuda.mem_get_info(device)
+        return int(0.85 * free)
+    except Exception:  # noqa: BLE001 - no torch or no GPU
+        return 64 << 30
+
+
 class ServerSolver:
     """A job's solve session behind the interface the job loop uses (server.py:63-109):
     ``initialize(frequencies)``, the metadata properties, ``solve_stream``."""
 
     def __init__(self, config: dict, *, precision: str = "mixed", device: int = 0, batch: int = 0,
-                 engine_factory: Callable | None = None):
+                 engine_factory: Callable | None = None, admission: MemoryAdmission | None = None):
         self.config = config
         self.precision = precision
         self.device = device
         self.batch = batch
         self.engine_factory = engine_factory or _server_engine_factory
+        self.admission = admission
         self.status_callback: Callable[[str], None] | None = None
         self.session = None
 
@@ -340,7 +386,7 @@ class ServerSolver:
         request = contract.SolveRequest(self.config, np.asarray(frequencies_hz, dtype=np.float32),
                                         status_callback=self.status_callback)
         self.session = Gb300BemSession(request, engine_factory=self.engine_factory, precision=self.precision,
-                                       device=self.device, batch=self.batch)
+                                       device=self.device, batch=self.batch, admission=self.admission)
 
     def _meta(self):
         if self.session is None:
@@ -366,9 +412,13 @@ class ServerSolver:
 
 
 def gb300_solver_factory(*, precision: str = "mixed", device: int = 0, batch: int = 0,
-                         engine_factory: Callable | None = None) -> Callable[[dict], ServerSolver]:
+                         engine_factory: Callable | None = None,
+                         memory_budget_bytes: int | None = None) -> Callable[[dict], ServerSolver]:
+    """Solvers for the job loop.  With a memory budget, every solver this factory makes shares
+    one MemoryAdmission, so concurrent jobs start their solves only when they fit."""
+    admission = MemoryAdmission(memory_budget_bytes) if memory_budget_bytes else None
     return lambda config: ServerSolver(config, precision=precision, device=device, batch=batch,
-                                       engine_factory=engine_factory)
+                                       engine_factory=engine_factory, admission=admission)
 
 
 # -------------------------------------------------------------- job store ---
@@ -923,14 +973,22 @@ def main(argv: list[str] | None = None) -> int:
     parser.add_argument("--event-stream-window-seconds", type=float, default=DEFAULT_EVENT_STREAM_WINDOW_SECONDS)
     parser.add_argument("--artifact-dir", type=Path, default=DEFAULT_ARTIFACT_ROOT)
     parser.add_argument("--access-token", default="", help="require 'Authorization: Bearer <token>'")
+    parser.add_argument("--memory-budget-gb", type=float, default=None,
+                        help="device memory the running jobs may hold together (default with more than one "
+                             "running job: 85%% of the free memory; 0 turns admission off)")
     parser.add_argument("--log-level", default="INFO")
     args = parser.parse_args(argv)
+    if args.memory_budget_gb is None:
+        budget = default_memory_budget(args.device) if args.max_running_jobs > 1 else None
+    else:
+        budget = int(args.memory_budget_gb * (1 << 30)) or None
     logging.basicConfig(level=getattr(logging, str(args.log_level).upper(), logging.INFO))
     orch = JobOrchestrator(
         max_running_jobs=args.max_running_jobs, max_queued_jobs=args.max_queued_jobs,
         max_asset_bytes=max(1, int(args.max_asset_mb * MEBIBYTE)), max_frequencies=args.max_frequencies,
         job_retention_hours=args.job_retention_hours, artifact_root=args.artifact_dir,
-        solver_factory=gb300_solver_factory(precision=args.precision, device=args.device))
+        solver_factory=gb300_solver_factory(precision=args.precision, device=args.device,
+                                            memory_budget_bytes=budget))
     server = JobHTTPServer((args.host, args.port), orch, access_token=args.access_token or None,
                            max_request_bytes=max(1, int(args.max_request_mb * MEBIBYTE)),
                            event_stream_window_seconds=args.event_stream_window_seconds)

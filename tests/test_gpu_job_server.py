@@ -80,8 +80,9 @@ def request_body(tmp_path_factory):
 
 def test_http_jobs_on_the_gpu(native, tmp_path, request_body):
     body, mesh_path = request_body
+    # with a memory budget, so every job's footprint is estimated on the device and admitted
     orch = js.JobOrchestrator(max_running_jobs=3, max_queued_jobs=4, artifact_root=tmp_path / "jobs",
-                              solver_factory=js.gb300_solver_factory())
+                              solver_factory=js.gb300_solver_factory(memory_budget_bytes=64 << 30))
     srv = js.JobHTTPServer(("127.0.0.1", 0), orch, event_stream_window_seconds=0.5)
     threading.Thread(target=srv.serve_forever, daemon=True).start()
     url = f"http://127.0.0.1:{srv.server_address[1]}"

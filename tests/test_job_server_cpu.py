@@ -586,3 +586,66 @@ def test_dataclass_config_assets_are_staged(tmp_path):
         assert orch.get(job.job_id).status == "completed"
     finally:
         orch.shutdown()
+
+
+def test_memory_admission_serialises_jobs_that_do_not_fit(served, mesh_file, tmp_path):
+    """Two real jobs (CPU oracle engine) whose footprints (60 and 70 units) do not fit together
+    in a budget of 100: the second starts solving only after the first has closed.  A budget of
+    200 lets them overlap.  MemoryAdmission itself: a job larger than the budget runs alone."""
+    timeline = []
+    lock = threading.Lock()
+
+    class Engine:
+        def __init__(self, **kw):
+            sys.path.insert(0, str(TESTS))
+            import oracle_engine
+
+            self.inner = oracle_engine.make_engine(**kw)
+            self.n = None
+
+        def prepare(self, vertices, faces, *a, **k):
+            self.n = len(faces)
+            self.inner.prepare(vertices, faces, *a, **k)
+
+        def device_bytes(self, n_freq):
+            return 60 if self.n == 80 else 70
+
+        def solve(self, *a, **k):
+            with lock:
+                timeline.append(("solve", self.n))
+            time.sleep(0.2)
+            return self.inner.solve(*a, **k)
+
+        def close(self):
+            with lock:
+                timeline.append(("close", self.n))
+
+    big = meshes.sphere_with_cap(0.1, 1, 40.0)
+    other = tmp_path / "other.msh"
+    v = big.vertices * 1.5
+    meshes.write_gmsh22(other, v * 1000.0, big.faces[:-4], big.tags[:-4])
+    for budget, serial in ((100, True), (200, False)):
+        timeline.clear()
+        http, orch = served(js.gb300_solver_factory(engine_factory=lambda **kw: Engine(**kw), memory_budget_bytes=budget),
+                            max_running_jobs=2)
+        ids = []
+        for path in (mesh_file, other):
+            cfg = {"mesh_file": str(path), "scale_factor": 0.001, "step_size": 90.0,
+                   "radiators": [{"name": "cap", "tag": 2, "channel": "main"}], "channels": [{"name": "main"}]}
+            ids.append(http.call("/jobs", {"config": cfg, "frequencies_hz": [300.0, 600.0]})[1]["job_id"])
+        for j in ids:
+            wait_terminal(orch, j, timeout=120)
+            assert orch.get(j).status == "completed", orch.get(j).error
+        first_close = min(i for i, e in enumerate(timeline) if e[0] == "close")
+        solves_after = [e for e in timeline[first_close:] if e[0] == "solve"]
+        closed = timeline[first_close][1]
+        later_job_solves_before_close = [e for e in timeline[:first_close] if e[0] == "solve" and e[1] != closed]
+        if serial:
+            assert not later_job_solves_before_close and solves_after
+        else:
+            assert later_job_solves_before_close
+    adm = js.MemoryAdmission(10)
+    t = adm.acquire(50)  # larger than the budget: admitted when nothing else holds memory
+    assert adm.free_bytes() == -40
+    adm.release(t)
+    assert adm.free_bytes() == 10
