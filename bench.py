@@ -249,6 +249,9 @@ def main() -> None:
     ap.add_argument("--serving-running", type=int, default=4, help="concurrent jobs on the GPU")
     ap.add_argument("--lu-block", type=int, default=0, choices=[0, 32, 64], help="LU panel width (0 automatic)")
     ap.add_argument("--form", default=None, choices=["mixed", "fp64"], help="override the workload's precision form")
+    ap.add_argument("--autotune", type=int, default=1, choices=[0, 1],
+                    help="time the candidate launch configurations on the workload's sweep before the run "
+                         "(autotune.tune) and use the winner's LU panel width and trailing update")
     ap.add_argument("--lu-gemm", type=int, default=0, choices=[0, 1, 2],
                     help="LU trailing update: 0 automatic, 1 cuBLAS cgemm, 2 tcgen05 3xTF32")
     args = ap.parse_args()
@@ -280,6 +283,18 @@ def main() -> None:
     m.set_excitation(drive)
     m.set_observation_points(points)
     form = native.BEM_PRECISION_FP64 if fp64_workload else native.BEM_PRECISION_MIXED
+    tune_info = None
+    if args.autotune and not args.no_extras and args.lu_block == 0 and args.lu_gemm == 0:
+        # The tuner scores configurations on the workload's whole sweep (ceil(n_freq / batch)
+        # batches); the timed steps keep their one-batch size and take the winner's LU
+        # panel width and trailing update.
+        try:
+            tr = pkg("autotune").tune(m, freqs, precision=form, sound_speed=SOUND_SPEED, rho=RHO, device=local_rank,
+                                      use_cache=False)
+            args.lu_block, args.lu_gemm = tr.best.lu_block, tr.best.lu_gemm
+            tune_info = tr.to_dict()
+        except Exception as exc:  # noqa: BLE001 - the run goes on with the library's own choice
+            tune_info = {"error": f"{type(exc).__name__}: {exc}"}
     B = min(args.batch if args.batch > 0 else m.auto_batch(0, form), len(freqs))
     stream = torch.cuda.ExternalStream(ctx.stream_handle, device=f"cuda:{local_rank}")
     p_dev = torch.empty((B, 1, mesh.n_vertices), dtype=torch.complex128, device="cuda")
@@ -350,6 +365,8 @@ def main() -> None:
                    "l2": "256 MiB buffer written before every timed step (> 129 MB L2)",
                    "parallelism": f"replicas x{world}, frequencies sharded"},
         "clocks": clocks.summary(),
+        "launch": {"batch": B, "lu_block": args.lu_block, "lu_gemm": args.lu_gemm},
+        "autotune": tune_info,
         "stage_ms_per_freq": per_freq_ms,
         "step_ms": step_ms,
         # timed region minus the steps: the L2 flushes and host time between steps

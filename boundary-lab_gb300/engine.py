@@ -63,7 +63,7 @@ class CudaEngine:
     name = "gb300_cuda"
 
     def __init__(self, device: int = 0, precision: str = "mixed", batch: int = 0, refine_tol: float = 1e-10,
-                 context: str = "shared"):
+                 context: str = "shared", autotune: bool = False):
         if precision not in PRECISIONS:
             raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
         if context not in ("shared", "thread"):
@@ -75,10 +75,16 @@ class CudaEngine:
         self.ctx, self.lock = shared_context(device) if context == "shared" else thread_context(device)
         self.context = context
         self.mesh: native.Mesh | None = None
+        # autotune: the first solve on a mesh times the candidate launch configurations
+        # (autotune.tune, cached per device and problem shape) and later solves use the winner
+        self.autotune = autotune
+        self.launch = None  # autotune.LaunchConfig once tuned
+        self.tune_result = None
 
     def prepare(self, vertices, faces, drives, points, regular_order: int = 4, singular_order: int = 4,
                 symmetry: str = "off") -> None:
         with self.lock:
+            self.launch = None
             self.mesh = self.ctx.upload_mesh(vertices, faces, regular_order, singular_order, symmetry=symmetry)
             self.mesh.set_excitation(drives)
             self.mesh.set_observation_points(points)
@@ -93,6 +99,9 @@ class CudaEngine:
         prec = PRECISIONS[self.precision]
         with self.lock:
             batch = self.batch or self.mesh.auto_batch(n_freq, prec)
+            if self.autotune and not self.batch:
+                # the tuner tries up to one frequency more than the library's own batch
+                batch = self.launch.batch if self.launch is not None else min(batch + 1, max(1, n_freq))
             return self.ctx.estimate_device_bytes(self.mesh.n_vertices, self.mesh.n_faces,
                                                   self.mesh.n_singular_pairs, self.n_rhs, self.n_points, batch, prec)
 
@@ -100,8 +109,18 @@ class CudaEngine:
         if self.mesh is None:
             raise RuntimeError("engine.prepare() must run before solve()")
         with self.lock:
+            kw = dict(batch=self.batch)
+            if self.autotune and not self.batch:
+                if self.launch is None:
+                    from . import autotune  # noqa: PLC0415
+
+                    self.tune_result = autotune.tune(self.mesh, freqs_hz, precision=PRECISIONS[self.precision],
+                                                     sound_speed=sound_speed, rho=rho, refine_tol=self.refine_tol,
+                                                     device=self.device)
+                    self.launch = self.tune_result.best
+                kw = dict(batch=self.launch.batch, lu_block=self.launch.lu_block, lu_gemm=self.launch.lu_gemm)
             p, u, stats = self.mesh.solve(freqs_hz, precision=PRECISIONS[self.precision], sound_speed=sound_speed,
-                                          rho=rho, refine_tol=self.refine_tol, batch=self.batch)
+                                          rho=rho, refine_tol=self.refine_tol, **kw)
         return EngineResult(p, u, stats)
 
     def close(self) -> None:
@@ -109,6 +128,7 @@ class CudaEngine:
             if self.mesh is not None:
                 self.mesh.release()
                 self.mesh = None
+            self.launch = None
             # a worker thread's own context keeps its solve scratch between jobs; a large
             # job's scratch (matrices of a whole batch) is returned to the pool afterwards
             if self.context == "thread" and self.ctx.scratch_bytes > TRIM_ABOVE_BYTES:
