@@ -105,6 +105,19 @@ class CudaEngine:
             return self.ctx.estimate_device_bytes(self.mesh.n_vertices, self.mesh.n_faces,
                                                   self.mesh.n_singular_pairs, self.n_rhs, self.n_points, batch, prec)
 
+    def preferred_chunk(self, n_freq: int) -> int:
+        """Frequencies per solve call for a sweep of n_freq: one batch of the size the solve
+        uses (bem_auto_batch splits a sweep into equal batches whose LU panels are resident
+        in one wave), so no call leaves a partial batch behind."""
+        if self.mesh is None:
+            raise RuntimeError("engine.prepare() must run before preferred_chunk()")
+        if self.batch:
+            return max(1, int(self.batch))
+        if self.autotune and self.launch is not None:
+            return max(1, int(self.launch.batch))
+        with self.lock:
+            return max(1, int(self.mesh.auto_batch(max(1, int(n_freq)), PRECISIONS[self.precision])))
+
     def solve(self, freqs_hz, sound_speed: float, rho: float) -> EngineResult:
         if self.mesh is None:
             raise RuntimeError("engine.prepare() must run before solve()")

@@ -120,7 +120,7 @@ class ExteriorJob:
                             self.singular_order, symmetry=self.symmetry)
         if self.admission is not None:
             footprint = getattr(self.engine, "device_bytes", None)
-            need = int(footprint(min(16, len(self.frequencies)))) if callable(footprint) else 0
+            need = int(footprint(len(self.frequencies))) if callable(footprint) else 0
             if need > self.admission.free_bytes():
                 self.status("Waiting for GPU memory")
             self._admitted = self.admission.acquire(need)
@@ -139,13 +139,19 @@ class ExteriorJob:
         return bool(self.cancel_path) and os.path.isfile(str(self.cancel_path))
 
     # -------------------------------------------------------------- results --
-    def results(self, stop: Callable[[], bool] | None = None, chunk: int = 16) -> Iterator[dict]:
+    def results(self, stop: Callable[[], bool] | None = None, chunk: int | None = None) -> Iterator[dict]:
         """Yield the `result` event payload of each frequency in request order.
-        Raises JobCancelled when a cancel request is seen between frequencies."""
+        Raises JobCancelled when a cancel request is seen between frequencies.
+        ``chunk`` is the number of frequencies per engine call; by default the engine's
+        preferred chunk (one full batch of the sweep), else 16."""
         if self.engine is None:
             self.setup()
         nh, nv = len(self.horizontal), len(self.vertical)
         total = len(self.frequencies)
+        if chunk is None:
+            preferred = getattr(self.engine, "preferred_chunk", None)
+            chunk = int(preferred(total)) if callable(preferred) else 16
+        chunk = max(1, int(chunk))
         solved = 0
         while solved < total:
             if self._cancel_requested(stop):

@@ -273,3 +273,32 @@ def test_symmetric_job_matches_full_model(half_and_full_files):
         assert np.linalg.norm(a - b) / np.linalg.norm(b) < 5e-5
     # impedance: the half model's radiator force times the reduction factor 2
     assert np.allclose(h["impedance"], f["impedance"], rtol=5e-5)
+
+
+def test_job_solves_in_the_engines_preferred_chunks(mesh_file):
+    """The frequency loop calls the engine once per preferred chunk (one full batch of the
+    sweep on the CUDA engine); an engine without preferred_chunk gets chunks of 16."""
+    sys.path.insert(0, str(TESTS))
+    import oracle_engine
+
+    calls = []
+
+    class Recording(oracle_engine.OracleEngine):
+        def solve(self, freqs, sound_speed, rho):
+            calls.append(len(freqs))
+            return super().solve(freqs, sound_speed, rho)
+
+    class Chunked(Recording):
+        def preferred_chunk(self, n_freq):
+            assert n_freq == 20
+            return 7
+
+    freqs = list(np.geomspace(100.0, 2000.0, 20))
+    for cls, expect in ((Chunked, [7, 7, 6]), (Recording, [16, 4])):
+        calls.clear()
+        job = job_mod.ExteriorJob({"config": base_config(mesh_file), "frequencies_hz": freqs},
+                                  engine_factory=lambda **kw: cls(**kw))
+        out = list(job.results())
+        job.close()
+        assert calls == expect
+        assert [e["solved_count"] for e in out] == list(range(1, 21))
