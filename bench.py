@@ -181,33 +181,45 @@ def cpu_oracle_step(mesh, points, freq, drive, threads: int, precision: str = "f
     return time.perf_counter() - t0, sol
 
 
+def workload_config(args, mesh, points, spec, world: int) -> dict:
+    """The ``config`` object both arms print (identical, so the two lines name the same run)."""
+    return {"workload": describe(mesh, points, spec), "name": args.workload, "form": spec["form"],
+            "l2": "GPU arm: a 256 MiB buffer is written before every timed step (> 129 MB L2); "
+                  "host arm: inputs in host memory",
+            "parallelism": f"frequencies sharded over {world} rank(s), no collective on the data path"}
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
     mesh, points, freqs, drive, spec = workload(args.workload, args.faces)
+    if args.form:
+        spec = {**spec, "form": args.form}
     threads = os.cpu_count() or 1
     cpu_prec = "f64" if spec["form"] == "fp64" else "f32"
     from oracle.build import build_oracle
 
     build_oracle()
-    # The host path has nothing to warm up beyond one small solve (page-in of the
-    # library and of OpenBLAS); timed steps are capped at 6 full-size frequencies so
-    # the run stays within a few minutes whatever --steps asks for.
+    # Warm-up steps: one small solve each (page-in of the library and of OpenBLAS).
+    # Timed steps: exactly --steps full-size frequencies of the workload's sweep.
     small_mesh, small_points, _, small_drive, _ = workload("box10k", 600)
     for _ in range(args.warmup):
         cpu_oracle_step(small_mesh, small_points[:64], 500.0, small_drive, threads)
-    timed = min(args.steps, 6)
-    sel = [freqs[(i * 13) % len(freqs)] for i in range(timed)]
+    sel = [freqs[(i * 13) % len(freqs)] for i in range(args.steps)]
+    t0 = time.perf_counter()
     times = [cpu_oracle_step(mesh, points, f, drive, threads, cpu_prec)[0] for f in sel]
-    total = sum(times)
+    total = time.perf_counter() - t0
     value = len(times) / total
+    sample = (f"1 full-size frequency of the workload per step ({len(times)} steps): {cpu_prec.upper()} restatement "
+              "of BEAT CPU assembly (colored OpenMP), BM system, LAPACK getrf/getrs (scipy OpenBLAS), field")
     line = {
         "impl": "reference",
         "metric": METRIC,
         "value": value,
         "unit": UNIT,
-        "n_gpus": args.gpus,
+        "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": 1e3 * total / len(times),
@@ -216,16 +228,52 @@ def run_reference(args) -> None:
         "vs_baseline": None,
         "dtype": "f64" if cpu_prec == "f64" else "f32",
         "data": "synthetic",
-        "config": {"workload": describe(mesh, points, spec), "step": "1 frequency (bounded sample)",
-                   "timed_steps": len(times), "warmup": "one small solve per warm-up step"},
-        "cpu_baseline": {
-            "value": value, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"1 frequency of the workload per step: {cpu_prec.upper()} restatement of BEAT CPU assembly "
-                      "(colored OpenMP), BM system, LAPACK getrf/getrs (scipy OpenBLAS), field",
-        },
+        "config": workload_config(args, mesh, points, spec, world),
+        "step": "1 frequency of the sweep on the host cores; warm-up: one small solve per warm-up step",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def launch_ranks(args) -> int:
+    """``--gpus N`` started without a launcher: start N ranks with torch.distributed.run
+    (one process per GPU, 127.0.0.1 rendezvous) running this script with the same
+    arguments, and return their exit status.  Rank 0 prints the JSON line."""
+    import socket
+
+    with socket.socket() as sock:
+        sock.bind(("127.0.0.1", 0))
+        port = sock.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", str(args.gpus),
+           "--master-addr", "127.0.0.1", "--master-port", str(port), str(Path(__file__).resolve()), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
+def run_plan(args) -> None:
+    """``--plan``: each rank reports the frequency batches it would solve (no GPU work);
+    rank 0 gathers them over gloo and prints one JSON line.  Shows the sharding that the
+    timed run uses: rank r takes batch (step x world + r) of the sweep."""
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    spec = WORKLOADS[args.workload]
+    lo, hi, n = spec["f"]
+    freqs = np.logspace(np.log10(lo), np.log10(hi), n)
+    B = min(args.batch or 15, len(freqs))
+    sharding = pkg("sharding")
+    mine = [[int(i) for i in np.arange(len(freqs))[sharding.step_batch(s, rank, world, B, len(freqs))]]
+            for s in range(args.warmup + args.steps)]
+    gathered = [mine]
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        gathered = [None] * world
+        dist.all_gather_object(gathered, mine)
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps({"plan": True, "n_gpus": world, "batch": B, "n_freq": len(freqs),
+                          "rank_batches": gathered}))
 
 
 def main() -> None:
@@ -240,7 +288,9 @@ def main() -> None:
     ap.add_argument("--workload", default="box10k", choices=sorted(WORKLOADS),
                     help="synthetic workload (box10k: the headline mixed-form configuration)")
     ap.add_argument("--faces", type=int, default=None, help="re-mesh the box workloads to about this many triangles")
-    ap.add_argument("--fp64-freqs", type=int, default=2, help="frequencies timed in the plain FP64 form")
+    ap.add_argument("--fp64-freqs", type=int, default=0,
+                    help="frequencies of the sweep solved in the plain FP64 form for the per-frequency error "
+                         "(0: every frequency)")
     ap.add_argument("--cpu-baseline", type=int, default=1, help="frequencies timed on the host for cpu_baseline")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-extras", action="store_true", help="skip FP64 form, e2e and CPU baseline (profiling runs)")
@@ -254,9 +304,16 @@ def main() -> None:
                          "(autotune.tune) and use the winner's LU panel width and trailing update")
     ap.add_argument("--lu-gemm", type=int, default=0, choices=[0, 1, 2],
                     help="LU trailing update: 0 automatic, 1 cuBLAS cgemm, 2 tcgen05 3xTF32")
+    ap.add_argument("--plan", action="store_true",
+                    help="print the frequency batches each rank would solve (no GPU work)")
     args = ap.parse_args()
     if args.warmup < 3 and not args.no_extras:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_ranks(args))
+    if args.plan:
+        run_plan(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return
@@ -361,9 +418,8 @@ def main() -> None:
         "vs_baseline": None,
         "dtype": "f64" if fp64_workload else "f32 (compensated) + f64 refinement",
         "data": "synthetic",
-        "config": {"workload": describe(mesh, points, spec), "name": args.workload, "form": spec["form"], "batch": B,
-                   "l2": "256 MiB buffer written before every timed step (> 129 MB L2)",
-                   "parallelism": f"replicas x{world}, frequencies sharded"},
+        "config": workload_config(args, mesh, points, spec, world),
+        "step": f"one batch of {B} frequencies of the sweep per rank",
         "clocks": clocks.summary(),
         "launch": {"batch": B, "lu_block": args.lu_block, "lu_gemm": args.lu_gemm},
         "autotune": tune_info,
@@ -388,7 +444,8 @@ def main() -> None:
     reg_s = kernel_s["regular"] / (args.steps * B)  # seconds per frequency
     achieved = regular_qpairs * flops_per_qpair / reg_s / 1e12 if reg_s > 0 else None
     clock = result["clocks"]["sm_mhz"] or 1920.0
-    fp32_peak = 152 * 128 * 2 * clock * 1e6 / 1e12
+    n_sm = torch.cuda.get_device_properties(local_rank).multi_processor_count
+    fp32_peak = n_sm * 128 * 2 * clock * 1e6 / 1e12
     result["roofline"] = {
         "kernel": "regular_f32_kernel (regular face-pair assembly)",
         "bound": "fp32",
@@ -401,7 +458,7 @@ def main() -> None:
         # current source); the algorithmic bytes are the extended-row output,
         # 3 x N_f x ldR x 8 B = 1.360e9 per frequency
         "traffic": REGULAR_DRAM_BYTES_PER_FREQ if args.workload == "box10k" and args.faces in (None, 10000) else None,
-        "peak_source": "152 SMs x 128 FP32 lanes x 2 flop x median SM clock sampled during the run "
+        "peak_source": f"{n_sm} SMs (device query) x 128 FP32 lanes x 2 flop x median SM clock sampled during the run "
                        "(MEASURED_PEAKS.json has no FP32 figure)",
         "work_per_frequency": f"{regular_qpairs:.4g} q-pairs x {flops_per_qpair} flop",
     }
@@ -423,39 +480,7 @@ def main() -> None:
         result["max_rel_surface_pressure_err_vs_cpu_fp64"] = float(
             np.linalg.norm(p_g[0, 0] - ref.pressure[:, 0]) / np.linalg.norm(ref.pressure[:, 0]))
     if not args.no_extras and rank == 0 and not fp64_workload:
-        # plain FP64 form on a subset, and the mixed-form error against it
-        n_f = len(freqs)
-        if args.fp64_freqs <= 4:
-            sel = freqs[[int(x * (n_f - 1)) for x in (0.16, 0.8, 0.48, 0.95)][: args.fp64_freqs]]
-        else:  # accuracy sweep: evenly spread frequencies, at most one batch of 64
-            sel = freqs[np.unique(np.linspace(0, n_f - 1, min(args.fp64_freqs, 64)).round().astype(int))]
-        ev_a, ev_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        p64 = torch.empty((len(sel), 1, mesh.n_vertices), dtype=torch.complex128, device="cuda")
-        u64 = torch.empty((len(sel), 1, len(points)), dtype=torch.complex128, device="cuda")
-        # warm-up: the FP64 form's first call loads its kernels (cuBLAS zgemm, FP64 kernels) lazily
-        m.solve_device(sel[:1], p64.data_ptr(), u64.data_ptr(), precision=native.BEM_PRECISION_FP64,
-                       sound_speed=SOUND_SPEED, rho=RHO, batch=1)
-        torch.cuda.synchronize()
-        with torch.cuda.stream(stream):
-            ev_a.record(stream)
-            st64 = m.solve_device(sel, p64.data_ptr(), u64.data_ptr(), precision=native.BEM_PRECISION_FP64,
-                                  sound_speed=SOUND_SPEED, rho=RHO, batch=len(sel), profile=1)
-            ev_b.record(stream)
-        torch.cuda.synchronize()
-        t64 = ev_a.elapsed_time(ev_b) / 1e3
-        pm = torch.empty_like(p64)
-        um = torch.empty_like(u64)
-        m.solve_device(sel, pm.data_ptr(), um.data_ptr(), **{**opts, "batch": len(sel)})
-        torch.cuda.synchronize()
-        errs = [float(torch.linalg.norm(um[i] - u64[i]) / torch.linalg.norm(u64[i])) for i in range(len(sel))]
-        perr = [float(torch.linalg.norm(pm[i] - p64[i]) / torch.linalg.norm(p64[i])) for i in range(len(sel))]
-        v64 = len(sel) / t64
-        result["fp64_form"] = {"value": v64, "unit": UNIT, "freqs_hz": [float(f) for f in sel],
-                               "stage_ms_per_freq": {k: 1e3 * v / len(sel) for k, v in st64["kernel_s"].items()},
-                               "far_field_err_per_freq": errs, "surface_pressure_err_per_freq": perr}
-        result["speedup_vs_fp64"] = value / world / v64
-        result["max_rel_far_field_err_vs_fp64"] = max(errs)
-        result["max_rel_surface_pressure_err_vs_fp64"] = max(perr)
+        result.update(accuracy_sweep(m, freqs, mesh, points, opts, args, stream, value / world))
 
     if not args.no_extras and rank == 0:
         # end to end through the C ABI with host buffers: upload mesh + caches, solve a batch, copy results back
@@ -507,7 +532,6 @@ def main() -> None:
         # retained-trace field (the bem_field operation): one request per call, host traces
         if args.workload == "box10k":
             result["retained_field"] = retained_field_run(mesh, local_rank)
-            result["job_server"] = job_server_run(local_rank)
     # gpu_launches: this library's kernels launched in the timed region, counted by
     # the library itself per call (bem_solve_stats.kernel_launches)
     result["gpu_launches"] = int(sum(st["kernel_launches"] for st in stats_list))
@@ -517,6 +541,59 @@ def main() -> None:
         print(json.dumps(result))
     if dist:
         dist.destroy_process_group()
+
+
+def accuracy_sweep(m, freqs, mesh, points, opts, args, stream, mixed_rate: float) -> dict:
+    """The plain FP64 GPU form on the sweep's frequencies (every one by default) and the
+    mixed form's relative error against it, per frequency: far field and surface
+    pressure, with the mixed form's refinement steps and final relative residual per
+    frequency (one frequency per call).  The FP64 form runs in batches of at most 16
+    and is timed with CUDA events on the library's stream."""
+    import torch
+
+    native = pkg("native")
+    n_f = len(freqs)
+    n_sel = n_f if args.fp64_freqs <= 0 else min(args.fp64_freqs, n_f)
+    sel = freqs[np.unique(np.linspace(0, n_f - 1, n_sel).round().astype(int))]
+    chunk = min(16, len(sel))
+    p64 = torch.empty((len(sel), 1, mesh.n_vertices), dtype=torch.complex128, device="cuda")
+    u64 = torch.empty((len(sel), 1, len(points)), dtype=torch.complex128, device="cuda")
+    fp64 = dict(precision=native.BEM_PRECISION_FP64, sound_speed=SOUND_SPEED, rho=RHO)
+    # warm-up: the FP64 form's first call loads its kernels (cuBLAS zgemm, FP64 kernels) lazily
+    m.solve_device(sel[:1], p64.data_ptr(), u64.data_ptr(), batch=1, **fp64)
+    torch.cuda.synchronize()
+    ev_a, ev_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kernel_s: dict = {}
+    with torch.cuda.stream(stream):
+        ev_a.record(stream)
+        for i in range(0, len(sel), chunk):
+            st = m.solve_device(sel[i:i + chunk], p64[i].data_ptr(), u64[i].data_ptr(), batch=min(chunk, len(sel) - i),
+                                profile=1, **fp64)
+            for k, v in st["kernel_s"].items():
+                kernel_s[k] = kernel_s.get(k, 0.0) + v
+        ev_b.record(stream)
+    torch.cuda.synchronize()
+    t64 = ev_a.elapsed_time(ev_b) / 1e3
+    pm = torch.empty((1, 1, mesh.n_vertices), dtype=torch.complex128, device="cuda")
+    um = torch.empty((1, 1, len(points)), dtype=torch.complex128, device="cuda")
+    errs, perr, steps, resid = [], [], [], []
+    for i, f in enumerate(sel):
+        st = m.solve_device([f], pm.data_ptr(), um.data_ptr(), **{**opts, "batch": 1})
+        torch.cuda.synchronize()
+        errs.append(float(torch.linalg.norm(um[0] - u64[i]) / torch.linalg.norm(u64[i])))
+        perr.append(float(torch.linalg.norm(pm[0] - p64[i]) / torch.linalg.norm(p64[i])))
+        steps.append(int(st["max_refine_steps"]))
+        resid.append(float(st["max_rel_residual"]))
+    v64 = len(sel) / t64
+    return {
+        "fp64_form": {"value": v64, "unit": UNIT, "freqs_hz": [float(f) for f in sel],
+                      "stage_ms_per_freq": {k: 1e3 * v / len(sel) for k, v in kernel_s.items()},
+                      "far_field_err_per_freq": errs, "surface_pressure_err_per_freq": perr,
+                      "mixed_refine_steps_per_freq": steps, "mixed_rel_residual_per_freq": resid},
+        "speedup_vs_fp64": mixed_rate / v64,
+        "max_rel_far_field_err_vs_fp64": max(errs),
+        "max_rel_surface_pressure_err_vs_fp64": max(perr),
+    }
 
 
 def retained_field_run(mesh, device: int, n_points: int = 5000, calls: int = 8) -> dict:
@@ -547,86 +624,6 @@ def retained_field_run(mesh, device: int, n_points: int = 5000, calls: int = 8) 
                     "C ABI bem_evaluate_field), 3-point rule, mixed form, 2,500 Hz, 5,000 points at 2 m",
             "ms_per_request": dt * 1e3, "points": n_points, "faces": int(mesh.n_faces),
             "green_evaluations_per_s": pairs / dt}
-
-
-def job_server_run(device: int, n_jobs: int = 6, n_freq: int = 16, faces: int = 5000) -> dict:
-    """Whole requests through the HTTP job server (job_server.py): each job uploads its
-    mesh as an asset, is parsed, planned, solved and post-processed, and a client per
-    job reads its event windows.  Run with four jobs on the GPU at once and with one
-    (the reference server's default); event latency = client receipt - event time."""
-    import base64
-    import shutil
-    import tempfile
-    import urllib.request
-
-    js = pkg("job_server")
-    meshes = pkg("meshes")
-    mesh = meshes.box_with_piston((0.3, 0.2, 0.25), faces, 0.05, "+z")
-    tmp = Path(tempfile.mkdtemp(prefix="bench-jobs-"))
-    meshes.write_gmsh22(tmp / "box.msh", mesh.vertices * 1000.0, mesh.faces, mesh.tags)
-    body = {"schema_version": 2,
-            "config": {"mesh_file": "box.msh", "scale_factor": 0.001, "rho": RHO, "sound_speed": SOUND_SPEED,
-                       "step_size": 5.0, "distance": 2.0,
-                       "radiators": [{"name": "piston", "tag": int(meshes.RADIATOR_TAG), "channel": "main"}],
-                       "channels": [{"name": "main"}], "spherical_sampling_enabled": True,
-                       "spherical_sampling_points": 500},
-            "frequencies_hz": np.geomspace(200.0, 6000.0, n_freq).tolist(),
-            "assets": [{"original_path": "box.msh", "filename": "box.msh",
-                        "content_base64": base64.b64encode((tmp / "box.msh").read_bytes()).decode()}]}
-    payload = json.dumps(body).encode()
-    out = {"what": f"{n_jobs} jobs x {n_freq} freqs (200 Hz-6 kHz) on a {mesh.n_faces}-triangle box, mesh uploaded "
-                   "as a base64 asset, 2x73 polar + 500 sphere points, mixed form; POST /jobs to the last "
-                   "completed event, events read through GET /jobs/{id}/events windows"}
-    for name, running in (("concurrent_jobs", 4), ("one_job_at_a_time", 1)):
-        budget = js.default_memory_budget(device) if running > 1 else None
-        orch = js.JobOrchestrator(max_running_jobs=running, max_queued_jobs=n_jobs, artifact_root=tmp / name,
-                                  solver_factory=js.gb300_solver_factory(device=device, memory_budget_bytes=budget))
-        srv = js.JobHTTPServer(("127.0.0.1", 0), orch)
-        threading.Thread(target=srv.serve_forever, daemon=True).start()
-        url = f"http://127.0.0.1:{srv.server_address[1]}"
-        lat: list[float] = []
-        failures: list[str] = []
-
-        def read(job_id):
-            since = 0
-            while True:
-                with urllib.request.urlopen(f"{url}/jobs/{job_id}/events?since={since}", timeout=600) as resp:
-                    for line in resp:
-                        now = time.time()
-                        ev = json.loads(line)
-                        since = ev["index"] + 1
-                        if ev["type"] == "result":
-                            lat.append(now - ev["timestamp"])
-                        if ev["type"] in js.TERMINAL_STATES:
-                            if ev["type"] != "completed":
-                                failures.append(str(ev.get("error", ev["type"])))
-                            return
-
-        try:
-            t0 = time.perf_counter()
-            ids = []
-            for _ in range(n_jobs):
-                req = urllib.request.Request(url + "/jobs", data=payload, method="POST",
-                                             headers={"Content-Type": "application/json"})
-                with urllib.request.urlopen(req, timeout=60) as resp:
-                    ids.append(json.loads(resp.read())["job_id"])
-            readers = [threading.Thread(target=read, args=(j,)) for j in ids]
-            for t in readers:
-                t.start()
-            for t in readers:
-                t.join(900)
-            wall = time.perf_counter() - t0
-        finally:
-            srv.shutdown()
-            srv.server_close()
-            orch.shutdown()
-        lat_ms = np.asarray(lat) * 1e3
-        out[name] = {"max_running_jobs": running, "wall_s": wall, "failed": failures[:3],
-                     "frequency_solves_per_s": n_jobs * n_freq / wall,
-                     "result_event_latency_ms_p50": float(np.percentile(lat_ms, 50)) if lat else None,
-                     "result_event_latency_ms_p99": float(np.percentile(lat_ms, 99)) if lat else None}
-    shutil.rmtree(tmp, ignore_errors=True)
-    return out
 
 
 def serving_run(args, device: int) -> dict:

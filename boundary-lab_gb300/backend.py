@@ -12,11 +12,21 @@ session runs in-process and drives the CUDA library through its C ABI.
 application's registry (registry.py:21-83) and to the job server's solver
 sets (server.py:46-52), so ``create_backend("gb300_cuda")`` and
 ``blab server --solver gb300_cuda`` find it.
+
+Concurrent jobs.  The reference's job server runs ``max_running_jobs`` jobs
+on a thread pool (server.py:185); its BEAT adapter then serialises them on
+one worker per GPU.  With ``concurrent=True`` (or GB300_BEM_CONCURRENT_JOBS=1
+in the environment) each server thread solves on its own library context (its
+own CUDA stream and scratch), so those jobs share the GPU, and a process-wide
+``MemoryAdmission`` per device holds each job's device footprint (mesh caches
+plus one frequency batch) from its mesh upload to its end: a job waits while
+it does not fit beside the running ones.
 """
 
 from __future__ import annotations
 
 import dataclasses
+import os
 import threading
 from typing import Any, Callable, Iterator
 
@@ -33,6 +43,64 @@ CAPABILITIES = contract.SolverCapabilities(
     supports_channel_resynthesis=True,
     is_remote=False,
 )
+
+
+class MemoryAdmission:
+    """Device-memory budget shared by concurrent jobs on one GPU.  ``acquire(n)`` blocks
+    until n bytes fit beside the bytes already held (a request larger than the whole
+    budget is let through once nothing else is held) and returns a token for
+    ``release``."""
+
+    def __init__(self, budget_bytes: int):
+        if budget_bytes <= 0:
+            raise ValueError("budget_bytes must be > 0")
+        self.budget = int(budget_bytes)
+        self._held: dict[int, int] = {}
+        self._next = 0
+        self._cv = threading.Condition()
+
+    def in_use(self) -> int:
+        with self._cv:
+            return sum(self._held.values())
+
+    def free_bytes(self) -> int:
+        return self.budget - self.in_use()
+
+    def acquire(self, nbytes: int) -> int:
+        want = max(0, int(nbytes))
+        with self._cv:
+            self._cv.wait_for(lambda: not self._held or sum(self._held.values()) + want <= self.budget)
+            self._next += 1
+            self._held[self._next] = want
+            return self._next
+
+    def release(self, token: int) -> None:
+        with self._cv:
+            self._held.pop(int(token), None)
+            self._cv.notify_all()
+
+
+def default_memory_budget(device: int) -> int:
+    """85% of the device memory that is free now; 64 GiB when it cannot be queried."""
+    try:
+        import torch  # noqa: PLC0415
+
+        free, _ = torch.cuda.mem_get_info(device)
+        return int(0.85 * free)
+    except Exception:  # noqa: BLE001 - no torch or no GPU
+        return 64 << 30
+
+
+_admission_lock = threading.Lock()
+_admissions: dict[int, MemoryAdmission] = {}
+
+
+def device_admission(device: int, budget_bytes: int | None = None) -> MemoryAdmission:
+    """The process-wide admission of ``device`` (created on first use)."""
+    with _admission_lock:
+        if device not in _admissions:
+            _admissions[device] = MemoryAdmission(budget_bytes or default_memory_budget(device))
+        return _admissions[device]
 
 
 def config_to_dict(config: Any) -> dict:
@@ -102,17 +170,27 @@ class Gb300BemBackend:
     capabilities = CAPABILITIES
 
     def __init__(self, *, device: int = 0, precision: str = "mixed", batch: int = 0,
-                 engine_factory: Callable | None = None, **_ignored: Any):
+                 engine_factory: Callable | None = None, concurrent: bool | None = None,
+                 memory_budget_bytes: int | None = None, **_ignored: Any):
         # _ignored absorbs the keyword arguments the application passes to every
         # backend factory (julia_executable, julia_threads, ...; server.py:870-889).
         self.device = device
         self.precision = precision
         self.batch = batch
+        if concurrent is None:
+            concurrent = os.environ.get("GB300_BEM_CONCURRENT_JOBS", "").strip().lower() in ("1", "true", "yes")
+        self.concurrent = bool(concurrent)
+        self.memory_budget_bytes = memory_budget_bytes
         self.engine_factory = engine_factory
+        if self.concurrent and engine_factory is None:
+            from .engine import engine_from_env  # noqa: PLC0415
+
+            self.engine_factory = lambda **kw: engine_from_env(context="thread", **kw)
 
     def create_session(self, request) -> Gb300BemSession:
+        admission = device_admission(self.device, self.memory_budget_bytes) if self.concurrent else None
         return Gb300BemSession(request, engine_factory=self.engine_factory, precision=self.precision,
-                               device=self.device, batch=self.batch)
+                               device=self.device, batch=self.batch, admission=admission)
 
     def warm_up(self, mode: str = "worker", *, status_callback: Callable[[str], None] | None = None) -> None:
         """`worker`: load the library and create the CUDA context; `tiny`: also solve a tetrahedron at

@@ -1,13 +1,13 @@
 // Exterior field evaluation for callers that cannot allocate device memory.
 //
 // Some hosts of this library are not allowed to call cudaMalloc at the point
-// where they need a field: an audio plug-in's real-time processing callback,
-// a framework that owns all device memory through its own pool and forbids
-// raw allocations, or code that runs while another component is recording
-// work into a CUDA graph.  bem_evaluate_field_noalloc serves them: the caller
-// passes every input and output as a device buffer it already owns, and the
-// only other memory the call touches is one fixed scratch array compiled into
-// the library (g_field_scratch below).
+// where they need a field: an audio plug-in's real-time processing callback
+// (an allocation can block for an unbounded time and must not happen there),
+// or a framework that owns all device memory through its own pool and forbids
+// raw allocations.  bem_evaluate_field_noalloc serves them: the caller passes
+// every input and output as a device buffer it already owns, and the only
+// other memory the call touches is one fixed scratch array compiled into the
+// library (g_field_scratch below).
 //
 // Consequences a caller must know:
 //  * The scratch array exists once per GPU for the life of the process
@@ -19,7 +19,14 @@
 //    each call writes every scratch entry it later reads.
 //  * The first call on a device looks up the device address of the scratch
 //    array (cudaGetSymbolAddress) with that device current, so make the first
-//    call on each device before any stream capture begins.
+//    call on each device before any stream capture begins.  The address is kept
+//    for the life of the process: do not use the entry point across a
+//    cudaDeviceReset of that device.  The stream must belong to the current
+//    device (checked).
+//  * Each call waits for its stream (cudaStreamSynchronize) before it returns,
+//    to read the mesh check the kernels wrote.
+//  * On an error return the contents of d_field_out are undefined (a bad mesh
+//    is reported after the field kernels ran).
 //  * Limits: n_faces <= kNoAllocMaxFaces; larger meshes are rejected with
 //    BEM_ERR_INVALID_ARGUMENT and a message.
 #include <cuda_runtime.h>
@@ -217,11 +224,16 @@ extern "C" int bem_evaluate_field_noalloc(const double* d_vertices, int n_vertic
     }
     base = g_scratch_addr[dev];
   }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (s) {
+    int sdev = -1;
+    if (cudaStreamGetDevice(s, &sdev) != cudaSuccess) return fail(BEM_ERR_INVALID_ARGUMENT, "invalid stream");
+    if (sdev != dev) return fail(BEM_ERR_INVALID_ARGUMENT, "stream belongs to another device than the current one");
+  }
   char* records = (char*)base;
   char* sources = records + kRecordBytes;
   char* drive = sources + kSourceBytes;
   char* params = drive + kDriveBytes;
-  cudaStream_t s = (cudaStream_t)stream;
 
   double pts[2 * kMaxQ] = {0}, w[kMaxQ] = {0};
   int Q = 0;

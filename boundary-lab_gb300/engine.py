@@ -118,6 +118,25 @@ class CudaEngine:
         with self.lock:
             return max(1, int(self.mesh.auto_batch(max(1, int(n_freq)), PRECISIONS[self.precision])))
 
+    def tune_sweep(self, freqs_hz, sound_speed: float, rho: float) -> None:
+        """With autotune on, time the candidate launch configurations on the whole sweep
+        (autotune.tune scores each by the sweep's rate, n_freq / (ceil(n_freq / batch) x
+        batch time)) before the first solve; later chunks use the winner's batch."""
+        if self.mesh is None:
+            raise RuntimeError("engine.prepare() must run before tune_sweep()")
+        if not self.autotune or self.batch or self.launch is not None:
+            return
+        with self.lock:
+            self._tune(freqs_hz, sound_speed, rho)
+
+    def _tune(self, freqs_hz, sound_speed: float, rho: float) -> None:
+        from . import autotune  # noqa: PLC0415
+
+        self.tune_result = autotune.tune(self.mesh, freqs_hz, precision=PRECISIONS[self.precision],
+                                         sound_speed=sound_speed, rho=rho, refine_tol=self.refine_tol,
+                                         device=self.device)
+        self.launch = self.tune_result.best
+
     def solve(self, freqs_hz, sound_speed: float, rho: float) -> EngineResult:
         if self.mesh is None:
             raise RuntimeError("engine.prepare() must run before solve()")
@@ -125,12 +144,7 @@ class CudaEngine:
             kw = dict(batch=self.batch)
             if self.autotune and not self.batch:
                 if self.launch is None:
-                    from . import autotune  # noqa: PLC0415
-
-                    self.tune_result = autotune.tune(self.mesh, freqs_hz, precision=PRECISIONS[self.precision],
-                                                     sound_speed=sound_speed, rho=rho, refine_tol=self.refine_tol,
-                                                     device=self.device)
-                    self.launch = self.tune_result.best
+                    self._tune(freqs_hz, sound_speed, rho)
                 kw = dict(batch=self.launch.batch, lu_block=self.launch.lu_block, lu_gemm=self.launch.lu_gemm)
             p, u, stats = self.mesh.solve(freqs_hz, precision=PRECISIONS[self.precision], sound_speed=sound_speed,
                                           rho=rho, refine_tol=self.refine_tol, **kw)

@@ -148,6 +148,9 @@ class ExteriorJob:
             self.setup()
         nh, nv = len(self.horizontal), len(self.vertical)
         total = len(self.frequencies)
+        tune = getattr(self.engine, "tune_sweep", None)
+        if callable(tune):  # the tuner sees the whole sweep, not its first chunk
+            tune(self.frequencies.astype(np.float64), self.sound_speed, self.rho)
         if chunk is None:
             preferred = getattr(self.engine, "preferred_chunk", None)
             chunk = int(preferred(total)) if callable(preferred) else 16

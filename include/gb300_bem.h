@@ -200,22 +200,26 @@ int bem_evaluate_field(bem_mesh* mesh, double k, int precision, const double* pr
 
 /* Exterior field for callers that cannot allocate device memory (no
  * counterpart in the reference).  Some callers cannot call cudaMalloc where they
- * need a field, e.g. a real-time audio callback, a host framework that owns all
- * device memory through its own pool, or code running while another component
- * records a CUDA graph.  This entry point allocates nothing: every input and
- * output is a device buffer the caller owns, and its scratch is one fixed
- * array inside the library (about 6.5 MB per GPU, held until the process
- * exits).  Inputs (device pointers): vertices [n_vertices][3] doubles, faces
- * [n_faces][3] int32, pressure [n_vertices] complex, neumann [n_faces] complex
- * (q = i rho omega v_n), points [n_points][3]; output field [n_points] complex.
- * Same quadrature and precision forms as bem_solve_frequencies (regular_order
- * 1..4; BEM_PRECISION_FP64 or BEM_PRECISION_MIXED).  Limits: n_faces <= 16384,
- * else BEM_ERR_INVALID_ARGUMENT.  All calls share the scratch array: calls whose
- * work overlaps on the GPU race and must be serialised by the caller.  The
- * first call on a device resolves the scratch address with that device
- * current; make it before any stream capture.  `stream` is a cudaStream_t
- * (NULL = legacy default stream); the call returns after its work finished.
- * err/err_cap: optional buffer for a message on failure. */
+ * need a field: a real-time audio callback, where an allocation may block for an
+ * unbounded time, or a host framework that owns all device memory through its
+ * own pool and forbids raw allocations.  This entry point allocates nothing:
+ * every input and output is a device buffer the caller owns, and its scratch is
+ * one fixed array inside the library (about 6.5 MB per GPU, held until the
+ * process exits).  Inputs (device pointers): vertices [n_vertices][3] doubles,
+ * faces [n_faces][3] int32, pressure [n_vertices] complex, neumann [n_faces]
+ * complex (q = i rho omega v_n), points [n_points][3]; output field [n_points]
+ * complex.  Same quadrature and precision forms as bem_solve_frequencies
+ * (regular_order 1..4; BEM_PRECISION_FP64 or BEM_PRECISION_MIXED).  Limits:
+ * n_faces <= 16384, else BEM_ERR_INVALID_ARGUMENT.  All calls share the scratch
+ * array: calls whose work overlaps on the GPU race and must be serialised by the
+ * caller.  The first call on a device resolves the scratch address with that
+ * device current (kept for the process's life: not valid across a
+ * cudaDeviceReset); make that first call before any stream capture.  `stream` is
+ * a cudaStream_t of the current device (NULL = legacy default stream); the call
+ * synchronises that stream before it returns.  On an error return the contents
+ * of field_out are undefined (an out-of-range vertex index or a zero-area
+ * triangle is reported after the kernels ran).  err/err_cap: optional buffer for
+ * a message on failure. */
 int bem_evaluate_field_noalloc(const double* d_vertices, int n_vertices, const int* d_faces, int n_faces,
                                int regular_order, double k, const double* d_pressure, const double* d_neumann,
                                const double* d_points, int n_points, int precision, double* d_field_out,

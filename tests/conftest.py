@@ -36,3 +36,15 @@ def gpu_ctx(native):
     ctx = native.Context(0)
     yield ctx
     ctx.close()
+
+
+def reference_checkout() -> Path | None:
+    """A Boundary Lab source checkout, for the CPU tests that import or read the
+    reference's own files: the directory named by BOUNDARY_LAB_REFERENCE, else a
+    ``reference`` directory beside this repository.  None when neither exists."""
+    import os
+
+    for cand in (os.environ.get("BOUNDARY_LAB_REFERENCE"), ROOT.parent / "reference"):
+        if cand and (Path(cand) / "src" / "blab").is_dir():
+            return Path(cand)
+    return None

@@ -196,3 +196,53 @@ def test_result_dict_is_json():
     res = autotune.tune(FakeMesh(clock, batch_cost(6)), FREQS, clock=clock)
     d = json.loads(json.dumps(res.to_dict()))
     assert d["best"]["batch"] == res.best.batch and len(d["trials"]) == len(res.trials)
+
+
+def test_job_tunes_on_the_whole_sweep(tmp_path):
+    """The job loop hands the whole sweep to the engine's tuner before it asks for its
+    chunk size, so the tuner scores batches on every frequency of the job (not on the
+    first chunk) and the chunks that follow are the winner's batch."""
+    meshes = pkg_module("meshes")
+    job_mod = pkg_module("job")
+    mesh = meshes.sphere_with_cap(0.1, 1, 40.0)
+    path = tmp_path / "s.msh"
+    meshes.write_gmsh22(path, mesh.vertices * 1000.0, mesh.faces, mesh.tags)
+    seen = {}
+
+    class Engine:
+        def __init__(self, **kw):
+            self.batch = None
+
+        def prepare(self, vertices, faces, drives, points, *a, **k):
+            self.nv, self.n_rhs, self.n_points = len(vertices), len(drives), len(points)
+
+        def tune_sweep(self, freqs, sound_speed, rho):
+            seen["tuned"] = np.asarray(freqs).copy()
+            self.batch = 5
+
+        def preferred_chunk(self, n):
+            seen["chunk_asked_after_tune"] = "tuned" in seen
+            return self.batch
+
+        def solve(self, freqs, c, rho):
+            seen.setdefault("calls", []).append(len(freqs))
+            n = len(freqs)
+
+            class R:
+                pressure = np.ones((n, self.n_rhs, self.nv), complex)
+                field = np.ones((n, self.n_rhs, self.n_points), complex)
+                stats = {}
+
+            return R()
+
+        def close(self):
+            pass
+
+    freqs = np.geomspace(100, 3000, 12)
+    cfg = {"mesh_file": str(path), "scale_factor": 0.001, "step_size": 90.0,
+           "radiators": [{"name": "cap", "tag": 2, "channel": "main"}], "channels": [{"name": "main"}]}
+    job = job_mod.ExteriorJob({"config": cfg, "frequencies_hz": freqs.tolist()}, engine_factory=lambda **kw: Engine())
+    out = list(job.results())
+    assert len(out) == 12
+    assert np.allclose(seen["tuned"], freqs.astype(np.float32))
+    assert seen["chunk_asked_after_tune"] and seen["calls"] == [5, 5, 2]

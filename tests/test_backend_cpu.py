@@ -17,11 +17,12 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from conftest import pkg_module
+from conftest import pkg_module, reference_checkout
 
 TESTS = Path(__file__).resolve().parent
 ROOT = TESTS.parent
-REF_SRC = Path("/root/reference/src")
+_REF = reference_checkout()
+REF_SRC = _REF / "src" if _REF is not None else Path("/nonexistent-boundary-lab/src")
 meshes = pkg_module("meshes")
 job_mod = pkg_module("job")
 backend_mod = pkg_module("backend")
@@ -302,3 +303,84 @@ def test_job_solves_in_the_engines_preferred_chunks(mesh_file):
         job.close()
         assert calls == expect
         assert [e["solved_count"] for e in out] == list(range(1, 21))
+
+
+def test_memory_admission_budget():
+    """MemoryAdmission: a request that does not fit waits for a release; one larger than
+    the whole budget is let through when nothing else is held."""
+    import threading
+    import time
+
+    adm = backend_mod.MemoryAdmission(100)
+    a = adm.acquire(60)
+    got = []
+    t = threading.Thread(target=lambda: got.append(adm.acquire(70)))
+    t.start()
+    time.sleep(0.2)
+    assert not got and adm.free_bytes() == 40
+    adm.release(a)
+    t.join(5)
+    assert got and adm.in_use() == 70
+    adm.release(got[0])
+    big = adm.acquire(500)  # larger than the budget: admitted alone
+    assert adm.free_bytes() == -400
+    adm.release(big)
+    assert adm.free_bytes() == 100
+
+
+def test_concurrent_sessions_hold_their_footprint(mesh_file):
+    """With concurrent=True, sessions on two threads share one device admission: with a
+    budget of 100 and footprints of 60 and 70 the second job solves only after the first
+    has closed; with 200 they overlap.  Results equal the serial ones."""
+    import threading
+    import time
+
+    timeline, lock = [], threading.Lock()
+
+    class Engine:
+        def __init__(self, **kw):
+            self.inner = oracle_factory(**kw)
+            self.n = None
+
+        def prepare(self, vertices, faces, *a, **k):
+            self.n = len(faces)
+            self.inner.prepare(vertices, faces, *a, **k)
+
+        def device_bytes(self, n_freq):
+            return 60 if self.n == 80 else 70
+
+        def solve(self, *a, **k):
+            with lock:
+                timeline.append(("solve", self.n))
+            time.sleep(0.2)
+            return self.inner.solve(*a, **k)
+
+        def close(self):
+            with lock:
+                timeline.append(("close", self.n))
+
+    small = meshes.sphere_with_cap(0.1, 1, 40.0)
+    other = mesh_file.parent / "other.msh"
+    meshes.write_gmsh22(other, small.vertices * 1500.0, small.faces[:-4], small.tags[:-4])
+    for budget, serial in ((100, True), (200, False)):
+        timeline.clear()
+        backend_mod._admissions.pop(7, None)
+        be = backend_mod.Gb300BemBackend(device=7, concurrent=True, memory_budget_bytes=budget,
+                                         engine_factory=lambda **kw: Engine(**kw))
+        outs = {}
+
+        def run(path):
+            req = contract.SolveRequest(base_config(path, step_size=90.0), np.asarray([300.0, 600.0], np.float32))
+            outs[str(path)] = list(be.create_session(req).solve_stream())
+
+        threads = [threading.Thread(target=run, args=(p,)) for p in (mesh_file, other)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join(120)
+        assert len(outs) == 2 and all(len(v) == 2 for v in outs.values())
+        first_close = min(i for i, e in enumerate(timeline) if e[0] == "close")
+        closed = timeline[first_close][1]
+        other_before = [e for e in timeline[:first_close] if e[0] == "solve" and e[1] != closed]
+        assert (not other_before) if serial else other_before
+    backend_mod._admissions.pop(7, None)

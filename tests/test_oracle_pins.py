@@ -13,7 +13,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from conftest import pkg_module
+from conftest import pkg_module, reference_checkout
 
 meshes = pkg_module("meshes")
 GOLDEN = Path(__file__).resolve().parent / "golden"
@@ -58,8 +58,9 @@ def test_reference_fixture_mesh_counts():
 
 
 def test_loader_on_reference_fixture_meshes():
-    root = Path("/root/reference/src/blab/solvers/julia_local/test_meshes")
-    if not root.exists():
+    ref = reference_checkout()
+    root = ref / "src/blab/solvers/julia_local/test_meshes" if ref is not None else None
+    if root is None or not root.exists():
         pytest.skip("reference checkout not present")
     counts = json.loads((GOLDEN / "reference_mesh_counts.json").read_text())
     for name, c in counts.items():
@@ -133,3 +134,22 @@ def test_singular_pairs_are_the_vertex_sharing_pairs(O):
     expected = sum(1 for i in range(len(f)) for j in range(len(f)) if set(f[i]) & set(f[j]))
     assert O.singular_pair_count(mesh, 4) == expected
     assert O.color_count(mesh) >= 7  # valence-6 vertices need at least 7 colours
+
+
+@pytest.mark.parametrize("name", ["sample_half", "sample_quarter", "sample_detailed"])
+def test_fixture_meshes_match_the_reference_files(name):
+    """The committed .npz fixtures hold the reference's test meshes: their counts are the
+    counts read from the .msh files, and where the checkout is present the fixture equals
+    what the loader (read_gmsh22, BeatEngineCore.jl:193-234) reads from the file."""
+    z = np.load(GOLDEN / f"{name}.npz")
+    counts = json.loads((GOLDEN / "reference_mesh_counts.json").read_text())[f"{name}.msh"]
+    assert z["nodes_mm"].shape == (counts["nodes"], 3)
+    assert z["faces"].shape == (counts["triangles"], 3)
+    assert z["faces"].min() >= 0 and z["faces"].max() < counts["nodes"]
+    ref = reference_checkout()
+    path = None if ref is None else ref / "src/blab/solvers/julia_local/test_meshes" / f"{name}.msh"
+    if path is None or not path.exists():
+        pytest.skip("reference checkout not present")
+    mesh = meshes.read_gmsh22(path, 1.0)
+    assert np.array_equal(mesh.vertices, z["nodes_mm"])
+    assert np.array_equal(mesh.faces, z["faces"]) and np.array_equal(mesh.tags, z["tags"])

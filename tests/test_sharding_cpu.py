@@ -78,3 +78,26 @@ def test_two_gloo_ranks_match_single_process(tmp_path):
     p_ref, u_ref = sharding.sweep(_solve, freqs, 2)
     assert np.array_equal(got["p"], p_ref) and np.array_equal(got["u"], u_ref)
     assert torch is not None
+
+
+def test_bench_gpus_flag_starts_one_rank_per_gpu():
+    """``bench.py --gpus 2`` started without a launcher starts two ranks itself
+    (torch.distributed.run); in --plan mode each rank reports its frequency batches
+    (no GPU work) and rank 0 prints them: two ranks, disjoint batches in every step."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parents[1]
+    env = {k: v for k, v in __import__("os").environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    out = subprocess.run([sys.executable, str(root / "bench.py"), "--gpus", "2", "--plan", "--batch", "8",
+                          "--steps", "3", "--warmup", "3"], capture_output=True, text=True, timeout=240, env=env)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    plan = json.loads(lines[0])
+    assert plan["n_gpus"] == 2 and len(plan["rank_batches"]) == 2
+    for step in range(3 + 3):
+        a, b = (set(plan["rank_batches"][r][step]) for r in range(2))
+        assert len(a) == len(b) == 8 and not (a & b)
