@@ -61,6 +61,14 @@ WORKLOADS = {
                    text="closed box 0.3x0.2x0.25 m, {nf} triangles ({nv} P1 dofs), circular piston r=5 cm on +z "
                         "({nr} faces); 64 log-spaced freqs 200 Hz-12 kHz; {npt} observation points (2x73 polar + "
                         "2000 Fibonacci at 2 m)"),
+    "box1k": dict(mesh="box1k", f=(100.0, 8000.0, 16), polar=True, n_far=1000, form="mixed",
+                  text="closed box 0.3x0.2x0.25 m, {nf} triangles ({nv} dofs), circular piston r=5 cm on +z ({nr} "
+                       "faces); 16 log-spaced freqs 100 Hz-8 kHz; {npt} observation points (2x73 polar + 1000 "
+                       "Fibonacci at 2 m): the small jobs of the serving stream"),
+    "box2k": dict(mesh="box2k", f=(100.0, 8000.0, 16), polar=True, n_far=1000, form="mixed",
+                  text="closed box 0.3x0.2x0.25 m, {nf} triangles ({nv} dofs), circular piston r=5 cm on +z ({nr} "
+                       "faces); 16 log-spaced freqs 100 Hz-8 kHz; {npt} observation points (2x73 polar + 1000 "
+                       "Fibonacci at 2 m): the small jobs of the serving stream"),
     "horn20k": dict(mesh="horn20k", f=(500.0, 16000.0, 32), polar=False, n_far=5000, form="mixed",
                     text="exponential horn (throat r=2.5 cm, mouth r=15 cm, length 20 cm) in a 0.5x0.4x0.4 m box, "
                          "{nf} triangles ({nv} dofs), driven throat disc ({nr} faces); 32 log-spaced freqs "
@@ -75,6 +83,8 @@ def workload(name: str = "box10k", faces: int | None = None):
     spec = WORKLOADS[name]
     if faces is not None and name.startswith("box"):
         mesh = meshes.box_with_piston((0.3, 0.2, 0.25), faces, 0.05, "+z")
+    elif name in ("box1k", "box2k"):
+        mesh = meshes.box_with_piston((0.3, 0.2, 0.25), 1000 if name == "box1k" else 2000, 0.05, "+z")
     else:
         mesh = meshes.config_mesh(spec["mesh"])
     parts = []

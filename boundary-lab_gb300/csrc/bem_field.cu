@@ -178,6 +178,148 @@ __global__ void __launch_bounds__(256) field_f32_kernel(const FaceF32* __restric
   }
 }
 
+// The same sums for NFQ frequencies of a batch per CTA (blockIdx.y = group of
+// NFQ frequencies starting at NFQ * blockIdx.y).  Everything that does not
+// depend on the frequency is formed once per (point, face) and once per
+// (point, source) and shared by the NFQ frequencies: the double-float
+// distance |c_g - x| to the face anchor, the FP32 offset geometry, 1/r, the
+// compensated r - |c_g - x| and the normal derivative factor t.  Per frequency
+// remain the reduction of k|c_g - x|, the phase of each source, e^{ikr} and the
+// accumulation, with the arithmetic and the order of every sum of
+// field_f32_kernel.  Frequencies of
+// the last group beyond the batch are computed on the batch's last frequency and
+// not stored.
+template <int Q, int NC, int NFQ>
+__global__ void __launch_bounds__(256) field_f32_freqs_kernel(const FaceF32* __restrict__ faces, int nf,
+                                                              const float2* __restrict__ src,
+                                                              const float2* __restrict__ drive,  // NC x nf
+                                                              const double* __restrict__ obs, int nobs,
+                                                              const FieldParamsF32* __restrict__ prm, int batch,
+                                                              double2* __restrict__ out, FieldRule<float> fr, int ntr,
+                                                              int4 trs) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int o = blockIdx.x * 32 + lane;
+  const int f0 = blockIdx.y * NFQ;
+  const bool live = o < nobs;
+  const int oc = live ? o : nobs - 1;  // idle lanes repeat a live point; their result is dropped
+  const double xo[3] = {obs[3 * oc], obs[3 * oc + 1], obs[3 * oc + 2]};
+  float xhi[3], xlo[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    xhi[d] = (float)xo[d];
+    xlo[d] = (float)(xo[d] - (double)xhi[d]);
+  }
+  int bt[NFQ];
+  df kdf[NFQ];
+  float k[NFQ];
+  float2 qs[NFQ];
+#pragma unroll
+  for (int f = 0; f < NFQ; ++f) {
+    bt[f] = min(f0 + f, batch - 1);
+    kdf[f] = prm->kdf[bt[f]];
+    k[f] = prm->k[bt[f]];
+    qs[f] = prm->qscale[bt[f]];
+  }
+  float ar[NFQ][NC], ac[NFQ][NC], br[NFQ][NC], bcmp[NFQ][NC];
+#pragma unroll
+  for (int f = 0; f < NFQ; ++f)
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      ar[f][c] = 0.f;
+      ac[f][c] = 0.f;
+      br[f][c] = 0.f;
+      bcmp[f][c] = 0.f;
+    }
+  for (int ti = 0; ti < ntr; ++ti)
+  for (int g = wid; g < nf; g += kFieldWarps) {
+    const FaceF32& F = faces[g];
+    const int tr = ti == 0 ? trs.x : ti == 1 ? trs.y : ti == 2 ? trs.z : trs.w;
+    const float sg[3] = {(tr & 1) ? -1.f : 1.f, (tr & 2) ? -1.f : 1.f, 1.f};
+    const float nrm[3] = {sg[0] * F.normal[0], sg[1] * F.normal[1], F.normal[2]};
+    df C[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      df s = two_sum(sg[d] * F.anchor_hi[d], -xhi[d]);
+      s.lo += sg[d] * F.anchor_lo[d] - xlo[d];
+      C[d] = quick_two_sum(s.hi, s.lo);
+    }
+    df r2 = df_add(df_add(df_mul(C[0], C[0]), df_mul(C[1], C[1])), df_mul(C[2], C[2]));
+    df R = df_sqrt(r2);
+    const float R0 = R.hi + R.lo;
+    float theta0[NFQ];
+#pragma unroll
+    for (int f = 0; f < NFQ; ++f) theta0[f] = df_reduce_two_pi(df_mul(kdf[f], R));
+    const float Cf[3] = {C[0].hi + C[0].lo, C[1].hi + C[1].lo, C[2].hi + C[2].lo};
+    const float Cn = fmaf(Cf[0], nrm[0], fmaf(Cf[1], nrm[1], Cf[2] * nrm[2]));
+    float2 qg[NFQ][NC], fs[NFQ][NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const float2 dr = drive[(size_t)c * nf + g];
+#pragma unroll
+      for (int f = 0; f < NFQ; ++f) {
+        qg[f][c] = cscale(cmul(qs[f], dr), F.area2);
+        fs[f][c] = make_float2(0.f, 0.f);
+      }
+    }
+#pragma unroll
+    for (int n = 0; n < Q; ++n) {
+      const float d[3] = {sg[0] * F.off[3 * n], sg[1] * F.off[3 * n + 1], F.off[3 * n + 2]};
+      const float rv[3] = {Cf[0] + d[0], Cf[1] + d[1], Cf[2] + d[2]};
+      const float rr = fmaf(rv[0], rv[0], fmaf(rv[1], rv[1], rv[2] * rv[2]));
+      const float rinv = rr > 1e-30f ? rsqrt_ftz(rr) : 0.f;
+      const float r = rr * rinv;
+      const float cd = fmaf(Cf[0], d[0], fmaf(Cf[1], d[1], Cf[2] * d[2]));
+      const float dd = fmaf(d[0], d[0], fmaf(d[1], d[1], d[2] * d[2]));
+      const float delta = fmaf(2.f, cd, dd) * rcp_ftz(fmaxf(r + R0, 1e-30f));
+      const float sc = rinv * BEM_INV_FOUR_PI;
+      const float t = (Cn + fmaf(d[0], nrm[0], fmaf(d[1], nrm[1], d[2] * nrm[2]))) * rinv;
+      const float wn = fr.w[n];
+#pragma unroll
+      for (int f = 0; f < NFQ; ++f) {
+        const float th = reduce_two_pi(fmaf(k[f], delta, theta0[f]));
+        float sn, cs;
+        sincos_ftz(th, &sn, &cs);
+        const float2 G = make_float2(cs * sc, sn * sc);
+        const float2 Dk = make_float2(t * (-G.x * rinv - G.y * k[f]), t * (G.x * k[f] - G.y * rinv));
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          const float2 ps = src[(((size_t)bt[f] * NC + c) * nf + g) * Q + n];
+          const float2 qq = cscale(qg[f][c], wn);
+          fs[f][c] = cadd(fs[f][c], csub(cmul(Dk, ps), cmul(G, qq)));
+        }
+      }
+    }
+#pragma unroll
+    for (int f = 0; f < NFQ; ++f)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        kahan_add(ar[f][c], ac[f][c], fs[f][c].x);
+        kahan_add(br[f][c], bcmp[f][c], fs[f][c].y);
+      }
+  }
+  __shared__ double2 red[kFieldWarps][NC][32];
+#pragma unroll
+  for (int f = 0; f < NFQ; ++f) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+      red[wid][c][lane] =
+          make_double2((double)ar[f][c] - (double)ac[f][c], (double)br[f][c] - (double)bcmp[f][c]);
+    __syncthreads();
+    if (wid == 0 && live && f0 + f < batch) {
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        double vr = 0.0, vi = 0.0;
+        for (int w = 0; w < kFieldWarps; ++w) {
+          vr += red[w][c][lane].x;
+          vi += red[w][c][lane].y;
+        }
+        out[((size_t)(f0 + f) * NC + c) * nobs + o] = make_double2(vr, vi);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 struct FieldParamsF64 {
   double k[64];
   double2 qscale[64];
@@ -258,6 +400,8 @@ __global__ void __launch_bounds__(256) field_f64_kernel(const FaceF64* __restric
 
 }  // namespace
 
+int sm_count();
+
 static df host_df(double x) {
   df r;
   r.hi = (float)x;
@@ -281,7 +425,6 @@ cudaError_t launch_field(const DeviceMesh& m, Precision prec, int batch, const d
   }
   const int total = batch * nc * m.nf * m.Q;
   dim3 grid(nobs, batch);
-  dim3 grid32((nobs + 31) / 32, batch);  // FP32 kernel: 32 observation points per CTA
   if (prec == Precision::Mixed) {
     field_sources_kernel<float><<<(total + 255) / 256, 256, 0, stream>>>(m.faces, m.area, m.nf, m.Q, nc,
                                                                          (const float2*)pressure, ldp,
@@ -294,23 +437,45 @@ cudaError_t launch_field(const DeviceMesh& m, Precision prec, int batch, const d
     }
     FieldParamsF32* dp = (FieldParamsF32*)((char*)sources + (((size_t)total * sizeof(float2) + 255) / 256) * 256);
     cudaMemcpyAsync(dp, &hp, sizeof(hp), cudaMemcpyHostToDevice, stream);
-#define BEM_F32(QQ, NCC)                                                                                   \
-  field_f32_kernel<QQ, NCC><<<grid32, 256, 0, stream>>>(m.faces32, m.nf, (const float2*)sources,           \
-                                                      (const float2*)drive, obs, nobs, dp, out, fr32, m.ntr, \
-                                                      make_int4(m.tr[0], m.tr[1], m.tr[2], m.tr[3]))
-#define BEM_F32_Q(NCC)    \
-  if (m.Q == 6)           \
-    BEM_F32(6, NCC);      \
-  else if (m.Q == 3)      \
-    BEM_F32(3, NCC);      \
-  else                    \
-    BEM_F32(1, NCC);
-    switch (nc) {
-      case 1: BEM_F32_Q(1) break;
-      case 2: BEM_F32_Q(2) break;
-      case 3: BEM_F32_Q(3) break;
-      default: BEM_F32_Q(4) break;
+    // NFQ frequencies per CTA share the frequency-independent geometry; the
+    // largest NFQ (4 or 2, NFQ x nc <= 4) whose grid still fills every SM twice
+    const long long pt_blocks = (nobs + 31) / 32;
+    int nfq = 1;
+    for (int cand = 4; cand >= 2; cand /= 2)
+      if (cand * nc <= 4 && cand <= batch && pt_blocks * ((batch + cand - 1) / cand) >= 2LL * sm_count()) {
+        nfq = cand;
+        break;
+      }
+    const int4 trs = make_int4(m.tr[0], m.tr[1], m.tr[2], m.tr[3]);
+    auto run = [&](auto kern, int nf_per_cta) {
+      dim3 g((unsigned)pt_blocks, (unsigned)((batch + nf_per_cta - 1) / nf_per_cta));
+      kern<<<g, 256, 0, stream>>>(m.faces32, m.nf, (const float2*)sources, (const float2*)drive, obs, nobs, dp,
+                                  batch, out, fr32, m.ntr, trs);
+    };
+#define BEM_F32(QQ, NCC, NFQQ) run(field_f32_freqs_kernel<QQ, NCC, NFQQ>, NFQQ)
+#define BEM_F32_Q(NCC, NFQQ) \
+  if (m.Q == 6)              \
+    BEM_F32(6, NCC, NFQQ);   \
+  else if (m.Q == 3)         \
+    BEM_F32(3, NCC, NFQQ);   \
+  else                       \
+    BEM_F32(1, NCC, NFQQ);
+    if (nc == 1 && nfq == 4) {
+      BEM_F32_Q(1, 4)
+    } else if (nc == 1 && nfq == 2) {
+      BEM_F32_Q(1, 2)
+    } else if (nc == 2 && nfq == 2) {
+      BEM_F32_Q(2, 2)
+    } else {
+      switch (nc) {
+        case 1: BEM_F32_Q(1, 1) break;
+        case 2: BEM_F32_Q(2, 1) break;
+        case 3: BEM_F32_Q(3, 1) break;
+        default: BEM_F32_Q(4, 1) break;
+      }
     }
+#undef BEM_F32_Q
+#undef BEM_F32
   } else {
     field_sources_kernel<double><<<(total + 255) / 256, 256, 0, stream>>>(m.faces, m.area, m.nf, m.Q, nc,
                                                                           (const double2*)pressure, ldp,
