@@ -539,6 +539,7 @@ def main() -> None:
         # serving stream: seeded Poisson arrivals of mixed-size jobs, latency per job
         if args.serving_jobs > 0 and args.workload == "box10k":
             result["serving"] = serving_run(args, local_rank)
+            result["small_jobs"] = small_jobs_run(local_rank)
         # retained-trace field (the bem_field operation): one request per call, host traces
         if args.workload == "box10k":
             result["retained_field"] = retained_field_run(mesh, local_rank)
@@ -634,6 +635,44 @@ def retained_field_run(mesh, device: int, n_points: int = 5000, calls: int = 8) 
                     "C ABI bem_evaluate_field), 3-point rule, mixed form, 2,500 Hz, 5,000 points at 2 m",
             "ms_per_request": dt * 1e3, "points": n_points, "faces": int(mesh.n_faces),
             "green_evaluations_per_s": pairs / dt}
+
+
+def small_jobs_run(device: int, n_jobs: int = 24, n_freq: int = 8) -> dict:
+    """Small jobs submitted at once (seeded boxes and cube-spheres of 900-1,200 triangles,
+    8 log-spaced frequencies 300 Hz - 6 kHz each), run three ways on one GPU: one job at a
+    time, four jobs at a time on their own streams, and four workers whose small jobs of
+    similar size share launches (bem_solve_jobs).  Frequency solves/s from first submit
+    to last result, mixed form."""
+    serving = pkg("serving")
+    meshes = pkg("meshes")
+    request = pkg("request")
+    _, horizontal, vertical, _ = request.polar_observation_points({"step_size": 5.0, "distance": 2.0})
+    points = np.concatenate([horizontal, vertical, request.fibonacci_sphere(500, 2.0)])
+    rng = np.random.default_rng(5)
+    specs = [(meshes.seeded_piston_mesh(int(rng.integers(900, 1200)), int(rng.integers(1 << 30))),
+              np.geomspace(300.0, 6000.0, n_freq)) for _ in range(n_jobs)]
+
+    def jobs():
+        return [serving.ServingJob(vertices=m.vertices, faces=m.faces,
+                                   drive=(m.tags == meshes.RADIATOR_TAG).astype(np.complex128)[None, :],
+                                   points=points, freqs_hz=f, chunk=n_freq, job_id=f"small-{i}")
+                for i, (m, f) in enumerate(specs)]
+
+    out = {"what": f"{n_jobs} jobs of 900-1,200 triangles x {n_freq} freqs (300 Hz - 6 kHz) submitted at once, "
+                   "2x73 polar + 500 Fibonacci points, mixed form; frequency solves/s from first submit to last result"}
+    for name, running, group in (("one_at_a_time", 1, 0), ("four_streams", 4, 0), ("shared_launches", 4, 3000)):
+        with serving.ServingScheduler(device, max_running=running, policy="fifo", group_faces=group) as sch:
+            warm = sch.submit(jobs()[0])  # page in kernels of this worker set
+            sch.drain(300)
+            t0 = time.perf_counter()
+            js = [sch.submit(j) for j in jobs()]
+            sch.drain(600)
+            wall = time.perf_counter() - t0
+        done = [j for j in js if j.status == "completed"]
+        out[name] = {"max_running": running, "frequency_solves_per_s": len(done) * n_freq / wall, "wall_s": wall,
+                     "jobs_in_shared_launches": sum(j.group_size > 1 for j in done),
+                     "failed": [j.error for j in js if j.status != "completed"][:2], "warm_status": warm.status}
+    return out
 
 
 def serving_run(args, device: int) -> dict:

@@ -252,14 +252,17 @@ Layout layout_for(const bem::DeviceMesh& dm, bem::Precision prec) {
 int assembly_group(bem::Precision prec) { return prec == bem::Precision::Mixed ? 2 : 1; }
 
 // Assemble the LHS (c[i].cD, cH, cM) of cnt frequencies into A[i] (and A2[i] if
-// given) and, if nc > 0, the RHS into b[i] (nc columns, leading dimension ldb,
-// permuted rows).  Returns the number of kernels launched.
+// given; column-major, leading dimension lda) and, if nc > 0, the RHS into b[i]
+// (nc columns, leading dimension ldb, permuted rows).  lda / ldb <= 0: the mesh's
+// own layout.  Returns the number of kernels launched.
 long long assemble_frequencies(bem_mesh* m, bem::Precision prec, int cnt, const double* k,
                                const bem::OperatorCoeffs* c, void* const* A, void* const* A2, const double2* qscale,
-                               int nc, const void* drive, void* const* b) {
+                               int nc, const void* drive, void* const* b, long long lda = 0, long long ldb = 0) {
   bem_context* ctx = m->ctx;
   const bem::DeviceMesh& dm = m->dm;
   Layout L = layout_for(dm, prec);
+  if (lda > 0) L.lda = lda;
+  if (ldb > 0) L.ldb = ldb;
   const int G = std::min(assembly_group(prec), cnt);
   const size_t rext_n = (size_t)L.ldR * 3 * dm.nf;         // elements per extended-row buffer
   const size_t sblk_n = (size_t)std::max(dm.npairs, 1) * 12;  // elements per singular-block buffer
@@ -693,14 +696,303 @@ namespace {
 // Automatic batch: the matrices of a batch within ~16 GiB, at most 32, and at
 // most as many as the LU's cluster panels keep resident at once (a larger batch
 // runs every panel in two waves); the sweep is then split into equal batches.
-int auto_batch(const bem_mesh* m, bem::Precision prec, int n_freq) {
-  const Layout L = layout_for(m->dm, prec);
-  const double per = (double)L.lda * m->dm.nv * L.esz * (prec == bem::Precision::Mixed ? 2 : 1);
+int auto_batch_order(int nv, bem::Precision prec, int n_freq) {
+  const double esz = prec == bem::Precision::Mixed ? sizeof(float2) : sizeof(double2);
+  const double per = (double)round_up(nv, 32) * nv * esz * (prec == bem::Precision::Mixed ? 2 : 1);
   int cap = (int)std::max(1.0, std::min(32.0, std::floor(16.0 * (1ull << 30) / per)));
-  cap = std::max(1, std::min(cap, bem::lu_resident_batch(prec, m->dm.nv)));
+  cap = std::max(1, std::min(cap, bem::lu_resident_batch(prec, nv)));
   if (n_freq <= 0) return cap;  // the largest batch
   const int nbatch = (n_freq + cap - 1) / cap;
   return (n_freq + nbatch - 1) / nbatch;
+}
+int auto_batch(const bem_mesh* m, bem::Precision prec, int n_freq) { return auto_batch_order(m->dm.nv, prec, n_freq); }
+
+// Rows and columns nv .. n-1 of cnt matrices of order n (leading dimension lda,
+// stride) hold the identity: zero below row nv in columns < nv, and a unit
+// column in each column >= nv.  Grid (n, cnt).
+template <typename C2>
+__global__ void pad_identity_kernel(C2* A, C2* A2, long long lda, long long stride, int nv, int n) {
+  const int j = blockIdx.x;
+  const size_t off = (size_t)blockIdx.y * stride + (size_t)j * lda;
+  for (int r = (j < nv ? nv : 0) + threadIdx.x; r < n; r += blockDim.x) {
+    C2 v;
+    v.x = r == j ? 1 : 0;
+    v.y = 0;
+    A[off + r] = v;
+    if (A2) A2[off + r] = v;
+  }
+}
+
+// cnt consecutive frequencies of one mesh inside a combined batch, with the
+// places their results go (already offset; either may be null).
+struct Slice {
+  bem_mesh* m;
+  const double* freqs;
+  int cnt;
+  double* pressure_out;  // [cnt][nc][nv] complex
+  double* field_out;     // [cnt][nc][nobs] complex
+};
+
+// Totals over the batches of one call.
+struct SolveTotals {
+  double kacc[BEM_K_SLOTS] = {0};
+  double t_asm = 0, t_sol = 0, t_fld = 0, max_res = 0;
+  int max_steps = 0, batches = 0, gemm_used = 0;
+  long long launches = 0;
+};
+
+// One batch: every slice's frequencies are assembled on the slice's own mesh into
+// matrices of order n (n >= each slice mesh's nv; the rows and columns beyond a
+// mesh's nv hold the identity and its right-hand sides are zero there), all the
+// matrices are factored, solved and refined together (one launch sequence), and
+// each slice's field is evaluated on its own mesh.  The identity block cannot
+// change a pivot (its rows are zero in the mesh's columns), so each mesh's
+// factors are those of its own matrix.  Every slice has the same number of
+// excitations nc.
+void solve_combined(bem_context* ctx, const std::vector<Slice>& sl, int n, const bem_solve_options& o, int nc,
+                    SolveTotals& T) {
+  const bem::Precision prec = o.precision == BEM_PRECISION_MIXED ? bem::Precision::Mixed : bem::Precision::FP64;
+  const bool mixed = prec == bem::Precision::Mixed;
+  const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
+  const long long lda = round_up(n, 32), ldb = round_up(n, 32);
+  int B = 0;
+  for (const Slice& x : sl) B += x.cnt;
+  const int nb = o.lu_block > 0 ? std::min(o.lu_block, 64) : 0;  // 0: the LU chooses
+  const size_t matsz = (size_t)lda * n * esz;
+  ck(ctx->mats.ensure(matsz * B), "alloc matrices");
+  if (mixed) ck(ctx->mats2.ensure(matsz * B), "alloc matrix copies");
+  ck(ctx->ipiv.ensure((size_t)B * n * sizeof(int)), "alloc pivots");
+  ck(ctx->perm.ensure((size_t)B * n * sizeof(int)), "alloc permutation");
+  ck(ctx->info.ensure((size_t)B * sizeof(int)), "alloc info");
+  ck(ctx->rowmap.ensure((size_t)B * bem::kRowmapStride * sizeof(int)), "alloc row map");
+  const size_t vecn = (size_t)B * nc * ldb;
+  ck(ctx->b32.ensure(vecn * esz), "alloc rhs");
+  if (mixed) {
+    ck(ctx->b64.ensure(vecn * sizeof(double2)), "alloc rhs64");
+    ck(ctx->x64.ensure(vecn * sizeof(double2)), "alloc x");
+    ck(ctx->r64.ensure(vecn * sizeof(double2)), "alloc r");
+    ck(ctx->d32.ensure(vecn * sizeof(float2)), "alloc d");
+    ck(ctx->xsplit.ensure(vecn * sizeof(float4)), "alloc x split");
+    ck(ctx->norms.ensure((size_t)B * nc * 2 * sizeof(double)), "alloc norms");
+  }
+  bool any_field = false;
+  for (const Slice& x : sl) {
+    if (!x.field_out) continue;
+    any_field = true;
+    const bem::DeviceMesh& dm = x.m->dm;
+    const size_t srcb = (size_t)x.cnt * nc * dm.nf * dm.Q * esz;
+    ck(ctx->fsrc.ensure(round_up(srcb, 256) + 4096), "alloc field sources");
+    ck(ctx->fout.ensure((size_t)x.cnt * nc * x.m->nobs * sizeof(double2)), "alloc field out");
+  }
+  if (any_field && mixed) ck(ctx->pout.ensure(vecn * sizeof(float2)), "alloc pressure f32");
+  std::vector<double> norms((size_t)B * nc * 2);
+  std::vector<int> info(B);
+  std::vector<double> ks(B), fz(B);
+  std::vector<double2> qs(B);
+  std::vector<bem::OperatorCoeffs> cs(B);
+  std::vector<void*> As(B), A2s(B), bs(B);
+  ++T.batches;
+  cudaEventRecord(ctx->ev[0], ctx->stream);
+  prof_begin(ctx);
+  int i0 = 0;
+  for (const Slice& x : sl) {
+    for (int i = 0; i < x.cnt; ++i) {
+      const int g = i0 + i;
+      const double omega = 2.0 * M_PI * x.freqs[i];
+      const double k = omega / o.sound_speed;
+      fz[g] = x.freqs[i];
+      ks[g] = k;
+      qs[g] = make_double2(0.0, o.rho * omega);
+      cs[g] = bm_coeffs(k);
+      As[g] = (char*)ctx->mats.p + matsz * g;
+      A2s[g] = mixed ? (char*)ctx->mats2.p + matsz * g : nullptr;
+      bs[g] = (char*)ctx->b32.p + (size_t)g * nc * ldb * esz;
+    }
+    const int nvm = x.m->dm.nv;
+    if (nvm < n)
+      ck(cudaMemsetAsync(bs[i0], 0, (size_t)x.cnt * nc * ldb * esz, ctx->stream), "memset padded rhs");
+    const void* drive = mixed ? x.m->drive32.p : x.m->drive64.p;
+    T.launches += assemble_frequencies(x.m, prec, x.cnt, ks.data() + i0, cs.data() + i0, As.data() + i0,
+                                       mixed ? A2s.data() + i0 : nullptr, qs.data() + i0, nc, drive, bs.data() + i0,
+                                       lda, ldb);
+    if (nvm < n) {
+      dim3 g((unsigned)n, (unsigned)x.cnt);
+      if (mixed)
+        pad_identity_kernel<float2><<<g, 128, 0, ctx->stream>>>((float2*)As[i0], (float2*)A2s[i0], lda,
+                                                                (long long)lda * n, nvm, n);
+      else
+        pad_identity_kernel<double2><<<g, 128, 0, ctx->stream>>>((double2*)As[i0], nullptr, lda, (long long)lda * n,
+                                                                 nvm, n);
+      ck(cudaGetLastError(), "pad kernel");
+      T.launches += 1;
+    }
+    i0 += x.cnt;
+  }
+  cudaEventRecord(ctx->ev[1], ctx->stream);
+  ck(cudaMemsetAsync(ctx->info.p, 0, (size_t)B * sizeof(int), ctx->stream), "memset info");
+  bool used_tensor = false;
+  int* tc_err = nullptr;
+  void* tcws = nullptr;
+  if (mixed && o.lu_gemm != (int)bem::LuGemm::Cublas && bem::tc_gemm_available()) {
+    ck(ctx->tcws.ensure(bem::tc_gemm_workspace_bytes(n, B)), "alloc tensor-core workspace");
+    tcws = ctx->tcws.p;
+  }
+  int lu_launches = 0;
+  ck(bem::lu_factor_batched(prec, ctx->mats.p, lda, n, B, (int*)ctx->ipiv.p, (int*)ctx->info.p, nb, ctx->cublas,
+                            ctx->stream, (bem::LuGemm)o.lu_gemm, tcws, &used_tensor, &tc_err, (int*)ctx->rowmap.p,
+                            &lu_launches),
+     "LU factorisation");
+  // kernels of this batch besides the assembly: the LU, the permutation, the solves
+  // (mixed: 6 + 6 per refinement step), the field (2, +1 mixed, per slice)
+  T.launches += lu_launches + 1;
+  T.gemm_used = mixed ? (used_tensor ? 2 : 1) : 0;
+  ck(bem::lu_perm_batched((const int*)ctx->ipiv.p, n, B, (int*)ctx->perm.p, ctx->stream), "pivot permutation");
+  prof_mark(ctx, BEM_K_LU);
+  ck(cudaMemcpyAsync(info.data(), ctx->info.p, (size_t)B * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream),
+     "copy info");
+  const long long nvec = (long long)B * nc * ldb;
+  if (!mixed) {
+    ck(bem::lu_solve_cluster_batched(prec, ctx->mats.p, lda, n, B, (const int*)ctx->perm.p, ctx->b32.p, ldb, nc,
+                                     ctx->stream),
+       "LU solve");
+    T.launches += 1;
+  } else {
+    double2* x = (double2*)ctx->x64.p;
+    double2* r = (double2*)ctx->r64.p;
+    double2* b64 = (double2*)ctx->b64.p;
+    float2* d = (float2*)ctx->d32.p;
+    ck(bem::convert_f32_to_f64((const float2*)ctx->b32.p, b64, nvec, ctx->stream), "convert rhs");
+    ck(cudaMemcpyAsync(d, ctx->b32.p, nvec * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream), "copy rhs");
+    ck(bem::lu_solve_cluster_batched(prec, ctx->mats.p, lda, n, B, (const int*)ctx->perm.p, d, ldb, nc, ctx->stream),
+       "LU solve");
+    ck(cudaMemsetAsync(x, 0, nvec * sizeof(double2), ctx->stream), "memset x");
+    ck(bem::axpy_f32_into_f64(d, x, nvec, ctx->stream), "axpy");
+    int steps = 0;
+    double worst = 0;
+    for (;;) {
+      ck(bem::residual_batched(prec, ctx->mats2.p, lda, n, B, x, b64, ldb, nc, r, ctx->xsplit.p, ctx->stream),
+         "residual");
+      ck(bem::norms_batched(r, b64, ldb, n, B * nc, (double*)ctx->norms.p, ctx->stream), "norms");
+      ck(cudaMemcpyAsync(norms.data(), ctx->norms.p, (size_t)B * nc * 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                         ctx->stream),
+         "copy norms");
+      ck(cudaStreamSynchronize(ctx->stream), "refinement sync");
+      worst = 0;
+      for (int i = 0; i < B * nc; ++i) {
+        const double rel = norms[2 * i + 1] > 0 ? std::sqrt(norms[2 * i] / norms[2 * i + 1]) : std::sqrt(norms[2 * i]);
+        if (!std::isfinite(rel)) worst = INFINITY;
+        else worst = std::max(worst, rel);
+      }
+      if (worst <= o.refine_tol || steps >= o.max_refine || !std::isfinite(worst)) break;
+      ck(bem::convert_f64_to_f32(r, d, nvec, ctx->stream), "convert residual");
+      ck(bem::lu_solve_cluster_batched(prec, ctx->mats.p, lda, n, B, (const int*)ctx->perm.p, d, ldb, nc,
+                                       ctx->stream),
+         "LU solve");
+      ck(bem::axpy_f32_into_f64(d, x, nvec, ctx->stream), "axpy");
+      ++steps;
+    }
+    T.max_steps = std::max(T.max_steps, steps);
+    T.max_res = std::max(T.max_res, worst);
+    T.launches += 6 + 6LL * steps;  // 3 + (x split, residual, norms) per check + (convert, solve, axpy) per step
+  }
+  prof_mark(ctx, BEM_K_SOLVE);
+  cudaEventRecord(ctx->ev[2], ctx->stream);
+  ck(cudaStreamSynchronize(ctx->stream), "solve sync");
+  if (used_tensor && tc_err) {
+    int h = 0;
+    ck(cudaMemcpyAsync(&h, tc_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "read tensor-core status");
+    ck(cudaStreamSynchronize(ctx->stream), "read tensor-core status");
+    if (h != 0)
+      throw BemError{BEM_ERR_CUDA, "tensor-core LU update gave up waiting (status " + std::to_string(h) + ")"};
+  }
+  for (int i = 0; i < B; ++i)
+    if (info[i] != 0)
+      throw BemError{BEM_ERR_SINGULAR, "zero pivot in LU factorisation (frequency " + std::to_string(fz[i]) + " Hz)"};
+  // solutions (vertex order) as [B][nc][ldb]
+  const char* sol = mixed ? (const char*)ctx->x64.p : (const char*)ctx->b32.p;
+  const cudaMemcpyKind kind = o.outputs_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (any_field && mixed)
+    ck(bem::convert_f64_to_f32((const double2*)ctx->x64.p, (float2*)ctx->pout.p, nvec, ctx->stream), "convert");
+  i0 = 0;
+  for (const Slice& x : sl) {
+    if (x.field_out) {
+      const bem::DeviceMesh& dm = x.m->dm;
+      const void* p_for_field = mixed ? (const void*)((const float2*)ctx->pout.p + (size_t)i0 * nc * ldb)
+                                      : (const void*)((const double2*)ctx->b32.p + (size_t)i0 * nc * ldb);
+      const void* drive = mixed ? x.m->drive32.p : x.m->drive64.p;
+      ck(bem::launch_field(dm, prec, x.cnt, ks.data() + i0, qs.data() + i0, p_for_field, ldb, nc, drive,
+                           (const double*)x.m->obs.p, x.m->nobs, ctx->fsrc.p, (double2*)ctx->fout.p, ctx->stream),
+         "field kernel");
+      T.launches += 2;
+      ck(cudaMemcpyAsync(x.field_out, ctx->fout.p, (size_t)x.cnt * nc * x.m->nobs * sizeof(double2), kind,
+                         ctx->stream),
+         "copy field");
+    }
+    i0 += x.cnt;
+  }
+  if (any_field) {
+    if (mixed) T.launches += 1;
+    prof_mark(ctx, BEM_K_FIELD);
+  }
+  cudaEventRecord(ctx->ev[3], ctx->stream);
+  i0 = 0;
+  for (const Slice& x : sl) {
+    if (x.pressure_out) {  // [cnt][nc][nv] complex128 from [cnt][nc][ldb]
+      const int nvm = x.m->dm.nv;
+      ck(cudaMemcpy2DAsync(x.pressure_out, (size_t)nvm * sizeof(double2), sol + (size_t)i0 * nc * ldb * sizeof(double2),
+                           (size_t)ldb * sizeof(double2), (size_t)nvm * sizeof(double2), (size_t)x.cnt * nc, kind,
+                           ctx->stream),
+         "copy pressure");
+    }
+    i0 += x.cnt;
+  }
+  ck(cudaStreamSynchronize(ctx->stream), "batch sync");
+  prof_collect(ctx, T.kacc);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+  T.t_asm += ms * 1e-3;
+  cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+  T.t_sol += ms * 1e-3;
+  cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+  T.t_fld += ms * 1e-3;
+}
+
+void fill_stats(bem_solve_stats* stats, const SolveTotals& T) {
+  if (!stats) return;
+  stats->assembly_s = T.t_asm;
+  stats->solve_s = T.t_sol;
+  stats->field_s = T.t_fld;
+  stats->max_refine_steps = T.max_steps;
+  stats->max_rel_residual = T.max_res;
+  stats->batches = T.batches;
+  for (int i = 0; i < 8; ++i) stats->kernel_s[i] = T.kacc[i];
+  stats->lu_gemm_used = T.gemm_used;
+  stats->kernel_launches = T.launches;
+}
+
+bool valid_options(bem_context* ctx, const bem_solve_options& o) {
+  if (!(o.sound_speed > 0) || !(o.rho > 0)) {
+    fail(ctx, BEM_ERR_INVALID_ARGUMENT, "sound_speed and rho must be > 0");
+    return false;
+  }
+  if (o.precision != BEM_PRECISION_FP64 && o.precision != BEM_PRECISION_MIXED) {
+    fail(ctx, BEM_ERR_INVALID_ARGUMENT, "unknown precision");
+    return false;
+  }
+  return true;
+}
+
+bool valid_freqs(bem_context* ctx, const double* freqs_hz, int n_freq) {
+  if (!freqs_hz || n_freq < 1) {
+    fail(ctx, BEM_ERR_INVALID_ARGUMENT, "need at least one frequency");
+    return false;
+  }
+  for (int i = 0; i < n_freq; ++i)
+    if (!(freqs_hz[i] > 0) || !std::isfinite(freqs_hz[i])) {
+      fail(ctx, BEM_ERR_INVALID_ARGUMENT, "frequencies must be finite and positive");
+      return false;
+    }
+  return true;
 }
 }  // namespace
 
@@ -739,214 +1031,97 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
     bem_solve_options o;
     bem_default_options(&o);
     if (opt) o = *opt;
-    if (!freqs_hz || n_freq < 1) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "need at least one frequency");
+    if (!valid_freqs(ctx, freqs_hz, n_freq)) return BEM_ERR_INVALID_ARGUMENT;
     if (m->nc < 1) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "no excitation set (bem_set_excitation)");
     if (field_out && m->nobs < 1) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "no observation points set");
-    if (!(o.sound_speed > 0) || !(o.rho > 0)) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "sound_speed and rho must be > 0");
-    if (o.precision != BEM_PRECISION_FP64 && o.precision != BEM_PRECISION_MIXED)
-      return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "unknown precision");
-    for (int i = 0; i < n_freq; ++i)
-      if (!(freqs_hz[i] > 0) || !std::isfinite(freqs_hz[i]))
-        return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "frequencies must be finite and positive");
+    if (!valid_options(ctx, o)) return BEM_ERR_INVALID_ARGUMENT;
     const bem::Precision prec = o.precision == BEM_PRECISION_MIXED ? bem::Precision::Mixed : bem::Precision::FP64;
-    const bool mixed = prec == bem::Precision::Mixed;
     const bem::DeviceMesh& dm = m->dm;
     const int nv = dm.nv, nc = m->nc;
-    Layout L = layout_for(dm, prec);
     int B = o.batch > 0 ? std::min(o.batch, 64) : auto_batch(m, prec, n_freq);
     B = std::min(B, n_freq);
-    const int nb = o.lu_block > 0 ? std::min(o.lu_block, 64) : 0;  // 0: the LU chooses
-    const size_t matsz = (size_t)L.lda * nv * L.esz;
-    ck(ctx->mats.ensure(matsz * B), "alloc matrices");
-    if (mixed) ck(ctx->mats2.ensure(matsz * B), "alloc matrix copies");
-    ck(ctx->ipiv.ensure((size_t)B * nv * sizeof(int)), "alloc pivots");
-    ck(ctx->perm.ensure((size_t)B * nv * sizeof(int)), "alloc permutation");
-    ck(ctx->info.ensure((size_t)B * sizeof(int)), "alloc info");
-    ck(ctx->rowmap.ensure((size_t)B * bem::kRowmapStride * sizeof(int)), "alloc row map");
-    const size_t vecn = (size_t)B * nc * L.ldb;
-    ck(ctx->b32.ensure(vecn * L.esz), "alloc rhs");
-    if (mixed) {
-      ck(ctx->b64.ensure(vecn * sizeof(double2)), "alloc rhs64");
-      ck(ctx->x64.ensure(vecn * sizeof(double2)), "alloc x");
-      ck(ctx->r64.ensure(vecn * sizeof(double2)), "alloc r");
-      ck(ctx->d32.ensure(vecn * sizeof(float2)), "alloc d");
-      ck(ctx->xsplit.ensure(vecn * sizeof(float4)), "alloc x split");
-      ck(ctx->norms.ensure((size_t)B * nc * 2 * sizeof(double)), "alloc norms");
-    }
-    if (field_out) {
-      const size_t srcb = (size_t)B * nc * dm.nf * dm.Q * L.esz;
-      ck(ctx->fsrc.ensure(round_up(srcb, 256) + 4096), "alloc field sources");
-      ck(ctx->fout.ensure((size_t)B * nc * m->nobs * sizeof(double2)), "alloc field out");
-      if (mixed) ck(ctx->pout.ensure(vecn * sizeof(float2)), "alloc pressure f32");
-    }
-    const void* drive = mixed ? m->drive32.p : m->drive64.p;
-    std::vector<double> norms((size_t)B * nc * 2);
-    std::vector<int> info(B);
-    double kacc[BEM_K_SLOTS] = {0};
-    int gemm_used = 0;
-    long long launches = 0;
     ctx->prof = o.profile != 0;
-    double t_asm = 0, t_sol = 0, t_fld = 0, max_res = 0;
-    int max_steps = 0, batches = 0;
+    SolveTotals T;
     for (int f0 = 0; f0 < n_freq; f0 += B) {
       const int bt = std::min(B, n_freq - f0);
-      ++batches;
-      std::vector<double> ks(bt);
-      std::vector<double2> qs(bt);
-      cudaEventRecord(ctx->ev[0], ctx->stream);
-      prof_begin(ctx);
-      std::vector<bem::OperatorCoeffs> cs(bt);
-      std::vector<void*> As(bt), A2s(bt), bs(bt);
-      for (int i = 0; i < bt; ++i) {
-        const double omega = 2.0 * M_PI * freqs_hz[f0 + i];
-        const double k = omega / o.sound_speed;
-        ks[i] = k;
-        qs[i] = make_double2(0.0, o.rho * omega);
-        cs[i] = bm_coeffs(k);
-        As[i] = (char*)ctx->mats.p + matsz * i;
-        A2s[i] = mixed ? (char*)ctx->mats2.p + matsz * i : nullptr;
-        bs[i] = (char*)ctx->b32.p + (size_t)i * nc * L.ldb * L.esz;
-      }
-      launches += assemble_frequencies(m, prec, bt, ks.data(), cs.data(), As.data(), mixed ? A2s.data() : nullptr,
-                                       qs.data(), nc, drive, bs.data());
-      cudaEventRecord(ctx->ev[1], ctx->stream);
-      ck(cudaMemsetAsync(ctx->info.p, 0, (size_t)bt * sizeof(int), ctx->stream), "memset info");
-      bool used_tensor = false;
-      int* tc_err = nullptr;
-      void* tcws = nullptr;
-      if (mixed && o.lu_gemm != (int)bem::LuGemm::Cublas && bem::tc_gemm_available()) {
-        ck(ctx->tcws.ensure(bem::tc_gemm_workspace_bytes(nv, B)), "alloc tensor-core workspace");
-        tcws = ctx->tcws.p;
-      }
-      int lu_launches = 0;
-      ck(bem::lu_factor_batched(prec, ctx->mats.p, L.lda, nv, bt, (int*)ctx->ipiv.p, (int*)ctx->info.p, nb,
-                                ctx->cublas, ctx->stream, (bem::LuGemm)o.lu_gemm, tcws, &used_tensor, &tc_err,
-                                (int*)ctx->rowmap.p, &lu_launches),
-         "LU factorisation");
-      // kernels of this batch besides the assembly: the LU, the permutation, the solves
-      // (mixed: 5 + 5 per refinement step), the field (2, +1 mixed)
-      launches += lu_launches + 1;
-      gemm_used = mixed ? (used_tensor ? 2 : 1) : 0;
-      ck(bem::lu_perm_batched((const int*)ctx->ipiv.p, nv, bt, (int*)ctx->perm.p, ctx->stream), "pivot permutation");
-      prof_mark(ctx, BEM_K_LU);
-      ck(cudaMemcpyAsync(info.data(), ctx->info.p, (size_t)bt * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream),
-         "copy info");
-      const long long nvec = (long long)bt * nc * L.ldb;
-      if (!mixed) {
-        ck(bem::lu_solve_cluster_batched(prec, ctx->mats.p, L.lda, nv, bt, (const int*)ctx->perm.p, ctx->b32.p, L.ldb, nc, ctx->stream),
-           "LU solve");
-        launches += 1;
-      } else {
-        double2* x = (double2*)ctx->x64.p;
-        double2* r = (double2*)ctx->r64.p;
-        double2* b64 = (double2*)ctx->b64.p;
-        float2* d = (float2*)ctx->d32.p;
-        ck(bem::convert_f32_to_f64((const float2*)ctx->b32.p, b64, nvec, ctx->stream), "convert rhs");
-        ck(cudaMemcpyAsync(d, ctx->b32.p, nvec * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream), "copy rhs");
-        ck(bem::lu_solve_cluster_batched(prec, ctx->mats.p, L.lda, nv, bt, (const int*)ctx->perm.p, d, L.ldb, nc, ctx->stream),
-           "LU solve");
-        ck(cudaMemsetAsync(x, 0, nvec * sizeof(double2), ctx->stream), "memset x");
-        ck(bem::axpy_f32_into_f64(d, x, nvec, ctx->stream), "axpy");
-        int steps = 0;
-        double worst = 0;
-        for (;;) {
-          ck(bem::residual_batched(prec, ctx->mats2.p, L.lda, nv, bt, x, b64, L.ldb, nc, r, ctx->xsplit.p, ctx->stream),
-             "residual");
-          ck(bem::norms_batched(r, b64, L.ldb, nv, bt * nc, (double*)ctx->norms.p, ctx->stream), "norms");
-          ck(cudaMemcpyAsync(norms.data(), ctx->norms.p, (size_t)bt * nc * 2 * sizeof(double), cudaMemcpyDeviceToHost,
-                             ctx->stream),
-             "copy norms");
-          ck(cudaStreamSynchronize(ctx->stream), "refinement sync");
-          worst = 0;
-          for (int i = 0; i < bt * nc; ++i) {
-            const double rel = norms[2 * i + 1] > 0 ? std::sqrt(norms[2 * i] / norms[2 * i + 1]) : std::sqrt(norms[2 * i]);
-            if (!std::isfinite(rel)) worst = INFINITY;
-            else worst = std::max(worst, rel);
-          }
-          if (worst <= o.refine_tol || steps >= o.max_refine || !std::isfinite(worst)) break;
-          ck(bem::convert_f64_to_f32(r, d, nvec, ctx->stream), "convert residual");
-          ck(bem::lu_solve_cluster_batched(prec, ctx->mats.p, L.lda, nv, bt, (const int*)ctx->perm.p, d, L.ldb, nc, ctx->stream),
-             "LU solve");
-          ck(bem::axpy_f32_into_f64(d, x, nvec, ctx->stream), "axpy");
-          ++steps;
-        }
-        max_steps = std::max(max_steps, steps);
-        max_res = std::max(max_res, worst);
-        launches += 6 + 6LL * steps;  // 3 + (x split, residual, norms) per check + (convert, solve, axpy) per step
-      }
-      prof_mark(ctx, BEM_K_SOLVE);
-      cudaEventRecord(ctx->ev[2], ctx->stream);
-      ck(cudaStreamSynchronize(ctx->stream), "solve sync");
-      if (used_tensor && tc_err) {
-        int h = 0;
-        ck(cudaMemcpyAsync(&h, tc_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "read tensor-core status");
-      ck(cudaStreamSynchronize(ctx->stream), "read tensor-core status");
-        if (h != 0)
-          return fail(ctx, BEM_ERR_CUDA, "tensor-core LU update gave up waiting (status " + std::to_string(h) + ")");
-      }
-      for (int i = 0; i < bt; ++i)
-        if (info[i] != 0) return fail(ctx, BEM_ERR_SINGULAR, "zero pivot in LU factorisation (frequency " +
-                                                                std::to_string(freqs_hz[f0 + i]) + " Hz)");
-      // solution (vertex order) as [bt][nc][ldb]
-      const void* sol = mixed ? (const void*)ctx->x64.p : (const void*)ctx->b32.p;
-      if (field_out) {
-        const void* p_for_field = sol;
-        if (mixed) {
-          ck(bem::convert_f64_to_f32((const double2*)ctx->x64.p, (float2*)ctx->pout.p, nvec, ctx->stream), "convert");
-          p_for_field = ctx->pout.p;
-        }
-        ck(bem::launch_field(dm, prec, bt, ks.data(), qs.data(), p_for_field, L.ldb, nc, drive, (const double*)m->obs.p,
-                             m->nobs, ctx->fsrc.p, (double2*)ctx->fout.p, ctx->stream),
-           "field kernel");
-        launches += mixed ? 3 : 2;
-        prof_mark(ctx, BEM_K_FIELD);
-        double* dst = field_out + 2 * (size_t)f0 * nc * m->nobs;
-        ck(cudaMemcpyAsync(dst, ctx->fout.p, (size_t)bt * nc * m->nobs * sizeof(double2),
-                           o.outputs_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream),
-           "copy field");
-      }
-      cudaEventRecord(ctx->ev[3], ctx->stream);
-      if (pressure_out) {
-        // [bt][nc][nv] complex128 from [bt][nc][ldb]
-        const cudaMemcpyKind kind = o.outputs_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-        if (mixed) {
-          ck(cudaMemcpy2DAsync(pressure_out + 2 * (size_t)f0 * nc * nv, (size_t)nv * sizeof(double2), sol,
-                               (size_t)L.ldb * sizeof(double2), (size_t)nv * sizeof(double2), (size_t)bt * nc, kind,
-                               ctx->stream),
-             "copy pressure");
-        } else {
-          ck(cudaMemcpy2DAsync(pressure_out + 2 * (size_t)f0 * nc * nv, (size_t)nv * sizeof(double2), sol,
-                               (size_t)L.ldb * sizeof(double2), (size_t)nv * sizeof(double2), (size_t)bt * nc, kind,
-                               ctx->stream),
-             "copy pressure");
-        }
-      }
-      ck(cudaStreamSynchronize(ctx->stream), "batch sync");
-      prof_collect(ctx, kacc);
-      float ms = 0;
-      cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
-      t_asm += ms * 1e-3;
-      cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
-      t_sol += ms * 1e-3;
-      cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
-      t_fld += ms * 1e-3;
+      Slice x{m, freqs_hz + f0, bt, pressure_out ? pressure_out + 2 * (size_t)f0 * nc * nv : nullptr,
+              field_out ? field_out + 2 * (size_t)f0 * nc * m->nobs : nullptr};
+      solve_combined(ctx, {x}, nv, o, nc, T);
     }
+    fill_stats(stats, T);
     if (stats) {
-      stats->assembly_s = t_asm;
-      stats->solve_s = t_sol;
-      stats->field_s = t_fld;
-      stats->max_refine_steps = max_steps;
-      stats->max_rel_residual = max_res;
-      stats->batches = batches;
-      for (int i = 0; i < 8; ++i) stats->kernel_s[i] = kacc[i];
       stats->regular_pairs = (long long)dm.ntr * dm.nf * dm.nf - dm.npairs;  // identity and image pairs
       stats->singular_pairs = dm.npairs;
       stats->singular_points = m->singular_points;
-      stats->lu_gemm_used = gemm_used;
-      stats->kernel_launches = launches;
     }
-    if (mixed && !(max_res <= o.refine_tol)) {
-      ctx->err = "iterative refinement stopped at relative residual " + std::to_string(max_res);
+    if (prec == bem::Precision::Mixed && !(T.max_res <= o.refine_tol)) {
+      ctx->err = "iterative refinement stopped at relative residual " + std::to_string(T.max_res);
+      return BEM_ERR_NOT_CONVERGED;
+    }
+    return BEM_OK;
+  });
+}
+
+int bem_solve_jobs(bem_context* ctx, const bem_job* jobs, int n_jobs, const bem_solve_options* opt,
+                   bem_solve_stats* stats) {
+  if (!ctx) return BEM_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&]() -> int {
+    bem_solve_options o;
+    bem_default_options(&o);
+    if (opt) o = *opt;
+    if (!jobs || n_jobs < 1) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "need at least one job");
+    if (!valid_options(ctx, o)) return BEM_ERR_INVALID_ARGUMENT;
+    int n = 0, nc = -1, total = 0;
+    for (int j = 0; j < n_jobs; ++j) {
+      const bem_job& J = jobs[j];
+      if (!J.mesh || J.mesh->ctx != ctx) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "job mesh missing or of another context");
+      if (!valid_freqs(ctx, J.freqs_hz, J.n_freq)) return BEM_ERR_INVALID_ARGUMENT;
+      if (J.mesh->nc < 1) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "no excitation set (bem_set_excitation)");
+      if (nc >= 0 && J.mesh->nc != nc)
+        return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "every job of a call needs the same number of excitations");
+      nc = J.mesh->nc;
+      if (J.field_out && J.mesh->nobs < 1) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "no observation points set");
+      n = std::max(n, J.mesh->dm.nv);
+      total += J.n_freq;
+    }
+    const bem::Precision prec = o.precision == BEM_PRECISION_MIXED ? bem::Precision::Mixed : bem::Precision::FP64;
+    int B = o.batch > 0 ? std::min(o.batch, 64) : auto_batch_order(n, prec, total);
+    B = std::max(1, std::min(B, total));
+    ctx->prof = o.profile != 0;
+    SolveTotals T;
+    // walk the jobs' frequencies in order, cutting them into batches of B
+    int j = 0, f = 0;
+    while (j < n_jobs) {
+      std::vector<Slice> batch;
+      int left = B;
+      while (left > 0 && j < n_jobs) {
+        const bem_job& J = jobs[j];
+        const int take = std::min(left, J.n_freq - f);
+        const int nvj = J.mesh->dm.nv;
+        batch.push_back(Slice{J.mesh, J.freqs_hz + f, take,
+                              J.pressure_out ? J.pressure_out + 2 * (size_t)f * nc * nvj : nullptr,
+                              J.field_out ? J.field_out + 2 * (size_t)f * nc * J.mesh->nobs : nullptr});
+        left -= take;
+        f += take;
+        if (f == J.n_freq) {
+          ++j;
+          f = 0;
+        }
+      }
+      solve_combined(ctx, batch, n, o, nc, T);
+    }
+    fill_stats(stats, T);
+    if (stats) {  // summed over the jobs' meshes
+      stats->regular_pairs = stats->singular_pairs = stats->singular_points = 0;
+      for (int q = 0; q < n_jobs; ++q) {
+        const bem::DeviceMesh& dm = jobs[q].mesh->dm;
+        stats->regular_pairs += (long long)dm.ntr * dm.nf * dm.nf - dm.npairs;
+        stats->singular_pairs += dm.npairs;
+        stats->singular_points += jobs[q].mesh->singular_points;
+      }
+    }
+    if (prec == bem::Precision::Mixed && !(T.max_res <= o.refine_tol)) {
+      ctx->err = "iterative refinement stopped at relative residual " + std::to_string(T.max_res);
       return BEM_ERR_NOT_CONVERGED;
     }
     return BEM_OK;

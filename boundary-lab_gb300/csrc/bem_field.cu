@@ -400,8 +400,6 @@ __global__ void __launch_bounds__(256) field_f64_kernel(const FaceF64* __restric
 
 }  // namespace
 
-int sm_count();
-
 static df host_df(double x) {
   df r;
   r.hi = (float)x;

@@ -109,6 +109,8 @@ enum class LuGemm : int { Auto = 0, Cublas = 1, Tensor = 2 };
 struct TcGemmPlan;
 size_t tc_gemm_workspace_bytes(int n, int batch);
 bool tc_gemm_available();
+// Number of SMs of the current device, cached per device (bem_gemm_tc.cu).
+int sm_count();
 int* tc_gemm_error_word(TcGemmPlan* p);
 // Factor `batch` matrices in place.  tc_workspace (tc_gemm_workspace_bytes(n,
 // batch) bytes, may be null) enables the tensor-core update; *used_tensor tells

@@ -42,6 +42,7 @@ EXPORTED_SYMBOLS = (
     "bem_set_observation_points",
     "bem_default_options",
     "bem_solve_frequencies",
+    "bem_solve_jobs",
     "bem_assemble_lhs",
     "bem_apply_rhs_operator",
     "bem_estimate_device_bytes",
@@ -76,6 +77,18 @@ class BemError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
         self.status = status
+
+
+class Job(ctypes.Structure):
+    """bem_job: one mesh's frequencies and output buffers in a bem_solve_jobs call."""
+
+    _fields_ = [
+        ("mesh", ctypes.c_void_p),
+        ("freqs_hz", ctypes.POINTER(ctypes.c_double)),
+        ("n_freq", ctypes.c_int),
+        ("pressure_out", ctypes.c_void_p),
+        ("field_out", ctypes.c_void_p),
+    ]
 
 
 class SolveOptions(ctypes.Structure):
@@ -172,6 +185,9 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         lib.bem_solve_frequencies.argtypes = [vp, dp, ip, ctypes.POINTER(SolveOptions), vp, vp,
                                               ctypes.POINTER(SolveStats)]
         lib.bem_solve_frequencies.restype = ip
+        lib.bem_solve_jobs.argtypes = [vp, ctypes.POINTER(Job), ip, ctypes.POINTER(SolveOptions),
+                                       ctypes.POINTER(SolveStats)]
+        lib.bem_solve_jobs.restype = ip
         lib.bem_assemble_lhs.argtypes = [vp, ctypes.c_double, ip, dp, dp]
         lib.bem_assemble_lhs.restype = ip
         lib.bem_apply_rhs_operator.argtypes = [vp, ctypes.c_double, ip, dp, dp, ip, dp]
@@ -192,7 +208,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         lib.bem_evaluate_field_noalloc.argtypes = [vp, ip, vp, ip, ip, ctypes.c_double, vp, vp, vp, ip, ip, vp, vp,
                                                    ctypes.c_char_p, ip]
         lib.bem_evaluate_field_noalloc.restype = ip
-        if lib.bem_abi_version() != 1:
+        if lib.bem_abi_version() != 2:
             raise NativeLibraryError(f"unexpected ABI version {lib.bem_abi_version()} in {path}")
         _lib = lib
         return lib
@@ -252,6 +268,43 @@ class Context:
             self._h, _dptr(v), len(v), f.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(f), int(regular_order),
             int(singular_order), sym, ctypes.byref(handle)))
         return Mesh(self, handle, len(v), len(f))
+
+    def solve_jobs(self, jobs, *, precision: int = BEM_PRECISION_MIXED, sound_speed: float = 343.0, rho: float = 1.21,
+                   refine_tol: float = 1e-10, max_refine: int = 8, batch: int = 0, lu_block: int = 0,
+                   want_field: bool = True, profile: bool = False, lu_gemm: int = 0):
+        """Solve several uploaded meshes together (bem_solve_jobs): ``jobs`` is a sequence of
+        (Mesh, freqs_hz).  Returns ([(pressure, field) per job], stats dict), with the shapes
+        of Mesh.solve."""
+        items = (Job * len(jobs))()
+        keep = []
+        outs = []
+        for i, (mesh, freqs) in enumerate(jobs):
+            if mesh.ctx is not self:
+                raise ValueError("every mesh of solve_jobs must belong to this context")
+            f = np.ascontiguousarray(freqs, dtype=np.float64).reshape(-1)
+            pressure = np.zeros((len(f), mesh.n_rhs, mesh.n_vertices), np.complex128)
+            field = np.zeros((len(f), mesh.n_rhs, mesh.n_points), np.complex128) if want_field else None
+            keep.append(f)
+            outs.append((pressure, field))
+            items[i].mesh = mesh._h
+            items[i].freqs_hz = _dptr(f)
+            items[i].n_freq = len(f)
+            items[i].pressure_out = pressure.ctypes.data_as(ctypes.c_void_p)
+            items[i].field_out = None if field is None else field.ctypes.data_as(ctypes.c_void_p)
+        opt = SolveOptions()
+        self._lib.bem_default_options(ctypes.byref(opt))
+        opt.precision = int(precision)
+        opt.sound_speed = float(sound_speed)
+        opt.rho = float(rho)
+        opt.refine_tol = float(refine_tol)
+        opt.max_refine = int(max_refine)
+        opt.batch = int(batch)
+        opt.lu_block = int(lu_block)
+        opt.profile = int(bool(profile))
+        opt.lu_gemm = int(lu_gemm)
+        stats = SolveStats()
+        self._check(self._lib.bem_solve_jobs(self._h, items, len(jobs), ctypes.byref(opt), ctypes.byref(stats)))
+        return outs, stats_dict(stats)
 
     def lu_factor_dense(self, a: np.ndarray, precision: int = BEM_PRECISION_FP64, lu_gemm: int = 0):
         """(LU, ipiv) of a dense complex matrix, LAPACK getrf conventions (0-based ipiv)."""

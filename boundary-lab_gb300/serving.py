@@ -19,12 +19,20 @@ This module keeps that contract and replaces the per-GPU serialisation:
 * policy ``"fifo"`` (arrival order, as the reference) or ``"sjf"`` (least
   estimated GPU work first; a job that has waited ``aging_s`` goes first);
 * long sweeps run in frequency chunks, so results stream per chunk and cancel
-  takes effect between chunks.
+  takes effect between chunks;
+* small jobs share launches: a worker that takes a job of at most
+  ``group_faces`` triangles also takes the queued small jobs of similar size
+  (largest / smallest vertex count <= ``group_size_ratio``, same physics and
+  excitation count, memory permitting, ``group_max_freqs`` frequencies in all)
+  and solves them in one ``bem_solve_jobs`` call: their matrices, padded to the
+  largest, are factored, solved and refined in one launch sequence.
 
 Results are independent of the mix: every frequency's assembly, LU and field
 are computed by the same kernels on the same inputs whatever runs beside it
-(no cross-job batching, deterministic kernels), so a job's output is bitwise
-the same alone or under load.
+(deterministic kernels), so a job that runs on its own is bitwise the same alone
+or under load.  A job solved in a group is the same up to the rounding of its
+sums (FP64 form) or its refinement (a group refines until every system in it
+reaches the tolerance): within 1e-8 in the mixed form.
 
 The executor doing the GPU work is injectable (``executor_factory``), which lets
 the scheduling logic be tested on hosts without a GPU.
@@ -77,6 +85,7 @@ class ServingJob:
     field: np.ndarray | None = None      # [n_freq, n_rhs, n_points] complex128
     estimated_bytes: int = 0
     estimated_work: float = 0.0
+    group_size: int = 1             # jobs solved together with this one (bem_solve_jobs), itself included
     _cancel: threading.Event = dc_field(default_factory=threading.Event, repr=False)
     _done: threading.Event = dc_field(default_factory=threading.Event, repr=False)
 
@@ -150,6 +159,28 @@ class NativeExecutor:
         if self.ctx.scratch_bytes > self.trim_above_bytes:
             self.ctx.trim()
 
+    def run_group(self, jobs: Sequence[ServingJob],
+                  on_chunks: Sequence[Callable[[int, np.ndarray, np.ndarray], None]]) -> None:
+        """Solve several jobs (same precision, physics and excitation count) in one
+        bem_solve_jobs call; each job's results are delivered as one chunk."""
+        meshes = []
+        try:
+            for job in jobs:
+                m = self.ctx.upload_mesh(job.vertices, job.faces)
+                meshes.append(m)
+                m.set_excitation(job.drive)
+                m.set_observation_points(job.points)
+            j0 = jobs[0]
+            outs, _ = self.ctx.solve_jobs([(m, j.freqs_hz) for m, j in zip(meshes, jobs)], precision=j0.precision,
+                                          sound_speed=j0.sound_speed, rho=j0.rho)
+        finally:
+            for m in meshes:
+                m.release()
+        for (p, u), cb in zip(outs, on_chunks):
+            cb(0, p, u)
+        if self.ctx.scratch_bytes > self.trim_above_bytes:
+            self.ctx.trim()
+
     def close(self) -> None:
         self.ctx.close()
 
@@ -160,7 +191,8 @@ class ServingScheduler:
     def __init__(self, device: int = 0, *, max_running: int = 4, max_queued: int = 256,
                  memory_budget_bytes: int | None = None, policy: str = "sjf", aging_s: float = 30.0,
                  executor_factory: Callable[[int], object] | None = None,
-                 on_result: Callable[[ServingJob, int, np.ndarray, np.ndarray], None] | None = None):
+                 on_result: Callable[[ServingJob, int, np.ndarray, np.ndarray], None] | None = None,
+                 group_faces: int = 3000, group_max_freqs: int = 64, group_size_ratio: float = 1.25):
         if policy not in ("fifo", "sjf"):
             raise ValueError("policy must be 'fifo' or 'sjf'")
         if max_running < 1:
@@ -171,6 +203,9 @@ class ServingScheduler:
         self.policy = policy
         self.aging_s = aging_s
         self.on_result = on_result
+        self.group_faces = int(group_faces)
+        self.group_max_freqs = int(group_max_freqs)
+        self.group_size_ratio = float(group_size_ratio)
         self._factory = executor_factory or (lambda dev: NativeExecutor(dev))
         self._budget = memory_budget_bytes if memory_budget_bytes is not None else self._default_budget(device)
         self._lock = threading.Condition()
@@ -264,6 +299,32 @@ class ServingScheduler:
                 return None
         return None
 
+    def _group_locked(self, job: ServingJob, ex) -> list[ServingJob]:
+        """``job`` and the queued jobs that can share its launches (see the module notes)."""
+        if (self.group_faces <= 0 or job.n_faces > self.group_faces or not callable(getattr(ex, "run_group", None))
+                or len(job.freqs_hz) >= self.group_max_freqs):
+            return [job]
+        free = self._budget - self._reserved - job.estimated_bytes
+        lo = hi = job.n_vertices
+        nfreq = len(job.freqs_hz)
+        group = [job]
+        order = self._queue if self.policy == "fifo" else sorted(self._queue, key=lambda j: (j.estimated_work, j.arrival_s))
+        for j in order:
+            if j is job or j.n_faces > self.group_faces:
+                continue
+            if (j.precision, j.sound_speed, j.rho, j.drive.shape[0]) != (job.precision, job.sound_speed, job.rho,
+                                                                         job.drive.shape[0]):
+                continue
+            nlo, nhi = min(lo, j.n_vertices), max(hi, j.n_vertices)
+            if nhi > self.group_size_ratio * nlo or nfreq + len(j.freqs_hz) > self.group_max_freqs:
+                continue
+            if j.estimated_bytes > free:
+                continue
+            group.append(j)
+            lo, hi, nfreq = nlo, nhi, nfreq + len(j.freqs_hz)
+            free -= j.estimated_bytes
+        return group
+
     def _worker(self, ready: threading.Barrier) -> None:
         try:
             ex = self._factory(self.device)
@@ -286,27 +347,35 @@ class ServingScheduler:
                         if job is not None:
                             break
                         self._lock.wait(timeout=0.05 if self.policy == "sjf" else None)
-                    self._queue.remove(job)
-                    self._running.append(job)
-                    self._reserved += job.estimated_bytes
-                    job.status = "running"
-                    job.start_s = self.now()
+                    group = self._group_locked(job, ex)
+                    for j in group:
+                        j.group_size = len(group)
+                        self._queue.remove(j)
+                        self._running.append(j)
+                        self._reserved += j.estimated_bytes
+                        j.status = "running"
+                        j.start_s = self.now()
                 try:
-                    self._run_one(ex, job)
+                    if len(group) == 1:
+                        self._run_one(ex, job)
+                    else:
+                        self._run_group(ex, group)
                 finally:
                     with self._lock:
-                        self._running.remove(job)
-                        self._reserved -= job.estimated_bytes
-                        job.finish_s = self.now()
-                        self._done_jobs.append(job)
+                        for j in group:
+                            self._running.remove(j)
+                            self._reserved -= j.estimated_bytes
+                            j.finish_s = self.now()
+                            self._done_jobs.append(j)
                         self._lock.notify_all()
-                    job._done.set()
+                    for j in group:
+                        j._done.set()
         finally:
             close = getattr(ex, "close", None)
             if close:
                 close()
 
-    def _run_one(self, ex, job: ServingJob) -> None:
+    def _chunk_sink(self, job: ServingJob) -> Callable[[int, np.ndarray, np.ndarray], None]:
         n = len(job.freqs_hz)
 
         def on_chunk(start: int, p: np.ndarray, u: np.ndarray) -> None:
@@ -321,14 +390,35 @@ class ServingScheduler:
             if self.on_result is not None:
                 self.on_result(job, start, p, u)
 
+        return on_chunk
+
+    def _run_one(self, ex, job: ServingJob) -> None:
         try:
-            ex.run(job, on_chunk, job._cancel.is_set)
+            ex.run(job, self._chunk_sink(job), job._cancel.is_set)
             job.status = "completed"
         except JobCancelledError:
             job.status = "cancelled"
         except Exception as e:  # noqa: BLE001 - a failed job does not stop the worker
             job.status = "failed"
             job.error = f"{type(e).__name__}: {e}"
+
+    def _run_group(self, ex, group: list[ServingJob]) -> None:
+        live = []
+        for j in group:
+            if j._cancel.is_set():
+                j.status = "cancelled"
+            else:
+                live.append(j)
+        if not live:
+            return
+        try:
+            ex.run_group(live, [self._chunk_sink(j) for j in live])
+            for j in live:
+                j.status = "completed"
+        except Exception as e:  # noqa: BLE001 - a failed group does not stop the worker
+            for j in live:
+                j.status = "failed"
+                j.error = f"{type(e).__name__}: {e}"
 
     # ------------------------------------------------------------------- close
     def drain(self, timeout: float | None = None) -> bool:
@@ -387,6 +477,7 @@ def latency_summary(jobs: Sequence[ServingJob]) -> dict:
         "makespan_s": float(span),
         "frequency_solves_per_s": float(freqs / span) if span > 0 else None,
         "failed": sum(j.status == "failed" for j in jobs),
+        "jobs_in_shared_launches": sum(j.group_size > 1 for j in done),
     }
 
 

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define GB300_BEM_ABI_VERSION 1
+#define GB300_BEM_ABI_VERSION 2
 
 typedef struct bem_context bem_context;
 typedef struct bem_mesh bem_mesh;
@@ -162,6 +162,31 @@ void bem_default_options(bem_solve_options* opt);
  * stats may be NULL. */
 int bem_solve_frequencies(bem_mesh* mesh, const double* freqs_hz, int n_freq, const bem_solve_options* opt,
                           double* pressure_out, double* field_out, bem_solve_stats* stats);
+
+/* Several jobs solved together (no single counterpart in the reference, which
+ * runs one job per GPU at a time: beat_engine_backend.py:314-334; each job is
+ * one solve_request_impl sweep, solver.jl:805-920).  The jobs' meshes belong to
+ * this context and carry their excitations (the same n_rhs for every job) and,
+ * for a field, their observation points.  Their frequencies are taken in job
+ * order and cut into batches (options.batch, or automatic for the largest
+ * mesh); inside a batch every (job, frequency) is assembled on its own mesh into
+ * a matrix of the order of the largest mesh in the call, padded with an identity
+ * block, and all the matrices of the batch are factored, solved and refined in
+ * one launch sequence, so many small jobs share the LU's launches instead of
+ * running one after the other.  The padding changes no pivot, so each job's
+ * results are those of bem_solve_frequencies on its own mesh up to the rounding
+ * of its sums; the padding costs (n_max / n_job)^3 of the LU work, so callers
+ * group jobs of similar size.  Outputs per job as in bem_solve_frequencies;
+ * stats cover the whole call (pair counts summed over the jobs' meshes). */
+typedef struct bem_job {
+  bem_mesh* mesh;
+  const double* freqs_hz;
+  int n_freq;
+  double* pressure_out; /* [n_freq][n_rhs][n_vertices] complex, or NULL */
+  double* field_out;    /* [n_freq][n_rhs][n_points] complex, or NULL */
+} bem_job;
+int bem_solve_jobs(bem_context* ctx, const bem_job* jobs, int n_jobs, const bem_solve_options* opt,
+                   bem_solve_stats* stats);
 
 /* The batch bem_solve_frequencies uses for options.batch = 0 on a sweep of
  * n_freq frequencies (returned; 0 on a bad argument): at most B_max, the sweep

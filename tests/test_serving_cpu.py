@@ -182,3 +182,59 @@ def test_poisson_stream_is_seeded():
     gaps = np.diff([0.0] + [t for t, _ in serving.poisson_jobs(200, 20.0, seed=5, sizes=(1000,), max_freqs=1,
                                                                   n_far=4)])
     assert 0.035 < gaps.mean() < 0.07  # exponential gaps, mean 1 / 20 s
+
+
+class GroupingExecutor(FakeExecutor):
+    """FakeExecutor that also solves groups of jobs (bem_solve_jobs): records each group."""
+
+    groups: list = []
+
+    def run_group(self, jobs, on_chunks):
+        cls = GroupingExecutor
+        with cls.lock:
+            cls.groups.append([j.job_id for j in jobs])
+        time.sleep(self.per_freq_s * sum(len(j.freqs_hz) for j in jobs) / 4)
+        for j, cb in zip(jobs, on_chunks):
+            n = len(j.freqs_hz)
+            cb(0, np.full((n, 1, j.n_vertices), j.n_faces, dtype=np.complex128),
+               np.zeros((n, 1, len(j.points)), dtype=np.complex128))
+
+
+def test_small_jobs_of_similar_size_share_launches():
+    """Queued small jobs of similar size are taken together by one worker; a large job, a
+    job of a very different size and jobs beyond the frequency cap are not."""
+    GroupingExecutor.groups = []
+    gate = threading.Event()
+
+    class Gated(GroupingExecutor):
+        def run(self, job, on_chunk, should_stop):
+            if job.job_id == "blocker":
+                gate.wait(10)
+            super().run(job, on_chunk, should_stop)
+
+    with serving.ServingScheduler(max_running=1, memory_budget_bytes=1 << 40, executor_factory=Gated,
+                                  policy="fifo", group_faces=3000, group_max_freqs=40) as sch:
+        sch.submit(make_job(20000, 2, "blocker"))  # holds the only worker while the queue fills
+        time.sleep(0.1)
+        a = [sch.submit(make_job(1000 + 20 * i, 8, f"a{i}")) for i in range(4)]  # similar sizes, 32 freqs
+        b = sch.submit(make_job(1100, 12, "b"))        # similar size, but beyond the 40-frequency cap
+        c = sch.submit(make_job(2800, 4, "c"))         # small, but 2.7x the vertices of a0
+        big = sch.submit(make_job(6000, 4, "big"))     # not small
+        gate.set()
+        assert sch.drain(30)
+    groups = GroupingExecutor.groups
+    assert ["a0", "a1", "a2", "a3"] in groups
+    assert all(len(g) <= 5 for g in groups)
+    assert all("c" not in g or g == ["c"] for g in groups) and all("big" not in g for g in groups)
+    assert all(j.status == "completed" and j.group_size == 4 for j in a)
+    assert b.status == c.status == big.status == "completed"
+    assert np.all(a[2].pressure == a[2].n_faces) and a[2].pressure.shape == (8, 1, a[2].n_vertices)
+
+
+def test_grouping_can_be_switched_off():
+    GroupingExecutor.groups = []
+    with serving.ServingScheduler(max_running=1, memory_budget_bytes=1 << 40, executor_factory=GroupingExecutor,
+                                  group_faces=0) as sch:
+        jobs = [sch.submit(make_job(1000, 4, f"s{i}")) for i in range(4)]
+        assert sch.drain(30)
+    assert GroupingExecutor.groups == [] and all(j.group_size == 1 for j in jobs)
