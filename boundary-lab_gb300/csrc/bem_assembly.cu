@@ -19,7 +19,8 @@
 //                         combined with the k-independent FP64 moments
 //                         precomputed once per mesh -> per-pair 3x3 blocks
 //   singular_scatter      adds the singular blocks into Rext (one thread per
-//                         trial face: deterministic, no atomics)
+//                         target entry, contributions in pair order:
+//                         deterministic, no atomics)
 //   gather_columns        A[:, j] = sum over (g, b) in star(j) of Rext[g*3+b],
 //                         then halo extended rows folded into their rows
 #include <map>
@@ -166,8 +167,16 @@ template <int NFQ, bool DT> struct RegParamsF32 {
 // reduction: k|C| is reduced mod 2pi per pair in double-float and
 // |k(r - |C|)| <= k h (h the element size), so |kr| stays a few pi at most
 // for any mesh that resolves the wavelength.
+// Resident CTAs per SM the regular kernel is compiled for: three with up to two
+// frequencies per launch (<= 168 registers), two with three or four (<= 255
+// registers; the per-warp accumulators of four frequencies take 112 KB per CTA
+// on 291-row tiles, so two CTAs still fit in shared memory).
+template <int NFQ> struct RegularOccupancy {
+  static constexpr int kCtasPerSm = NFQ <= 2 ? 3 : 2;
+};
+
 template <int Q, int WARPS, int NFQ, bool DT>
-__global__ void __launch_bounds__(WARPS * 32, 3)  // three CTAs per SM (<= 168 registers)
+__global__ void __launch_bounds__(WARPS * 32, RegularOccupancy<NFQ>::kCtasPerSm)
     regular_f32_kernel(const FaceF32* __restrict__ faces, int nf, const int* __restrict__ tile_group_ptr,
                        const LaneSlot* __restrict__ slots, const float* __restrict__ group_faces,
                        const int* __restrict__ tile_row_base, int max_rows,
@@ -1098,24 +1107,21 @@ __global__ void __launch_bounds__(256, 2)
   }
 }
 
-// One thread per trial face: add its singular blocks into the extended rows.
+// The singular blocks into the extended rows: one thread per distinct target
+// entry (planned once per mesh), adding that entry's contributions in pair order,
+// so the sums are those of one thread walking each trial face's pairs, without
+// that walk's chain of dependent read-modify-writes.
 template <typename C2>
-__global__ void singular_scatter_kernel(const SingularPair* __restrict__ pairs, const int* __restrict__ by_trial_ptr,
-                                        const int* __restrict__ face_ext, const C2* __restrict__ blocks, int nf,
-                                        C2* __restrict__ Rext, long long ldR) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= nf) return;
-  for (int k = by_trial_ptr[g]; k < by_trial_ptr[g + 1]; ++k) {
-    const int f = pairs[k].test;
-    const C2* blk = blocks + (size_t)kSingOut * k;
-    for (int a = 0; a < 3; ++a) {
-      const int e = face_ext[3 * f + a];
-      for (int b = 0; b < 3; ++b) {
-        C2* dst = &Rext[(size_t)(3 * g + b) * ldR + e];
-        *dst = cadd(*dst, blk[3 * a + b]);
-      }
-    }
-  }
+__global__ void singular_scatter_kernel(const int* __restrict__ scat_col, const int* __restrict__ scat_row,
+                                        const int* __restrict__ scat_ptr, const int* __restrict__ scat_src,
+                                        int n_entries, const C2* __restrict__ blocks, C2* __restrict__ Rext,
+                                        long long ldR) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_entries) return;
+  C2* dst = &Rext[(size_t)scat_col[i] * ldR + scat_row[i]];
+  C2 v = *dst;
+  for (int s = scat_ptr[i]; s < scat_ptr[i + 1]; ++s) v = cadd(v, blocks[scat_src[s]]);
+  *dst = v;
 }
 
 // One CTA per column: A[:, j] in permuted row order.
@@ -1439,21 +1445,66 @@ cudaError_t launch_regular_f32(const DeviceMesh& m, const double* k, const doubl
 }
 }  // namespace
 
+// Frequencies per regular-kernel launch for a group of n that all carry the
+// double-layer term: fours, with a remainder of 1 taken as 3 + 2 (a single
+// frequency per launch shares nothing); NFQ 4 only while two CTAs of its
+// accumulators fit in shared memory, else twos.
+int regular_quad_ok(const DeviceMesh& m) {
+  const size_t per_cta = (size_t)4 * 4 * 3 * m.max_tile_rows * sizeof(float2);
+  return per_cta <= (size_t)112 * 1024 ? 1 : 0;
+}
+
+int regular_split(int n, bool quad, int* sizes) {
+  int cnt = 0;
+  if (!quad) {
+    for (; n >= 2; n -= 2) sizes[cnt++] = 2;
+    if (n) sizes[cnt++] = 1;
+    return cnt;
+  }
+  int q = n / 4, r = n % 4;
+  if (r == 1 && q >= 1) {
+    --q;
+    r = 5;
+  }
+  for (int i = 0; i < q; ++i) sizes[cnt++] = 4;
+  if (r == 5) {
+    sizes[cnt++] = 3;
+    sizes[cnt++] = 2;
+  } else if (r) {
+    sizes[cnt++] = r;
+  }
+  return cnt;
+}
+
 cudaError_t launch_regular(const DeviceMesh& m, Precision prec, int nfreq, const double* k, const double2* cD,
                            const double2* cH, void* Rext, long long ldR, long long strideR, cudaStream_t stream) {
   if (prec == Precision::Mixed) {
-    // two frequencies per launch share the frequency-independent geometry; an
-    // operator without the double-layer term (cD = 0) runs one per launch
+    // up to four frequencies per launch share the frequency-independent geometry;
+    // an operator without the double-layer term (cD = 0) runs one per launch
+    const bool quad = regular_quad_ok(m);
     int f = 0;
     while (f < nfreq) {
       float2* R = (float2*)Rext + (size_t)f * strideR;
-      const bool dt = cD[f].x != 0.0 || cD[f].y != 0.0;
-      const bool two = f + 1 < nfreq && dt && (cD[f + 1].x != 0.0 || cD[f + 1].y != 0.0);
-      cudaError_t e = two  ? launch_regular_f32<2, true>(m, k + f, cD + f, cH + f, R, ldR, strideR, stream)
-                      : dt ? launch_regular_f32<1, true>(m, k + f, cD + f, cH + f, R, ldR, strideR, stream)
-                           : launch_regular_f32<1, false>(m, k + f, cD + f, cH + f, R, ldR, strideR, stream);
-      if (e != cudaSuccess) return e;
-      f += two ? 2 : 1;
+      auto dt_at = [&](int i) { return cD[i].x != 0.0 || cD[i].y != 0.0; };
+      if (!dt_at(f)) {
+        cudaError_t e = launch_regular_f32<1, false>(m, k + f, cD + f, cH + f, R, ldR, strideR, stream);
+        if (e != cudaSuccess) return e;
+        ++f;
+        continue;
+      }
+      int run = 1;  // consecutive frequencies with the double-layer term
+      while (f + run < nfreq && dt_at(f + run)) ++run;
+      int sizes[64];
+      const int cnt = regular_split(run, quad, sizes);
+      for (int i = 0; i < cnt; ++i) {
+        R = (float2*)Rext + (size_t)f * strideR;
+        cudaError_t e = sizes[i] == 4   ? launch_regular_f32<4, true>(m, k + f, cD + f, cH + f, R, ldR, strideR, stream)
+                        : sizes[i] == 3 ? launch_regular_f32<3, true>(m, k + f, cD + f, cH + f, R, ldR, strideR, stream)
+                        : sizes[i] == 2 ? launch_regular_f32<2, true>(m, k + f, cD + f, cH + f, R, ldR, strideR, stream)
+                                        : launch_regular_f32<1, true>(m, k + f, cD + f, cH + f, R, ldR, strideR, stream);
+        if (e != cudaSuccess) return e;
+        f += sizes[i];
+      }
     }
     return cudaSuccess;
   }
@@ -1464,7 +1515,18 @@ cudaError_t launch_regular(const DeviceMesh& m, Precision prec, int nfreq, const
   return cudaSuccess;
 }
 
-int regular_launches(Precision prec, int nfreq) { return prec == Precision::Mixed ? (nfreq + 1) / 2 : nfreq; }
+int regular_groups(const DeviceMesh& m, Precision prec, int nfreq, int* sizes) {
+  if (prec != Precision::Mixed) {
+    for (int i = 0; i < nfreq; ++i) sizes[i] = 1;
+    return nfreq;
+  }
+  return regular_split(nfreq, regular_quad_ok(m), sizes);
+}
+
+int regular_launches(const DeviceMesh& m, Precision prec, int nfreq) {
+  int sizes[64];
+  return regular_groups(m, prec, nfreq, sizes);
+}
 
 cudaError_t launch_regular_f64(const DeviceMesh& m, double k, double2 cD, double2 cH, double2* Rext, long long ldR,
                                cudaStream_t stream) {
@@ -1544,14 +1606,15 @@ cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, double k, c
 
 cudaError_t launch_singular_scatter(const DeviceMesh& m, Precision prec, const void* blocks, void* Rext,
                                     long long ldR, cudaStream_t stream) {
-  const int threads = 128;
-  const int nblk = (m.nf + threads - 1) / threads;
+  if (m.n_scat == 0) return cudaSuccess;
+  const int threads = 256;
+  const int nblk = (m.n_scat + threads - 1) / threads;
   if (prec == Precision::Mixed)
-    singular_scatter_kernel<float2><<<nblk, threads, 0, stream>>>(m.pairs, m.pairs_by_trial_ptr, m.face_ext,
-                                                                  (const float2*)blocks, m.nf, (float2*)Rext, ldR);
+    singular_scatter_kernel<float2><<<nblk, threads, 0, stream>>>(m.scat_col, m.scat_row, m.scat_ptr, m.scat_src,
+                                                                  m.n_scat, (const float2*)blocks, (float2*)Rext, ldR);
   else
-    singular_scatter_kernel<double2><<<nblk, threads, 0, stream>>>(m.pairs, m.pairs_by_trial_ptr, m.face_ext,
-                                                                   (const double2*)blocks, m.nf, (double2*)Rext,
+    singular_scatter_kernel<double2><<<nblk, threads, 0, stream>>>(m.scat_col, m.scat_row, m.scat_ptr, m.scat_src,
+                                                                   m.n_scat, (const double2*)blocks, (double2*)Rext,
                                                                    ldR);
   return cudaGetLastError();
 }

@@ -247,9 +247,9 @@ Layout layout_for(const bem::DeviceMesh& dm, bem::Precision prec) {
 }
 
 // Frequencies assembled together: the mixed form evaluates the regular pairs of
-// two frequencies in one launch (shared geometry), each into its own
+// up to four frequencies in one launch (shared geometry), each into its own
 // extended-row buffer.
-int assembly_group(bem::Precision prec) { return prec == bem::Precision::Mixed ? 2 : 1; }
+int assembly_group(bem::Precision prec) { return prec == bem::Precision::Mixed ? 4 : 1; }
 
 // Assemble the LHS (c[i].cD, cH, cM) of cnt frequencies into A[i] (and A2[i] if
 // given; column-major, leading dimension lda) and, if nc > 0, the RHS into b[i]
@@ -263,7 +263,10 @@ long long assemble_frequencies(bem_mesh* m, bem::Precision prec, int cnt, const 
   Layout L = layout_for(dm, prec);
   if (lda > 0) L.lda = lda;
   if (ldb > 0) L.ldb = ldb;
-  const int G = std::min(assembly_group(prec), cnt);
+  int sizes[64];
+  const int ngroups = bem::regular_groups(dm, prec, cnt, sizes);
+  int G = 1;
+  for (int i = 0; i < ngroups; ++i) G = std::max(G, sizes[i]);
   const size_t rext_n = (size_t)L.ldR * 3 * dm.nf;         // elements per extended-row buffer
   const size_t sblk_n = (size_t)std::max(dm.npairs, 1) * 12;  // elements per singular-block buffer
   ck(ctx->rext.ensure(rext_n * L.esz * G), "alloc extended rows");
@@ -272,9 +275,10 @@ long long assemble_frequencies(bem_mesh* m, bem::Precision prec, int cnt, const 
   auto rext = [&](int i) { return (void*)((char*)ctx->rext.p + rext_n * L.esz * i); };
   auto sblk = [&](int i) { return (void*)((char*)ctx->sblocks.p + sblk_n * L.esz * i); };
   long long launches = 0;
-  for (int f0 = 0; f0 < cnt; f0 += G) {
-    const int g = std::min(G, cnt - f0);
-    double2 cD[2], cH[2];
+  int f0 = 0;
+  for (int gi = 0; gi < ngroups; f0 += sizes[gi], ++gi) {
+    const int g = sizes[gi];
+    double2 cD[4], cH[4];
     for (int i = 0; i < g; ++i) {
       cD[i] = c[f0 + i].cD;
       cH[i] = c[f0 + i].cH;
@@ -307,7 +311,7 @@ long long assemble_frequencies(bem_mesh* m, bem::Precision prec, int cnt, const 
       prof_mark(ctx, BEM_K_RHS);
     }
     // per frequency: singular, scatter, gather (+ isolated rows), right-hand side (2)
-    launches += (long long)g * (3 + (dm.n_isolated ? 1 : 0) + (nc > 0 ? 2 : 0)) + bem::regular_launches(prec, g);
+    launches += (long long)g * (3 + (dm.n_isolated ? 1 : 0) + (nc > 0 ? 2 : 0)) + bem::regular_launches(dm, prec, g);
   }
   return launches;
 }
@@ -459,6 +463,7 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
       d.n_halo = (int)P.halo_ext.size();
       d.n_halo_rows = (int)P.halo_row.size();
       d.npairs = (int)P.pairs.size();
+      d.n_scat = (int)P.scat_col.size();
       d.ntr = (int)P.transforms.size();
       for (int i = 0; i < d.ntr && i < 4; ++i) d.tr[i] = P.transforms[i];
       std::vector<int> iso;
@@ -499,6 +504,10 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
       pack.add(d.pairs_by_trial_ptr, P.pairs_by_trial_ptr);
       pack.add(d.pairs_by_test_ptr, P.pairs_by_test_ptr);
       pack.add(d.pairs_by_test, P.pairs_by_test);
+      pack.add(d.scat_col, P.scat_col);
+      pack.add(d.scat_row, P.scat_row);
+      pack.add(d.scat_ptr, P.scat_ptr);
+      pack.add(d.scat_src, P.scat_src);
       pack.add(d.rule_ptr, P.rule_ptr);
       pack.add(d.duffy, P.duffy);
       pack.add(d.duffy32, duffy32);
@@ -1010,10 +1019,10 @@ long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int np
   const long long lda = round_up(nv, 32);
   const long long n_ext = (long long)(nv * 1.3) + 64;
   long long bytes = 0;
-  const long long group = precision == BEM_PRECISION_MIXED ? 2 : 1;        // frequencies assembled together
+  const long long group = precision == BEM_PRECISION_MIXED ? 4 : 1;        // frequencies assembled together
   bytes += round_up(n_ext, 32) * 3LL * nf * esz * group;                    // extended rows
   bytes += (long long)batch * lda * nv * esz * (precision == BEM_PRECISION_MIXED ? 2 : 1);  // matrices (+copy)
-  bytes += (long long)npairs * (12 * esz * group + 24 * 8 + 48 + (bem::kPairRec + bem::kPairGeoDf) * 4);  // singular blocks, moments, pairs, records
+  bytes += (long long)npairs * (12 * esz * group + 24 * 8 + 48 + (bem::kPairRec + bem::kPairGeoDf) * 4 + 96);  // singular blocks, moments, pairs, records, scatter plan
   bytes += (long long)batch * nrhs * lda * (esz + 3 * 16 + 16);             // rhs, x, r, b64, d
   bytes += (long long)batch * nrhs * ((long long)nf * 6 * esz + (long long)npts * 16);  // field sources + out
   bytes += (long long)nf * (2 * 160 + 288 + 64);                            // face records (+ lane-group copy), maps

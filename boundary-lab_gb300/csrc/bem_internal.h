@@ -115,6 +115,12 @@ struct MeshPlan {
   std::vector<int> pairs_by_trial_ptr;  // nf + 1 (pairs are sorted by trial)
   std::vector<int> pairs_by_test;       // pair ids grouped by test face
   std::vector<int> pairs_by_test_ptr;   // nf + 1
+  // singular scatter: the distinct extended-row entries (column 3 g + b of trial
+  // face g, extended row e) that the pairs' 3 x 3 blocks add into, each with its
+  // contributions (block element 12 k + 3 a + b of pair k) in pair order
+  std::vector<int> scat_col, scat_row;  // per entry
+  std::vector<int> scat_ptr;            // entries + 1
+  std::vector<int> scat_src;            // 9 per pair
   // Duffy rules: concatenated points; rule r occupies [rule_ptr[r], rule_ptr[r+1])
   std::vector<int> rule_ptr;
   std::vector<double> duffy;  // 5 doubles per point: test xi, test eta, trial xi, trial eta, w

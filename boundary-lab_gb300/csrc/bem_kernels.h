@@ -51,6 +51,11 @@ struct DeviceMesh {
   int* pairs_by_trial_ptr = nullptr;
   int* pairs_by_test_ptr = nullptr;
   int* pairs_by_test = nullptr;
+  int n_scat = 0;  // singular scatter entries (see MeshPlan::scat_*)
+  int* scat_col = nullptr;
+  int* scat_row = nullptr;
+  int* scat_ptr = nullptr;
+  int* scat_src = nullptr;
   int* rule_ptr = nullptr;
   double* duffy = nullptr;
   float* duffy32 = nullptr;  // the same table rounded to float (mixed form)
@@ -84,7 +89,11 @@ struct DeviceMesh {
 // f * strideR elements); the mixed form evaluates two frequencies per launch.
 cudaError_t launch_regular(const DeviceMesh& m, Precision prec, int nfreq, const double* k, const double2* cD,
                            const double2* cH, void* Rext, long long ldR, long long strideR, cudaStream_t stream);
-int regular_launches(Precision prec, int nfreq);
+// Frequencies assembled per regular-kernel launch for a batch of nfreq (mixed:
+// fours, or twos when four frequencies' accumulators do not fit two CTAs per SM;
+// FP64: ones); writes the group sizes (nfreq <= 64) and returns their count.
+int regular_groups(const DeviceMesh& m, Precision prec, int nfreq, int* sizes);
+int regular_launches(const DeviceMesh& m, Precision prec, int nfreq);
 cudaError_t launch_regular_f64(const DeviceMesh& m, double k, double2 cD, double2 cH, double2* Rext, long long ldR,
                                cudaStream_t stream);
 // Per-pair FP32 record written at upload by the pair setup and moments kernels (see bem_assembly.cu).

@@ -821,6 +821,48 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
     std::vector<int> fill(P.pairs_by_test_ptr.begin(), P.pairs_by_test_ptr.end() - 1);
     for (size_t i = 0; i < P.pairs.size(); ++i) P.pairs_by_test[fill[P.pairs[i].test]++] = (int)i;
   }
+  // singular scatter plan: every (trial column 3 g + b, extended row e) entry the
+  // pairs of trial face g add into, with its contributions in pair order (pair k,
+  // then test vertex a), so a thread per entry adds them in the order one thread
+  // per trial face would have
+  {
+    const size_t np = P.pairs.size();
+    std::vector<int> entry_of(3 * (size_t)std::max(P.n_ext, 1), -1);
+    std::vector<int> touched;
+    std::vector<int> contrib_entry(9 * np), contrib_src(9 * np);
+    P.scat_col.clear();
+    P.scat_row.clear();
+    size_t c = 0;
+    for (int g = 0; g < nf; ++g) {
+      touched.clear();
+      for (int k = P.pairs_by_trial_ptr[g]; k < P.pairs_by_trial_ptr[g + 1]; ++k) {
+        const int f = P.pairs[k].test;
+        for (int a = 0; a < 3; ++a) {
+          const int e = P.face_ext[3 * (size_t)f + a];
+          for (int b = 0; b < 3; ++b) {
+            int& slot = entry_of[3 * (size_t)e + b];
+            if (slot < 0) {
+              slot = (int)P.scat_col.size();
+              P.scat_col.push_back(3 * g + b);
+              P.scat_row.push_back(e);
+              touched.push_back(3 * e + b);
+            }
+            contrib_entry[c] = slot;
+            contrib_src[c] = 12 * k + 3 * a + b;
+            ++c;
+          }
+        }
+      }
+      for (int t : touched) entry_of[t] = -1;
+    }
+    const size_t ne = P.scat_col.size();
+    P.scat_ptr.assign(ne + 1, 0);
+    for (size_t i = 0; i < c; ++i) P.scat_ptr[contrib_entry[i] + 1]++;
+    for (size_t i = 0; i < ne; ++i) P.scat_ptr[i + 1] += P.scat_ptr[i];
+    P.scat_src.assign(c, 0);
+    std::vector<int> fill(P.scat_ptr.begin(), P.scat_ptr.end() - 1);
+    for (size_t i = 0; i < c; ++i) P.scat_src[fill[contrib_entry[i]]++] = contrib_src[i];
+  }
   return std::string();
 }
 

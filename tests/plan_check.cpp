@@ -34,5 +34,14 @@ int main(int argc, char** argv) {
         if (s.face >= 0) std::printf("slot %d %d %d %d %d\n", g, s.face, s.loc[0], s.loc[1], s.loc[2]);
       }
   }
+  // singular pairs (trial, test), the faces' extended rows and the scatter plan
+  std::printf("npairs %zu next %d\n", p.pairs.size(), p.n_ext);
+  for (size_t k = 0; k < p.pairs.size(); ++k) std::printf("pair %d %d\n", p.pairs[k].trial, p.pairs[k].test);
+  for (int f = 0; f < nf; ++f) std::printf("fext %d %d %d\n", p.face_ext[3 * f], p.face_ext[3 * f + 1], p.face_ext[3 * f + 2]);
+  for (size_t i = 0; i < p.scat_col.size(); ++i) {
+    std::printf("scat %d %d", p.scat_col[i], p.scat_row[i]);
+    for (int s = p.scat_ptr[i]; s < p.scat_ptr[i + 1]; ++s) std::printf(" %d", p.scat_src[s]);
+    std::printf("\n");
+  }
   return 0;
 }

@@ -46,6 +46,8 @@ def run_plan(tool, tmp_path, mesh, tile_faces=512):
     tiles = []
     for line in out.splitlines():
         w = line.split()
+        if w[0] in ("npairs", "pair", "fext", "scat"):
+            continue
         if w[0] == "tile":
             tiles.append({"rows": int(w[3]), "groups": int(w[5]), "slots": defaultdict(list)})
         elif w[0] == "slot":
@@ -95,3 +97,49 @@ def test_lane_groups_are_vertex_disjoint_and_dense(plan_tool, tmp_path, name, fa
     # bound; small tiles leave the packer fewer groups to trade faces between
     slack = max(1, len(tiles) // 10) if tile_faces >= 512 else int(0.15 * minimum)
     assert total_groups <= minimum + slack, (total_groups, minimum)
+
+
+def test_singular_scatter_plan_keeps_the_pair_order(plan_tool, tmp_path):
+    """The singular scatter runs one thread per target entry of the extended rows,
+    adding that entry's contributions in pair order.  On random float32 blocks its
+    sums must equal, bit for bit, those of the sequential walk it replaced (one
+    thread per trial face: its pairs in order, rows of test vertex a, columns b),
+    and every block element must land exactly once."""
+    mesh = meshes.box_with_piston((0.3, 0.2, 0.25), 900, 0.05, "+z")
+    path = tmp_path / "mesh.bin"
+    with open(path, "wb") as f:
+        np.array([mesh.n_vertices, len(mesh.faces)], np.int32).tofile(f)
+        np.ascontiguousarray(mesh.vertices, np.float64).tofile(f)
+        np.ascontiguousarray(mesh.faces, np.int32).tofile(f)
+    out = subprocess.run([str(plan_tool), str(path), "128"], check=True, capture_output=True, text=True).stdout
+    pairs, fext, scat, n_ext = [], [], [], 0
+    for line in out.splitlines():
+        w = line.split()
+        if w[0] == "npairs":
+            n_ext = int(w[3])
+        elif w[0] == "pair":
+            pairs.append((int(w[1]), int(w[2])))
+        elif w[0] == "fext":
+            fext.append(tuple(map(int, w[1:])))
+        elif w[0] == "scat":
+            scat.append((int(w[1]), int(w[2]), [int(x) for x in w[3:]]))
+    nf = len(mesh.faces)
+    rng = np.random.default_rng(0)
+    blocks = rng.normal(size=12 * len(pairs)).astype(np.float32)
+    base = rng.normal(size=(3 * nf, n_ext)).astype(np.float32)
+    walk = base.copy()
+    for k, (g, f) in enumerate(pairs):  # pairs are sorted by trial face
+        for a in range(3):
+            for b in range(3):
+                walk[3 * g + b, fext[f][a]] = np.float32(walk[3 * g + b, fext[f][a]] + blocks[12 * k + 3 * a + b])
+    planned = base.copy()
+    used = np.zeros(12 * len(pairs), int)
+    for col, row, srcs in scat:
+        v = planned[col, row]
+        for s in srcs:
+            v = np.float32(v + blocks[s])
+            used[s] += 1
+        planned[col, row] = v
+    assert np.array_equal(walk.view(np.int32), planned.view(np.int32))
+    assert len({(c, r) for c, r, _ in scat}) == len(scat)
+    assert np.all(used.reshape(-1, 12)[:, :9] == 1) and np.all(used.reshape(-1, 12)[:, 9:] == 0)
