@@ -446,13 +446,14 @@ def main() -> None:
     # dominant kernel roofline: regular-pair assembly, FP32 pipe (mixed form)
     st0 = stats_list[0]
     regular_qpairs = st0["regular_pairs"] * 36
-    # per q-pair and frequency, counted from the regular_f32_kernel source (FMA = 2 flop):
-    # half of the q-pair geometry shared by the launch's two frequencies (23 flop), the
-    # phase and weight (7), e^{ikr} E'' and the basis sums (22), and per test point the
-    # W and S0 updates and its geometry (8.6, per q-pair)
-    flops_per_qpair = 49
+    # FP32 flop the regular kernel executed (FMA = 2), counted by the library from the
+    # kernel's source for the launch widths it used: per q-pair and frequency
+    # 35.67 + 26.83 / w, w = frequencies sharing one launch's geometry (4 at this size:
+    # 42.4 flop; 49.1 with pairs of frequencies)
+    reg_flop = sum(st["regular_flop"] for st in stats_list)
+    flops_per_qpair = reg_flop / (regular_qpairs * args.steps * B) if regular_qpairs else 0.0
     reg_s = kernel_s["regular"] / (args.steps * B)  # seconds per frequency
-    achieved = regular_qpairs * flops_per_qpair / reg_s / 1e12 if reg_s > 0 else None
+    achieved = reg_flop / kernel_s["regular"] / 1e12 if kernel_s["regular"] > 0 else None
     clock = result["clocks"]["sm_mhz"] or 1920.0
     n_sm = torch.cuda.get_device_properties(local_rank).multi_processor_count
     fp32_peak = n_sm * 128 * 2 * clock * 1e6 / 1e12
@@ -463,14 +464,18 @@ def main() -> None:
         "peak": fp32_peak,
         "unit": "TFLOP/s",
         "frac": (achieved / fp32_peak) if achieved else None,
-        # DRAM bytes per frequency (half of one two-frequency launch) from one ncu capture
-        # of this kernel at this workload (dram__bytes_read.sum + dram__bytes_write.sum,
-        # current source); the algorithmic bytes are the extended-row output,
-        # 3 x N_f x ldR x 8 B = 1.360e9 per frequency
+        # DRAM bytes per frequency from one ncu capture of this kernel at this workload
+        # (dram__bytes_read.sum + dram__bytes_write.sum, current source); the algorithmic
+        # bytes are the extended-row output, 3 x N_f x ldR x 8 B = 1.360e9 per frequency
         "traffic": REGULAR_DRAM_BYTES_PER_FREQ if args.workload == "box10k" and args.faces in (None, 10000) else None,
         "peak_source": f"{n_sm} SMs (device query) x 128 FP32 lanes x 2 flop x median SM clock sampled during the run "
                        "(MEASURED_PEAKS.json has no FP32 figure)",
-        "work_per_frequency": f"{regular_qpairs:.4g} q-pairs x {flops_per_qpair} flop",
+        "work_per_frequency": f"{regular_qpairs:.4g} q-pairs x {flops_per_qpair:.2f} flop",
+        "ms_per_frequency": 1e3 * reg_s,
+        # the same time against the reference's own arithmetic per q-pair (about 160 flop:
+        # S, D, K' and H integrands formed separately, BeatEngineCpuAssembly.jl:316-346),
+        # context only: this kernel folds them and shares the geometry across frequencies
+        "reference_flop_equivalent_frac": (regular_qpairs * 160 / reg_s / 1e12 / fp32_peak) if reg_s > 0 else None,
     }
 
     if fp64_workload:

@@ -1446,33 +1446,33 @@ cudaError_t launch_regular_f32(const DeviceMesh& m, const double* k, const doubl
 }  // namespace
 
 // Frequencies per regular-kernel launch for a group of n that all carry the
-// double-layer term: fours, with a remainder of 1 taken as 3 + 2 (a single
-// frequency per launch shares nothing); NFQ 4 only while two CTAs of its
-// accumulators fit in shared memory, else twos.
-int regular_quad_ok(const DeviceMesh& m) {
-  const size_t per_cta = (size_t)4 * 4 * 3 * m.max_tile_rows * sizeof(float2);
-  return per_cta <= (size_t)112 * 1024 ? 1 : 0;
+// double-layer term: the widest NFQ (4, else 3, else 2) whose per-warp
+// accumulators still let two CTAs share an SM's shared memory; a remainder that
+// would leave a single frequency alone (which shares nothing) is split into
+// 3 + 2 (NFQ 4) or 2 + 2 (NFQ 3).
+int regular_width(const DeviceMesh& m) {
+  for (int w = 4; w >= 3; --w)
+    if ((size_t)4 * w * 3 * m.max_tile_rows * sizeof(float2) <= (size_t)112 * 1024) return w;
+  return 2;
 }
 
-int regular_split(int n, bool quad, int* sizes) {
+int regular_split(int n, int width, int* sizes) {
   int cnt = 0;
-  if (!quad) {
+  if (width <= 2) {
     for (; n >= 2; n -= 2) sizes[cnt++] = 2;
     if (n) sizes[cnt++] = 1;
     return cnt;
   }
-  int q = n / 4, r = n % 4;
-  if (r == 1 && q >= 1) {
+  int q = n / width, r = n % width;
+  if (r == 1 && q >= 1) {  // width + 1 = (width - 1) + 2
     --q;
-    r = 5;
-  }
-  for (int i = 0; i < q; ++i) sizes[cnt++] = 4;
-  if (r == 5) {
-    sizes[cnt++] = 3;
+    for (int i = 0; i < q; ++i) sizes[cnt++] = width;
+    sizes[cnt++] = width - 1;
     sizes[cnt++] = 2;
-  } else if (r) {
-    sizes[cnt++] = r;
+    return cnt;
   }
+  for (int i = 0; i < q; ++i) sizes[cnt++] = width;
+  if (r) sizes[cnt++] = r;
   return cnt;
 }
 
@@ -1481,7 +1481,7 @@ cudaError_t launch_regular(const DeviceMesh& m, Precision prec, int nfreq, const
   if (prec == Precision::Mixed) {
     // up to four frequencies per launch share the frequency-independent geometry;
     // an operator without the double-layer term (cD = 0) runs one per launch
-    const bool quad = regular_quad_ok(m);
+    const int width = regular_width(m);
     int f = 0;
     while (f < nfreq) {
       float2* R = (float2*)Rext + (size_t)f * strideR;
@@ -1495,7 +1495,7 @@ cudaError_t launch_regular(const DeviceMesh& m, Precision prec, int nfreq, const
       int run = 1;  // consecutive frequencies with the double-layer term
       while (f + run < nfreq && dt_at(f + run)) ++run;
       int sizes[64];
-      const int cnt = regular_split(run, quad, sizes);
+      const int cnt = regular_split(run, width, sizes);
       for (int i = 0; i < cnt; ++i) {
         R = (float2*)Rext + (size_t)f * strideR;
         cudaError_t e = sizes[i] == 4   ? launch_regular_f32<4, true>(m, k + f, cD + f, cH + f, R, ldR, strideR, stream)
@@ -1520,7 +1520,16 @@ int regular_groups(const DeviceMesh& m, Precision prec, int nfreq, int* sizes) {
     for (int i = 0; i < nfreq; ++i) sizes[i] = 1;
     return nfreq;
   }
-  return regular_split(nfreq, regular_quad_ok(m), sizes);
+  return regular_split(nfreq, regular_width(m), sizes);
+}
+
+double regular_flop_per_qpair(int w) {
+  // per quadrature pair and frequency, counted from regular_f32_kernel: the
+  // frequency-independent geometry of the pair (23) and of its test point (23 / Q
+  // with Q = 6 trial points) shared by the w frequencies of a launch; per
+  // frequency the phase and weight (7), e^{ikr} E'' and the basis sums (22), and
+  // the test point's W and S0 updates (40 / 6)
+  return 7.0 + 22.0 + 40.0 / 6.0 + (23.0 + 23.0 / 6.0) / (double)w;
 }
 
 int regular_launches(const DeviceMesh& m, Precision prec, int nfreq) {

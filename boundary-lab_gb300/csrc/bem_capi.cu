@@ -257,7 +257,8 @@ int assembly_group(bem::Precision prec) { return prec == bem::Precision::Mixed ?
 // own layout.  Returns the number of kernels launched.
 long long assemble_frequencies(bem_mesh* m, bem::Precision prec, int cnt, const double* k,
                                const bem::OperatorCoeffs* c, void* const* A, void* const* A2, const double2* qscale,
-                               int nc, const void* drive, void* const* b, long long lda = 0, long long ldb = 0) {
+                               int nc, const void* drive, void* const* b, long long lda = 0, long long ldb = 0,
+                               double* regular_flop = nullptr) {
   bem_context* ctx = m->ctx;
   const bem::DeviceMesh& dm = m->dm;
   Layout L = layout_for(dm, prec);
@@ -312,6 +313,10 @@ long long assemble_frequencies(bem_mesh* m, bem::Precision prec, int cnt, const 
     }
     // per frequency: singular, scatter, gather (+ isolated rows), right-hand side (2)
     launches += (long long)g * (3 + (dm.n_isolated ? 1 : 0) + (nc > 0 ? 2 : 0)) + bem::regular_launches(dm, prec, g);
+    if (regular_flop && prec == bem::Precision::Mixed) {
+      const double qpairs = ((double)dm.ntr * dm.nf * dm.nf - dm.npairs) * dm.Q * dm.Q;
+      *regular_flop += g * qpairs * bem::regular_flop_per_qpair(g);
+    }
   }
   return launches;
 }
@@ -745,6 +750,7 @@ struct Slice {
 // Totals over the batches of one call.
 struct SolveTotals {
   double kacc[BEM_K_SLOTS] = {0};
+  double regular_flop = 0;
   double t_asm = 0, t_sol = 0, t_fld = 0, max_res = 0;
   int max_steps = 0, batches = 0, gemm_used = 0;
   long long launches = 0;
@@ -823,7 +829,7 @@ void solve_combined(bem_context* ctx, const std::vector<Slice>& sl, int n, const
     const void* drive = mixed ? x.m->drive32.p : x.m->drive64.p;
     T.launches += assemble_frequencies(x.m, prec, x.cnt, ks.data() + i0, cs.data() + i0, As.data() + i0,
                                        mixed ? A2s.data() + i0 : nullptr, qs.data() + i0, nc, drive, bs.data() + i0,
-                                       lda, ldb);
+                                       lda, ldb, &T.regular_flop);
     if (nvm < n) {
       dim3 g((unsigned)n, (unsigned)x.cnt);
       if (mixed)
@@ -977,6 +983,7 @@ void fill_stats(bem_solve_stats* stats, const SolveTotals& T) {
   for (int i = 0; i < 8; ++i) stats->kernel_s[i] = T.kacc[i];
   stats->lu_gemm_used = T.gemm_used;
   stats->kernel_launches = T.launches;
+  stats->regular_flop = T.regular_flop;
 }
 
 bool valid_options(bem_context* ctx, const bem_solve_options& o) {

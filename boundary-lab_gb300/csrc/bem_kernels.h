@@ -94,6 +94,9 @@ cudaError_t launch_regular(const DeviceMesh& m, Precision prec, int nfreq, const
 // FP64: ones); writes the group sizes (nfreq <= 64) and returns their count.
 int regular_groups(const DeviceMesh& m, Precision prec, int nfreq, int* sizes);
 int regular_launches(const DeviceMesh& m, Precision prec, int nfreq);
+// FP32 flop per quadrature pair and frequency of the mixed-form regular kernel
+// when w frequencies share a launch (FMA = 2, counted from its source).
+double regular_flop_per_qpair(int w);
 cudaError_t launch_regular_f64(const DeviceMesh& m, double k, double2 cD, double2 cH, double2* Rext, long long ldR,
                                cudaStream_t stream);
 // Per-pair FP32 record written at upload by the pair setup and moments kernels (see bem_assembly.cu).

@@ -535,6 +535,25 @@ __global__ void lu_perm_kernel(const int* __restrict__ ipiv, int n, int* __restr
 constexpr int kSolveThreads = 512;
 
 // One cluster per (matrix, right-hand side): x = U^{-1} L^{-1} (P b), in place in B.
+// Pull rows [lo, hi) of columns [c0, c0 + 32) of M (column-major, clipped to
+// the n x n matrix) into L2 ahead of their use: one prefetch per 128-byte line,
+// spread over the CTA's threads.
+template <typename C2>
+__device__ __forceinline__ void prefetch_strip_l2(const C2* M, long long lda, int n, int c0, int lo, int hi) {
+  constexpr int kPerLine = 128 / (int)sizeof(C2);
+  lo = max(lo, 0);
+  hi = min(hi, n);
+  if (hi <= lo || c0 >= n) return;
+  const int first = lo / kPerLine, last = (hi - 1) / kPerLine;
+  const int lines = last - first + 1;
+  const int cols = min(32, n - c0);
+  for (int i = threadIdx.x; i < lines * cols; i += blockDim.x) {
+    const int c = i / lines, l = i - c * lines;
+    const C2* ptr = M + (size_t)(c0 + c) * lda + (size_t)(first + l) * kPerLine;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
+  }
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kSolveThreads) lu_solve_cluster_kernel(const typename CT2<R>::C2* A, long long lda,
                                                                          long long strideA, int n,
@@ -559,10 +578,13 @@ __global__ void __launch_bounds__(kSolveThreads) lu_solve_cluster_kernel(const t
   cluster.sync();  // every CTA has read b before anyone writes it back
   const int nblk = (n + 31) / 32;
   // forward substitution with unit lower L
+  if (rows > 0) prefetch_strip_l2(M, lda, n, 0, r0, r0 + rows);
   for (int t = 0; t < nblk; ++t) {
     const int k0 = t * 32, kb = min(32, n - k0);
     const int owner = k0 / chunk;
     C2* slot = pub + 32 * (t & 1);
+    // the next step's columns of my rows (its diagonal block included) stream into L2 meanwhile
+    if (rows > 0 && t + 1 < nblk) prefetch_strip_l2(M, lda, n, k0 + 32, max(r0, k0 + 32), r0 + rows);
     if (rank == owner && tid < 32) {
       // this lane's row of the diagonal block, loaded up front (independent loads)
       C2 Lr[32];
@@ -602,21 +624,36 @@ __global__ void __launch_bounds__(kSolveThreads) lu_solve_cluster_kernel(const t
       const int r = r0 + i;
       if (r < k0 + kb) continue;
       C2 v = x[i];
+      if (sizeof(C2) == sizeof(float2) && kb == 32) {  // FP32: all 32 loads in flight at once
+        C2 l[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) l[j] = M[(size_t)(k0 + j) * lda + r];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const C2 s = xs[j];
+          v.x -= l[j].x * s.x - l[j].y * s.y;
+          v.y -= l[j].x * s.y + l[j].y * s.x;
+        }
+      } else {
 #pragma unroll 8
-      for (int j = 0; j < kb; ++j) {
-        const C2 l = M[(size_t)(k0 + j) * lda + r];
-        const C2 s = xs[j];
-        v.x -= l.x * s.x - l.y * s.y;
-        v.y -= l.x * s.y + l.y * s.x;
+        for (int j = 0; j < kb; ++j) {
+          const C2 l = M[(size_t)(k0 + j) * lda + r];
+          const C2 s = xs[j];
+          v.x -= l.x * s.x - l.y * s.y;
+          v.y -= l.x * s.y + l.y * s.x;
+        }
       }
       x[i] = v;
     }
     __syncthreads();
   }
   // backward substitution with U
+  if (rows > 0) prefetch_strip_l2(M, lda, n, (nblk - 1) * 32, r0, min(r0 + rows, n));
   for (int t = nblk - 1; t >= 0; --t) {
     const int k0 = t * 32, kb = min(32, n - k0);
     const int owner = k0 / chunk;
+    // the next (lower) block's columns of my rows above its diagonal block's end
+    if (rows > 0 && t > 0) prefetch_strip_l2(M, lda, n, k0 - 32, r0, min(r0 + rows, k0));
     // the slot alternates over the whole sequence of blocks (forward then backward)
     C2* slot = pub + 32 * ((nblk + (nblk - 1 - t)) & 1);
     if (rank == owner && tid < 32) {
@@ -662,12 +699,24 @@ __global__ void __launch_bounds__(kSolveThreads) lu_solve_cluster_kernel(const t
       const int r = r0 + i;
       if (r >= k0) continue;
       C2 v = x[i];
+      if (sizeof(C2) == sizeof(float2) && kb == 32) {  // FP32: all 32 loads in flight at once
+        C2 u[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) u[j] = M[(size_t)(k0 + j) * lda + r];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const C2 s = ys[j];
+          v.x -= u[j].x * s.x - u[j].y * s.y;
+          v.y -= u[j].x * s.y + u[j].y * s.x;
+        }
+      } else {
 #pragma unroll 8
-      for (int j = 0; j < kb; ++j) {
-        const C2 u = M[(size_t)(k0 + j) * lda + r];
-        const C2 s = ys[j];
-        v.x -= u.x * s.x - u.y * s.y;
-        v.y -= u.x * s.y + u.y * s.x;
+        for (int j = 0; j < kb; ++j) {
+          const C2 u = M[(size_t)(k0 + j) * lda + r];
+          const C2 s = ys[j];
+          v.x -= u.x * s.x - u.y * s.y;
+          v.y -= u.x * s.y + u.y * s.x;
+        }
       }
       x[i] = v;
     }

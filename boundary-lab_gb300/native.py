@@ -120,6 +120,7 @@ class SolveStats(ctypes.Structure):
         ("singular_points", ctypes.c_longlong),
         ("lu_gemm_used", ctypes.c_int),
         ("kernel_launches", ctypes.c_longlong),
+        ("regular_flop", ctypes.c_double),
     ]
 
 KERNEL_SLOTS = ("singular", "regular", "gather", "rhs", "lu", "solve", "field")

@@ -147,6 +147,9 @@ typedef struct bem_solve_stats {
   long long singular_points; /* Duffy points summed over the singular pairs, per frequency */
   int lu_gemm_used;       /* trailing update that ran: 1 cuBLAS, 2 tensor cores (0 FP64 form) */
   long long kernel_launches; /* kernels of this library launched by the call (cuBLAS kernels not counted) */
+  double regular_flop;    /* mixed form: FP32 flop (FMA = 2) the regular-pair kernel executed in the call,
+                             counted from its source per quadrature pair and frequency: 35.67 + 26.83 / w,
+                             w = frequencies sharing one launch's frequency-independent geometry */
 } bem_solve_stats;
 
 void bem_default_options(bem_solve_options* opt);
