@@ -40,7 +40,7 @@ UNIT = "frequency-solves/s"
 SOUND_SPEED = 343.0
 RHO = 1.205
 # regular_f32_kernel DRAM bytes per frequency on box10k (ncu, profiles/regular_f32_kernel_box10k.md)
-REGULAR_DRAM_BYTES_PER_FREQ = 1.3804e9  # (70.4 MB read + 2,690.4 MB written) / 2 frequencies
+REGULAR_DRAM_BYTES_PER_FREQ = 1.3964e9  # (152.0 MB read + 5,433.6 MB written) / 4 frequencies
 
 
 def pkg(name: str):

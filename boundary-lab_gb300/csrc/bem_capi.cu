@@ -921,6 +921,8 @@ void solve_combined(bem_context* ctx, const std::vector<Slice>& sl, int n, const
       throw BemError{BEM_ERR_CUDA, "tensor-core LU update gave up waiting (status " + std::to_string(h) + ")"};
   }
   for (int i = 0; i < B; ++i)
+    if (info[i] < 0) throw BemError{BEM_ERR_CUDA, "LU panel exchange gave up waiting (frequency " + std::to_string(fz[i]) + " Hz)"};
+  for (int i = 0; i < B; ++i)
     if (info[i] != 0)
       throw BemError{BEM_ERR_SINGULAR, "zero pivot in LU factorisation (frequency " + std::to_string(fz[i]) + " Hz)"};
   // solutions (vertex order) as [B][nc][ldb]
@@ -1205,6 +1207,7 @@ int bem_lu_factor_dense(bem_context* ctx, int n, double* a, int* ipiv, int preci
         a[2 * ((size_t)j * n + i)] = re;
         a[2 * ((size_t)j * n + i) + 1] = im;
       }
+    if (info < 0) return fail(ctx, BEM_ERR_CUDA, "LU panel exchange gave up waiting");
     if (info != 0) return fail(ctx, BEM_ERR_SINGULAR, "zero pivot at column " + std::to_string(info - 1));
     return BEM_OK;
   });
