@@ -23,8 +23,6 @@
 #include <cooperative_groups.h>
 #include <limits.h>
 
-#include <cstdlib>
-#include <string>
 #include <type_traits>
 
 #include "bem_common.cuh"
@@ -333,50 +331,6 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_cluster_kernel(typenam
 //     lg; every other active row stores l = a[0] / pivot, subtracts l u and
 //     shifts; the next candidate is reduced per warp; CTA barrier.
 // Requires a full panel (kb = 32) and chunk <= kRegPanelThreads.
-// Cluster exchange through mbarriers (the register panel's ASYNC form): each
-// CTA keeps one mbarrier per slot; remote CTAs write into the slot with
-// st.async, whose bytes complete a transaction count on the receiving CTA's
-// barrier, and the receiver waits for that barrier's phase with cluster-scope
-// acquire.  No writer fence and no cluster barrier per column.  Waits give up
-// after kXWaitLimit polls (1 us suspend hint each, about a second).
-constexpr long long kXWaitLimit = 1LL << 20;
-__device__ __forceinline__ uint32_t cta_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ uint32_t peer_addr(const void* p, int rank) {
-  uint32_t r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(cta_addr(p)), "r"(rank));
-  return r;
-}
-__device__ __forceinline__ void st_async_f2(uint32_t raddr, float2 v, uint32_t rbar) {
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(raddr),
-               "f"(v.x), "f"(v.y), "r"(rbar)
-               : "memory");
-}
-__device__ __forceinline__ void st_async_b32(uint32_t raddr, uint32_t v, uint32_t rbar) {
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(raddr), "r"(v),
-               "r"(rbar)
-               : "memory");
-}
-__device__ __forceinline__ void xbar_init(uint64_t* bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(cta_addr(bar)) : "memory");
-}
-__device__ __forceinline__ void xbar_expect(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(cta_addr(bar)), "r"(bytes) : "memory");
-}
-// bounded wait for the phase of the given parity; false after kXWaitLimit polls
-__device__ __forceinline__ bool xbar_wait(uint64_t* bar, uint32_t parity) {
-  for (long long i = 0; i < kXWaitLimit; ++i) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2, %3;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(cta_addr(bar)), "r"(parity), "r"(1000)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
-}
-
 constexpr int kRegPanelThreads = 640;
 constexpr int kRegPanelWarps = kRegPanelThreads / 32;
 
@@ -394,7 +348,6 @@ __device__ __forceinline__ void warp_argmax_at(float& b, int& x, int& at) {
   }
 }
 
-template <bool ASYNC>
 __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float2* A, long long lda, long long strideA,
                                                                            int n, int k, int kb, int chunk, int* ipiv,
                                                                            int* info, int* rowmap) {
@@ -413,22 +366,6 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
   __shared__ float wval[NW];
   __shared__ int widx[NW], wlane[NW];
   __shared__ int s_pivs[NB];
-  __shared__ float2 dgr[2][NB];           // ASYNC: row j, pushed by the CTA that holds it
-  __shared__ __align__(8) uint64_t xbar[2];  // ASYNC: one exchange barrier per slot
-  // ASYNC: bytes each CTA receives per column step: from every CTA its candidate
-  // row and (value, row index), and row j from its holder
-  const uint32_t x_bytes = (uint32_t)(CL * (NB * 8 + 8) + NB * 8);
-  bool x_dead = false;  // ASYNC: a wait gave up; later steps skip their waits
-  if (ASYNC) {
-    if (tid == 0) {
-      xbar_init(&xbar[0]);
-      xbar_init(&xbar[1]);
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-      xbar_expect(&xbar[0], x_bytes);
-      xbar_expect(&xbar[1], x_bytes);
-    }
-    cluster.sync();  // every barrier is armed before any CTA writes into it
-  }
   float2* M = A + (size_t)blockIdx.y * strideA;
   int* piv = ipiv + (size_t)blockIdx.y * n;
   const int m = n - k;
@@ -479,49 +416,22 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
         for (int c = 0; c < NB; ++c) dg[s][c] = a[c];
       }
       const int cnt = __syncthreads_or(hasj);
-      if (ASYNC) {
-        // every CTA sends a candidate row and (value, index) to every CTA, and the
-        // holder of row j sends it, so each CTA receives x_bytes per step
-        if (tid < CL * NB) {
-          const int dst = tid / NB, c = tid & (NB - 1);
-          const uint32_t rbar = peer_addr(&xbar[s], dst);
-          st_async_f2(peer_addr(&rowsC[s][rank][c], dst), pub[c], rbar);
-          if (cnt) st_async_f2(peer_addr(&dgr[s][c], dst), dg[s][c], rbar);
-        }
-        if (tid < CL) {
-          const uint32_t rbar = peer_addr(&xbar[s], tid);
-          st_async_b32(peer_addr(&cval[s][rank], tid), __float_as_uint(bi != INT_MAX ? bv : -1.0f), rbar);
-          st_async_b32(peer_addr(&cidx[s][rank], tid), (uint32_t)bi, rbar);
-        }
-      } else {
-        bool wrote = hasj;
-        if (bi != INT_MAX && tid < CL * NB) {  // the candidate row into every CTA
-          *cluster.map_shared_rank(&rowsC[s][rank][tid & (NB - 1)], tid / NB) = pub[tid & (NB - 1)];
-          wrote = true;
-        }
-        if (tid < CL) {
-          *cluster.map_shared_rank(&cval[s][rank], tid) = bi != INT_MAX ? bv : -1.0f;
-          *cluster.map_shared_rank(&cidx[s][rank], tid) = bi;
-          *cluster.map_shared_rank(&chasj[s][rank], tid) = cnt;
-          wrote = true;
-        }
-        if (wrote) asm volatile("fence.acq_rel.cluster;" ::: "memory");
+      bool wrote = hasj;
+      if (bi != INT_MAX && tid < CL * NB) {  // the candidate row into every CTA
+        *cluster.map_shared_rank(&rowsC[s][rank][tid & (NB - 1)], tid / NB) = pub[tid & (NB - 1)];
+        wrote = true;
       }
-    }
-    if (ASYNC) {
-      // 2. this slot's bytes from every CTA have arrived (acquire, cluster scope)
-      if (!x_dead && !xbar_wait(&xbar[s], (uint32_t)((j >> 1) & 1))) {
-        x_dead = true;
-        atomicExch(&info[blockIdx.y], -1);
+      if (tid < CL) {
+        *cluster.map_shared_rank(&cval[s][rank], tid) = bi != INT_MAX ? bv : -1.0f;
+        *cluster.map_shared_rank(&cidx[s][rank], tid) = bi;
+        *cluster.map_shared_rank(&chasj[s][rank], tid) = cnt;
+        wrote = true;
       }
-      // the slot's next use is two steps on; its bytes can only come after this
-      // CTA's next push, which follows the CTA barrier at the end of this step
-      if (tid == 0 && j + 2 < NB) xbar_expect(&xbar[s], x_bytes);
-    } else {
-      // 2. the writes above were fenced by their writers; the wait acquires them
-      asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
-      asm volatile("barrier.cluster.wait.aligned;" ::: "memory");
+      if (wrote) asm volatile("fence.acq_rel.cluster;" ::: "memory");
     }
+    // 2. the writes above were fenced by their writers; the wait acquires them
+    asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.aligned;" ::: "memory");
     // 3. pivot (logical row p, held by CTA pr), in every warp
     float b = lane < CL ? cval[s][lane] : -1.0f;
     int x = lane < CL ? cidx[s][lane] : INT_MAX;
@@ -532,14 +442,10 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
     const float2* U = &rowsC[s][pr][0];  // the pivot row, u[c] = U(j, j + c) (zero beyond the panel)
     if (fallback) {  // every CTA takes this branch together
       if (wid == 0) {
-        if (ASYNC) {
-          urow[lane] = dgr[s][lane];
-        } else {
-          int jr = 0;  // CTA holding logical row j
-          const unsigned hb = __ballot_sync(0xffffffffu, lane < CL && chasj[s][lane] != 0);
-          if (hb) jr = __ffs(hb) - 1;
-          urow[lane] = *cluster.map_shared_rank(&dg[s][lane], jr);
-        }
+        int jr = 0;  // CTA holding logical row j
+        const unsigned hb = __ballot_sync(0xffffffffu, lane < CL && chasj[s][lane] != 0);
+        if (hb) jr = __ffs(hb) - 1;
+        urow[lane] = *cluster.map_shared_rank(&dg[s][lane], jr);
       }
       __syncthreads();
       U = urow;
@@ -897,9 +803,9 @@ template <typename R> bool choose_panel(int n, int want_nb, int batch, int& nb, 
     for (int c : {1, 2, 4, 8, 16}) {
       if ((n + c - 1) / c > kRegPanelThreads) continue;
       const size_t sm = (size_t)32 * kRegPanelThreads * sizeof(float2);
-      if (c > 1 && max_cluster(lu_panel_reg_kernel<false>, kRegPanelThreads, sm) < c) continue;
-      if (c == 1 && !ensure_smem_limit((const void*)lu_panel_reg_kernel<false>, sm)) continue;
-      const int act = active_clusters(lu_panel_reg_kernel<false>, kRegPanelThreads, sm, c);
+      if (c > 1 && max_cluster(lu_panel_reg_kernel, kRegPanelThreads, sm) < c) continue;
+      if (c == 1 && !ensure_smem_limit((const void*)lu_panel_reg_kernel, sm)) continue;
+      const int act = active_clusters(lu_panel_reg_kernel, kRegPanelThreads, sm, c);
       if (act < 1) continue;
       const int waves = (std::max(batch, 1) + act - 1) / act;
       if (!found || waves < best_waves) {
@@ -969,7 +875,7 @@ int lu_resident_batch(Precision prec, int n) {
   const int chunk = (n + cl - 1) / cl;
   int act = 0;
   if (prec == Precision::Mixed && nb == 32 && chunk <= kRegPanelThreads)
-    act = active_clusters(lu_panel_reg_kernel<false>, kRegPanelThreads, (size_t)32 * kRegPanelThreads * sizeof(float2), cl);
+    act = active_clusters(lu_panel_reg_kernel, kRegPanelThreads, (size_t)32 * kRegPanelThreads * sizeof(float2), cl);
   else if (prec == Precision::Mixed)
     act = nb == 64 ? active_clusters(lu_panel_cluster_kernel<float, 64>, kPanelThreads, panel_smem<float, 64>(chunk), cl)
                    : active_clusters(lu_panel_cluster_kernel<float, 32>, kPanelThreads, panel_smem<float, 32>(chunk), cl);
@@ -977,17 +883,6 @@ int lu_resident_batch(Precision prec, int n) {
     act = nb == 64 ? active_clusters(lu_panel_cluster_kernel<double, 64>, kPanelThreads, panel_smem<double, 64>(chunk), cl)
                    : active_clusters(lu_panel_cluster_kernel<double, 32>, kPanelThreads, panel_smem<double, 32>(chunk), cl);
   return std::max(1, act);
-}
-
-// Column exchange of the register panel: mbarrier-completed remote stores
-// (GB300_BEM_PANEL_EXCHANGE=mbarrier) or writer fences and one cluster barrier
-// per column (=barrier); read once per process.
-bool panel_exchange_mbarrier() {
-  static const bool v = [] {
-    const char* e = std::getenv("GB300_BEM_PANEL_EXCHANGE");
-    return e != nullptr && std::string(e) == "mbarrier";
-  }();
-  return v;
 }
 
 cudaError_t lu_panel_cluster(Precision prec, void* A, long long lda, long long strideA, int n, int k, int kb, int nb,
@@ -998,14 +893,9 @@ cudaError_t lu_panel_cluster(Precision prec, void* A, long long lda, long long s
   dim3 grid(cl, batch);
   if (prec == Precision::Mixed && nb == 32 && chunk <= kRegPanelThreads && kb == 32) {
     const size_t sm = (size_t)32 * kRegPanelThreads * sizeof(float2);
-    if (panel_exchange_mbarrier()) {
-      ensure_smem_limit((const void*)lu_panel_reg_kernel<true>, sm);
-      cudaFuncSetAttribute(lu_panel_reg_kernel<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-      return launch_cluster(lu_panel_reg_kernel<true>, grid, kRegPanelThreads, sm, cl, stream, args);
-    }
-    ensure_smem_limit((const void*)lu_panel_reg_kernel<false>, sm);
-    cudaFuncSetAttribute(lu_panel_reg_kernel<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    return launch_cluster(lu_panel_reg_kernel<false>, grid, kRegPanelThreads, sm, cl, stream, args);
+    ensure_smem_limit((const void*)lu_panel_reg_kernel, sm);
+    cudaFuncSetAttribute(lu_panel_reg_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return launch_cluster(lu_panel_reg_kernel, grid, kRegPanelThreads, sm, cl, stream, args);
   }
   if (prec == Precision::Mixed) {
     if (nb == 64) {
