@@ -985,10 +985,18 @@ struct SingParamsF32 {
   float m11m10[12];
 };
 
-__global__ void __launch_bounds__(256, 2)
+// NFQ frequencies per launch share each Duffy point's frequency-independent part
+// (the point, r, 1/r, the normal-derivative factors, the basis weights); per
+// frequency remain the phase, the remainder kernels and the 24 accumulators.
+template <int NFQ> struct SingParamsF32N {
+  SingParamsF32 f[NFQ];
+};
+
+template <int NFQ>
+__global__ void __launch_bounds__(NFQ == 1 ? 256 : 128, NFQ == 1 ? 2 : 3)
     singular_dyn_f32_kernel(const SingularPair* __restrict__ pairs, int npairs, const int* __restrict__ rule_ptr,
-                            const float* __restrict__ duffy, const float* __restrict__ rec, SingParamsF32 p,
-                            float2* __restrict__ out) {
+                            const float* __restrict__ duffy, const float* __restrict__ rec, SingParamsF32N<NFQ> pn,
+                            float2* __restrict__ out, long long out_stride) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= npairs) return;
@@ -1010,9 +1018,11 @@ __global__ void __launch_bounds__(256, 2)
   const float* e2r = g + kRecGeom + 12;
   const float* nt = g + kRecGeom + 15;
   const float* nr = g + kRecGeom + 18;
-  float2 acc2[24];  // SR[3], IR[9], IDh[9], IKh[3] as (re, im)
+  float2 acc2[NFQ][24];  // per frequency: SR[3], IR[9], IDh[9], IKh[3] as (re, im)
 #pragma unroll
-  for (int i = 0; i < 24; ++i) acc2[i] = make_float2(0.f, 0.f);
+  for (int f = 0; f < NFQ; ++f)
+#pragma unroll
+    for (int i = 0; i < 24; ++i) acc2[f][i] = make_float2(0.f, 0.f);
   const float inv4pi = (float)(0.25 / CUDART_PI);
   const int q0 = rule_ptr[P.rule], q1 = rule_ptr[P.rule + 1];
   // the next point's five values are loaded one iteration ahead
@@ -1034,76 +1044,84 @@ __global__ void __launch_bounds__(256, 2)
     for (int d = 0; d < 3; ++d) rv[d] = (d0[d] + ru * e1r[d] + rvv * e2r[d]) - (tu * e1t[d] + tv * e2t[d]);
     const float r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
     if (r2 == 0.f) continue;
-    float sh, ch;
     const float rinv = rsqrt_ftz(r2);
     const float r = r2 * rinv;
-    sincos_taylor(0.5f * p.k * r, &sh, &ch);
-    const float z = p.k * r;
     const float s = rinv * inv4pi;
-    const float sinz = 2.f * sh * ch;
-    const float omc = 2.f * sh * sh;  // 1 - cos z
-    const float cosz = 1.f - omc;
-    const float Rr = -s * omc, Ri = s * sinz;
-    const float hr = omc - z * sinz, hi = z * cosz - sinz;
     const float fy = (rv[0] * nr[0] + rv[1] * nr[1] + rv[2] * nr[2]) * s * rinv * rinv;
     const float fx = -(rv[0] * nt[0] + rv[1] * nt[1] + rv[2] * nt[2]) * s * rinv * rinv;
-    const float2 G2 = make_float2(Rr, Ri), Hy = make_float2(hr * fy, hi * fy), Hx = make_float2(hr * fx, hi * fx);
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const float wa = w * px[a];
-      const float2 wa2 = make_float2(wa, wa);
-      acc2[a] = __ffma2_rn(wa2, G2, acc2[a]);
-      acc2[21 + a] = __ffma2_rn(wa2, Hx, acc2[21 + a]);
+    for (int f = 0; f < NFQ; ++f) {
+      const SingParamsF32& p = pn.f[f];
+      float sh, ch;
+      sincos_taylor(0.5f * p.k * r, &sh, &ch);
+      const float z = p.k * r;
+      const float sinz = 2.f * sh * ch;
+      const float omc = 2.f * sh * sh;  // 1 - cos z
+      const float cosz = 1.f - omc;
+      const float Rr = -s * omc, Ri = s * sinz;
+      const float hr = omc - z * sinz, hi = z * cosz - sinz;
+      const float2 G2 = make_float2(Rr, Ri), Hy = make_float2(hr * fy, hi * fy), Hx = make_float2(hr * fx, hi * fx);
 #pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        const float2 wab = __fmul2_rn(wa2, make_float2(py[b], py[b]));
-        acc2[3 + 3 * a + b] = __ffma2_rn(wab, G2, acc2[3 + 3 * a + b]);
-        acc2[12 + 3 * a + b] = __ffma2_rn(wab, Hy, acc2[12 + 3 * a + b]);
+      for (int a = 0; a < 3; ++a) {
+        const float wa = w * px[a];
+        const float2 wa2 = make_float2(wa, wa);
+        acc2[f][a] = __ffma2_rn(wa2, G2, acc2[f][a]);
+        acc2[f][21 + a] = __ffma2_rn(wa2, Hx, acc2[f][21 + a]);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          const float2 wab = __fmul2_rn(wa2, make_float2(py[b], py[b]));
+          acc2[f][3 + 3 * a + b] = __ffma2_rn(wab, G2, acc2[f][3 + 3 * a + b]);
+          acc2[f][12 + 3 * a + b] = __ffma2_rn(wab, Hy, acc2[f][12 + 3 * a + b]);
+        }
       }
     }
   }
-#pragma unroll
-  for (int i = 0; i < 24; ++i) acc2[i] = make_float2(warp_sum(acc2[i].x), warp_sum(acc2[i].y));
-  if (lane >= 12) return;
   const float jac = g[kRecJac];
   const bool coincident = P.kind == 1 && P.tr == 0;  // mass terms: the face with itself, never with an image
   const float a2 = g[kRecA2];
-  float2* o = out + (size_t)kSingOut * warp;
-  if (lane < 9) {
-    const int i = lane;
-    // S0 = sum w G (static + dynamic)
-    float2 S0 = make_float2(G[kRecS0], 0.f);
 #pragma unroll
-    for (int a = 0; a < 3; ++a) S0 = cadd(S0, make_float2(acc2[a].x * jac, acc2[a].y * jac));
-    float2 IR = make_float2(0.f, 0.f), IDh = make_float2(0.f, 0.f);
+  for (int f = 0; f < NFQ; ++f) {
+    const SingParamsF32& p = pn.f[f];
 #pragma unroll
-    for (int j = 0; j < 9; ++j)
-      if (j == i) {
-        IR = make_float2(acc2[3 + j].x * jac, acc2[3 + j].y * jac);
-        IDh = make_float2(acc2[12 + j].x * jac, acc2[12 + j].y * jac);
-      }
-    const float kk_nn = p.k2 * g[kRecNprod];
-    const float cc = G[kRecCurl + i];
-    const float2 D = make_float2(G[kRecMom + 12 + i] + IDh.x, IDh.y);
-    const float2 IGt = make_float2(G[kRecMom + 3 + i] + IR.x, IR.y);
-    const float2 H = make_float2(cc * S0.x - kk_nn * IGt.x, cc * S0.y - kk_nn * IGt.y);
-    float2 L = cadd(cmul(p.cD, D), cmul(p.cH, H));
-    if (coincident) L = cadd(L, cscale(p.cM, a2 * p.m11m10[i]));
-    o[i] = L;
-  } else {
-    const int a = lane - 9;
-    float2 SR = make_float2(0.f, 0.f), IKh = make_float2(0.f, 0.f);
+    for (int i = 0; i < 24; ++i) acc2[f][i] = make_float2(warp_sum(acc2[f][i].x), warp_sum(acc2[f][i].y));
+    if (lane >= 12) continue;
+    float2* o = out + (size_t)f * out_stride + (size_t)kSingOut * warp;
+    if (lane < 9) {
+      const int i = lane;
+      // S0 = sum w G (static + dynamic)
+      float2 S0 = make_float2(G[kRecS0], 0.f);
 #pragma unroll
-    for (int j = 0; j < 3; ++j)
-      if (j == a) {
-        SR = make_float2(acc2[j].x * jac, acc2[j].y * jac);
-        IKh = make_float2(acc2[21 + j].x * jac, acc2[21 + j].y * jac);
-      }
-    const float2 S = make_float2(G[kRecMom + a] + SR.x, SR.y);
-    const float2 K = make_float2(G[kRecMom + 21 + a] + IKh.x, IKh.y);
-    float2 rhs = cadd(cmul(p.cS, S), cmul(p.cK, K));
-    if (coincident) rhs = cadd(rhs, cscale(p.cM10, a2 * p.m11m10[9 + a]));
-    o[9 + a] = rhs;
+      for (int a = 0; a < 3; ++a) S0 = cadd(S0, make_float2(acc2[f][a].x * jac, acc2[f][a].y * jac));
+      float2 IR = make_float2(0.f, 0.f), IDh = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < 9; ++j)
+        if (j == i) {
+          IR = make_float2(acc2[f][3 + j].x * jac, acc2[f][3 + j].y * jac);
+          IDh = make_float2(acc2[f][12 + j].x * jac, acc2[f][12 + j].y * jac);
+        }
+      const float kk_nn = p.k2 * g[kRecNprod];
+      const float cc = G[kRecCurl + i];
+      const float2 D = make_float2(G[kRecMom + 12 + i] + IDh.x, IDh.y);
+      const float2 IGt = make_float2(G[kRecMom + 3 + i] + IR.x, IR.y);
+      const float2 H = make_float2(cc * S0.x - kk_nn * IGt.x, cc * S0.y - kk_nn * IGt.y);
+      float2 L = cadd(cmul(p.cD, D), cmul(p.cH, H));
+      if (coincident) L = cadd(L, cscale(p.cM, a2 * p.m11m10[i]));
+      o[i] = L;
+    } else {
+      const int a = lane - 9;
+      float2 SR = make_float2(0.f, 0.f), IKh = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        if (j == a) {
+          SR = make_float2(acc2[f][j].x * jac, acc2[f][j].y * jac);
+          IKh = make_float2(acc2[f][21 + j].x * jac, acc2[f][21 + j].y * jac);
+        }
+      const float2 S = make_float2(G[kRecMom + a] + SR.x, SR.y);
+      const float2 K = make_float2(G[kRecMom + 21 + a] + IKh.x, IKh.y);
+      float2 rhs = cadd(cmul(p.cS, S), cmul(p.cK, K));
+      if (coincident) rhs = cadd(rhs, cscale(p.cM10, a2 * p.m11m10[9 + a]));
+      o[9 + a] = rhs;
+    }
   }
 }
 
@@ -1577,41 +1595,68 @@ cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, float* 
   return cudaGetLastError();
 }
 
-cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, double k, const OperatorCoeffs& c,
-                                void* blocks, cudaStream_t stream) {
+cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, int nfreq, const double* k,
+                                const OperatorCoeffs* c, void* blocks, long long blocks_stride, cudaStream_t stream) {
   if (m.npairs == 0) return cudaSuccess;
   SingularGeom geo{m.verts, m.faces, m.normal};
+  if (prec == Precision::Mixed) {
+    auto params = [&](int f) {
+      SingParamsF32 p;
+      p.k = (float)k[f];
+      p.k2 = (float)(k[f] * k[f]);
+      p.cD = f2(c[f].cD);
+      p.cH = f2(c[f].cH);
+      p.cM = f2(c[f].cM);
+      p.cS = f2(c[f].cS);
+      p.cK = f2(c[f].cK);
+      p.cM10 = f2(c[f].cM10);
+      for (int i = 0; i < 12; ++i) p.m11m10[i] = m.m11m10f[i];
+      return p;
+    };
+    // two frequencies per launch share each point's geometry; a lone last one runs alone
+    for (int f = 0; f < nfreq;) {
+      float2* o = (float2*)blocks + (size_t)f * blocks_stride;
+      if (f + 1 < nfreq) {
+        SingParamsF32N<2> pn;
+        pn.f[0] = params(f);
+        pn.f[1] = params(f + 1);
+        const int threads = 128;
+        const int nblk = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
+        singular_dyn_f32_kernel<2><<<nblk, threads, 0, stream>>>(m.pairs, m.npairs, m.rule_ptr, m.duffy32, m.pairrec,
+                                                                 pn, o, blocks_stride);
+        f += 2;
+      } else {
+        SingParamsF32N<1> pn;
+        pn.f[0] = params(f);
+        const int threads = 256;
+        const int nblk = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
+        singular_dyn_f32_kernel<1><<<nblk, threads, 0, stream>>>(m.pairs, m.npairs, m.rule_ptr, m.duffy32, m.pairrec,
+                                                                 pn, o, blocks_stride);
+        f += 1;
+      }
+    }
+    return cudaGetLastError();
+  }
   const int threads = 256;
   const int nblk = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
-  if (prec == Precision::Mixed) {
-    SingParamsF32 p;
-    p.k = (float)k;
-    p.k2 = (float)(k * k);
-    p.cD = f2(c.cD);
-    p.cH = f2(c.cH);
-    p.cM = f2(c.cM);
-    p.cS = f2(c.cS);
-    p.cK = f2(c.cK);
-    p.cM10 = f2(c.cM10);
-    for (int i = 0; i < 12; ++i) p.m11m10[i] = m.m11m10f[i];
-    singular_dyn_f32_kernel<<<nblk, threads, 0, stream>>>(m.pairs, m.npairs, m.rule_ptr, m.duffy32, m.pairrec, p,
-                                                          (float2*)blocks);
-  } else {
+  for (int f = 0; f < nfreq; ++f) {
     SingParams<double> p;
-    p.k = k;
-    p.k2 = k * k;
-    p.cD = c.cD;
-    p.cH = c.cH;
-    p.cM = c.cM;
-    p.cS = c.cS;
-    p.cK = c.cK;
-    p.cM10 = c.cM10;
+    p.k = k[f];
+    p.k2 = k[f] * k[f];
+    p.cD = c[f].cD;
+    p.cH = c[f].cH;
+    p.cM = c[f].cM;
+    p.cS = c[f].cS;
+    p.cK = c[f].cK;
+    p.cM10 = c[f].cM10;
     singular_dyn_kernel<double><<<nblk, threads, 0, stream>>>(geo, m.pairs, m.npairs, m.rule_ptr, m.duffy,
                                                               m.moments, m.curls, m.area, m.m11m10, p,
-                                                              (double2*)blocks);
+                                                              (double2*)blocks + (size_t)f * blocks_stride);
   }
   return cudaGetLastError();
 }
+
+int singular_launches(Precision prec, int nfreq) { return prec == Precision::Mixed ? (nfreq + 1) / 2 : nfreq; }
 
 cudaError_t launch_singular_scatter(const DeviceMesh& m, Precision prec, const void* blocks, void* Rext,
                                     long long ldR, cudaStream_t stream) {

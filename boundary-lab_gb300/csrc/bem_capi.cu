@@ -290,8 +290,8 @@ long long assemble_frequencies(bem_mesh* m, bem::Precision prec, int cnt, const 
        "regular kernel");
     prof_mark(ctx, BEM_K_REGULAR);
     if (m->moments_ready) ck(cudaStreamWaitEvent(ctx->stream, m->moments_ready, 0), "wait for singular moments");
-    for (int i = 0; i < g; ++i)
-      ck(bem::launch_singular_dyn(dm, prec, k[f0 + i], c[f0 + i], sblk(i), ctx->stream), "singular kernel");
+    ck(bem::launch_singular_dyn(dm, prec, g, k + f0, c + f0, sblk(0), (long long)sblk_n, ctx->stream),
+       "singular kernel");
     prof_mark(ctx, BEM_K_SINGULAR);
     for (int i = 0; i < g; ++i) {
       void* Ai = A[f0 + i];
@@ -311,8 +311,10 @@ long long assemble_frequencies(bem_mesh* m, bem::Precision prec, int cnt, const 
            "rhs kernel");
       prof_mark(ctx, BEM_K_RHS);
     }
-    // per frequency: singular, scatter, gather (+ isolated rows), right-hand side (2)
-    launches += (long long)g * (3 + (dm.n_isolated ? 1 : 0) + (nc > 0 ? 2 : 0)) + bem::regular_launches(dm, prec, g);
+    // per frequency: scatter, gather (+ isolated rows), right-hand side (2); per group the
+    // regular and singular launches
+    launches += (long long)g * (2 + (dm.n_isolated ? 1 : 0) + (nc > 0 ? 2 : 0)) + bem::regular_launches(dm, prec, g) +
+                bem::singular_launches(prec, g);
     if (regular_flop && prec == bem::Precision::Mixed) {
       const double qpairs = ((double)dm.ntr * dm.nf * dm.nf - dm.npairs) * dm.Q * dm.Q;
       *regular_flop += g * qpairs * bem::regular_flop_per_qpair(g);
@@ -921,8 +923,6 @@ void solve_combined(bem_context* ctx, const std::vector<Slice>& sl, int n, const
       throw BemError{BEM_ERR_CUDA, "tensor-core LU update gave up waiting (status " + std::to_string(h) + ")"};
   }
   for (int i = 0; i < B; ++i)
-    if (info[i] < 0) throw BemError{BEM_ERR_CUDA, "LU panel exchange gave up waiting (frequency " + std::to_string(fz[i]) + " Hz)"};
-  for (int i = 0; i < B; ++i)
     if (info[i] != 0)
       throw BemError{BEM_ERR_SINGULAR, "zero pivot in LU factorisation (frequency " + std::to_string(fz[i]) + " Hz)"};
   // solutions (vertex order) as [B][nc][ldb]
@@ -1207,7 +1207,6 @@ int bem_lu_factor_dense(bem_context* ctx, int n, double* a, int* ipiv, int preci
         a[2 * ((size_t)j * n + i)] = re;
         a[2 * ((size_t)j * n + i) + 1] = im;
       }
-    if (info < 0) return fail(ctx, BEM_ERR_CUDA, "LU panel exchange gave up waiting");
     if (info != 0) return fail(ctx, BEM_ERR_SINGULAR, "zero pivot at column " + std::to_string(info - 1));
     return BEM_OK;
   });

@@ -103,8 +103,11 @@ cudaError_t launch_regular_f64(const DeviceMesh& m, double k, double2 cD, double
 constexpr int kPairRec = 64;
 constexpr int kPairGeoDf = 48;
 cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, float* pairrec, cudaStream_t stream);
-cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, double k, const OperatorCoeffs& c, void* blocks,
-                                cudaStream_t stream);
+// Singular blocks of nfreq frequencies; frequency f's blocks start at element
+// f * blocks_stride of blocks (the mixed form takes two frequencies per launch).
+cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, int nfreq, const double* k,
+                                const OperatorCoeffs* c, void* blocks, long long blocks_stride, cudaStream_t stream);
+int singular_launches(Precision prec, int nfreq);
 cudaError_t launch_singular_scatter(const DeviceMesh& m, Precision prec, const void* blocks, void* Rext,
                                     long long ldR, cudaStream_t stream);
 cudaError_t launch_gather(const DeviceMesh& m, Precision prec, const void* Rext, long long ldR, void* A, long long lda,
