@@ -270,8 +270,9 @@ def run_plan(args) -> None:
     lo, hi, n = spec["f"]
     freqs = np.logspace(np.log10(lo), np.log10(hi), n)
     B = min(args.batch or 15, len(freqs))
+    lanes = args.lanes if 2 * B <= len(freqs) else 1
     sharding = pkg("sharding")
-    mine = [[int(i) for i in np.arange(len(freqs))[sharding.step_batch(s, rank, world, B, len(freqs))]]
+    mine = [[int(i) for i in np.arange(len(freqs))[sharding.step_batch(s, rank, world, lanes * B, len(freqs))]]
             for s in range(args.warmup + args.steps)]
     gathered = [mine]
     if world > 1:
@@ -282,7 +283,7 @@ def run_plan(args) -> None:
         dist.all_gather_object(gathered, mine)
         dist.destroy_process_group()
     if rank == 0:
-        print(json.dumps({"plan": True, "n_gpus": world, "batch": B, "n_freq": len(freqs),
+        print(json.dumps({"plan": True, "n_gpus": world, "batch": B, "lanes": lanes, "n_freq": len(freqs),
                           "rank_batches": gathered}))
 
 
@@ -312,6 +313,8 @@ def main() -> None:
     ap.add_argument("--autotune", type=int, default=1, choices=[0, 1],
                     help="time the candidate launch configurations on the workload's sweep before the run "
                          "(autotune.tune) and use the winner's LU panel width and trailing update")
+    ap.add_argument("--lanes", type=int, default=2, choices=[1, 2],
+                    help="batches per step solved side by side on two streams (bem_solve_options.lanes)")
     ap.add_argument("--lu-gemm", type=int, default=0, choices=[0, 1, 2],
                     help="LU trailing update: 0 automatic, 1 cuBLAS cgemm, 2 tcgen05 3xTF32")
     ap.add_argument("--plan", action="store_true",
@@ -363,18 +366,20 @@ def main() -> None:
         except Exception as exc:  # noqa: BLE001 - the run goes on with the library's own choice
             tune_info = {"error": f"{type(exc).__name__}: {exc}"}
     B = min(args.batch if args.batch > 0 else m.auto_batch(0, form), len(freqs))
+    lanes = args.lanes if 2 * B <= len(freqs) else 1
+    SB = lanes * B  # frequencies per step: one batch per lane
     stream = torch.cuda.ExternalStream(ctx.stream_handle, device=f"cuda:{local_rank}")
-    p_dev = torch.empty((B, 1, mesh.n_vertices), dtype=torch.complex128, device="cuda")
-    u_dev = torch.empty((B, 1, len(points)), dtype=torch.complex128, device="cuda")
+    p_dev = torch.empty((SB, 1, mesh.n_vertices), dtype=torch.complex128, device="cuda")
+    u_dev = torch.empty((SB, 1, len(points)), dtype=torch.complex128, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    opts = dict(precision=form, sound_speed=SOUND_SPEED, rho=RHO, batch=B, refine_tol=1e-10,
+    opts = dict(precision=form, sound_speed=SOUND_SPEED, rho=RHO, batch=B, lanes=lanes, refine_tol=1e-10,
                 max_refine=8, lu_gemm=args.lu_gemm, lu_block=args.lu_block)
 
     sharding = pkg("sharding")
 
     def step_freqs(step: int):
         # weak scaling: rank r takes batch (step * world + r) of the sweep
-        return freqs[sharding.step_batch(step, rank, world, B, len(freqs))]
+        return freqs[sharding.step_batch(step, rank, world, SB, len(freqs))]
 
     for s in range(args.warmup):
         m.solve_device(step_freqs(s), p_dev.data_ptr(), u_dev.data_ptr(), **opts)
@@ -409,11 +414,12 @@ def main() -> None:
         t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
-    solved = args.steps * B * world
+    solved = args.steps * SB * world
     value = solved / elapsed
     step_ms = [a.elapsed_time(b) for a, b in step_events]
     kernel_s = {k: sum(st["kernel_s"][k] for st in stats_list) for k in stats_list[0]["kernel_s"]}
-    per_freq_ms = {k: 1e3 * v / (args.steps * B) for k, v in kernel_s.items()}
+    # per-lane stage intervals summed over both lanes (overlapping lanes inflate each stage)
+    per_freq_ms = {k: 1e3 * v / (args.steps * SB) for k, v in kernel_s.items()}
 
     result = {
         "metric": METRIC,
@@ -429,9 +435,10 @@ def main() -> None:
         "dtype": "f64" if fp64_workload else "f32 (compensated) + f64 refinement",
         "data": "synthetic",
         "config": workload_config(args, mesh, points, spec, world),
-        "step": f"one batch of {B} frequencies of the sweep per rank",
+        "step": (f"{lanes} batches of {B} frequencies of the sweep per rank, side by side on two streams"
+                 if lanes > 1 else f"one batch of {B} frequencies of the sweep per rank"),
         "clocks": clocks.summary(),
-        "launch": {"batch": B, "lu_block": args.lu_block, "lu_gemm": args.lu_gemm},
+        "launch": {"batch": B, "lanes": lanes, "lu_block": args.lu_block, "lu_gemm": args.lu_gemm},
         "autotune": tune_info,
         "stage_ms_per_freq": per_freq_ms,
         "step_ms": step_ms,
@@ -451,8 +458,8 @@ def main() -> None:
     # 35.67 + 26.83 / w, w = frequencies sharing one launch's geometry (4 at this size:
     # 42.4 flop; 49.1 with pairs of frequencies)
     reg_flop = sum(st["regular_flop"] for st in stats_list)
-    flops_per_qpair = reg_flop / (regular_qpairs * args.steps * B) if regular_qpairs else 0.0
-    reg_s = kernel_s["regular"] / (args.steps * B)  # seconds per frequency
+    flops_per_qpair = reg_flop / (regular_qpairs * args.steps * SB) if regular_qpairs else 0.0
+    reg_s = kernel_s["regular"] / (args.steps * SB)  # seconds per frequency
     achieved = reg_flop / kernel_s["regular"] / 1e12 if kernel_s["regular"] > 0 else None
     clock = result["clocks"]["sm_mhz"] or 1920.0
     n_sm = torch.cuda.get_device_properties(local_rank).multi_processor_count
@@ -500,8 +507,8 @@ def main() -> None:
     if not args.no_extras and rank == 0:
         # end to end through the C ABI with host buffers: upload mesh + caches, solve a batch, copy results back
         e2e_times = []
-        h2d = mesh.vertices.nbytes + mesh.faces.astype(np.int32).nbytes + drive.nbytes + points.nbytes + B * 8
-        d2h = B * (mesh.n_vertices + len(points)) * 16
+        h2d = mesh.vertices.nbytes + mesh.faces.astype(np.int32).nbytes + drive.nbytes + points.nbytes + SB * 8
+        d2h = SB * (mesh.n_vertices + len(points)) * 16
         for s in range(args.e2e_steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -511,10 +518,11 @@ def main() -> None:
             m2.solve(step_freqs(s), **opts)
             m2.release()
             e2e_times.append(time.perf_counter() - t0)
-        result["e2e"] = {"value": B / statistics.median(e2e_times), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+        result["e2e"] = {"value": SB / statistics.median(e2e_times), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                          "d2h_bytes_per_step": int(d2h),
                          "what": "per step: bem_upload_mesh (plan + singular moments) + excitation + points from "
-                                 "host arrays, bem_solve_frequencies of one batch with host output buffers"}
+                                 "host arrays, bem_solve_frequencies of the step's frequencies (one batch per lane) "
+                                 "with host output buffers"}
         # CPU baseline: the reference algorithm (FP32 restatement) on the host cores, bounded sample
         if args.cpu_baseline > 0:
             threads = os.cpu_count() or 1

@@ -10,6 +10,7 @@
 #include <functional>
 #include <string>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "../../include/gb300_bem.h"
@@ -96,6 +97,9 @@ struct bem_context {
   void* stage = nullptr;  // pinned host staging of mesh uploads (grown on demand)
   size_t stage_bytes = 0;
   std::vector<bem_mesh*> meshes;
+  // the second lane of a two-lane sweep (options.lanes = 2): a context of its own on the same
+  // device whose stream and scratch solve every other batch; created on first use
+  bem_context* lane2 = nullptr;
   // optional per-kernel-family timing (options.profile)
   bool prof = false;
   std::vector<cudaEvent_t> pev;
@@ -255,11 +259,10 @@ int assembly_group(bem::Precision prec) { return prec == bem::Precision::Mixed ?
 // given; column-major, leading dimension lda) and, if nc > 0, the RHS into b[i]
 // (nc columns, leading dimension ldb, permuted rows).  lda / ldb <= 0: the mesh's
 // own layout.  Returns the number of kernels launched.
-long long assemble_frequencies(bem_mesh* m, bem::Precision prec, int cnt, const double* k,
+long long assemble_frequencies(bem_context* ctx, bem_mesh* m, bem::Precision prec, int cnt, const double* k,
                                const bem::OperatorCoeffs* c, void* const* A, void* const* A2, const double2* qscale,
                                int nc, const void* drive, void* const* b, long long lda = 0, long long ldb = 0,
                                double* regular_flop = nullptr) {
-  bem_context* ctx = m->ctx;
   const bem::DeviceMesh& dm = m->dm;
   Layout L = layout_for(dm, prec);
   if (lda > 0) L.lda = lda;
@@ -325,7 +328,7 @@ long long assemble_frequencies(bem_mesh* m, bem::Precision prec, int cnt, const 
 
 void assemble_one(bem_mesh* m, bem::Precision prec, double k, const bem::OperatorCoeffs& c, void* A, void* A2,
                   double2 qscale, int nc, const void* drive, void* b) {
-  assemble_frequencies(m, prec, 1, &k, &c, &A, A2 ? &A2 : nullptr, &qscale, nc, drive, &b);
+  assemble_frequencies(m->ctx, m, prec, 1, &k, &c, &A, A2 ? &A2 : nullptr, &qscale, nc, drive, &b);
 }
 
 void free_mesh_device(bem_mesh* m) {
@@ -395,6 +398,10 @@ int bem_create_context(int device, bem_context** out) {
 
 void bem_destroy_context(bem_context* ctx) {
   if (!ctx) return;
+  if (ctx->lane2) {
+    bem_destroy_context(ctx->lane2);
+    ctx->lane2 = nullptr;
+  }
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   for (bem_mesh* m : ctx->meshes) {
@@ -421,6 +428,10 @@ int bem_trim_context(bem_context* ctx) {
   if (!ctx) return BEM_ERR_INVALID_ARGUMENT;
   return guarded(ctx, [&]() -> int {
     for (DevBuf* b : ctx->scratch()) b->release();
+    if (ctx->lane2) {
+      for (DevBuf* b : ctx->lane2->scratch()) b->release();
+      ck(cudaStreamSynchronize(ctx->lane2->stream), "trim scratch");
+    }
     ck(cudaStreamSynchronize(ctx->stream), "trim scratch");
     ck(cudaMemPoolTrimTo(ctx->pool, 0), "trim memory pool");
     return BEM_OK;
@@ -431,6 +442,7 @@ long long bem_context_scratch_bytes(const bem_context* ctx) {
   if (!ctx) return -1;
   long long total = 0;
   for (DevBuf* b : const_cast<bem_context*>(ctx)->scratch()) total += (long long)b->bytes;
+  if (ctx->lane2) total += bem_context_scratch_bytes(ctx->lane2);
   return total;
 }
 
@@ -704,6 +716,7 @@ void bem_default_options(bem_solve_options* opt) {
   opt->outputs_on_device = 0;
   opt->profile = 0;
   opt->lu_gemm = 0;
+  opt->lanes = 1;
 }
 
 }  // extern "C"
@@ -829,7 +842,7 @@ void solve_combined(bem_context* ctx, const std::vector<Slice>& sl, int n, const
     if (nvm < n)
       ck(cudaMemsetAsync(bs[i0], 0, (size_t)x.cnt * nc * ldb * esz, ctx->stream), "memset padded rhs");
     const void* drive = mixed ? x.m->drive32.p : x.m->drive64.p;
-    T.launches += assemble_frequencies(x.m, prec, x.cnt, ks.data() + i0, cs.data() + i0, As.data() + i0,
+    T.launches += assemble_frequencies(ctx, x.m, prec, x.cnt, ks.data() + i0, cs.data() + i0, As.data() + i0,
                                        mixed ? A2s.data() + i0 : nullptr, qs.data() + i0, nc, drive, bs.data() + i0,
                                        lda, ldb, &T.regular_flop);
     if (nvm < n) {
@@ -1059,12 +1072,59 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
     int B = o.batch > 0 ? std::min(o.batch, 64) : auto_batch(m, prec, n_freq);
     B = std::min(B, n_freq);
     ctx->prof = o.profile != 0;
+    const int nbatch = (n_freq + B - 1) / B;
+    auto slice_of = [&](int bi) {
+      const int f0 = bi * B, bt = std::min(B, n_freq - f0);
+      return Slice{m, freqs_hz + f0, bt, pressure_out ? pressure_out + 2 * (size_t)f0 * nc * nv : nullptr,
+                   field_out ? field_out + 2 * (size_t)f0 * nc * m->nobs : nullptr};
+    };
     SolveTotals T;
-    for (int f0 = 0; f0 < n_freq; f0 += B) {
-      const int bt = std::min(B, n_freq - f0);
-      Slice x{m, freqs_hz + f0, bt, pressure_out ? pressure_out + 2 * (size_t)f0 * nc * nv : nullptr,
-              field_out ? field_out + 2 * (size_t)f0 * nc * m->nobs : nullptr};
-      solve_combined(ctx, {x}, nv, o, nc, T);
+    if (o.lanes >= 2 && nbatch >= 2) {
+      // two lanes: even batches on this context, odd ones on the helper context, each
+      // lane's batches in order from its own host thread; the mesh is shared read-only
+      if (!ctx->lane2) {
+        bem_context* c2 = nullptr;
+        const int rc = bem_create_context(ctx->device, &c2);
+        if (rc != BEM_OK) return fail(ctx, rc, "cannot create the second lane's context");
+        ctx->lane2 = c2;
+      }
+      bem_context* c2 = ctx->lane2;
+      c2->prof = ctx->prof;
+      SolveTotals T2;
+      bool failed2 = false;
+      BemError err2{BEM_OK, std::string()};
+      std::thread lane([&] {
+        cudaSetDevice(ctx->device);
+        try {
+          for (int bi = 1; bi < nbatch; bi += 2) solve_combined(c2, {slice_of(bi)}, nv, o, nc, T2);
+        } catch (const BemError& e) {
+          err2 = e;
+          failed2 = true;
+        } catch (const std::exception& e) {
+          err2 = BemError{BEM_ERR_CUDA, std::string("second lane: ") + e.what()};
+          failed2 = true;
+        }
+      });
+      try {
+        for (int bi = 0; bi < nbatch; bi += 2) solve_combined(ctx, {slice_of(bi)}, nv, o, nc, T);
+      } catch (...) {
+        lane.join();
+        throw;
+      }
+      lane.join();
+      if (failed2) throw err2;
+      for (int i = 0; i < BEM_K_SLOTS; ++i) T.kacc[i] += T2.kacc[i];
+      T.regular_flop += T2.regular_flop;
+      T.t_asm += T2.t_asm;
+      T.t_sol += T2.t_sol;
+      T.t_fld += T2.t_fld;
+      T.max_res = std::max(T.max_res, T2.max_res);
+      T.max_steps = std::max(T.max_steps, T2.max_steps);
+      T.batches += T2.batches;
+      T.gemm_used = std::max(T.gemm_used, T2.gemm_used);
+      T.launches += T2.launches;
+    } else {
+      for (int bi = 0; bi < nbatch; ++bi) solve_combined(ctx, {slice_of(bi)}, nv, o, nc, T);
     }
     fill_stats(stats, T);
     if (stats) {

@@ -63,7 +63,7 @@ class CudaEngine:
     name = "gb300_cuda"
 
     def __init__(self, device: int = 0, precision: str = "mixed", batch: int = 0, refine_tol: float = 1e-10,
-                 context: str = "shared", autotune: bool = False):
+                 context: str = "shared", autotune: bool = False, lanes: int = 2):
         if precision not in PRECISIONS:
             raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
         if context not in ("shared", "thread"):
@@ -78,6 +78,9 @@ class CudaEngine:
         # autotune: the first solve on a mesh times the candidate launch configurations
         # (autotune.tune, cached per device and problem shape) and later solves use the winner
         self.autotune = autotune
+        # lanes = 2: a call of two or more batches runs them side by side on two streams
+        # (bem_solve_options.lanes), so the job loop asks for two batches per call
+        self.lanes = max(1, min(2, int(lanes)))
         self.launch = None  # autotune.LaunchConfig once tuned
         self.tune_result = None
 
@@ -102,21 +105,26 @@ class CudaEngine:
             if self.autotune and not self.batch:
                 # the tuner tries up to one frequency more than the library's own batch
                 batch = self.launch.batch if self.launch is not None else min(batch + 1, max(1, n_freq))
+            lanes = self.lanes if n_freq >= 2 * batch else 1  # each lane holds a batch's scratch
             return self.ctx.estimate_device_bytes(self.mesh.n_vertices, self.mesh.n_faces,
-                                                  self.mesh.n_singular_pairs, self.n_rhs, self.n_points, batch, prec)
+                                                  self.mesh.n_singular_pairs, self.n_rhs, self.n_points,
+                                                  batch * lanes, prec)
 
     def preferred_chunk(self, n_freq: int) -> int:
         """Frequencies per solve call for a sweep of n_freq: one batch of the size the solve
         uses (bem_auto_batch splits a sweep into equal batches whose LU panels are resident
-        in one wave), so no call leaves a partial batch behind."""
+        in one wave) per lane, so no call leaves a partial batch behind and, with two lanes,
+        each call keeps both streams busy."""
         if self.mesh is None:
             raise RuntimeError("engine.prepare() must run before preferred_chunk()")
         if self.batch:
-            return max(1, int(self.batch))
-        if self.autotune and self.launch is not None:
-            return max(1, int(self.launch.batch))
-        with self.lock:
-            return max(1, int(self.mesh.auto_batch(max(1, int(n_freq)), PRECISIONS[self.precision])))
+            b = max(1, int(self.batch))
+        elif self.autotune and self.launch is not None:
+            b = max(1, int(self.launch.batch))
+        else:
+            with self.lock:
+                b = max(1, int(self.mesh.auto_batch(max(1, int(n_freq)), PRECISIONS[self.precision])))
+        return b * self.lanes if n_freq >= b * self.lanes else b
 
     def tune_sweep(self, freqs_hz, sound_speed: float, rho: float) -> None:
         """With autotune on, time the candidate launch configurations on the whole sweep
@@ -147,7 +155,7 @@ class CudaEngine:
                     self._tune(freqs_hz, sound_speed, rho)
                 kw = dict(batch=self.launch.batch, lu_block=self.launch.lu_block, lu_gemm=self.launch.lu_gemm)
             p, u, stats = self.mesh.solve(freqs_hz, precision=PRECISIONS[self.precision], sound_speed=sound_speed,
-                                          rho=rho, refine_tol=self.refine_tol, **kw)
+                                          rho=rho, refine_tol=self.refine_tol, lanes=self.lanes, **kw)
         return EngineResult(p, u, stats)
 
     def close(self) -> None:

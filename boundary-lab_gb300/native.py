@@ -103,6 +103,7 @@ class SolveOptions(ctypes.Structure):
         ("outputs_on_device", ctypes.c_int),
         ("profile", ctypes.c_int),
         ("lu_gemm", ctypes.c_int),
+        ("lanes", ctypes.c_int),
     ]
 
 
@@ -382,8 +383,10 @@ class Mesh:
 
     def solve(self, freqs_hz, *, precision: int = BEM_PRECISION_MIXED, sound_speed: float = 343.0,
               rho: float = 1.21, refine_tol: float = 1e-10, max_refine: int = 8, batch: int = 0, lu_block: int = 0,
-              want_pressure: bool = True, want_field: bool = True, profile: bool = False, lu_gemm: int = 0):
-        """Returns (pressure [n_freq, n_rhs, n_vertices], field [n_freq, n_rhs, n_points], stats dict)."""
+              want_pressure: bool = True, want_field: bool = True, profile: bool = False, lu_gemm: int = 0,
+              lanes: int = 1):
+        """Returns (pressure [n_freq, n_rhs, n_vertices], field [n_freq, n_rhs, n_points], stats dict).
+        lanes = 2 runs a sweep of two or more batches on two streams (bem_solve_options.lanes)."""
         f = np.ascontiguousarray(freqs_hz, dtype=np.float64).reshape(-1)
         opt = SolveOptions()
         self.ctx._lib.bem_default_options(ctypes.byref(opt))
@@ -396,6 +399,7 @@ class Mesh:
         opt.lu_block = int(lu_block)
         opt.profile = int(bool(profile))
         opt.lu_gemm = int(lu_gemm)
+        opt.lanes = int(lanes)
         pressure = np.zeros((len(f), self.n_rhs, self.n_vertices), np.complex128) if want_pressure else None
         field = np.zeros((len(f), self.n_rhs, self.n_points), np.complex128) if want_field else None
         stats = SolveStats()

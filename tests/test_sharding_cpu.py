@@ -92,7 +92,8 @@ def test_bench_gpus_flag_starts_one_rank_per_gpu():
     root = Path(__file__).resolve().parents[1]
     env = {k: v for k, v in __import__("os").environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
     out = subprocess.run([sys.executable, str(root / "bench.py"), "--gpus", "2", "--plan", "--batch", "8",
-                          "--steps", "3", "--warmup", "3"], capture_output=True, text=True, timeout=240, env=env)
+                          "--lanes", "1", "--steps", "3", "--warmup", "3"], capture_output=True, text=True, timeout=240,
+                         env=env)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1
