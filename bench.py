@@ -418,8 +418,14 @@ def main() -> None:
     value = solved / elapsed
     step_ms = [a.elapsed_time(b) for a, b in step_events]
     kernel_s = {k: sum(st["kernel_s"][k] for st in stats_list) for k in stats_list[0]["kernel_s"]}
-    # per-lane stage intervals summed over both lanes (overlapping lanes inflate each stage)
-    per_freq_ms = {k: 1e3 * v / (args.steps * SB) for k, v in kernel_s.items()}
+    # per-lane stage intervals of the timed region, summed over the lanes: with two lanes
+    # the stages of one overlap the other's, so each interval includes the other lane's work
+    lane_sum_ms = {k: 1e3 * v / (args.steps * SB) for k, v in kernel_s.items()}
+    # stage breakdown of one batch on one lane, after the timed region (nothing overlaps it)
+    st1 = m.solve_device(step_freqs(0)[:B], p_dev.data_ptr(), u_dev.data_ptr(), profile=1, **{**opts, "lanes": 1})
+    torch.cuda.synchronize()
+    nb1 = len(step_freqs(0)[:B])
+    per_freq_ms = {k: 1e3 * v / nb1 for k, v in st1["kernel_s"].items()}
 
     result = {
         "metric": METRIC,
@@ -440,7 +446,8 @@ def main() -> None:
         "clocks": clocks.summary(),
         "launch": {"batch": B, "lanes": lanes, "lu_block": args.lu_block, "lu_gemm": args.lu_gemm},
         "autotune": tune_info,
-        "stage_ms_per_freq": per_freq_ms,
+        "stage_ms_per_freq": per_freq_ms,  # one batch on one lane, after the timed region
+        "stage_ms_per_freq_lane_sums": lane_sum_ms if lanes > 1 else None,
         "step_ms": step_ms,
         # timed region minus the steps: the L2 flushes and host time between steps
         "between_steps_ms": 1e3 * elapsed - sum(step_ms),
@@ -479,6 +486,14 @@ def main() -> None:
                        "(MEASURED_PEAKS.json has no FP32 figure)",
         "work_per_frequency": f"{regular_qpairs:.4g} q-pairs x {flops_per_qpair:.2f} flop",
         "ms_per_frequency": 1e3 * reg_s,
+        "timing": ("CUDA events around each regular launch on its lane's stream over the timed region; with "
+                   "two lanes the launches share the GPU with the other lane's kernels" if lanes > 1 else
+                   "CUDA events around each regular launch over the timed region"),
+        # the same kernel on one lane with nothing beside it (one batch after the timed region)
+        "one_lane": ({"achieved": st1["regular_flop"] / st1["kernel_s"]["regular"] / 1e12,
+                      "frac": st1["regular_flop"] / st1["kernel_s"]["regular"] / 1e12 / fp32_peak,
+                      "ms_per_frequency": 1e3 * st1["kernel_s"]["regular"] / nb1}
+                     if st1["kernel_s"]["regular"] > 0 else None),
         # the same time against the reference's own arithmetic per q-pair (about 160 flop:
         # S, D, K' and H integrands formed separately, BeatEngineCpuAssembly.jl:316-346),
         # context only: this kernel folds them and shares the geometry across frequencies
