@@ -121,11 +121,11 @@ typedef struct bem_solve_options {
   int lu_gemm;           /* LU trailing update of the mixed form: 0 automatic (tensor cores when
                             available), 1 cuBLAS cgemm (FP32), 2 tcgen05 3xTF32 tensor cores */
   int lanes;             /* 1 (default): batches one after another on the context's stream;
-                            2: a sweep of two or more batches alternates them between the context
-                            and a helper context of its own (own stream and scratch, created on first
+                            2: a sweep of several batches deals them round-robin to the context and a
+                            helper context of its own (own stream and scratch, created on first
                             use, freed with the context), so one batch's latency-bound LU panels overlap
-                            the other's assembly and tensor-core updates.  Per-kernel times in stats
-                            are then summed over both lanes. */
+                            the other's assembly and tensor-core updates; larger values act as 2.
+                            Per-kernel times in stats are then summed over the lanes. */
 } bem_solve_options;
 
 /* stats.kernel_s slots (filled when options.profile == 1), seconds summed over the call */
