@@ -316,7 +316,7 @@ def main() -> None:
     ap.add_argument("--lanes", type=int, default=2, choices=[1, 2],
                     help="batches per step solved side by side on two streams (bem_solve_options.lanes)")
     ap.add_argument("--lu-gemm", type=int, default=0, choices=[0, 1, 2],
-                    help="LU trailing update: 0 automatic, 1 cuBLAS cgemm, 2 tcgen05 3xTF32")
+                    help="LU trailing update: 0 automatic, 1 cuBLAS cgemm, 2 tcgen05 3xFP16")
     ap.add_argument("--plan", action="store_true",
                     help="print the frequency batches each rank would solve (no GPU work)")
     args = ap.parse_args()
@@ -453,7 +453,7 @@ def main() -> None:
         "between_steps_ms": 1e3 * elapsed - sum(step_ms),
         "host_ms": [[round(a, 3), round(b, 3)] for a, b in host_ms],  # (flush + event, solve call) per step
         "refine_steps_max": max(st["max_refine_steps"] for st in stats_list),
-        "lu_trailing_update": {1: "cublas cgemm", 2: "tcgen05 3xTF32"}.get(stats_list[0]["lu_gemm_used"]),
+        "lu_trailing_update": {1: "cublas cgemm", 2: "tcgen05 3xFP16"}.get(stats_list[0]["lu_gemm_used"]),
         "rel_residual_max": max(st["max_rel_residual"] for st in stats_list),
     }
 

@@ -6,7 +6,7 @@ The library picks its runtime launch configuration from a model of the device:
   are resident on the GPU at once (15 at 10k triangles on a GB300);
 * the LU's panel width and cluster size: the pair that runs every panel of
   the batch in the fewest waves (``lu_block`` 0);
-* the trailing update of the mixed form: tcgen05 3xTF32 when the device has it
+* the trailing update of the mixed form: tcgen05 3xFP16 when the device has it
   (``lu_gemm`` 0).
 
 ``tune`` checks that model by timing.  It solves a few frequencies of the
@@ -17,7 +17,7 @@ from the model's choice (a coordinate search):
 
 1. batch: the model's B, B - 1, B + 1 and B / 2 (within 1 .. min(64, n_freq));
 2. LU panel width: automatic, 32 and 64, at the best batch;
-3. LU trailing update, mixed form only: tcgen05 3xTF32 or cuBLAS cgemm.
+3. LU trailing update, mixed form only: tcgen05 3xFP16 or cuBLAS cgemm.
 
 A candidate that the library refuses (``BemError``) is skipped and recorded.
 A candidate whose pressure differs from the model choice's by more than the
@@ -49,7 +49,7 @@ CACHE_ENV = "GB300_BEM_AUTOTUNE_CACHE"  # optional JSON file that keeps winners 
 class LaunchConfig:
     batch: int  # frequencies factored together (bem_solve_options.batch)
     lu_block: int = 0  # 0 automatic, 32 or 64
-    lu_gemm: int = 0  # 0 automatic, 1 cuBLAS cgemm, 2 tcgen05 3xTF32
+    lu_gemm: int = 0  # 0 automatic, 1 cuBLAS cgemm, 2 tcgen05 3xFP16
 
 
 @dataclass

@@ -1051,7 +1051,7 @@ long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int np
   bytes += (long long)batch * nrhs * ((long long)nf * 6 * esz + (long long)npts * 16);  // field sources + out
   bytes += (long long)nf * (2 * 160 + 288 + 64);                            // face records (+ lane-group copy), maps
   if (precision == BEM_PRECISION_MIXED)                                      // tensor-core update operands
-    bytes += (long long)batch * (2 * round_up(2LL * nv, 128) + 2 * round_up(nv, 256)) * 256 * 4;
+    bytes += (long long)bem::tc_gemm_workspace_bytes(nv, batch);
   bytes += 64LL << 20;                                                      // cuBLAS workspace and slack
   return bytes;
 }

@@ -7,20 +7,30 @@
 // where B' is U12's memory read as reals and A' replaces every complex L21
 // entry a by the 2 x 2 real block [[re a, -im a], [im a, re a]].
 //
-// Precision: 3xTF32.  Every operand value x is split as x = hi + lo with hi
-// rounded to TF32 (low 13 mantissa bits zero) and lo = x - hi exact in FP32;
-// the MMA sums hi*hi + hi*lo + lo*hi with FP32 accumulation, which carries
-// about 2^-21 relative error per product (FP32 LU quality), so the FP64
-// refinement still converges in one or two steps.
+// Precision: 3xFP16 with power-of-two scaling (the split-precision tensor-core
+// product of Markidis et al., "NVIDIA Tensor Core Programmability, Performance
+// & Precision", 2018).  Every operand value x is scaled by a power of two s and
+// split as x s = hi + lo, hi = fp16(x s) and lo = fp16(x s - hi); the MMA sums
+// hi*hi + hi*lo + lo*hi with FP32 accumulation and the epilogue multiplies by
+// 1 / (s_A s_B), exactly.  hi and lo carry 11 significant bits each, like a
+// TF32 split, so a product keeps about 2^-22 relative error, while the f16 MMA
+// runs at twice the TF32 rate on half the operand bytes.  The scales keep the
+// values inside FP16's range: L21 holds the multipliers of partial pivoting,
+// |re|, |im| <= 1, scaled by s_A = 2^14; each column j of U12 is scaled by
+// s_j = 2^(14 - e_j), e_j the binary exponent of its largest |re| or |im|, so
+// its entries lie below 2^14 and an entry loses its lo part to the FP16
+// subnormal range only when it is 2^17 below its column's largest (a 2^-28
+// normwise error).
 //
 // Kernel: persistent, one CTA per SM, tiles of 128 x 256 of C'.  A prep kernel
-// writes A'hi, A'lo, B'hi, B'lo as K-major (K contiguous) buffers; a producer
-// warp brings 16-wide K blocks by TMA into 64-byte-swizzled shared memory
-// through a 4-stage mbarrier pipeline; one thread issues tcgen05.mma
-// (kind::tf32, M=128, N=256, K=8) into one of two TMEM accumulators; four
-// epilogue warps read the other accumulator back with tcgen05.ld, stage -D in
-// shared memory 32 columns at a time (double buffered per warp) and TMA
-// reduce-add it into C (cp.reduce.async.bulk.tensor .add.f32), so C is never
+// writes A'hi, A'lo, B'hi, B'lo as K-major (K contiguous) FP16 buffers and the
+// column scales; a producer warp brings 32-wide K blocks by TMA into
+// 64-byte-swizzled shared memory through a 4-stage mbarrier pipeline; one
+// thread issues tcgen05.mma (kind::f16, M=128, N=256, K=16) into one of two
+// TMEM accumulators; four epilogue warps read the other accumulator back with
+// tcgen05.ld, stage -D / (s_A s_j) in shared memory 32 columns at a time
+// (double buffered per warp) and TMA reduce-add it into C
+// (cp.reduce.async.bulk.tensor .add.f32), so C is never
 // read by the SM: the read-modify-write happens in L2, asynchronously, while
 // the next tile's MMAs run.  Every wait is bounded: on timeout the kernel
 // records an error, waits (bounded) for its own copies and MMAs, frees its
@@ -39,6 +49,7 @@
 // rows x >= 2n and columns y >= n are clipped by the map bounds, and rows or
 // columns of a tile beyond M or N receive -0 from zero-padded operands.
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -52,11 +63,13 @@ namespace {
 
 constexpr int TM = 128;       // tile rows of C' (real rows)
 constexpr int TN = 256;       // tile columns of C'
-constexpr int TK = 16;        // K block per stage (16 fp32 = 64 B rows, 64-byte swizzle)
+constexpr int TK = 32;        // K block per stage (32 fp16 = 64 B rows, 64-byte swizzle)
 constexpr int KP_MAX = 256;   // K' = 2 K <= 256 (K <= 128 complex), row stride of the split operands
-constexpr int A_BYTES = TM * TK * 4;   // 8 KB
-constexpr int B_BYTES = TN * TK * 4;   // 16 KB
+constexpr int A_BYTES = TM * TK * 2;   // 8 KB
+constexpr int B_BYTES = TN * TK * 2;   // 16 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi + lo of A and B: 48 KB
+constexpr float kAScale = 16384.0f;      // s_A = 2^14 (multipliers have |re|, |im| <= 1)
+constexpr int kBTarget = 14;             // column j of U12 scaled so its largest |re|, |im| is below 2^14
 // mbarrier waits give up after kWaitLimit polls with a 1 us suspend hint each
 // (about one second), far above any healthy wait (microseconds).
 constexpr long long kWaitLimit = 1LL << 20;
@@ -106,12 +119,14 @@ __device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t addr) {
   return d;
 }
 
-// Instruction descriptor: kind::tf32, D = F32, A = B = TF32, both K-major, M = 128, N = 256.
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+// Instruction descriptor: kind::f16, D = F32, A = B = F16 (format 0 for both:
+// the two operands of one MMA always have the same type), both K-major,
+// M = 128, N = 256.
+constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
 
-__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+__device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
   asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
           dtmem),
       "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
 }
@@ -149,60 +164,88 @@ __device__ __forceinline__ void bulk_wait_read() {
 }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-__device__ __forceinline__ float round_tf32(float x) {
-  uint32_t u = __float_as_uint(x);
-  if ((u & 0x7F800000u) != 0x7F800000u) u = (u + 0x1000u) & 0xFFFFE000u;
-  return __uint_as_float(u);
+// x (already scaled) as hi + lo in FP16, both rounded to nearest.
+__device__ __forceinline__ void split_f16(float x, __half& hi, __half& lo) {
+  hi = __float2half_rn(x);
+  lo = __float2half_rn(x - __half2float(hi));
 }
 
 // Both operand splits of one update in one launch.  Blocks [0, nta) split A:
-// each takes 32 rows x 8 columns of L21 (complex), loaded along the rows
-// (coalesced, through shared memory) and written as the 64 x 16 real-embedded
-// hi / lo tile with the K index fastest (float4 stores).  The remaining blocks
-// split B, 128 complex entries each (K fastest on both sides).  Entries beyond
-// M rows / N columns / K depth are written as zero.
+// each takes 32 rows x 16 columns of L21 (complex), loaded along the rows
+// (coalesced, through shared memory), scales them by s_A and writes the
+// 64 x 32 real-embedded hi / lo tile with the K index fastest (16-byte
+// stores).  The remaining blocks split B, one warp per column of U12: the
+// warp finds the column's largest |re| or |im|, writes the column scaled by
+// s_j = 2^(14 - e) as hi / lo (K fastest on both sides) and 1 / (s_A s_j) to
+// inv_scale.  Entries beyond M rows / N columns / K depth are written as zero.
 __global__ void __launch_bounds__(256) prep_ab_kernel(const float2* __restrict__ A, long long lda, long long strideA,
                                                       int row0, int col0, int kcol0, int M, int N, int K, int rows_pad,
                                                       int cols_pad, int rows_used, int cols_used, int kp, int nta,
-                                                      float* __restrict__ ahi, float* __restrict__ alo,
-                                                      float* __restrict__ bhi, float* __restrict__ blo) {
+                                                      __half* __restrict__ ahi, __half* __restrict__ alo,
+                                                      __half* __restrict__ bhi, __half* __restrict__ blo,
+                                                      float* __restrict__ inv_scale) {
   const int b = blockIdx.y;
   const float2* Ab = A + (size_t)b * strideA;
   const int t = threadIdx.x;
   if ((int)blockIdx.x < nta) {
-    __shared__ float2 tile[8][33];
-    const int tiles_k = kp / 16;
+    __shared__ float2 tile[16][33];
+    const int tiles_k = kp / 32;
     const int ti = blockIdx.x / tiles_k, tk = blockIdx.x - ti * tiles_k;
-    const int i0 = ti * 32, k0 = tk * 8;
-    {
-      const int i = t & 31, k = t >> 5;
+    const int i0 = ti * 32, k0 = tk * 16;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int i = t & 31, k = (t >> 5) + 8 * h;
       float2 a = make_float2(0.f, 0.f);
       if (i0 + i < M && k0 + k < K) a = Ab[(size_t)(kcol0 + k0 + k) * lda + row0 + i0 + i];
-      tile[k][i] = a;
+      tile[k][i] = make_float2(a.x * kAScale, a.y * kAScale);
     }
     __syncthreads();
-    const int rr = t >> 2, q = t & 3;  // embedded row 2 i + e, k pair (2q, 2q + 1)
+    const int rr = t >> 2, q = t & 3;  // embedded row 2 i + e, complex k 4q .. 4q + 3
     const int i = rr >> 1, e = rr & 1;
-    const float2 a0 = tile[2 * q][i], a1 = tile[2 * q + 1][i];
-    // row 2i: (re, -im) per k; row 2i + 1: (im, re)
-    const float4 v = e == 0 ? make_float4(a0.x, -a0.y, a1.x, -a1.y) : make_float4(a0.y, a0.x, a1.y, a1.x);
-    const float4 hi = make_float4(round_tf32(v.x), round_tf32(v.y), round_tf32(v.z), round_tf32(v.w));
-    const float4 lo = make_float4(v.x - hi.x, v.y - hi.y, v.z - hi.z, v.w - hi.w);
-    const size_t o = ((size_t)b * rows_pad + 2 * i0 + rr) * KP_MAX + 2 * k0 + 4 * q;
-    *reinterpret_cast<float4*>(ahi + o) = hi;
-    *reinterpret_cast<float4*>(alo + o) = lo;
+    __align__(16) __half hi[8], lo[8];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float2 a = tile[4 * q + c][i];
+      // row 2i: (re, -im) per k; row 2i + 1: (im, re)
+      split_f16(e == 0 ? a.x : a.y, hi[2 * c], lo[2 * c]);
+      split_f16(e == 0 ? -a.y : a.x, hi[2 * c + 1], lo[2 * c + 1]);
+    }
+    const size_t o = ((size_t)b * rows_pad + 2 * i0 + rr) * KP_MAX + 2 * k0 + 8 * q;
+    *reinterpret_cast<uint4*>(ahi + o) = *reinterpret_cast<const uint4*>(hi);
+    *reinterpret_cast<uint4*>(alo + o) = *reinterpret_cast<const uint4*>(lo);
     return;
   }
-  const long long idx = (long long)(blockIdx.x - nta) * blockDim.x + t;  // (column j, complex k)
-  const int kc = kp / 2;
-  if (idx >= (long long)cols_used * kc) return;
-  const int j = (int)(idx / kc), k = (int)(idx - (long long)j * kc);
-  float2 u = make_float2(0.f, 0.f);
-  if (j < N && k < K) u = Ab[(size_t)(col0 + j) * lda + kcol0 + k];
-  const float2 hi = make_float2(round_tf32(u.x), round_tf32(u.y));
-  const size_t o = ((size_t)b * cols_pad + j) * KP_MAX + 2 * k;
-  *reinterpret_cast<float2*>(bhi + o) = hi;
-  *reinterpret_cast<float2*>(blo + o) = make_float2(u.x - hi.x, u.y - hi.y);
+  const int lane = t & 31;
+  const int j = (int)(blockIdx.x - nta) * 8 + (t >> 5);  // column of U12 (one warp each)
+  if (j >= cols_used) return;
+  const int kc = kp / 2;  // complex K entries written per column (<= 128: four per lane)
+  float2 u[4];
+  float amax = 0.0f;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const int k = lane + 32 * c;
+    u[c] = make_float2(0.f, 0.f);
+    if (j < N && k < K) u[c] = Ab[(size_t)(col0 + j) * lda + kcol0 + k];
+    amax = fmaxf(amax, fmaxf(fabsf(u[c].x), fabsf(u[c].y)));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  int e = 0;
+  frexpf(amax, &e);  // amax = m 2^e, 0.5 <= m < 1 (e = 0 for zero)
+  const int sh = min(100, max(-114, kBTarget - e));  // s_j = 2^sh, 1 / (s_A s_j) stays a normal float
+  const float s = ldexpf(1.0f, sh);
+  if (lane == 0) inv_scale[(size_t)b * cols_pad + j] = ldexpf(1.0f, -sh - 14);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const int k = lane + 32 * c;
+    if (k >= kc) break;
+    __align__(4) __half hi[2], lo[2];
+    split_f16(u[c].x * s, hi[0], lo[0]);
+    split_f16(u[c].y * s, hi[1], lo[1]);
+    const size_t o = ((size_t)b * cols_pad + j) * KP_MAX + 2 * k;
+    *reinterpret_cast<__half2*>(bhi + o) = *reinterpret_cast<const __half2*>(hi);
+    *reinterpret_cast<__half2*>(blo + o) = *reinterpret_cast<const __half2*>(lo);
+  }
 }
 
 // One CTA per SM walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ... (rows
@@ -222,12 +265,13 @@ constexpr size_t P_EPI_BYTES = (size_t)P_EPI_WARPS * 8192;        // two 4 KB bu
 constexpr size_t P_SMEM = P_STAGE_AREA + P_EPI_BYTES + 1024;
 
 __global__ void __launch_bounds__(P_THREADS, 1)
-    trailing_update_tf32x3_persistent(const __grid_constant__ CUtensorMap map_ahi,
-                                      const __grid_constant__ CUtensorMap map_alo,
-                                      const __grid_constant__ CUtensorMap map_bhi,
-                                      const __grid_constant__ CUtensorMap map_blo,
-                                      const __grid_constant__ CUtensorMap map_c, int x0, int y0, int M2, int N, int KB,
-                                      int tiles_m, int tiles_n, int n_tiles, int* err) {
+    trailing_update_f16x3_persistent(const __grid_constant__ CUtensorMap map_ahi,
+                                     const __grid_constant__ CUtensorMap map_alo,
+                                     const __grid_constant__ CUtensorMap map_bhi,
+                                     const __grid_constant__ CUtensorMap map_blo,
+                                     const __grid_constant__ CUtensorMap map_c, const float* __restrict__ inv_scale,
+                                     int cols_pad, int x0, int y0, int M2, int N, int KB, int tiles_m, int tiles_n,
+                                     int n_tiles, int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full_bar[P_STAGES];
@@ -311,12 +355,12 @@ __global__ void __launch_bounds__(P_THREADS, 1)
         const uint32_t a_hi = smem_u32(st), a_lo = smem_u32(st + A_BYTES);
         const uint32_t b_hi = smem_u32(st + 2 * A_BYTES), b_lo = smem_u32(st + 2 * A_BYTES + B_BYTES);
 #pragma unroll
-        for (int ks = 0; ks < TK / 8; ++ks) {
+        for (int ks = 0; ks < TK / 16; ++ks) {  // K = 16 halves (32 bytes of a 64-byte row) per MMA
           const uint32_t off = ks * 32;
           const uint32_t acc = (kb > 0 || ks > 0) ? 1u : 0u;
-          mma_tf32(acc_addr, smem_desc_sw64(a_hi + off), smem_desc_sw64(b_hi + off), acc);
-          mma_tf32(acc_addr, smem_desc_sw64(a_hi + off), smem_desc_sw64(b_lo + off), 1u);
-          mma_tf32(acc_addr, smem_desc_sw64(a_lo + off), smem_desc_sw64(b_hi + off), 1u);
+          mma_f16(acc_addr, smem_desc_sw64(a_hi + off), smem_desc_sw64(b_hi + off), acc);
+          mma_f16(acc_addr, smem_desc_sw64(a_hi + off), smem_desc_sw64(b_lo + off), 1u);
+          mma_f16(acc_addr, smem_desc_sw64(a_lo + off), smem_desc_sw64(b_hi + off), 1u);
         }
         mma_commit(&empty_bar[s]);
       }
@@ -348,11 +392,12 @@ __global__ void __launch_bounds__(P_THREADS, 1)
         const int col = n0 + cc * 32;
         if (!rows_live || col >= N) continue;  // warp-uniform
         float* sb = stg + (chunk & 1) * 1024;
+        const float* isc = inv_scale + (size_t)bz * cols_pad + col;  // 1 / (s_A s_j) of these 32 columns
         // the group that last read this buffer (two chunks ago) must be done reading
         if (lane == 0) bulk_wait_read<1>();
         __syncwarp();
 #pragma unroll
-        for (int j = 0; j < 32; ++j) sb[j * 32 + lane] = -v[j];
+        for (int j = 0; j < 32; ++j) sb[j * 32 + lane] = -v[j] * __ldg(isc + j);
         fence_async_smem();
         __syncwarp();
         if (lane == 0) {
@@ -403,14 +448,15 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-bool make_map(CUtensorMap* map, float* buf, int rows_pad, int batch, int box_rows) {
+// Split operand map: x = K' (FP16, KP_MAX per row), y = row, z = matrix; box TK x box_rows.
+bool make_map(CUtensorMap* map, __half* buf, int rows_pad, int batch, int box_rows) {
   EncodeTiledFn enc = encode_fn();
   if (!enc) return false;
   cuuint64_t dims[3] = {(cuuint64_t)KP_MAX, (cuuint64_t)rows_pad, (cuuint64_t)batch};
-  cuuint64_t strides[2] = {(cuuint64_t)KP_MAX * 4, (cuuint64_t)rows_pad * KP_MAX * 4};
+  cuuint64_t strides[2] = {(cuuint64_t)KP_MAX * 2, (cuuint64_t)rows_pad * KP_MAX * 2};
   cuuint32_t box[3] = {(cuuint32_t)TK, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
-  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, buf, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, buf, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
              CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -449,9 +495,11 @@ int sm_count() {
 
 namespace bem {
 // Workspace for one batched factorisation: split operand buffers sized for the
-// first (largest) trailing update, tensor maps built once, and an error word.
+// first (largest) trailing update, the column scales of U12, tensor maps built
+// once, and an error word.
 struct TcGemmPlan {
-  float *ahi = nullptr, *alo = nullptr, *bhi = nullptr, *blo = nullptr;
+  __half *ahi = nullptr, *alo = nullptr, *bhi = nullptr, *blo = nullptr;
+  float* inv_scale = nullptr;
   int* err = nullptr;
   int rows_pad = 0, cols_pad = 0, batch = 0;
   CUtensorMap mahi, malo, mbhi, mblo, mc;
@@ -460,7 +508,7 @@ struct TcGemmPlan {
 size_t tc_gemm_workspace_bytes(int n, int batch) {
   const size_t rows_pad = ((size_t)2 * n + TM - 1) / TM * TM;
   const size_t cols_pad = ((size_t)n + TN - 1) / TN * TN;
-  return (2 * rows_pad + 2 * cols_pad) * KP_MAX * 4 * batch + 256 * 5;
+  return (2 * rows_pad + 2 * cols_pad) * KP_MAX * sizeof(__half) * batch + cols_pad * sizeof(float) * batch + 256 * 6;
 }
 
 bool tc_gemm_available() { return encode_fn() != nullptr; }
@@ -482,10 +530,11 @@ bool tc_gemm_plan(TcGemmPlan* p, void* workspace, int n, int batch, float2* A, l
   p->rows_pad = (int)rows_pad;
   p->cols_pad = (int)cols_pad;
   p->batch = batch;
-  p->ahi = (float*)take(rows_pad * KP_MAX * 4 * batch);
-  p->alo = (float*)take(rows_pad * KP_MAX * 4 * batch);
-  p->bhi = (float*)take(cols_pad * KP_MAX * 4 * batch);
-  p->blo = (float*)take(cols_pad * KP_MAX * 4 * batch);
+  p->ahi = (__half*)take(rows_pad * KP_MAX * sizeof(__half) * batch);
+  p->alo = (__half*)take(rows_pad * KP_MAX * sizeof(__half) * batch);
+  p->bhi = (__half*)take(cols_pad * KP_MAX * sizeof(__half) * batch);
+  p->blo = (__half*)take(cols_pad * KP_MAX * sizeof(__half) * batch);
+  p->inv_scale = (float*)take(cols_pad * sizeof(float) * batch);
   p->err = (int*)take(sizeof(int));
   return make_map(&p->mahi, p->ahi, (int)rows_pad, batch, TM) && make_map(&p->malo, p->alo, (int)rows_pad, batch, TM) &&
          make_map(&p->mbhi, p->bhi, (int)cols_pad, batch, TN) && make_map(&p->mblo, p->blo, (int)cols_pad, batch, TN) &&
@@ -506,19 +555,20 @@ cudaError_t tc_update(TcGemmPlan* p, float2* A, long long lda, long long strideA
   if (rows_used > p->rows_pad || cols_used > p->cols_pad) return cudaErrorInvalidValue;
   const int kp = (2 * K + TK - 1) / TK * TK;
   {
-    const int nta = (rows_used / 64) * (kp / 16);  // A tiles: 64 embedded rows x 16
-    const long long nb_b = ((long long)cols_used * (kp / 2) + 255) / 256;
+    const int nta = (rows_used / 64) * (kp / 32);  // A tiles: 64 embedded rows x 32
+    const int nb_b = cols_used / 8;                 // B: one warp per column, eight per block
     dim3 g((unsigned)(nta + nb_b), p->batch);
     prep_ab_kernel<<<g, 256, 0, stream>>>(A, lda, strideA, row0, col0, kcol0, M, N, K, p->rows_pad, p->cols_pad,
-                                          rows_used, cols_used, kp, nta, p->ahi, p->alo, p->bhi, p->blo);
+                                          rows_used, cols_used, kp, nta, p->ahi, p->alo, p->bhi, p->blo,
+                                          p->inv_scale);
   }
   const int tiles_m = rows_used / TM, tiles_n = cols_used / TN;
   const long long n_tiles = (long long)tiles_m * tiles_n * p->batch;
-  if (!ensure_smem_limit((const void*)trailing_update_tf32x3_persistent, P_SMEM)) return cudaErrorInvalidValue;
+  if (!ensure_smem_limit((const void*)trailing_update_f16x3_persistent, P_SMEM)) return cudaErrorInvalidValue;
   const int grid = (int)std::min<long long>(n_tiles, sm_count());
-  trailing_update_tf32x3_persistent<<<grid, P_THREADS, P_SMEM, stream>>>(
-      p->mahi, p->malo, p->mbhi, p->mblo, p->mc, 2 * row0, col0, M2, N, kp / TK, tiles_m, tiles_n, (int)n_tiles,
-      p->err);
+  trailing_update_f16x3_persistent<<<grid, P_THREADS, P_SMEM, stream>>>(
+      p->mahi, p->malo, p->mbhi, p->mblo, p->mc, p->inv_scale, p->cols_pad, 2 * row0, col0, M2, N, kp / TK, tiles_m,
+      tiles_n, (int)n_tiles, p->err);
   return cudaGetLastError();
 }
 

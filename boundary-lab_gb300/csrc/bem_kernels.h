@@ -119,7 +119,7 @@ cudaError_t launch_rhs(const DeviceMesh& m, Precision prec, double k, const Oper
 // dense LU and solves (bem_lu.cu).  Matrices are column-major, batched with a
 // stride of lda*n elements; pivots are 0-based, ipiv stride n.
 // Trailing-update GEMM of the mixed-precision LU: 0 = automatic (tensor cores
-// when available), 1 = cuBLAS cgemm (FP32), 2 = tcgen05 3xTF32 (bem_gemm_tc.cu).
+// when available), 1 = cuBLAS cgemm (FP32), 2 = tcgen05 3xFP16, scaled (bem_gemm_tc.cu).
 enum class LuGemm : int { Auto = 0, Cublas = 1, Tensor = 2 };
 struct TcGemmPlan;
 size_t tc_gemm_workspace_bytes(int n, int batch);

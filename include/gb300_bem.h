@@ -119,7 +119,7 @@ typedef struct bem_solve_options {
   int outputs_on_device; /* 1: pressure_out / field_out are device pointers of the context's device */
   int profile;           /* 1: also time each kernel family with CUDA events (stats.kernel_s) */
   int lu_gemm;           /* LU trailing update of the mixed form: 0 automatic (tensor cores when
-                            available), 1 cuBLAS cgemm (FP32), 2 tcgen05 3xTF32 tensor cores */
+                            available), 1 cuBLAS cgemm (FP32), 2 tcgen05 3xFP16 tensor cores  */
   int lanes;             /* 1 (default): batches one after another on the context's stream;
                             2: a sweep of several batches deals them round-robin to the context and a
                             helper context of its own (own stream and scratch, created on first

@@ -3,9 +3,10 @@
 FP64 form: pivots identical to LAPACK's (first maximum of |re| + |im|) and factors
 within 1e-11.  Mixed form, backward error ||P A - L U|| / ||A||:
   cuBLAS cgemm trailing updates (IEEE FP32):        <= 2e-6
-  tcgen05 3xTF32 trailing updates:                  <= 1e-4
+  tcgen05 3xFP16 trailing updates:                  <= 1e-4
 The tensor-core FP32 accumulation is coarser than IEEE round-to-nearest, so the
-backward error grows with n (measured 2.8e-6 at n = 200, 4.4e-5 at n = 2600);
+backward error grows with n (measured 1.9e-6 at n = 200, 3.4e-5 at n = 2600,
+5.3e-5 at n = 4000);
 the FP64 iterative refinement removes it, which the end-to-end solves below
 check against the oracle at 1e-5.
 """
