@@ -37,7 +37,7 @@
 // TMEM and returns.
 //
 // General block update (tc_update): C[row0:row0+M, col0:col0+N] -= L U with
-// L = A[row0:, kcol0:kcol0+K] and U = A[kcol0:kcol0+K, col0:], K <= 128, so one
+// L = A[row0:, kcol0:kcol0+K] and U = A[kcol0:kcol0+K, col0:], K <= 256, so one
 // kernel serves the trailing update, the updates inside a wide panel and the
 // blocked triangular solve of its U rows.
 //
@@ -64,7 +64,7 @@ namespace {
 constexpr int TM = 128;       // tile rows of C' (real rows)
 constexpr int TN = 256;       // tile columns of C'
 constexpr int TK = 32;        // K block per stage (32 fp16 = 64 B rows, 64-byte swizzle)
-constexpr int KP_MAX = 256;   // K' = 2 K <= 256 (K <= 128 complex), row stride of the split operands
+constexpr int KP_MAX = 512;   // K' = 2 K <= 512 (K <= 256 complex), row stride of the split operands
 constexpr int A_BYTES = TM * TK * 2;   // 8 KB
 constexpr int B_BYTES = TN * TK * 2;   // 16 KB
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi + lo of A and B: 48 KB
@@ -218,11 +218,12 @@ __global__ void __launch_bounds__(256) prep_ab_kernel(const float2* __restrict__
   const int lane = t & 31;
   const int j = (int)(blockIdx.x - nta) * 8 + (t >> 5);  // column of U12 (one warp each)
   if (j >= cols_used) return;
-  const int kc = kp / 2;  // complex K entries written per column (<= 128: four per lane)
-  float2 u[4];
+  constexpr int KL = KP_MAX / 64;  // complex K entries per lane
+  const int kc = kp / 2;           // complex K entries written per column (<= KP_MAX / 2)
+  float2 u[KL];
   float amax = 0.0f;
 #pragma unroll
-  for (int c = 0; c < 4; ++c) {
+  for (int c = 0; c < KL; ++c) {
     const int k = lane + 32 * c;
     u[c] = make_float2(0.f, 0.f);
     if (j < N && k < K) u[c] = Ab[(size_t)(col0 + j) * lda + kcol0 + k];
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(256) prep_ab_kernel(const float2* __restrict__
   const float s = ldexpf(1.0f, sh);
   if (lane == 0) inv_scale[(size_t)b * cols_pad + j] = ldexpf(1.0f, -sh - 14);
 #pragma unroll
-  for (int c = 0; c < 4; ++c) {
+  for (int c = 0; c < KL; ++c) {
     const int k = lane + 32 * c;
     if (k >= kc) break;
     __align__(4) __half hi[2], lo[2];
@@ -542,7 +543,7 @@ bool tc_gemm_plan(TcGemmPlan* p, void* workspace, int n, int batch, float2* A, l
 }
 
 // C[row0:row0+M, col0:col0+N] -= A[row0:row0+M, kcol0:kcol0+K] * A[kcol0:kcol0+K, col0:col0+N]
-// for every matrix of the batch (K <= 128).  Rows beyond M and columns beyond N
+// for every matrix of the batch (K <= 256).  Rows beyond M and columns beyond N
 // inside the last tiles receive -0 (their split operands are zero).
 cudaError_t tc_update(TcGemmPlan* p, float2* A, long long lda, long long strideA, int row0, int M, int col0, int N,
                       int kcol0, int K, cudaStream_t stream) {

@@ -593,7 +593,7 @@ cudaError_t block_update(const LuJob& j, int r0, int M, int c0, int N, int kc, i
   } while (0)
 
 // Two-level right-looking LU.  The matrix is factored in outer block columns of
-// width NB (128): each is factored as sub-panels of width nb (the cluster panel
+// width NB (kOuterBlock, 256): each is factored as sub-panels of width nb (the cluster panel
 // width, 32 or 64) with their row interchanges applied to every other column
 // and the rest of the outer block updated after each sub-panel; then the outer
 // block's U rows are solved block by block and the trailing matrix takes one

@@ -334,18 +334,22 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_cluster_kernel(typenam
 constexpr int kRegPanelThreads = 640;
 constexpr int kRegPanelWarps = kRegPanelThreads / 32;
 
-// first maximum over (value, logical row), also returning the lane that held it
-__device__ __forceinline__ void warp_argmax_at(float& b, int& x, int& at) {
+// Pivot candidates as one 64-bit key: the bits of |re| + |im| (non-negative,
+// so their unsigned order is the value order) above the complement of the
+// logical row, so the largest key is the first maximum (larger value, then
+// smaller row).  NaN values and rows without a candidate get key 0, which no
+// candidate key equals (the low word ~row is at least 2^31).
+__device__ __forceinline__ unsigned long long pivot_key(float v, int row) {
+  return v == v ? ((unsigned long long)__float_as_uint(v) << 32) | (unsigned)~row : 0ull;
+}
+__device__ __forceinline__ int key_row(unsigned long long key) { return (int)~(unsigned)key; }
+__device__ __forceinline__ unsigned long long warp_max_key(unsigned long long k) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    const float ov = __shfl_xor_sync(0xffffffffu, b, o);
-    const int oi = __shfl_xor_sync(0xffffffffu, x, o), oa = __shfl_xor_sync(0xffffffffu, at, o);
-    if (ov > b || (ov == b && oi < x)) {
-      b = ov;
-      x = oi;
-      at = oa;
-    }
+    const unsigned long long ok = __shfl_xor_sync(0xffffffffu, k, o);
+    k = ok > k ? ok : k;
   }
+  return k;
 }
 
 __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float2* A, long long lda, long long strideA,
@@ -360,11 +364,10 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* Lb = reinterpret_cast<float2*>(smem_raw);  // [NB][kRegPanelThreads] multipliers by column, thread
   __shared__ float2 rowsC[2][16][NB];  // pushed candidate rows, by source CTA
-  __shared__ float2 pub[NB], dg[2][NB], urow[NB];
-  __shared__ float cval[2][16];
-  __shared__ int cidx[2][16], chasj[2][16];
-  __shared__ float wval[NW];
-  __shared__ int widx[NW], wlane[NW];
+  __shared__ float2 pub[NB], dg[2][NB];
+  __shared__ float2 urow[NB];
+  __shared__ unsigned long long ckey[2][16], wkey[NW];
+  __shared__ int chasj[2][16];
   __shared__ int s_pivs[NB];
   float2* M = A + (size_t)blockIdx.y * strideA;
   int* piv = ipiv + (size_t)blockIdx.y * n;
@@ -380,50 +383,37 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
 #pragma unroll
     for (int c = 0; c < NB; ++c) a[c] = mine ? src[(size_t)c * lda] : make_float2(0.f, 0.f);
   }
-  auto candidate = [&](float& best, int& bi, int& bt) {  // this thread's candidate for the current column
-    best = -1.0f;
-    bi = INT_MAX;
-    bt = tid;
-    if (mine && done_at < 0) argmax_merge(best, bi, abs1(a[0]), lg);
-    warp_argmax_at(best, bi, bt);
+  auto candidate = [&]() {  // the warp's candidate key for the current column
+    return warp_max_key(mine && done_at < 0 ? pivot_key(abs1(a[0]), lg) : 0ull);
   };
   {
-    float best;
-    int bi, bt;
-    candidate(best, bi, bt);
-    if (lane == 0) {
-      wval[wid] = best;
-      widx[wid] = bi;
-      wlane[wid] = bt;
-    }
+    const unsigned long long key = candidate();
+    if (lane == 0) wkey[wid] = key;
   }
   __syncthreads();
 #pragma unroll 1
   for (int j = 0; j < NB; ++j) {
     const int s = j & 1;
     {  // 1. publish and push
-      float bv = lane < NW ? wval[lane] : -1.0f;
-      int bi = lane < NW ? widx[lane] : INT_MAX;
-      int bt = lane < NW ? wlane[lane] : 0;
-      warp_argmax_at(bv, bi, bt);
-      if (bi != INT_MAX && tid == bt) {
+      const unsigned long long key = warp_max_key(lane < NW ? wkey[lane] : 0ull);
+      const bool active = mine && done_at < 0;
+      if (key != 0ull && active && lg == key_row(key)) {  // this CTA's candidate row (logical rows are distinct)
 #pragma unroll
         for (int c = 0; c < NB; ++c) pub[c] = a[c];
       }
-      const bool hasj = mine && done_at < 0 && lg == j;
+      const bool hasj = active && lg == j;
       if (hasj) {
 #pragma unroll
         for (int c = 0; c < NB; ++c) dg[s][c] = a[c];
       }
       const int cnt = __syncthreads_or(hasj);
       bool wrote = hasj;
-      if (bi != INT_MAX && tid < CL * NB) {  // the candidate row into every CTA
+      if (key != 0ull && tid < CL * NB) {  // the candidate row into every CTA
         *cluster.map_shared_rank(&rowsC[s][rank][tid & (NB - 1)], tid / NB) = pub[tid & (NB - 1)];
         wrote = true;
       }
       if (tid < CL) {
-        *cluster.map_shared_rank(&cval[s][rank], tid) = bi != INT_MAX ? bv : -1.0f;
-        *cluster.map_shared_rank(&cidx[s][rank], tid) = bi;
+        *cluster.map_shared_rank(&ckey[s][rank], tid) = key;
         *cluster.map_shared_rank(&chasj[s][rank], tid) = cnt;
         wrote = true;
       }
@@ -433,13 +423,12 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
     asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
     asm volatile("barrier.cluster.wait.aligned;" ::: "memory");
     // 3. pivot (logical row p, held by CTA pr), in every warp
-    float b = lane < CL ? cval[s][lane] : -1.0f;
-    int x = lane < CL ? cidx[s][lane] : INT_MAX;
-    int pr = lane;
-    warp_argmax_at(b, x, pr);
-    const bool fallback = x == INT_MAX;  // no comparable candidate (all NaN): keep row j
-    const int p = fallback ? j : x;
-    const float2* U = &rowsC[s][pr][0];  // the pivot row, u[c] = U(j, j + c) (zero beyond the panel)
+    const unsigned long long ck = lane < CL ? ckey[s][lane] : 0ull;
+    const unsigned long long km = warp_max_key(ck);
+    const bool fallback = km == 0ull;  // no comparable candidate (all NaN): keep row j
+    const int pr = __ffs(__ballot_sync(0xffffffffu, lane < CL && ck == km)) - 1;  // keys are distinct
+    const int p = fallback ? j : key_row(km);
+    const float2* U = &rowsC[s][fallback ? 0 : pr][0];  // the pivot row, u[c] = U(j, j + c) (zero beyond the panel)
     if (fallback) {  // every CTA takes this branch together
       if (wid == 0) {
         int jr = 0;  // CTA holding logical row j
@@ -450,7 +439,8 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
       __syncthreads();
       U = urow;
     }
-    if (rank == 0 && wid == 0 && lane < NB - j) M[(size_t)(k + j + lane) * lda + k + j] = U[lane];  // U row j
+    if (rank == 0 && wid == 0 && lane < NB - j)  // U row j
+      M[(size_t)(k + j + lane) * lda + k + j] = U[lane];
     if (rank == 0 && tid == 0) {
       piv[k + j] = k + p;
       s_pivs[j] = p;
@@ -472,7 +462,10 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
         if (lg == j) lg = p;  // the old row j moves to the pivot's place
         const float2 l = cmul(a[0], inv);
         Lb[(size_t)j * kRegPanelThreads + tid] = l;
-        // a[c - 1] = a[c] - l u[c]: columns j + 1.. (from step 16 on, the upper half of the window is zero)
+        // a[c - 1] = a[c] - l u[c] for columns j + 1.. .  From step j the window holds 32 - j
+        // live columns, so the update runs over the smallest multiple of 8 covering them (the
+        // columns beyond are zero).  (Packed FP32x2 FMAs on a duplicated copy of the pivot
+        // row took 4 more registers than the 96 a 640-thread CTA allows and spilled.)
         auto update = [&](auto width) {
           constexpr int W = decltype(width)::value;
 #pragma unroll
@@ -483,21 +476,19 @@ __global__ void __launch_bounds__(kRegPanelThreads, 1) lu_panel_reg_kernel(float
           }
           a[W - 1] = make_float2(0.f, 0.f);
         };
-        if (j < NB / 2)
-          update(std::integral_constant<int, NB>{});
+        if (j < 8)
+          update(std::integral_constant<int, 32>{});
+        else if (j < 16)
+          update(std::integral_constant<int, 24>{});
+        else if (j < 24)
+          update(std::integral_constant<int, 16>{});
         else
-          update(std::integral_constant<int, NB / 2>{});
+          update(std::integral_constant<int, 8>{});
       }
     }
     {
-      float best;
-      int bi, bt;
-      candidate(best, bi, bt);
-      if (lane == 0) {  // every thread read wval / widx in this step's push, before the cluster barrier
-        wval[wid] = best;
-        widx[wid] = bi;
-        wlane[wid] = bt;
-      }
+      const unsigned long long key = candidate();
+      if (lane == 0) wkey[wid] = key;  // every thread read wkey in this step's push, before the cluster barrier
     }
     __syncthreads();
   }
