@@ -1079,11 +1079,59 @@ __global__ void __launch_bounds__(NFQ == 1 ? 256 : 128, NFQ == 1 ? 2 : 3)
   const float jac = g[kRecJac];
   const bool coincident = P.kind == 1 && P.tr == 0;  // mass terms: the face with itself, never with an image
   const float a2 = g[kRecA2];
+  // Warp reduction of the NFQ x 48 sums by recursive halving (reduce-scatter): at each
+  // level a lane sends the half of its values it does not keep, so the five levels move
+  // 48 + 24 + 12 + 6 + 3 values per lane instead of 5 x 96 for a full butterfly of every
+  // sum.  With two frequencies lane L ends with sums 3L .. 3L + 2 of the flattened array
+  // (acc2[f][i].x at 48 f + 2 i, .y next to it); with one, the four halvings leave lanes
+  // 2m and 2m + 1 each with half of sums 3m .. 3m + 2 and one exchange completes them.
+  // The sums go through shared memory to the lanes that form the outputs.
+  constexpr int T = NFQ * 48;
+  constexpr int WPB = (NFQ == 1 ? 256 : 128) / 32;
+  __shared__ float red[WPB][T];
+  {
+    float v[T];
+#pragma unroll
+    for (int f = 0; f < NFQ; ++f)
+#pragma unroll
+      for (int i = 0; i < 24; ++i) {
+        v[48 * f + 2 * i] = acc2[f][i].x;
+        v[48 * f + 2 * i + 1] = acc2[f][i].y;
+      }
+    auto level = [&](auto n_c, auto o_c) {
+      constexpr int N = decltype(n_c)::value, O = decltype(o_c)::value, H = N / 2;
+      const bool upper = (lane & O) != 0;
+#pragma unroll
+      for (int i = 0; i < H; ++i) {
+        const float send = upper ? v[i] : v[H + i];
+        const float keep = upper ? v[H + i] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, O);
+      }
+    };
+    level(std::integral_constant<int, T>{}, std::integral_constant<int, 16>{});
+    level(std::integral_constant<int, T / 2>{}, std::integral_constant<int, 8>{});
+    level(std::integral_constant<int, T / 4>{}, std::integral_constant<int, 4>{});
+    level(std::integral_constant<int, T / 8>{}, std::integral_constant<int, 2>{});
+    float* r = red[threadIdx.x >> 5];
+    if constexpr (NFQ == 2) {
+      level(std::integral_constant<int, T / 16>{}, std::integral_constant<int, 1>{});
+#pragma unroll
+      for (int j = 0; j < 3; ++j) r[3 * lane + j] = v[j];
+    } else {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) v[j] += __shfl_xor_sync(0xffffffffu, v[j], 1);
+      if ((lane & 1) == 0) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) r[3 * (lane >> 1) + j] = v[j];
+      }
+    }
+    __syncwarp();
+  }
+  const float* red_w = red[threadIdx.x >> 5];
+  auto sum2 = [&](int f, int i) { return make_float2(red_w[48 * f + 2 * i], red_w[48 * f + 2 * i + 1]); };
 #pragma unroll
   for (int f = 0; f < NFQ; ++f) {
     const SingParamsF32& p = pn.f[f];
-#pragma unroll
-    for (int i = 0; i < 24; ++i) acc2[f][i] = make_float2(warp_sum(acc2[f][i].x), warp_sum(acc2[f][i].y));
     if (lane >= 12) continue;
     float2* o = out + (size_t)f * out_stride + (size_t)kSingOut * warp;
     if (lane < 9) {
@@ -1091,14 +1139,12 @@ __global__ void __launch_bounds__(NFQ == 1 ? 256 : 128, NFQ == 1 ? 2 : 3)
       // S0 = sum w G (static + dynamic)
       float2 S0 = make_float2(G[kRecS0], 0.f);
 #pragma unroll
-      for (int a = 0; a < 3; ++a) S0 = cadd(S0, make_float2(acc2[f][a].x * jac, acc2[f][a].y * jac));
-      float2 IR = make_float2(0.f, 0.f), IDh = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int j = 0; j < 9; ++j)
-        if (j == i) {
-          IR = make_float2(acc2[f][3 + j].x * jac, acc2[f][3 + j].y * jac);
-          IDh = make_float2(acc2[f][12 + j].x * jac, acc2[f][12 + j].y * jac);
-        }
+      for (int a = 0; a < 3; ++a) {
+        const float2 sa = sum2(f, a);
+        S0 = cadd(S0, make_float2(sa.x * jac, sa.y * jac));
+      }
+      const float2 ir = sum2(f, 3 + i), idh = sum2(f, 12 + i);
+      const float2 IR = make_float2(ir.x * jac, ir.y * jac), IDh = make_float2(idh.x * jac, idh.y * jac);
       const float kk_nn = p.k2 * g[kRecNprod];
       const float cc = G[kRecCurl + i];
       const float2 D = make_float2(G[kRecMom + 12 + i] + IDh.x, IDh.y);
@@ -1109,13 +1155,8 @@ __global__ void __launch_bounds__(NFQ == 1 ? 256 : 128, NFQ == 1 ? 2 : 3)
       o[i] = L;
     } else {
       const int a = lane - 9;
-      float2 SR = make_float2(0.f, 0.f), IKh = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int j = 0; j < 3; ++j)
-        if (j == a) {
-          SR = make_float2(acc2[f][j].x * jac, acc2[f][j].y * jac);
-          IKh = make_float2(acc2[f][21 + j].x * jac, acc2[f][21 + j].y * jac);
-        }
+      const float2 sr = sum2(f, a), ikh = sum2(f, 21 + a);
+      const float2 SR = make_float2(sr.x * jac, sr.y * jac), IKh = make_float2(ikh.x * jac, ikh.y * jac);
       const float2 S = make_float2(G[kRecMom + a] + SR.x, SR.y);
       const float2 K = make_float2(G[kRecMom + 21 + a] + IKh.x, IKh.y);
       float2 rhs = cadd(cmul(p.cS, S), cmul(p.cK, K));
@@ -1368,6 +1409,172 @@ __global__ void rhs_faces_kernel(const typename FaceRec<R>::type* __restrict__ f
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int c = 0; c < NC; ++c) rb[((size_t)c * nf + f) * 3 + a] = acc[a][c];
+}
+
+// Right-hand side of NFQ frequencies at once (mixed form).  The frequency-independent part of
+// every q-pair (the pair's C and |C|, r, 1/r, the compensated r - |C| and the
+// adjoint-double-layer factor t) is formed once and shared; per frequency follow the phase,
+// e^{ikr} and the sums, in the operations and order of rhs_faces_kernel<float> and
+// rhs_pair_f32.  rb holds frequency fq's columns at rb[((fq NC + c) nf + f) 3 + a]; its
+// singular blocks start at sblocks + fq sblocks_stride.
+template <int NFQ> struct RhsParamsF32N {
+  df kdf[NFQ];
+  float k[NFQ];
+  float2 cS[NFQ], cK[NFQ], qscale[NFQ];
+  float cw[3 * kMaxQ];
+};
+
+template <int Q, int NFQ>
+__device__ __forceinline__ void rhs_pair_f32_freqs(const FaceF32& F, const FaceF32& Gf, const RhsParamsF32N<NFQ>& p,
+                                                   float2 S[NFQ][3], float2 K[NFQ][3], float sx, float sy) {
+  const float ghi[3] = {sx * Gf.anchor_hi[0], sy * Gf.anchor_hi[1], Gf.anchor_hi[2]};
+  const float glo[3] = {sx * Gf.anchor_lo[0], sy * Gf.anchor_lo[1], Gf.anchor_lo[2]};
+  const PairGeomF32 P = pair_geom_f32(ghi, glo, F.anchor_hi, F.anchor_lo);
+  const float R0 = P.R.hi + P.R.lo;
+  float th0[NFQ];
+#pragma unroll
+  for (int fq = 0; fq < NFQ; ++fq) {
+    th0[fq] = df_reduce_two_pi(df_mul(p.kdf[fq], P.R));
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      S[fq][a] = make_float2(0.f, 0.f);
+      K[fq][a] = make_float2(0.f, 0.f);
+    }
+  }
+#pragma unroll 1
+  for (int m = 0; m < Q; ++m) {
+    const float of[3] = {F.off[3 * m], F.off[3 * m + 1], F.off[3 * m + 2]};
+    float2 us[NFQ], uk[NFQ];
+#pragma unroll
+    for (int fq = 0; fq < NFQ; ++fq) {
+      us[fq] = make_float2(0.f, 0.f);
+      uk[fq] = make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int n = 0; n < Q; ++n) {
+      const float d[3] = {sx * Gf.off[3 * n] - of[0], sy * Gf.off[3 * n + 1] - of[1], Gf.off[3 * n + 2] - of[2]};
+      float rv[3];
+      rv[0] = P.Cf[0] + d[0];
+      rv[1] = P.Cf[1] + d[1];
+      rv[2] = P.Cf[2] + d[2];
+      const float r2 = fmaf(rv[0], rv[0], fmaf(rv[1], rv[1], rv[2] * rv[2]));
+      const float rinv = r2 > 1e-30f ? rsqrt_ftz(r2) : 0.0f;
+      const float r = r2 * rinv;
+      const float cd = fmaf(P.Cf[0], d[0], fmaf(P.Cf[1], d[1], P.Cf[2] * d[2]));
+      const float dd = fmaf(d[0], d[0], fmaf(d[1], d[1], d[2] * d[2]));
+      const float den = fmaxf(r + R0, 1e-30f);
+      const float delta = fmaf(2.0f, cd, dd) * rcp_ftz(den);
+      const float sc = rinv * BEM_INV_FOUR_PI;
+      // adjoint double layer: G (-1/r + ik) * (-(r . n_x)/r)
+      const float t = -fmaf(rv[0], F.normal[0], fmaf(rv[1], F.normal[1], rv[2] * F.normal[2])) * rinv;
+      const float wn = p.cw[n] + p.cw[Q + n] + p.cw[2 * Q + n];  // DP0 trial basis
+#pragma unroll
+      for (int fq = 0; fq < NFQ; ++fq) {
+        const float theta = reduce_two_pi(fmaf(p.k[fq], delta, th0[fq]));
+        float s, c;
+        sincos_ftz(theta, &s, &c);
+        const float2 G = make_float2(c * sc, s * sc);
+        const float2 Kk = make_float2(t * (-G.x * rinv - G.y * p.k[fq]), t * (G.x * p.k[fq] - G.y * rinv));
+        us[fq].x = fmaf(wn, G.x, us[fq].x);
+        us[fq].y = fmaf(wn, G.y, us[fq].y);
+        uk[fq].x = fmaf(wn, Kk.x, uk[fq].x);
+        uk[fq].y = fmaf(wn, Kk.y, uk[fq].y);
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float c = p.cw[a * Q + m];
+#pragma unroll
+      for (int fq = 0; fq < NFQ; ++fq) {
+        S[fq][a].x = fmaf(c, us[fq].x, S[fq][a].x);
+        S[fq][a].y = fmaf(c, us[fq].y, S[fq][a].y);
+        K[fq][a].x = fmaf(c, uk[fq].x, K[fq][a].x);
+        K[fq][a].y = fmaf(c, uk[fq].y, K[fq][a].y);
+      }
+    }
+  }
+  const float jac = F.area2 * Gf.area2;
+#pragma unroll
+  for (int fq = 0; fq < NFQ; ++fq)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      S[fq][a] = cscale(S[fq][a], jac);
+      K[fq][a] = cscale(K[fq][a], jac);
+    }
+}
+
+template <int Q, int NC, int NFQ>
+__global__ void __launch_bounds__(128) rhs_faces_f32_freqs_kernel(
+    const FaceF32* __restrict__ faces, int nf, const int* __restrict__ driven, int ndriven,
+    const float2* __restrict__ drive, const SingularPair* __restrict__ pairs, const int* __restrict__ by_test_ptr,
+    const int* __restrict__ by_test, const float2* __restrict__ sblocks, long long sblocks_stride,
+    RhsParamsF32N<NFQ> p, float2* __restrict__ rb, int ntr, int4 trs, const unsigned char* __restrict__ fix_mask) {
+  const int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (f >= nf) return;
+  const FaceF32& F = faces[f];
+  float2 acc[NFQ][3][NC];
+#pragma unroll
+  for (int fq = 0; fq < NFQ; ++fq)
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) acc[fq][a][c] = make_float2(0.f, 0.f);
+  // driven faces and their symmetry images (touching pairs are in the singular blocks)
+  for (int ti = 0; ti < ntr; ++ti)
+    for (int i = lane; i < ndriven; i += 32) {
+      const int tr = ti == 0 ? trs.x : ti == 1 ? trs.y : ti == 2 ? trs.z : trs.w;
+      const int g = driven[i];
+      const FaceF32& Gf = faces[g];
+      int sv[3];
+#pragma unroll
+      for (int b = 0; b < 3; ++b) sv[b] = (tr == 0 || (fix_mask[Gf.verts[b]] & tr) == tr) ? Gf.verts[b] : -2;
+      if (share_vertex(F.verts, sv[0], sv[1], sv[2])) continue;
+      float2 S[NFQ][3], K[NFQ][3];
+      rhs_pair_f32_freqs<Q, NFQ>(F, Gf, p, S, K, (float)tr_sign_x(tr), (float)tr_sign_y(tr));
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const float2 dg = drive[(size_t)c * nf + g];
+#pragma unroll
+        for (int fq = 0; fq < NFQ; ++fq) {
+          const float2 q = cmul(p.qscale[fq], dg);
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+            acc[fq][a][c] = cadd(acc[fq][a][c], cmul(q, cadd(cmul(p.cS[fq], S[fq][a]), cmul(p.cK[fq], K[fq][a]))));
+        }
+      }
+    }
+#pragma unroll
+  for (int fq = 0; fq < NFQ; ++fq)
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        acc[fq][a][c].x = warp_sum(acc[fq][a][c].x);
+        acc[fq][a][c].y = warp_sum(acc[fq][a][c].y);
+      }
+  if (lane != 0) return;
+  for (int kk = by_test_ptr[f]; kk < by_test_ptr[f + 1]; ++kk) {
+    const int pid = by_test[kk];
+    const int g = pairs[pid].trial;
+#pragma unroll
+    for (int fq = 0; fq < NFQ; ++fq) {
+      const float2* blk = sblocks + (size_t)fq * sblocks_stride + (size_t)kSingOut * pid;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const float2 q = cmul(p.qscale[fq], drive[(size_t)c * nf + g]);
+        if (q.x == 0 && q.y == 0) continue;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) acc[fq][a][c] = cadd(acc[fq][a][c], cmul(q, blk[9 + a]));
+      }
+    }
+  }
+#pragma unroll
+  for (int fq = 0; fq < NFQ; ++fq)
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) rb[(((size_t)fq * NC + c) * nf + f) * 3 + a] = acc[fq][a][c];
 }
 
 // b[row(j)][c] = sum over (f, a) in star(j) of rb[c][f][a]
@@ -1769,6 +1976,74 @@ cudaError_t launch_rhs(const DeviceMesh& m, Precision prec, double k, const Oper
                                                                         (double2*)b, ldb, m.row_weight);
   }
   return cudaGetLastError();
+}
+
+// Frequencies that share one right-hand-side launch: four with one excitation, two with
+// two (the accumulators of NFQ x 3 x NC complex values stay in registers), else one.
+int rhs_width(Precision prec, int nc) { return prec == Precision::Mixed ? (nc == 1 ? 4 : nc == 2 ? 2 : 1) : 1; }
+
+cudaError_t launch_rhs_freqs(const DeviceMesh& m, Precision prec, int nfreq, const double* k, const OperatorCoeffs* c,
+                             const double2* qscale, const void* drive, int nc, const void* sblocks,
+                             long long sblocks_stride, void* rb, void* const* b, long long ldb, cudaStream_t stream) {
+  const int width = rhs_width(prec, nc);
+  const size_t esz = prec == Precision::Mixed ? sizeof(float2) : sizeof(double2);
+  for (int f0 = 0; f0 < nfreq;) {
+    const int w = std::min(width, nfreq - f0);
+    if (w == 1) {
+      const cudaError_t e = launch_rhs(m, prec, k[f0], c[f0], qscale[f0], drive, nc,
+                                       (const char*)sblocks + (size_t)f0 * sblocks_stride * esz, rb, b[f0], ldb, stream);
+      if (e != cudaSuccess) return e;
+      ++f0;
+      continue;
+    }
+    const int threads = 128;
+    const int nblk = (int)(((long long)m.nf * 32 + threads - 1) / threads);
+    const float2* sb = (const float2*)sblocks + (size_t)f0 * sblocks_stride;
+    const int4 trs = make_int4(m.tr[0], m.tr[1], m.tr[2], m.tr[3]);
+    auto run = [&](auto nfq_c, auto nc_c) {
+      constexpr int NFQ = decltype(nfq_c)::value, NC = decltype(nc_c)::value;
+      RhsParamsF32N<NFQ> p;
+      for (int i = 0; i < NFQ; ++i) {
+        p.kdf[i] = make_df(k[f0 + i]);
+        p.k[i] = (float)k[f0 + i];
+        p.cS[i] = f2(c[f0 + i].cS);
+        p.cK[i] = f2(c[f0 + i].cK);
+        p.qscale[i] = f2(qscale[f0 + i]);
+      }
+      for (int i = 0; i < 3 * kMaxQ; ++i) p.cw[i] = (float)m.rule_cw[i];
+      auto go = [&](auto kern) {
+        kern<<<nblk, threads, 0, stream>>>(m.faces32, m.nf, m.driven, m.ndriven, (const float2*)drive, m.pairs,
+                                           m.pairs_by_test_ptr, m.pairs_by_test, sb, sblocks_stride, p, (float2*)rb,
+                                           m.ntr, trs, m.fix_mask);
+      };
+      if (m.Q == 6)
+        go(rhs_faces_f32_freqs_kernel<6, NC, NFQ>);
+      else if (m.Q == 3)
+        go(rhs_faces_f32_freqs_kernel<3, NC, NFQ>);
+      else
+        go(rhs_faces_f32_freqs_kernel<1, NC, NFQ>);
+    };
+    if (nc == 2)
+      run(std::integral_constant<int, 2>{}, std::integral_constant<int, 2>{});
+    else if (w == 4)
+      run(std::integral_constant<int, 4>{}, std::integral_constant<int, 1>{});
+    else if (w == 3)
+      run(std::integral_constant<int, 3>{}, std::integral_constant<int, 1>{});
+    else
+      run(std::integral_constant<int, 2>{}, std::integral_constant<int, 1>{});
+    for (int i = 0; i < w; ++i)
+      rhs_gather_kernel<float2><<<(m.nv + 127) / 128, 128, 0, stream>>>(
+          (const float2*)rb + (size_t)i * nc * m.nf * 3, m.nf, nc, m.col_ptr, m.col_fb, m.vertex_row, m.nv,
+          (float2*)b[f0 + i], ldb, m.row_weight);
+    f0 += w;
+  }
+  return cudaGetLastError();
+}
+
+// Kernel launches of launch_rhs_freqs for nfreq frequencies.
+int rhs_launches(Precision prec, int nc, int nfreq) {
+  const int width = rhs_width(prec, nc);
+  return nfreq + (nfreq + width - 1) / width;  // one gather per frequency, one face kernel per group
 }
 
 }  // namespace bem

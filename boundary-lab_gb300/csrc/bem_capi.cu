@@ -275,7 +275,7 @@ long long assemble_frequencies(bem_context* ctx, bem_mesh* m, bem::Precision pre
   const size_t sblk_n = (size_t)std::max(dm.npairs, 1) * 12;  // elements per singular-block buffer
   ck(ctx->rext.ensure(rext_n * L.esz * G), "alloc extended rows");
   ck(ctx->sblocks.ensure(sblk_n * L.esz * G), "alloc singular blocks");
-  if (nc > 0) ck(ctx->rb.ensure((size_t)nc * dm.nf * 3 * L.esz), "alloc rhs faces");
+  if (nc > 0) ck(ctx->rb.ensure((size_t)std::max(4, nc) * dm.nf * 3 * L.esz), "alloc rhs faces");
   auto rext = [&](int i) { return (void*)((char*)ctx->rext.p + rext_n * L.esz * i); };
   auto sblk = [&](int i) { return (void*)((char*)ctx->sblocks.p + sblk_n * L.esz * i); };
   long long launches = 0;
@@ -308,16 +308,15 @@ long long assemble_frequencies(bem_context* ctx, bem_mesh* m, bem::Precision pre
     }
     prof_mark(ctx, BEM_K_GATHER);
     if (nc > 0) {
-      for (int i = 0; i < g; ++i)
-        ck(bem::launch_rhs(dm, prec, k[f0 + i], c[f0 + i], qscale[f0 + i], drive, nc, sblk(i), ctx->rb.p, b[f0 + i],
-                           L.ldb, ctx->stream),
-           "rhs kernel");
+      ck(bem::launch_rhs_freqs(dm, prec, g, k + f0, c + f0, qscale + f0, drive, nc, sblk(0), (long long)sblk_n,
+                               ctx->rb.p, b + f0, L.ldb, ctx->stream),
+         "rhs kernel");
       prof_mark(ctx, BEM_K_RHS);
     }
-    // per frequency: scatter, gather (+ isolated rows), right-hand side (2); per group the
-    // regular and singular launches
-    launches += (long long)g * (2 + (dm.n_isolated ? 1 : 0) + (nc > 0 ? 2 : 0)) + bem::regular_launches(dm, prec, g) +
-                bem::singular_launches(prec, g);
+    // per frequency: scatter, gather (+ isolated rows); per group the regular, singular and
+    // right-hand-side launches
+    launches += (long long)g * (2 + (dm.n_isolated ? 1 : 0)) + (nc > 0 ? bem::rhs_launches(prec, nc, g) : 0) +
+                bem::regular_launches(dm, prec, g) + bem::singular_launches(prec, g);
     if (regular_flop && prec == bem::Precision::Mixed) {
       const double qpairs = ((double)dm.ntr * dm.nf * dm.nf - dm.npairs) * dm.Q * dm.Q;
       *regular_flop += g * qpairs * bem::regular_flop_per_qpair(g);

@@ -251,18 +251,21 @@ __global__ void __launch_bounds__(256) prep_ab_kernel(const float2* __restrict__
 
 // One CTA per SM walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ... (rows
 // of C' fastest, then columns, then matrices).  Warp 0 is the TMA producer,
-// warp 1 issues the MMAs, warps 2-5 are the epilogue.  Operands flow through a
+// warp 1 issues the MMAs, warps 2-9 are the epilogue.  Operands flow through a
 // 4-stage pipeline (192 KB) and the accumulator is double-buffered in TMEM
 // (2 x 256 columns), so the epilogue of one tile runs while the MMAs of the
 // next tile proceed.  A warp reads only its own TMEM lane quarter (warp % 4),
-// so epilogue warp w handles rows 32 (w % 4) of a tile.  (The one-tile-per-CTA
-// kernel with two CTAs per SM that this replaced was 2-3% slower on the LU.)
+// so epilogue warp w handles rows 32 (w % 4) of a tile, in the even or the odd
+// 32-column chunks ((w - 2) / 4): with K = 32 (the updates inside an outer
+// block) a tile's MMAs take less time than its epilogue, and two warps per
+// quarter halve that.  (The one-tile-per-CTA kernel with two CTAs per SM that
+// this replaced was 2-3% slower on the LU.)
 constexpr int P_STAGES = 4;
-constexpr int P_EPI_WARPS = 4;
+constexpr int P_EPI_WARPS = 8;
 constexpr int P_THREADS = 64 + 32 * P_EPI_WARPS;
 constexpr int P_TMEM_COLS = 2 * TN;
 constexpr size_t P_STAGE_AREA = (size_t)P_STAGES * STAGE_BYTES;  // 192 KB
-constexpr size_t P_EPI_BYTES = (size_t)P_EPI_WARPS * 8192;        // two 4 KB buffers per epilogue warp
+constexpr size_t P_EPI_BYTES = (size_t)P_EPI_WARPS * 4096;        // one 4 KB buffer per epilogue warp
 constexpr size_t P_SMEM = P_STAGE_AREA + P_EPI_BYTES + 1024;
 
 __global__ void __launch_bounds__(P_THREADS, 1)
@@ -375,8 +378,9 @@ __global__ void __launch_bounds__(P_THREADS, 1)
   } else if (warp >= 2) {
     // epilogue: TMEM lane quarter q = warp % 4 holds rows m0 + 32 q .. + 31
     const int q = warp & 3;
-    float* stg = (float*)(base + P_STAGE_AREA + (size_t)(warp - 2) * 8192);
-    int chunk = 0, local = 0;
+    const int half = (warp - 2) >> 2;  // this warp's chunks: half, half + 2, ...
+    float* sb = (float*)(base + P_STAGE_AREA + (size_t)(warp - 2) * 4096);
+    int local = 0;
     for (int t = blockIdx.x; t < n_tiles && !s_fail; t += gridDim.x, ++local) {
       const int buf = local & 1;
       if (!mbar_wait(&acc_full[buf], (local >> 1) & 1, err, 3)) {
@@ -387,15 +391,14 @@ __global__ void __launch_bounds__(P_THREADS, 1)
       const int bz = t / per_matrix, rem = t - bz * per_matrix;
       const int m0 = (rem % tiles_m) * TM, n0 = (rem / tiles_m) * TN;
       const bool rows_live = m0 + q * 32 < M2;
-      for (int cc = 0; cc < TN / 32; ++cc) {
-        float v[32];
-        tmem_ld_32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * TN + cc * 32), v);
+      for (int cc = half; cc < TN / 32; cc += 2) {
         const int col = n0 + cc * 32;
         if (!rows_live || col >= N) continue;  // warp-uniform
-        float* sb = stg + (chunk & 1) * 1024;
+        float v[32];
+        tmem_ld_32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * TN + cc * 32), v);
         const float* isc = inv_scale + (size_t)bz * cols_pad + col;  // 1 / (s_A s_j) of these 32 columns
-        // the group that last read this buffer (two chunks ago) must be done reading
-        if (lane == 0) bulk_wait_read<1>();
+        // the reduce that last read this buffer must be done reading it
+        if (lane == 0) bulk_wait_read<0>();
         __syncwarp();
 #pragma unroll
         for (int j = 0; j < 32; ++j) sb[j * 32 + lane] = -v[j] * __ldg(isc + j);
@@ -405,7 +408,6 @@ __global__ void __launch_bounds__(P_THREADS, 1)
           tma_reduce_add_3d(&map_c, sb, x0 + m0 + q * 32, y0 + col, bz);
           bulk_commit();
         }
-        ++chunk;
       }
       // this warp has read its quarter of the accumulator: the MMA warp may reuse it
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

@@ -115,6 +115,14 @@ cudaError_t launch_gather(const DeviceMesh& m, Precision prec, const void* Rext,
 cudaError_t launch_rhs(const DeviceMesh& m, Precision prec, double k, const OperatorCoeffs& c, double2 qscale,
                        const void* drive, int nc, const void* sblocks, void* rb, void* b, long long ldb,
                        cudaStream_t stream);
+// Right-hand sides of nfreq frequencies, up to rhs_width(prec, nc) per face-kernel launch;
+// frequency f's singular blocks start at element f * sblocks_stride of sblocks, and rb needs
+// room for max(4, nc) * nf * 3 complex values.
+int rhs_width(Precision prec, int nc);
+cudaError_t launch_rhs_freqs(const DeviceMesh& m, Precision prec, int nfreq, const double* k, const OperatorCoeffs* c,
+                             const double2* qscale, const void* drive, int nc, const void* sblocks,
+                             long long sblocks_stride, void* rb, void* const* b, long long ldb, cudaStream_t stream);
+int rhs_launches(Precision prec, int nc, int nfreq);
 
 // dense LU and solves (bem_lu.cu).  Matrices are column-major, batched with a
 // stride of lda*n elements; pivots are 0-based, ipiv stride n.
