@@ -23,6 +23,7 @@
 //                         deterministic, no atomics)
 //   gather_columns        A[:, j] = sum over (g, b) in star(j) of Rext[g*3+b],
 //                         then halo extended rows folded into their rows
+#include <complex>
 #include <map>
 #include <mutex>
 
@@ -973,6 +974,34 @@ __global__ void __launch_bounds__(256, 1)
   }
 }
 
+// Warp reduce-scatter by recursive halving of N = 3 x 2^j values per lane (N <= 96).  At
+// exchange offset O a lane keeps one half of its values (the upper half when bit O of its
+// lane index is set) and adds its partner's copy of that half, so each level moves half as
+// many values as the one before; once three values remain, the remaining offsets are plain
+// butterflies.  Afterwards v[0..3) of lane l hold the warp sums of entries 3 (l >> s) ..
+// 3 (l >> s) + 2, s = 5 - log2(N / 3).  For 96 values the five levels move 48 + 24 + 12 +
+// 6 + 3 values per lane, against 5 x 96 for a butterfly of every value.
+template <int N, int O>
+__device__ __forceinline__ void warp_reduce_halving(float* v, int lane) {
+  if constexpr (O > 0) {
+    if constexpr (N > 3) {
+      constexpr int H = N / 2;
+      const bool upper = (lane & O) != 0;
+#pragma unroll
+      for (int i = 0; i < H; ++i) {
+        const float send = upper ? v[i] : v[H + i];
+        const float keep = upper ? v[H + i] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, O);
+      }
+      warp_reduce_halving<H, O / 2>(v, lane);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], O);
+      warp_reduce_halving<N, O / 2>(v, lane);
+    }
+  }
+}
+
 // The mixed form's singular kernel: the same Duffy remainder as
 // singular_dyn_kernel<float>, with every per-pair FP64 quantity (geometry,
 // curl products, static moments) read from the pair record instead of being
@@ -1079,12 +1108,9 @@ __global__ void __launch_bounds__(NFQ == 1 ? 256 : 128, NFQ == 1 ? 2 : 3)
   const float jac = g[kRecJac];
   const bool coincident = P.kind == 1 && P.tr == 0;  // mass terms: the face with itself, never with an image
   const float a2 = g[kRecA2];
-  // Warp reduction of the NFQ x 48 sums by recursive halving (reduce-scatter): at each
-  // level a lane sends the half of its values it does not keep, so the five levels move
-  // 48 + 24 + 12 + 6 + 3 values per lane instead of 5 x 96 for a full butterfly of every
-  // sum.  With two frequencies lane L ends with sums 3L .. 3L + 2 of the flattened array
-  // (acc2[f][i].x at 48 f + 2 i, .y next to it); with one, the four halvings leave lanes
-  // 2m and 2m + 1 each with half of sums 3m .. 3m + 2 and one exchange completes them.
+  // Warp reduction of the NFQ x 48 sums by recursive halving (warp_reduce_halving): with
+  // two frequencies lane L ends with sums 3L .. 3L + 2 of the flattened array (acc2[f][i].x
+  // at 48 f + 2 i, .y next to it); with one, lanes 2m and 2m + 1 both hold sums 3m .. 3m + 2.
   // The sums go through shared memory to the lanes that form the outputs.
   constexpr int T = NFQ * 48;
   constexpr int WPB = (NFQ == 1 ? 256 : 128) / 32;
@@ -1098,32 +1124,12 @@ __global__ void __launch_bounds__(NFQ == 1 ? 256 : 128, NFQ == 1 ? 2 : 3)
         v[48 * f + 2 * i] = acc2[f][i].x;
         v[48 * f + 2 * i + 1] = acc2[f][i].y;
       }
-    auto level = [&](auto n_c, auto o_c) {
-      constexpr int N = decltype(n_c)::value, O = decltype(o_c)::value, H = N / 2;
-      const bool upper = (lane & O) != 0;
-#pragma unroll
-      for (int i = 0; i < H; ++i) {
-        const float send = upper ? v[i] : v[H + i];
-        const float keep = upper ? v[H + i] : v[i];
-        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, O);
-      }
-    };
-    level(std::integral_constant<int, T>{}, std::integral_constant<int, 16>{});
-    level(std::integral_constant<int, T / 2>{}, std::integral_constant<int, 8>{});
-    level(std::integral_constant<int, T / 4>{}, std::integral_constant<int, 4>{});
-    level(std::integral_constant<int, T / 8>{}, std::integral_constant<int, 2>{});
+    warp_reduce_halving<T, 16>(v, lane);
     float* r = red[threadIdx.x >> 5];
-    if constexpr (NFQ == 2) {
-      level(std::integral_constant<int, T / 16>{}, std::integral_constant<int, 1>{});
+    constexpr int sh = NFQ == 2 ? 0 : 1;
+    if ((lane & ((1 << sh) - 1)) == 0) {
 #pragma unroll
-      for (int j = 0; j < 3; ++j) r[3 * lane + j] = v[j];
-    } else {
-#pragma unroll
-      for (int j = 0; j < 3; ++j) v[j] += __shfl_xor_sync(0xffffffffu, v[j], 1);
-      if ((lane & 1) == 0) {
-#pragma unroll
-        for (int j = 0; j < 3; ++j) r[3 * (lane >> 1) + j] = v[j];
-      }
+      for (int j = 0; j < 3; ++j) r[3 * (lane >> sh) + j] = v[j];
     }
     __syncwarp();
   }
@@ -1157,6 +1163,217 @@ __global__ void __launch_bounds__(NFQ == 1 ? 256 : 128, NFQ == 1 ? 2 : 3)
       const int a = lane - 9;
       const float2 sr = sum2(f, a), ikh = sum2(f, 21 + a);
       const float2 SR = make_float2(sr.x * jac, sr.y * jac), IKh = make_float2(ikh.x * jac, ikh.y * jac);
+      const float2 S = make_float2(G[kRecMom + a] + SR.x, SR.y);
+      const float2 K = make_float2(G[kRecMom + 21 + a] + IKh.x, IKh.y);
+      float2 rhs = cadd(cmul(p.cS, S), cmul(p.cK, K));
+      if (coincident) rhs = cadd(rhs, cscale(p.cM10, a2 * p.m11m10[9 + a]));
+      o[9 + a] = rhs;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
+// The mixed form's singular remainder through a Chebyshev expansion in r.
+//
+// singular_dyn_f32_kernel sums, over a pair's Duffy points, basis weights times
+//   G2 = (e^{ikr} - 1) / (4 pi r)             (SR, IR: 12 sums)
+//   Hy = g2(r) (r . n_r) / (4 pi r),  Hx = -g2(r) (r . n_t) / (4 pi r)   (IDh, IKh: 12 sums)
+// with g2(r) = (1 - (1 - ikr) e^{ikr}) / r^2: the point's G2 = f1(r) / (4 pi) with
+// f1(r) = (e^{ikr} - 1) / r, and its hr + i hi = 1 - (1 - ikr) e^{ikr}.  f1 and g2 are
+// smooth (entire) functions of r, so on [0, R], R bounding every pair's point distances,
+// f1(r) = sum_n c1_n T_n(2 r / R - 1) and g2 likewise with c2_n, to a truncation error
+// that the host checks per frequency.  The k-independent sums
+//   M[n][i] = sum over the pair's Duffy points of (the point's weight for sum i) T_n(x)
+// are formed once per mesh, and each frequency's 24 sums become sum_n c_n M[n][i]: the same
+// quadrature (the reference's Duffy rules), evaluated with 24 terms per sum instead of one
+// kernel evaluation per point and frequency.
+// ------------------------------------------------------------------------
+
+// Chebyshev moments (once per mesh, for the first nterms terms, a multiple of four): one
+// warp per pair, lanes over the Duffy points (point geometry as in singular_dyn_f32_kernel,
+// from the pair record), the terms in chunks of four (96 sums per lane), reduced by
+// recursive halving; lane L then holds entries 3L .. 3L + 2 of the chunk, which are
+// contiguous in cheb[((pair kChebN) + n) 24 + i].  The single-layer sums SR[a] (entries
+// 0-2) are not formed: the P1 trial basis sums to one, so SR[a] = IR[a][0] + IR[a][1] +
+// IR[a][2], and the per-frequency kernel adds them up there.
+__global__ void __launch_bounds__(256)
+    singular_cheb_moments_kernel(const SingularPair* __restrict__ pairs, int npairs, const int* __restrict__ rule_ptr,
+                                 const float* __restrict__ duffy, const float* __restrict__ rec, float two_over_R,
+                                 int nterms, float* __restrict__ cheb) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= npairs) return;
+  const SingularPair P = pairs[warp];
+  const float* G = rec + (size_t)kPairRec * warp;
+  float g[21];
+#pragma unroll
+  for (int i = 0; i < 21; ++i) g[i] = __ldg(G + kRecGeom + i);
+  const float* e1t = g;
+  const float* e2t = g + 3;
+  const float* d0 = g + 6;
+  const float* e1r = g + 9;
+  const float* e2r = g + 12;
+  const float* nt = g + 15;
+  const float* nr = g + 18;
+  const float inv4pi = (float)(0.25 / CUDART_PI);
+  const int q0 = rule_ptr[P.rule], q1 = rule_ptr[P.rule + 1];
+  constexpr int NCH = 4;
+  static_assert(kChebN % NCH == 0, "whole chunks");
+  // one chunk of NCH terms starting at N0 (a compile-time constant, so that every register
+  // index below is one)
+  auto chunk = [&](auto n0_c) {
+    constexpr int n0 = decltype(n0_c)::value;
+    float v[NCH * 24];
+#pragma unroll
+    for (int i = 0; i < NCH * 24; ++i) v[i] = 0.f;
+    for (int q = q0 + lane; q < q1; q += 32) {
+      const float tu = __ldg(duffy + 5 * (size_t)q), tv = __ldg(duffy + 5 * (size_t)q + 1);
+      const float ru = __ldg(duffy + 5 * (size_t)q + 2), rvv = __ldg(duffy + 5 * (size_t)q + 3);
+      const float w = __ldg(duffy + 5 * (size_t)q + 4);
+      const float px[3] = {1.f - tu - tv, tu, tv};
+      const float py[3] = {1.f - ru - rvv, ru, rvv};
+      float rv[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) rv[d] = (d0[d] + ru * e1r[d] + rvv * e2r[d]) - (tu * e1t[d] + tv * e2t[d]);
+      const float r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+      if (r2 == 0.f) continue;
+      const float rinv = rsqrt_ftz(r2);
+      const float r = r2 * rinv;
+      const float s = rinv * inv4pi;
+      const float fy = (rv[0] * nr[0] + rv[1] * nr[1] + rv[2] * nr[2]) * s;     // (r . n_r) / (4 pi r)
+      const float fx = -(rv[0] * nt[0] + rv[1] * nt[1] + rv[2] * nt[2]) * s;    // -(r . n_t) / (4 pi r)
+      const float x = fminf(1.f, fmaf(r, two_over_R, -1.f));
+      // T_n(x) for the chunk's n by the three-term recurrence
+      float T[NCH];
+      {
+        float tm1 = 1.f, t0 = x;
+#pragma unroll
+        for (int n = 0; n < n0 + NCH; ++n) {
+          float tn;
+          if (n == 0) {
+            tn = 1.f;
+          } else if (n == 1) {
+            tn = x;
+          } else {
+            tn = fmaf(2.f * x, t0, -tm1);
+            tm1 = t0;
+            t0 = tn;
+          }
+          if (n >= n0) T[n - n0] = tn;
+        }
+      }
+      float wa[3], wab[9];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        wa[a] = w * px[a];
+#pragma unroll
+        for (int b = 0; b < 3; ++b) wab[3 * a + b] = wa[a] * py[b];
+      }
+#pragma unroll
+      for (int j = 0; j < NCH; ++j) {
+        float* vj = v + 24 * j;
+        const float tg = T[j] * inv4pi;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) vj[21 + a] = fmaf(wa[a] * fx, T[j], vj[21 + a]);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+          vj[3 + i] = fmaf(wab[i], tg, vj[3 + i]);
+          vj[12 + i] = fmaf(wab[i] * fy, T[j], vj[12 + i]);
+        }
+      }
+    }
+    warp_reduce_halving<NCH * 24, 16>(v, lane);
+    float* o = cheb + ((size_t)warp * kChebN + n0) * 24 + 3 * lane;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) o[j] = v[j];
+  };
+  chunk(std::integral_constant<int, 0>{});
+  chunk(std::integral_constant<int, 4>{});
+  if (nterms > 8) chunk(std::integral_constant<int, 8>{});
+  if (nterms > 12) chunk(std::integral_constant<int, 12>{});
+  if (nterms > 16) chunk(std::integral_constant<int, 16>{});
+  if (nterms > 20) chunk(std::integral_constant<int, 20>{});
+  static_assert(kChebN == 24, "one chunk call per four terms");
+}
+
+// Per frequency: the 24 sums from the moments and the expansion coefficients (c1 for sums
+// 0-11, c2 for 12-23), then the nine LHS and three RHS-operator entries exactly as in
+// singular_dyn_f32_kernel.  One warp per pair; lane i < 24 forms sum i of every frequency
+// (the pair's moments are read once for the NFQ frequencies).
+template <int NFQ> struct ChebParamsF32 {
+  float2 c1[NFQ][kChebN], c2[NFQ][kChebN];
+  SingParamsF32 f[NFQ];
+  long long off[NFQ];  // element offset of each frequency's blocks in out
+};
+
+template <int NFQ>
+__global__ void __launch_bounds__(128)
+    singular_cheb_f32_kernel(const SingularPair* __restrict__ pairs, int npairs, const float* __restrict__ rec,
+                             const float* __restrict__ cheb, int nterms, ChebParamsF32<NFQ> cp,
+                             float2* __restrict__ out) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= npairs) return;
+  const SingularPair P = pairs[warp];
+  const float* G = rec + (size_t)kPairRec * warp;
+  float2 acc[NFQ];
+#pragma unroll
+  for (int f = 0; f < NFQ; ++f) acc[f] = make_float2(0.f, 0.f);
+  if (lane >= 3 && lane < 24) {
+    const float* M = cheb + (size_t)warp * kChebN * 24 + lane;
+    const bool second = lane >= 12;
+#pragma unroll 4
+    for (int n = 0; n < nterms; ++n) {
+      const float m = __ldg(M + 24 * n);
+#pragma unroll
+      for (int f = 0; f < NFQ; ++f) {
+        const float2 c = second ? cp.c2[f][n] : cp.c1[f][n];
+        acc[f].x = fmaf(c.x, m, acc[f].x);
+        acc[f].y = fmaf(c.y, m, acc[f].y);
+      }
+    }
+  }
+  const float jac = G[kRecJac];
+  const bool coincident = P.kind == 1 && P.tr == 0;  // mass terms: the face with itself, never with an image
+  const float a2 = G[kRecA2];
+  const int srcA = 3 + lane;   // IR (lanes 0-8)
+  const int srcB = 12 + lane;  // IDh (lanes 0-8) or IKh (lanes 9-11)
+#pragma unroll
+  for (int f = 0; f < NFQ; ++f) {
+    float2 s3[3];  // SR[a] = IR[a][0] + IR[a][1] + IR[a][2]
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      s3[a] = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+        s3[a] = cadd(s3[a], make_float2(__shfl_sync(0xffffffffu, acc[f].x, 3 + 3 * a + b),
+                                        __shfl_sync(0xffffffffu, acc[f].y, 3 + 3 * a + b)));
+    }
+    const float2 ir = make_float2(__shfl_sync(0xffffffffu, acc[f].x, srcA & 31),
+                                  __shfl_sync(0xffffffffu, acc[f].y, srcA & 31));
+    const float2 sb = make_float2(__shfl_sync(0xffffffffu, acc[f].x, srcB & 31),
+                                  __shfl_sync(0xffffffffu, acc[f].y, srcB & 31));
+    if (lane >= 12) continue;
+    const SingParamsF32& p = cp.f[f];
+    float2* o = out + cp.off[f] + (size_t)kSingOut * warp;
+    if (lane < 9) {
+      const int i = lane;
+      float2 S0 = make_float2(G[kRecS0], 0.f);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) S0 = cadd(S0, make_float2(s3[a].x * jac, s3[a].y * jac));
+      const float2 IR = make_float2(ir.x * jac, ir.y * jac), IDh = make_float2(sb.x * jac, sb.y * jac);
+      const float kk_nn = p.k2 * G[kRecNprod];
+      const float cc = G[kRecCurl + i];
+      const float2 D = make_float2(G[kRecMom + 12 + i] + IDh.x, IDh.y);
+      const float2 IGt = make_float2(G[kRecMom + 3 + i] + IR.x, IR.y);
+      const float2 H = make_float2(cc * S0.x - kk_nn * IGt.x, cc * S0.y - kk_nn * IGt.y);
+      float2 L = cadd(cmul(p.cD, D), cmul(p.cH, H));
+      if (coincident) L = cadd(L, cscale(p.cM, a2 * p.m11m10[i]));
+      o[i] = L;
+    } else {
+      const int a = lane - 9;
+      const float2 sr = a == 0 ? s3[0] : a == 1 ? s3[1] : s3[2];
+      const float2 SR = make_float2(sr.x * jac, sr.y * jac), IKh = make_float2(sb.x * jac, sb.y * jac);
       const float2 S = make_float2(G[kRecMom + a] + SR.x, SR.y);
       const float2 K = make_float2(G[kRecMom + 21 + a] + IKh.x, IKh.y);
       float2 rhs = cadd(cmul(p.cS, S), cmul(p.cK, K));
@@ -1802,10 +2019,103 @@ cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, float* 
   return cudaGetLastError();
 }
 
+double singular_pair_radius(const double* verts, const int* faces, const SingularPair* pairs, int npairs) {
+  double r2 = 0.0;
+  for (int p = 0; p < npairs; ++p) {
+    const int* ft = faces + 3 * (size_t)pairs[p].test;
+    const int* fr = faces + 3 * (size_t)pairs[p].trial;
+    const double sx = tr_sx(pairs[p].tr), sy = tr_sy(pairs[p].tr);
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) {
+        const double* t = verts + 3 * (size_t)ft[a];
+        const double* q = verts + 3 * (size_t)fr[b];
+        const double dx = sx * q[0] - t[0], dy = sy * q[1] - t[1], dz = q[2] - t[2];
+        r2 = std::max(r2, dx * dx + dy * dy + dz * dz);
+      }
+  }
+  return std::sqrt(r2);
+}
+
+namespace {
+// Chebyshev coefficients on r in [0, R] of f1(r) = (e^{ikr} - 1) / r and
+// g2(r) = (1 - (1 - ikr) e^{ikr}) / r^2 (FP64), by interpolation at the N <= kChebN
+// Chebyshev points: f(r) ~ sum_n c_n T_n(2 r / R - 1).  Below z = kr = 1/2 both come from their
+// Taylor series (f1 = k sum_{n>=1} i^n z^(n-1) / n!, g2 = k^2 sum_{n>=2} (n - 1) i^n
+// z^(n-2) / n!), which has no cancellation.  Returns false when the last two coefficients
+// of either are above 1e-9 of its largest: the expansion has not converged (kR too large
+// for N terms) and the caller integrates point by point instead.
+bool cheb_coefficients(double k, double R, int N, double2* c1, double2* c2) {
+  typedef std::complex<double> cd;
+  cd f1[kChebN], g2[kChebN];
+  const double pi = 3.14159265358979323846;
+  for (int j = 0; j < N; ++j) {
+    const double x = std::cos(pi * (j + 0.5) / N), r = 0.5 * R * (1.0 + x), z = k * r;
+    if (z < 0.5) {
+      cd s1(0.0, 0.0), s2(0.0, 0.0), ipow(0.0, 1.0);  // ipow = i^n, from n = 1
+      double zp1 = 1.0, zp2 = 0.0, fact = 1.0;        // z^(n-1), z^(n-2), n!
+      for (int n = 1; n <= 30; ++n) {
+        fact *= n;
+        s1 += ipow * (zp1 / fact);                           // i^n z^(n-1) / n!
+        if (n >= 2) s2 += ipow * ((n - 1) * zp2 / fact);     // i^n (n-1) z^(n-2) / n!
+        zp2 = zp1;
+        zp1 *= z;
+        ipow *= cd(0.0, 1.0);
+      }
+      f1[j] = k * s1;
+      g2[j] = k * k * s2;
+    } else {
+      const double sh = std::sin(0.5 * z), sz = std::sin(z), cz = std::cos(z);
+      const cd e(cz, sz);
+      f1[j] = cd(-2.0 * sh * sh, sz) / r;
+      g2[j] = (cd(1.0, 0.0) - cd(1.0, -z) * e) / (r * r);
+    }
+  }
+  double m1 = 0.0, m2 = 0.0;
+  cd a1[kChebN], a2[kChebN];
+  for (int n = 0; n < N; ++n) {
+    cd s1(0.0, 0.0), s2(0.0, 0.0);
+    for (int j = 0; j < N; ++j) {
+      const double t = std::cos(pi * n * (j + 0.5) / N);
+      s1 += f1[j] * t;
+      s2 += g2[j] * t;
+    }
+    const double sc = (n == 0 ? 1.0 : 2.0) / N;
+    a1[n] = s1 * sc;
+    a2[n] = s2 * sc;
+    m1 = std::max(m1, std::abs(a1[n]));
+    m2 = std::max(m2, std::abs(a2[n]));
+    c1[n] = make_double2(a1[n].real(), a1[n].imag());
+    c2[n] = make_double2(a2[n].real(), a2[n].imag());
+  }
+  const double t1 = std::abs(a1[N - 1]) + std::abs(a1[N - 2]), t2 = std::abs(a2[N - 1]) + std::abs(a2[N - 2]);
+  return t1 <= 1e-9 * m1 && t2 <= 1e-9 * m2;
+}
+}  // namespace
+
+int cheb_terms(double k, double R) {
+  if (!(R > 0.0)) return 0;
+  double2 c1[kChebN], c2[kChebN];
+  for (int n = 8; n <= kChebN; n += 4)
+    if (cheb_coefficients(k, R, n, c1, c2)) return n;
+  return 0;
+}
+
+cudaError_t launch_cheb_moments(const DeviceMesh& m, int nterms, cudaStream_t stream) {
+  if (m.npairs == 0 || !m.cheb || nterms < 4 || nterms > kChebN || nterms % 4 || !(m.cheb_R > 0.0))
+    return cudaErrorInvalidValue;
+  const int threads = 256;
+  const int blocks = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
+  singular_cheb_moments_kernel<<<blocks, threads, 0, stream>>>(m.pairs, m.npairs, m.rule_ptr, m.duffy32, m.pairrec,
+                                                               (float)(2.0 / m.cheb_R), nterms, m.cheb);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, int nfreq, const double* k,
-                                const OperatorCoeffs* c, void* blocks, long long blocks_stride, cudaStream_t stream) {
+                                const OperatorCoeffs* c, void* blocks, long long blocks_stride, cudaStream_t stream,
+                                long long* launched, long long* cheb_freqs) {
   if (m.npairs == 0) return cudaSuccess;
   SingularGeom geo{m.verts, m.faces, m.normal};
+  long long nl = 0;
   if (prec == Precision::Mixed) {
     auto params = [&](int f) {
       SingParamsF32 p;
@@ -1820,28 +2130,79 @@ cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, int nfreq, 
       for (int i = 0; i < 12; ++i) p.m11m10[i] = m.m11m10f[i];
       return p;
     };
-    // two frequencies per launch share each point's geometry; a lone last one runs alone
-    for (int f = 0; f < nfreq;) {
-      float2* o = (float2*)blocks + (size_t)f * blocks_stride;
-      if (f + 1 < nfreq) {
-        SingParamsF32N<2> pn;
-        pn.f[0] = params(f);
-        pn.f[1] = params(f + 1);
-        const int threads = 128;
-        const int nblk = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
-        singular_dyn_f32_kernel<2><<<nblk, threads, 0, stream>>>(m.pairs, m.npairs, m.rule_ptr, m.duffy32, m.pairrec,
-                                                                 pn, o, blocks_stride);
-        f += 2;
-      } else {
-        SingParamsF32N<1> pn;
-        pn.f[0] = params(f);
-        const int threads = 256;
-        const int nblk = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
-        singular_dyn_f32_kernel<1><<<nblk, threads, 0, stream>>>(m.pairs, m.npairs, m.rule_ptr, m.duffy32, m.pairrec,
-                                                                 pn, o, blocks_stride);
-        f += 1;
+    // point by point: two frequencies per launch share each point's geometry; a lone last one runs alone
+    auto direct = [&](int f0, int count) {
+      for (int f = f0; f < f0 + count;) {
+        float2* o = (float2*)blocks + (size_t)f * blocks_stride;
+        if (f + 1 < f0 + count) {
+          SingParamsF32N<2> pn;
+          pn.f[0] = params(f);
+          pn.f[1] = params(f + 1);
+          const int threads = 128;
+          const int nblk = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
+          singular_dyn_f32_kernel<2><<<nblk, threads, 0, stream>>>(m.pairs, m.npairs, m.rule_ptr, m.duffy32,
+                                                                   m.pairrec, pn, o, blocks_stride);
+          f += 2;
+        } else {
+          SingParamsF32N<1> pn;
+          pn.f[0] = params(f);
+          const int threads = 256;
+          const int nblk = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
+          singular_dyn_f32_kernel<1><<<nblk, threads, 0, stream>>>(m.pairs, m.npairs, m.rule_ptr, m.duffy32,
+                                                                   m.pairrec, pn, o, blocks_stride);
+          f += 1;
+        }
+        ++nl;
       }
+    };
+    // through the Chebyshev moments: up to four frequencies per launch read each pair's
+    // moments once; the frequencies whose expansion does not converge with the moments'
+    // terms run point by point, consecutive ones paired
+    std::vector<double2> c1((size_t)nfreq * kChebN), c2((size_t)nfreq * kChebN);
+    std::vector<int> good, bad;
+    for (int f = 0; f < nfreq; ++f) {
+      const bool ok = m.cheb != nullptr && m.cheb_n > 0 && m.cheb_R > 0.0 &&
+                      cheb_coefficients(k[f], m.cheb_R, m.cheb_n, &c1[(size_t)f * kChebN], &c2[(size_t)f * kChebN]);
+      (ok ? good : bad).push_back(f);
     }
+    for (size_t g0 = 0; g0 < good.size(); g0 += 4) {
+      const int w = (int)std::min<size_t>(4, good.size() - g0);
+      const int threads = 128;
+      const int nblk = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
+      auto run = [&](auto nfq_c) {
+        constexpr int NFQ = decltype(nfq_c)::value;
+        ChebParamsF32<NFQ> cp;
+        for (int i = 0; i < NFQ; ++i) {
+          const int f = good[g0 + i];
+          cp.f[i] = params(f);
+          cp.off[i] = (long long)f * blocks_stride;
+          for (int n = 0; n < kChebN; ++n) {
+            const double2 a = c1[(size_t)f * kChebN + n], b = c2[(size_t)f * kChebN + n];
+            cp.c1[i][n] = n < m.cheb_n ? make_float2((float)a.x, (float)a.y) : make_float2(0.f, 0.f);
+            cp.c2[i][n] = n < m.cheb_n ? make_float2((float)b.x, (float)b.y) : make_float2(0.f, 0.f);
+          }
+        }
+        singular_cheb_f32_kernel<NFQ><<<nblk, threads, 0, stream>>>(m.pairs, m.npairs, m.pairrec, m.cheb, m.cheb_n,
+                                                                    cp, (float2*)blocks);
+      };
+      if (w == 4)
+        run(std::integral_constant<int, 4>{});
+      else if (w == 3)
+        run(std::integral_constant<int, 3>{});
+      else if (w == 2)
+        run(std::integral_constant<int, 2>{});
+      else
+        run(std::integral_constant<int, 1>{});
+      ++nl;
+      if (cheb_freqs) *cheb_freqs += w;
+    }
+    for (size_t i = 0; i < bad.size();) {
+      size_t j = i + 1;
+      while (j < bad.size() && bad[j] == bad[j - 1] + 1) ++j;
+      direct(bad[i], (int)(j - i));
+      i = j;
+    }
+    if (launched) *launched += nl;
     return cudaGetLastError();
   }
   const int threads = 256;
@@ -1860,10 +2221,9 @@ cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, int nfreq, 
                                                               m.moments, m.curls, m.area, m.m11m10, p,
                                                               (double2*)blocks + (size_t)f * blocks_stride);
   }
+  if (launched) *launched += nfreq;
   return cudaGetLastError();
 }
-
-int singular_launches(Precision prec, int nfreq) { return prec == Precision::Mixed ? (nfreq + 1) / 2 : nfreq; }
 
 cudaError_t launch_singular_scatter(const DeviceMesh& m, Precision prec, const void* blocks, void* Rext,
                                     long long ldR, cudaStream_t stream) {

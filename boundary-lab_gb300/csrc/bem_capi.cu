@@ -117,7 +117,9 @@ struct bem_mesh {
   int nobs = 0;
   DevBuf driven;
   cudaEvent_t moments_ready = nullptr;  // recorded on ctx->side after the singular moments kernel
+  cudaEvent_t cheb_ready = nullptr;     // recorded on ctx->side after the Chebyshev moments kernel
   long long singular_points = 0;
+  long long mixed_freqs = 0;            // frequencies solved on this mesh in the mixed form, over all calls
 };
 
 namespace {
@@ -250,11 +252,6 @@ Layout layout_for(const bem::DeviceMesh& dm, bem::Precision prec) {
   return L;
 }
 
-// Frequencies assembled together: the mixed form evaluates the regular pairs of
-// up to four frequencies in one launch (shared geometry), each into its own
-// extended-row buffer.
-int assembly_group(bem::Precision prec) { return prec == bem::Precision::Mixed ? 4 : 1; }
-
 // Assemble the LHS (c[i].cD, cH, cM) of cnt frequencies into A[i] (and A2[i] if
 // given; column-major, leading dimension lda) and, if nc > 0, the RHS into b[i]
 // (nc columns, leading dimension ldb, permuted rows).  lda / ldb <= 0: the mesh's
@@ -262,7 +259,7 @@ int assembly_group(bem::Precision prec) { return prec == bem::Precision::Mixed ?
 long long assemble_frequencies(bem_context* ctx, bem_mesh* m, bem::Precision prec, int cnt, const double* k,
                                const bem::OperatorCoeffs* c, void* const* A, void* const* A2, const double2* qscale,
                                int nc, const void* drive, void* const* b, long long lda = 0, long long ldb = 0,
-                               double* regular_flop = nullptr) {
+                               double* regular_flop = nullptr, long long* cheb_freqs = nullptr) {
   const bem::DeviceMesh& dm = m->dm;
   Layout L = layout_for(dm, prec);
   if (lda > 0) L.lda = lda;
@@ -293,7 +290,10 @@ long long assemble_frequencies(bem_context* ctx, bem_mesh* m, bem::Precision pre
        "regular kernel");
     prof_mark(ctx, BEM_K_REGULAR);
     if (m->moments_ready) ck(cudaStreamWaitEvent(ctx->stream, m->moments_ready, 0), "wait for singular moments");
-    ck(bem::launch_singular_dyn(dm, prec, g, k + f0, c + f0, sblk(0), (long long)sblk_n, ctx->stream),
+    if (m->cheb_ready) ck(cudaStreamWaitEvent(ctx->stream, m->cheb_ready, 0), "wait for Chebyshev moments");
+    long long sing_launches = 0;
+    ck(bem::launch_singular_dyn(dm, prec, g, k + f0, c + f0, sblk(0), (long long)sblk_n, ctx->stream,
+                                &sing_launches, cheb_freqs),
        "singular kernel");
     prof_mark(ctx, BEM_K_SINGULAR);
     for (int i = 0; i < g; ++i) {
@@ -316,7 +316,7 @@ long long assemble_frequencies(bem_context* ctx, bem_mesh* m, bem::Precision pre
     // per frequency: scatter, gather (+ isolated rows); per group the regular, singular and
     // right-hand-side launches
     launches += (long long)g * (2 + (dm.n_isolated ? 1 : 0)) + (nc > 0 ? bem::rhs_launches(prec, nc, g) : 0) +
-                bem::regular_launches(dm, prec, g) + bem::singular_launches(prec, g);
+                bem::regular_launches(dm, prec, g) + sing_launches;
     if (regular_flop && prec == bem::Precision::Mixed) {
       const double qpairs = ((double)dm.ntr * dm.nf * dm.nf - dm.npairs) * dm.Q * dm.Q;
       *regular_flop += g * qpairs * bem::regular_flop_per_qpair(g);
@@ -331,7 +331,12 @@ void assemble_one(bem_mesh* m, bem::Precision prec, double k, const bem::Operato
 }
 
 void free_mesh_device(bem_mesh* m) {
-  if (m->moments_ready) {  // the side stream may still read the mesh data
+  if (m->cheb_ready) {  // the side stream may still read the mesh data
+    cudaStreamWaitEvent(m->ctx->stream, m->cheb_ready, 0);
+    cudaEventDestroy(m->cheb_ready);
+    m->cheb_ready = nullptr;
+  }
+  if (m->moments_ready) {
     cudaStreamWaitEvent(m->ctx->stream, m->moments_ready, 0);
     cudaEventDestroy(m->moments_ready);
     m->moments_ready = nullptr;
@@ -550,6 +555,10 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
         d.moments = (double*)mesh_alloc(m, (size_t)d.npairs * 24 * sizeof(double), "allocate singular moments");
         d.pairrec = (float*)mesh_alloc(m, (size_t)d.npairs * bem::kPairRec * sizeof(float), "allocate pair records");
         d.pairgeo_df = (float*)mesh_alloc(m, (size_t)d.npairs * bem::kPairGeoDf * sizeof(float), "allocate pair geometry");
+        // the Chebyshev expansion interval of the singular remainder: every point distance
+        // of a pair lies below the largest distance between its vertices (a little margin
+        // for rounding); the moments themselves are formed by the first sweep that uses them
+        d.cheb_R = 1.000001 * bem::singular_pair_radius(P.verts.data(), P.faces.data(), P.pairs.data(), d.npairs);
       }
       ck(cudaStreamSynchronize(ctx->stream), "mesh upload");
       if (d.npairs > 0) {
@@ -767,6 +776,7 @@ struct Slice {
 struct SolveTotals {
   double kacc[BEM_K_SLOTS] = {0};
   double regular_flop = 0;
+  long long cheb_freqs = 0;
   double t_asm = 0, t_sol = 0, t_fld = 0, max_res = 0;
   int max_steps = 0, batches = 0, gemm_used = 0;
   long long launches = 0;
@@ -845,7 +855,7 @@ void solve_combined(bem_context* ctx, const std::vector<Slice>& sl, int n, const
     const void* drive = mixed ? x.m->drive32.p : x.m->drive64.p;
     T.launches += assemble_frequencies(ctx, x.m, prec, x.cnt, ks.data() + i0, cs.data() + i0, As.data() + i0,
                                        mixed ? A2s.data() + i0 : nullptr, qs.data() + i0, nc, drive, bs.data() + i0,
-                                       lda, ldb, &T.regular_flop);
+                                       lda, ldb, &T.regular_flop, &T.cheb_freqs);
     if (nvm < n) {
       dim3 g((unsigned)n, (unsigned)x.cnt);
       if (mixed)
@@ -1000,6 +1010,7 @@ void fill_stats(bem_solve_stats* stats, const SolveTotals& T) {
   stats->lu_gemm_used = T.gemm_used;
   stats->kernel_launches = T.launches;
   stats->regular_flop = T.regular_flop;
+  stats->singular_cheb_freqs = T.cheb_freqs;
 }
 
 bool valid_options(bem_context* ctx, const bem_solve_options& o) {
@@ -1045,7 +1056,8 @@ long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int np
   const long long group = precision == BEM_PRECISION_MIXED ? 4 : 1;        // frequencies assembled together
   bytes += round_up(n_ext, 32) * 3LL * nf * esz * group;                    // extended rows
   bytes += (long long)batch * lda * nv * esz * (precision == BEM_PRECISION_MIXED ? 2 : 1);  // matrices (+copy)
-  bytes += (long long)npairs * (12 * esz * group + 24 * 8 + 48 + (bem::kPairRec + bem::kPairGeoDf) * 4 + 96);  // singular blocks, moments, pairs, records, scatter plan
+  bytes += (long long)npairs * (12 * esz * group + 24 * 8 + 48 + (bem::kPairRec + bem::kPairGeoDf) * 4 + 96 +
+                                bem::kChebN * 24 * 4);  // singular blocks, moments, pairs, records, scatter plan, Chebyshev moments
   bytes += (long long)batch * nrhs * lda * (esz + 3 * 16 + 16);             // rhs, x, r, b64, d
   bytes += (long long)batch * nrhs * ((long long)nf * 6 * esz + (long long)npts * 16);  // field sources + out
   bytes += (long long)nf * (2 * 160 + 288 + 64);                            // face records (+ lane-group copy), maps
@@ -1054,6 +1066,47 @@ long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int np
   bytes += 64LL << 20;                                                      // cuBLAS workspace and slack
   return bytes;
 }
+
+namespace {
+// Mixed-form frequencies a mesh must have been solved at (over all calls, this one
+// included) before its Chebyshev moments are formed: forming them costs about as much as
+// 15 frequencies of the point-by-point singular kernel, and each frequency through them
+// costs a tenth of one.  A job's sweep usually arrives in several calls (one per batch
+// and lane), so the count is kept per mesh, not per call.
+constexpr int kChebMinFreqs = 16;
+
+// Forms (or extends) the mesh's Chebyshev moments on the side stream for a sweep whose
+// highest wavenumber is k_max: with the fewest terms (a multiple of four) that expand the
+// remainder at k_max, or twice the terms it had, up to kChebN.  Nothing when the sweep is
+// short or even kChebN terms do not converge at k_max (its lower frequencies then still use
+// moments formed by an earlier sweep, if any).
+void ensure_cheb(bem_context* ctx, bem_mesh* m, double k_max) {
+  bem::DeviceMesh& d = m->dm;
+  if (d.npairs == 0 || !(d.cheb_R > 0.0)) return;
+  const int need = bem::cheb_terms(k_max, d.cheb_R);
+  if (need == 0 || d.cheb_n >= need) return;
+  const int nterms = std::min(bem::kChebN, std::max(need, 2 * d.cheb_n));
+  if (!d.cheb)
+    d.cheb = (float*)mesh_alloc(m, (size_t)d.npairs * bem::kChebN * 24 * sizeof(float), "allocate Chebyshev moments");
+  // the side stream must see the allocation (made on the context's stream), the pair
+  // records (written on the side stream) are in order there, and no singular kernel of an
+  // earlier sweep may still read the moments being rewritten
+  // (nor one still running on a lane's stream)
+  std::vector<cudaStream_t> before{ctx->stream};
+  for (bem_context* cl : ctx->lanes) before.push_back(cl->stream);
+  for (cudaStream_t st : before) {
+    cudaEvent_t ev = nullptr;
+    ck(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "create event");
+    ck(cudaEventRecord(ev, st), "record event");
+    ck(cudaStreamWaitEvent(ctx->side, ev, 0), "wait for an earlier stream");
+    cudaEventDestroy(ev);
+  }
+  ck(bem::launch_cheb_moments(d, nterms, ctx->side), "Chebyshev moments kernel");
+  if (!m->cheb_ready) ck(cudaEventCreateWithFlags(&m->cheb_ready, cudaEventDisableTiming), "create event");
+  ck(cudaEventRecord(m->cheb_ready, ctx->side), "record event");
+  d.cheb_n = nterms;
+}
+}  // namespace
 
 int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const bem_solve_options* opt,
                           double* pressure_out, double* field_out, bem_solve_stats* stats) {
@@ -1068,6 +1121,8 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
     if (field_out && m->nobs < 1) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "no observation points set");
     if (!valid_options(ctx, o)) return BEM_ERR_INVALID_ARGUMENT;
     const bem::Precision prec = o.precision == BEM_PRECISION_MIXED ? bem::Precision::Mixed : bem::Precision::FP64;
+    if (prec == bem::Precision::Mixed && (m->mixed_freqs += n_freq) >= kChebMinFreqs)
+      ensure_cheb(ctx, m, 2.0 * M_PI * *std::max_element(freqs_hz, freqs_hz + n_freq) / o.sound_speed);
     const bem::DeviceMesh& dm = m->dm;
     const int nv = dm.nv, nc = m->nc;
     int B = o.batch > 0 ? std::min(o.batch, 64) : auto_batch(m, prec, n_freq);
@@ -1122,6 +1177,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
       for (const SolveTotals& T2 : TL) {
         for (int i = 0; i < BEM_K_SLOTS; ++i) T.kacc[i] += T2.kacc[i];
         T.regular_flop += T2.regular_flop;
+        T.cheb_freqs += T2.cheb_freqs;
         T.t_asm += T2.t_asm;
         T.t_sol += T2.t_sol;
         T.t_fld += T2.t_fld;

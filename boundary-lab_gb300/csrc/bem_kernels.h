@@ -63,6 +63,12 @@ struct DeviceMesh {
   float* pairgeo_df = nullptr;  // npairs x kPairGeoDf: per-pair geometry as double-float (moments kernel)
   double* moments = nullptr;
   float* pairrec = nullptr;  // npairs x kPairRec: FP32 record of each pair for the mixed-form singular kernel
+  // Chebyshev moments of the singular remainder (mixed form; npairs x kChebN x 24 floats, see
+  // singular_cheb_moments_kernel) on r in [0, cheb_R], cheb_R bounding every vertex-sharing
+  // pair's point distances; allocated by the first sweep that uses them
+  float* cheb = nullptr;
+  double cheb_R = 0.0;
+  int cheb_n = 0;  // terms the moments hold (0: none yet)
   double* verts = nullptr;
   int* faces = nullptr;
   double* normal = nullptr;
@@ -101,13 +107,25 @@ cudaError_t launch_regular_f64(const DeviceMesh& m, double k, double2 cD, double
                                cudaStream_t stream);
 // Per-pair FP32 record written at upload by the pair setup and moments kernels (see bem_assembly.cu).
 constexpr int kPairRec = 64;
+// Chebyshev terms of the mixed form's singular remainder expansion (bem_assembly.cu).
+constexpr int kChebN = 24;
 constexpr int kPairGeoDf = 48;
 cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, float* pairrec, cudaStream_t stream);
 // Singular blocks of nfreq frequencies; frequency f's blocks start at element
 // f * blocks_stride of blocks (the mixed form takes two frequencies per launch).
+// Adds the kernels it launched to *launched and the frequencies it formed from the mesh's
+// Chebyshev moments to *cheb_freqs (when not null).
 cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, int nfreq, const double* k,
-                                const OperatorCoeffs* c, void* blocks, long long blocks_stride, cudaStream_t stream);
-int singular_launches(Precision prec, int nfreq);
+                                const OperatorCoeffs* c, void* blocks, long long blocks_stride, cudaStream_t stream,
+                                long long* launched = nullptr, long long* cheb_freqs = nullptr);
+// Chebyshev terms (a multiple of four, 8..kChebN) that expand the singular remainder of
+// wavenumber k on [0, R] to 1e-9; 0 when kChebN terms are not enough.
+int cheb_terms(double k, double R);
+// The mesh's Chebyshev moments for the first nterms terms into m.cheb (after the pair setup).
+cudaError_t launch_cheb_moments(const DeviceMesh& m, int nterms, cudaStream_t stream);
+// Largest distance between a point of a vertex-sharing pair's test face and one of its trial
+// face (the trial face reflected for image pairs): the maximum over vertex pairs.
+double singular_pair_radius(const double* verts, const int* faces, const SingularPair* pairs, int npairs);
 cudaError_t launch_singular_scatter(const DeviceMesh& m, Precision prec, const void* blocks, void* Rext,
                                     long long ldR, cudaStream_t stream);
 cudaError_t launch_gather(const DeviceMesh& m, Precision prec, const void* Rext, long long ldR, void* A, long long lda,

@@ -18,8 +18,7 @@
 //    own face records and sources; nothing in it has to start at zero, because
 //    each call writes every scratch entry it later reads.
 //  * The first call on a device looks up the device address of the scratch
-//    array (cudaGetSymbolAddress) with that device current, so make the first
-//    call on each device before any stream capture begins.  The address is kept
+//    array (cudaGetSymbolAddress) with that device current.  The address is kept
 //    for the life of the process: do not use the entry point across a
 //    cudaDeviceReset of that device.  The stream must belong to the current
 //    device (checked).

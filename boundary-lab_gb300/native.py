@@ -122,6 +122,7 @@ class SolveStats(ctypes.Structure):
         ("lu_gemm_used", ctypes.c_int),
         ("kernel_launches", ctypes.c_longlong),
         ("regular_flop", ctypes.c_double),
+        ("singular_cheb_freqs", ctypes.c_longlong),
     ]
 
 KERNEL_SLOTS = ("singular", "regular", "gather", "rhs", "lu", "solve", "field")
@@ -210,7 +211,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         lib.bem_evaluate_field_noalloc.argtypes = [vp, ip, vp, ip, ip, ctypes.c_double, vp, vp, vp, ip, ip, vp, vp,
                                                    ctypes.c_char_p, ip]
         lib.bem_evaluate_field_noalloc.restype = ip
-        if lib.bem_abi_version() != 2:
+        if lib.bem_abi_version() != 3:
             raise NativeLibraryError(f"unexpected ABI version {lib.bem_abi_version()} in {path}")
         _lib = lib
         return lib

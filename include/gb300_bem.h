@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define GB300_BEM_ABI_VERSION 2
+#define GB300_BEM_ABI_VERSION 3
 
 typedef struct bem_context bem_context;
 typedef struct bem_mesh bem_mesh;
@@ -156,6 +156,8 @@ typedef struct bem_solve_stats {
   double regular_flop;    /* mixed form: FP32 flop (FMA = 2) the regular-pair kernel executed in the call,
                              counted from its source per quadrature pair and frequency: 35.67 + 26.83 / w,
                              w = frequencies sharing one launch's frequency-independent geometry */
+  long long singular_cheb_freqs; /* mixed form: frequencies whose singular remainder was formed from the
+                                    mesh's Chebyshev moments (the rest point by point on the Duffy rules) */
 } bem_solve_stats;
 
 void bem_default_options(bem_solve_options* opt);
@@ -248,7 +250,7 @@ int bem_evaluate_field(bem_mesh* mesh, double k, int precision, const double* pr
  * array: calls whose work overlaps on the GPU race and must be serialised by the
  * caller.  The first call on a device resolves the scratch address with that
  * device current (kept for the process's life: not valid across a
- * cudaDeviceReset); make that first call before any stream capture.  `stream` is
+ * cudaDeviceReset).  `stream` is
  * a cudaStream_t of the current device (NULL = legacy default stream); the call
  * synchronises that stream before it returns.  On an error return the contents
  * of field_out are undefined (an out-of-range vertex index or a zero-area

@@ -100,6 +100,54 @@ def test_bm_lhs_mixed_matches_oracle(gpu_ctx, native, box_small):
     assert rel(A, lhs) < 2e-6
 
 
+@pytest.mark.parametrize("freq", [2000.0, 12000.0])
+def test_singular_remainder_both_paths(gpu_ctx, native, box_small, freq):
+    """The mixed form integrates the singular remainder through the mesh's Chebyshev
+    moments, which a sweep of at least 16 frequencies forms, while their expansion on the
+    pair radius R (0.104 m on this coarse box) converges; otherwise point by point on the
+    Duffy rules.  After a 16-frequency sweep up to 2.5 kHz (all 16 through the moments),
+    2 kHz (kR = 3.8) takes the moments and 12 kHz (kR = 22.8) the point-by-point kernel.
+    Both must give the full BM operator and the right-hand-side operator to 2e-6."""
+    O = _oracle()
+    k = 2 * np.pi * freq / 343.0
+    rng = np.random.default_rng(11)
+    q = rng.normal(size=(box_small.n_faces, 1)) + 1j * rng.normal(size=(box_small.n_faces, 1))
+    m = gpu_ctx.upload_mesh(box_small.vertices, box_small.faces)
+    try:
+        m.set_excitation((box_small.tags == meshes.RADIATOR_TAG).astype(np.complex128)[None, :])
+        m.set_observation_points(np.array([[0.0, 0.0, 2.0]]))
+        _, _, st = m.solve(np.geomspace(300.0, 2500.0, 16), precision=native.BEM_PRECISION_MIXED)
+        assert st["singular_cheb_freqs"] == 16
+        _, _, st = m.solve([2000.0, 12000.0], precision=native.BEM_PRECISION_MIXED)
+        assert st["singular_cheb_freqs"] == 1  # 2 kHz only
+        A = m.assemble_lhs(k, precision=native.BEM_PRECISION_MIXED)
+        Sq = m.apply_rhs_operator(k, q, coeffs=(1.0, 0.0, 0.0), precision=native.BEM_PRECISION_MIXED)
+        Kq = m.apply_rhs_operator(k, q, coeffs=(0.0, 1.0, 0.0), precision=native.BEM_PRECISION_MIXED)
+    finally:
+        m.release()
+    ops = O.assemble(box_small, k)
+    M11, M10 = O.mass(box_small)
+    lhs, _ = O.burton_miller_matrices(ops, M11, M10, k)
+    assert rel(A, lhs) < 2e-6
+    assert rel(Sq, ops.single_layer @ q) < 2e-6
+    assert rel(Kq, ops.adjoint_double_layer @ q) < 2e-6
+
+
+def test_moments_form_after_sixteen_frequencies(gpu_ctx, native, sphere320):
+    """A mesh solved at fewer than 16 frequencies (over all calls) integrates point by
+    point; the call that brings the count to 16 forms the moments and uses them."""
+    m = gpu_ctx.upload_mesh(sphere320.vertices, sphere320.faces)
+    try:
+        m.set_excitation((sphere320.tags == meshes.RADIATOR_TAG).astype(np.complex128)[None, :])
+        m.set_observation_points(np.array([[0.0, 0.0, 2.0]]))
+        _, _, st = m.solve(np.geomspace(300.0, 900.0, 8), precision=native.BEM_PRECISION_MIXED)
+        assert st["singular_cheb_freqs"] == 0
+        _, _, st = m.solve(np.geomspace(1000.0, 2500.0, 8), precision=native.BEM_PRECISION_MIXED)
+        assert st["singular_cheb_freqs"] == 8
+    finally:
+        m.release()
+
+
 @pytest.mark.parametrize("precision,tol", [(0, 1e-11), (1, 2e-6)])
 def test_rhs_operator_matches_oracle(gpu_ctx, native, box_small, precision, tol):
     O = _oracle()

@@ -203,7 +203,7 @@ def test_library_exports_every_header_symbol():
     assert declared and declared == set(native.EXPORTED_SYMBOLS)
     for name in declared:
         assert hasattr(lib, name), name
-    assert lib.bem_abi_version() == 2
+    assert lib.bem_abi_version() == 3
     assert lib_path.exists()
 
 
