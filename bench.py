@@ -421,10 +421,12 @@ def main() -> None:
     # per-lane stage intervals of the timed region, summed over the lanes: with two lanes
     # the stages of one overlap the other's, so each interval includes the other lane's work
     lane_sum_ms = {k: 1e3 * v / (args.steps * SB) for k, v in kernel_s.items()}
-    # stage breakdown of one batch on one lane, after the timed region (nothing overlaps it)
-    st1 = m.solve_device(step_freqs(0)[:B], p_dev.data_ptr(), u_dev.data_ptr(), profile=1, **{**opts, "lanes": 1})
+    # stage breakdown of one step's frequencies on one lane, after the timed region (nothing
+    # overlaps it; a call of the timed calls' size takes the same kernels, e.g. the singular
+    # remainder through the Chebyshev moments in calls of at least 12 frequencies)
+    st1 = m.solve_device(step_freqs(0), p_dev.data_ptr(), u_dev.data_ptr(), profile=1, **{**opts, "lanes": 1})
     torch.cuda.synchronize()
-    nb1 = len(step_freqs(0)[:B])
+    nb1 = len(step_freqs(0))
     per_freq_ms = {k: 1e3 * v / nb1 for k, v in st1["kernel_s"].items()}
 
     result = {
@@ -446,7 +448,7 @@ def main() -> None:
         "clocks": clocks.summary(),
         "launch": {"batch": B, "lanes": lanes, "lu_block": args.lu_block, "lu_gemm": args.lu_gemm},
         "autotune": tune_info,
-        "stage_ms_per_freq": per_freq_ms,  # one batch on one lane, after the timed region
+        "stage_ms_per_freq": per_freq_ms,  # one step's frequencies on one lane, after the timed region
         "stage_ms_per_freq_lane_sums": lane_sum_ms if lanes > 1 else None,
         "step_ms": step_ms,
         # timed region minus the steps: the L2 flushes and host time between steps

@@ -2112,7 +2112,7 @@ cudaError_t launch_cheb_moments(const DeviceMesh& m, int nterms, cudaStream_t st
 
 cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, int nfreq, const double* k,
                                 const OperatorCoeffs* c, void* blocks, long long blocks_stride, cudaStream_t stream,
-                                long long* launched, long long* cheb_freqs) {
+                                long long* launched, long long* cheb_freqs, bool use_cheb) {
   if (m.npairs == 0) return cudaSuccess;
   SingularGeom geo{m.verts, m.faces, m.normal};
   long long nl = 0;
@@ -2156,14 +2156,22 @@ cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, int nfreq, 
       }
     };
     // through the Chebyshev moments: up to four frequencies per launch read each pair's
-    // moments once; the frequencies whose expansion does not converge with the moments'
-    // terms run point by point, consecutive ones paired
-    std::vector<double2> c1((size_t)nfreq * kChebN), c2((size_t)nfreq * kChebN);
-    std::vector<int> good, bad;
+    // moments once.  Frequency f uses exactly the N(k_f) terms its expansion needs
+    // (cheb_terms; the coefficients beyond are zero), so its blocks do not depend on how
+    // many terms the moments hold or on which frequencies share the launch.  Frequencies
+    // whose expansion needs more terms than the moments hold, or none converges, run point
+    // by point, consecutive ones paired.
+    std::vector<double2> c1((size_t)nfreq * kChebN, make_double2(0.0, 0.0)), c2((size_t)nfreq * kChebN,
+                                                                              make_double2(0.0, 0.0));
+    std::vector<int> good, bad, terms(nfreq, 0);
     for (int f = 0; f < nfreq; ++f) {
-      const bool ok = m.cheb != nullptr && m.cheb_n > 0 && m.cheb_R > 0.0 &&
-                      cheb_coefficients(k[f], m.cheb_R, m.cheb_n, &c1[(size_t)f * kChebN], &c2[(size_t)f * kChebN]);
-      (ok ? good : bad).push_back(f);
+      if (use_cheb && m.cheb != nullptr && m.cheb_n > 0 && m.cheb_R > 0.0) {
+        const int nt = cheb_terms(k[f], m.cheb_R);
+        if (nt > 0 && nt <= m.cheb_n &&
+            cheb_coefficients(k[f], m.cheb_R, nt, &c1[(size_t)f * kChebN], &c2[(size_t)f * kChebN]))
+          terms[f] = nt;
+      }
+      (terms[f] > 0 ? good : bad).push_back(f);
     }
     for (size_t g0 = 0; g0 < good.size(); g0 += 4) {
       const int w = (int)std::min<size_t>(4, good.size() - g0);
@@ -2172,18 +2180,20 @@ cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, int nfreq, 
       auto run = [&](auto nfq_c) {
         constexpr int NFQ = decltype(nfq_c)::value;
         ChebParamsF32<NFQ> cp;
+        int nmax = 0;
         for (int i = 0; i < NFQ; ++i) {
           const int f = good[g0 + i];
           cp.f[i] = params(f);
           cp.off[i] = (long long)f * blocks_stride;
+          nmax = std::max(nmax, terms[f]);
           for (int n = 0; n < kChebN; ++n) {
             const double2 a = c1[(size_t)f * kChebN + n], b = c2[(size_t)f * kChebN + n];
-            cp.c1[i][n] = n < m.cheb_n ? make_float2((float)a.x, (float)a.y) : make_float2(0.f, 0.f);
-            cp.c2[i][n] = n < m.cheb_n ? make_float2((float)b.x, (float)b.y) : make_float2(0.f, 0.f);
+            cp.c1[i][n] = n < terms[f] ? make_float2((float)a.x, (float)a.y) : make_float2(0.f, 0.f);
+            cp.c2[i][n] = n < terms[f] ? make_float2((float)b.x, (float)b.y) : make_float2(0.f, 0.f);
           }
         }
-        singular_cheb_f32_kernel<NFQ><<<nblk, threads, 0, stream>>>(m.pairs, m.npairs, m.pairrec, m.cheb, m.cheb_n,
-                                                                    cp, (float2*)blocks);
+        singular_cheb_f32_kernel<NFQ><<<nblk, threads, 0, stream>>>(m.pairs, m.npairs, m.pairrec, m.cheb, nmax, cp,
+                                                                    (float2*)blocks);
       };
       if (w == 4)
         run(std::integral_constant<int, 4>{});

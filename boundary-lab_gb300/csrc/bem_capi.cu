@@ -119,7 +119,6 @@ struct bem_mesh {
   cudaEvent_t moments_ready = nullptr;  // recorded on ctx->side after the singular moments kernel
   cudaEvent_t cheb_ready = nullptr;     // recorded on ctx->side after the Chebyshev moments kernel
   long long singular_points = 0;
-  long long mixed_freqs = 0;            // frequencies solved on this mesh in the mixed form, over all calls
 };
 
 namespace {
@@ -252,6 +251,45 @@ Layout layout_for(const bem::DeviceMesh& dm, bem::Precision prec) {
   return L;
 }
 
+// Frequencies a mixed-form call needs before its singular remainders go through the mesh's
+// Chebyshev moments: forming them costs about as much as 15 frequencies of the point-by-
+// point singular kernel at the full 24 terms (fewer terms cost proportionally less), and
+// each frequency through them costs a tenth of one.  A shorter call runs point by point
+// even when the moments exist, so a call's results depend on its own inputs only.
+constexpr int kChebMinFreqs = 12;
+
+// Forms (or extends) the mesh's Chebyshev moments on the side stream for the call's
+// wavenumbers k[0..n): with the fewest terms (a multiple of four) that cover every
+// frequency whose expansion converges within kChebN terms, or twice the terms the moments
+// had, up to kChebN.  Nothing when no frequency converges (those run point by point).
+void ensure_cheb(bem_context* ctx, bem_mesh* m, const double* k, int n) {
+  bem::DeviceMesh& d = m->dm;
+  if (d.npairs == 0 || !(d.cheb_R > 0.0)) return;
+  int need = 0;
+  for (int i = 0; i < n; ++i) need = std::max(need, bem::cheb_terms(k[i], d.cheb_R));
+  if (need == 0 || d.cheb_n >= need) return;
+  const int nterms = std::min(bem::kChebN, std::max(need, 2 * d.cheb_n));
+  if (!d.cheb)
+    d.cheb = (float*)mesh_alloc(m, (size_t)d.npairs * bem::kChebN * 24 * sizeof(float), "allocate Chebyshev moments");
+  // the side stream must see the allocation (made on the context's stream), the pair
+  // records (written on the side stream) are in order there, and no singular kernel of an
+  // earlier sweep may still read the moments being rewritten
+  // (nor one still running on a lane's stream)
+  std::vector<cudaStream_t> before{ctx->stream};
+  for (bem_context* cl : ctx->lanes) before.push_back(cl->stream);
+  for (cudaStream_t st : before) {
+    cudaEvent_t ev = nullptr;
+    ck(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "create event");
+    ck(cudaEventRecord(ev, st), "record event");
+    ck(cudaStreamWaitEvent(ctx->side, ev, 0), "wait for an earlier stream");
+    cudaEventDestroy(ev);
+  }
+  ck(bem::launch_cheb_moments(d, nterms, ctx->side), "Chebyshev moments kernel");
+  if (!m->cheb_ready) ck(cudaEventCreateWithFlags(&m->cheb_ready, cudaEventDisableTiming), "create event");
+  ck(cudaEventRecord(m->cheb_ready, ctx->side), "record event");
+  d.cheb_n = nterms;
+}
+
 // Assemble the LHS (c[i].cD, cH, cM) of cnt frequencies into A[i] (and A2[i] if
 // given; column-major, leading dimension lda) and, if nc > 0, the RHS into b[i]
 // (nc columns, leading dimension ldb, permuted rows).  lda / ldb <= 0: the mesh's
@@ -259,7 +297,8 @@ Layout layout_for(const bem::DeviceMesh& dm, bem::Precision prec) {
 long long assemble_frequencies(bem_context* ctx, bem_mesh* m, bem::Precision prec, int cnt, const double* k,
                                const bem::OperatorCoeffs* c, void* const* A, void* const* A2, const double2* qscale,
                                int nc, const void* drive, void* const* b, long long lda = 0, long long ldb = 0,
-                               double* regular_flop = nullptr, long long* cheb_freqs = nullptr) {
+                               double* regular_flop = nullptr, long long* cheb_freqs = nullptr,
+                               bool use_cheb = false) {
   const bem::DeviceMesh& dm = m->dm;
   Layout L = layout_for(dm, prec);
   if (lda > 0) L.lda = lda;
@@ -293,7 +332,7 @@ long long assemble_frequencies(bem_context* ctx, bem_mesh* m, bem::Precision pre
     if (m->cheb_ready) ck(cudaStreamWaitEvent(ctx->stream, m->cheb_ready, 0), "wait for Chebyshev moments");
     long long sing_launches = 0;
     ck(bem::launch_singular_dyn(dm, prec, g, k + f0, c + f0, sblk(0), (long long)sblk_n, ctx->stream,
-                                &sing_launches, cheb_freqs),
+                                &sing_launches, cheb_freqs, use_cheb),
        "singular kernel");
     prof_mark(ctx, BEM_K_SINGULAR);
     for (int i = 0; i < g; ++i) {
@@ -325,9 +364,14 @@ long long assemble_frequencies(bem_context* ctx, bem_mesh* m, bem::Precision pre
   return launches;
 }
 
+// One frequency's operators as a long sweep assembles them (the mixed form's singular
+// remainder through the mesh's Chebyshev moments wherever their expansion converges).
 void assemble_one(bem_mesh* m, bem::Precision prec, double k, const bem::OperatorCoeffs& c, void* A, void* A2,
                   double2 qscale, int nc, const void* drive, void* b) {
-  assemble_frequencies(m->ctx, m, prec, 1, &k, &c, &A, A2 ? &A2 : nullptr, &qscale, nc, drive, &b);
+  const bool cheb = prec == bem::Precision::Mixed;
+  if (cheb) ensure_cheb(m->ctx, m, &k, 1);
+  assemble_frequencies(m->ctx, m, prec, 1, &k, &c, &A, A2 ? &A2 : nullptr, &qscale, nc, drive, &b, 0, 0, nullptr,
+                       nullptr, cheb);
 }
 
 void free_mesh_device(bem_mesh* m) {
@@ -770,6 +814,7 @@ struct Slice {
   int cnt;
   double* pressure_out;  // [cnt][nc][nv] complex
   double* field_out;     // [cnt][nc][nobs] complex
+  bool cheb = false;     // mixed form: singular remainders through the mesh's Chebyshev moments
 };
 
 // Totals over the batches of one call.
@@ -855,7 +900,7 @@ void solve_combined(bem_context* ctx, const std::vector<Slice>& sl, int n, const
     const void* drive = mixed ? x.m->drive32.p : x.m->drive64.p;
     T.launches += assemble_frequencies(ctx, x.m, prec, x.cnt, ks.data() + i0, cs.data() + i0, As.data() + i0,
                                        mixed ? A2s.data() + i0 : nullptr, qs.data() + i0, nc, drive, bs.data() + i0,
-                                       lda, ldb, &T.regular_flop, &T.cheb_freqs);
+                                       lda, ldb, &T.regular_flop, &T.cheb_freqs, x.cheb);
     if (nvm < n) {
       dim3 g((unsigned)n, (unsigned)x.cnt);
       if (mixed)
@@ -1067,47 +1112,6 @@ long long bem_estimate_device_bytes(int nv, int nf, int npairs, int nrhs, int np
   return bytes;
 }
 
-namespace {
-// Mixed-form frequencies a mesh must have been solved at (over all calls, this one
-// included) before its Chebyshev moments are formed: forming them costs about as much as
-// 15 frequencies of the point-by-point singular kernel, and each frequency through them
-// costs a tenth of one.  A job's sweep usually arrives in several calls (one per batch
-// and lane), so the count is kept per mesh, not per call.
-constexpr int kChebMinFreqs = 16;
-
-// Forms (or extends) the mesh's Chebyshev moments on the side stream for a sweep whose
-// highest wavenumber is k_max: with the fewest terms (a multiple of four) that expand the
-// remainder at k_max, or twice the terms it had, up to kChebN.  Nothing when the sweep is
-// short or even kChebN terms do not converge at k_max (its lower frequencies then still use
-// moments formed by an earlier sweep, if any).
-void ensure_cheb(bem_context* ctx, bem_mesh* m, double k_max) {
-  bem::DeviceMesh& d = m->dm;
-  if (d.npairs == 0 || !(d.cheb_R > 0.0)) return;
-  const int need = bem::cheb_terms(k_max, d.cheb_R);
-  if (need == 0 || d.cheb_n >= need) return;
-  const int nterms = std::min(bem::kChebN, std::max(need, 2 * d.cheb_n));
-  if (!d.cheb)
-    d.cheb = (float*)mesh_alloc(m, (size_t)d.npairs * bem::kChebN * 24 * sizeof(float), "allocate Chebyshev moments");
-  // the side stream must see the allocation (made on the context's stream), the pair
-  // records (written on the side stream) are in order there, and no singular kernel of an
-  // earlier sweep may still read the moments being rewritten
-  // (nor one still running on a lane's stream)
-  std::vector<cudaStream_t> before{ctx->stream};
-  for (bem_context* cl : ctx->lanes) before.push_back(cl->stream);
-  for (cudaStream_t st : before) {
-    cudaEvent_t ev = nullptr;
-    ck(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "create event");
-    ck(cudaEventRecord(ev, st), "record event");
-    ck(cudaStreamWaitEvent(ctx->side, ev, 0), "wait for an earlier stream");
-    cudaEventDestroy(ev);
-  }
-  ck(bem::launch_cheb_moments(d, nterms, ctx->side), "Chebyshev moments kernel");
-  if (!m->cheb_ready) ck(cudaEventCreateWithFlags(&m->cheb_ready, cudaEventDisableTiming), "create event");
-  ck(cudaEventRecord(m->cheb_ready, ctx->side), "record event");
-  d.cheb_n = nterms;
-}
-}  // namespace
-
 int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const bem_solve_options* opt,
                           double* pressure_out, double* field_out, bem_solve_stats* stats) {
   if (!m) return BEM_ERR_INVALID_ARGUMENT;
@@ -1121,8 +1125,12 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
     if (field_out && m->nobs < 1) return fail(ctx, BEM_ERR_INVALID_ARGUMENT, "no observation points set");
     if (!valid_options(ctx, o)) return BEM_ERR_INVALID_ARGUMENT;
     const bem::Precision prec = o.precision == BEM_PRECISION_MIXED ? bem::Precision::Mixed : bem::Precision::FP64;
-    if (prec == bem::Precision::Mixed && (m->mixed_freqs += n_freq) >= kChebMinFreqs)
-      ensure_cheb(ctx, m, 2.0 * M_PI * *std::max_element(freqs_hz, freqs_hz + n_freq) / o.sound_speed);
+    const bool cheb = prec == bem::Precision::Mixed && n_freq >= kChebMinFreqs;
+    if (cheb) {
+      std::vector<double> kw(n_freq);
+      for (int i = 0; i < n_freq; ++i) kw[i] = 2.0 * M_PI * freqs_hz[i] / o.sound_speed;
+      ensure_cheb(ctx, m, kw.data(), n_freq);
+    }
     const bem::DeviceMesh& dm = m->dm;
     const int nv = dm.nv, nc = m->nc;
     int B = o.batch > 0 ? std::min(o.batch, 64) : auto_batch(m, prec, n_freq);
@@ -1132,7 +1140,7 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
     auto slice_of = [&](int bi) {
       const int f0 = bi * B, bt = std::min(B, n_freq - f0);
       return Slice{m, freqs_hz + f0, bt, pressure_out ? pressure_out + 2 * (size_t)f0 * nc * nv : nullptr,
-                   field_out ? field_out + 2 * (size_t)f0 * nc * m->nobs : nullptr};
+                   field_out ? field_out + 2 * (size_t)f0 * nc * m->nobs : nullptr, cheb};
     };
     SolveTotals T;
     const int nl = std::max(1, std::min({o.lanes, kMaxLanes, nbatch}));

@@ -113,11 +113,13 @@ constexpr int kPairGeoDf = 48;
 cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, float* pairrec, cudaStream_t stream);
 // Singular blocks of nfreq frequencies; frequency f's blocks start at element
 // f * blocks_stride of blocks (the mixed form takes two frequencies per launch).
-// Adds the kernels it launched to *launched and the frequencies it formed from the mesh's
-// Chebyshev moments to *cheb_freqs (when not null).
+// use_cheb (mixed form): take the mesh's Chebyshev moments for the frequencies whose
+// expansion they cover.  Adds the kernels it launched to *launched and the frequencies it
+// formed from the moments to *cheb_freqs (when not null).
 cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, int nfreq, const double* k,
                                 const OperatorCoeffs* c, void* blocks, long long blocks_stride, cudaStream_t stream,
-                                long long* launched = nullptr, long long* cheb_freqs = nullptr);
+                                long long* launched = nullptr, long long* cheb_freqs = nullptr,
+                                bool use_cheb = false);
 // Chebyshev terms (a multiple of four, 8..kChebN) that expand the singular remainder of
 // wavenumber k on [0, R] to 1e-9; 0 when kChebN terms are not enough.
 int cheb_terms(double k, double R);

@@ -157,7 +157,8 @@ typedef struct bem_solve_stats {
                              counted from its source per quadrature pair and frequency: 35.67 + 26.83 / w,
                              w = frequencies sharing one launch's frequency-independent geometry */
   long long singular_cheb_freqs; /* mixed form: frequencies whose singular remainder was formed from the
-                                    mesh's Chebyshev moments (the rest point by point on the Duffy rules) */
+                                    mesh's Chebyshev moments (calls of at least 12 frequencies, where the
+                                    expansion converges); the rest point by point on the Duffy rules */
 } bem_solve_stats;
 
 void bem_default_options(bem_solve_options* opt);
@@ -211,7 +212,10 @@ int bem_auto_batch(bem_mesh* mesh, int precision, int n_freq);
  * of column j at out[2*(j*n + i)]).  coeffs = {cD.re, cD.im, cH.re, cH.im,
  * cM.re, cM.im}.  The Burton-Miller left-hand side of
  * burton_miller_neumann_matrices (BeatEngineCpuSolve.jl:45-53) is
- * cD = -1, cH = i/k, cM = 1/2. */
+ * cD = -1, cH = i/k, cM = 1/2.  The mixed form assembles as a call of
+ * bem_solve_frequencies with at least 12 frequencies does (the singular
+ * remainder from the mesh's Chebyshev moments where their expansion converges;
+ * the first such use forms them). */
 int bem_assemble_lhs(bem_mesh* mesh, double k, int precision, const double* coeffs, double* out);
 
 /* Parity entry point: out = (cS*S + cK*K' + cM10*M10) q for n_rhs face-data
@@ -219,7 +223,8 @@ int bem_assemble_lhs(bem_mesh* mesh, double k, int precision, const double* coef
  * [n_rhs][n_vertices] complex.  coeffs = {cS, cK, cM10} as (re, im) pairs.
  * The Burton-Miller right-hand side operator of BeatEngineCpuSolve.jl:50 is
  * cS = -1, cK = -i/k, cM10 = -i/(2k); this is the matrix-free right-hand side
- * of _cuda_burton_miller_rhs (BeatEngineCore.jl:1178-1184). */
+ * of _cuda_burton_miller_rhs (BeatEngineCore.jl:1178-1184).  The mixed form
+ * assembles as bem_assemble_lhs does. */
 int bem_apply_rhs_operator(bem_mesh* mesh, double k, int precision, const double* coeffs, const double* q, int n_rhs,
                            double* out);
 

@@ -103,11 +103,11 @@ def test_bm_lhs_mixed_matches_oracle(gpu_ctx, native, box_small):
 @pytest.mark.parametrize("freq", [2000.0, 12000.0])
 def test_singular_remainder_both_paths(gpu_ctx, native, box_small, freq):
     """The mixed form integrates the singular remainder through the mesh's Chebyshev
-    moments, which a sweep of at least 16 frequencies forms, while their expansion on the
-    pair radius R (0.104 m on this coarse box) converges; otherwise point by point on the
-    Duffy rules.  After a 16-frequency sweep up to 2.5 kHz (all 16 through the moments),
-    2 kHz (kR = 3.8) takes the moments and 12 kHz (kR = 22.8) the point-by-point kernel.
-    Both must give the full BM operator and the right-hand-side operator to 2e-6."""
+    moments in calls of at least 12 frequencies, for every frequency whose expansion on the
+    pair radius R (0.104 m on this coarse box) converges, and point by point on the Duffy
+    rules otherwise.  The operator inspection entry points assemble as such a sweep does:
+    2 kHz (kR = 3.8) through the moments, 12 kHz (kR = 22.8) point by point.  Both must give
+    the full BM operator and the right-hand-side operator to 2e-6."""
     O = _oracle()
     k = 2 * np.pi * freq / 343.0
     rng = np.random.default_rng(11)
@@ -116,10 +116,9 @@ def test_singular_remainder_both_paths(gpu_ctx, native, box_small, freq):
     try:
         m.set_excitation((box_small.tags == meshes.RADIATOR_TAG).astype(np.complex128)[None, :])
         m.set_observation_points(np.array([[0.0, 0.0, 2.0]]))
-        _, _, st = m.solve(np.geomspace(300.0, 2500.0, 16), precision=native.BEM_PRECISION_MIXED)
-        assert st["singular_cheb_freqs"] == 16
-        _, _, st = m.solve([2000.0, 12000.0], precision=native.BEM_PRECISION_MIXED)
-        assert st["singular_cheb_freqs"] == 1  # 2 kHz only
+        freqs = np.concatenate([np.geomspace(300.0, 2500.0, 11), [12000.0]])
+        _, _, st = m.solve(freqs, precision=native.BEM_PRECISION_MIXED)
+        assert st["singular_cheb_freqs"] == 11  # all but 12 kHz
         A = m.assemble_lhs(k, precision=native.BEM_PRECISION_MIXED)
         Sq = m.apply_rhs_operator(k, q, coeffs=(1.0, 0.0, 0.0), precision=native.BEM_PRECISION_MIXED)
         Kq = m.apply_rhs_operator(k, q, coeffs=(0.0, 1.0, 0.0), precision=native.BEM_PRECISION_MIXED)
@@ -133,17 +132,21 @@ def test_singular_remainder_both_paths(gpu_ctx, native, box_small, freq):
     assert rel(Kq, ops.adjoint_double_layer @ q) < 2e-6
 
 
-def test_moments_form_after_sixteen_frequencies(gpu_ctx, native, sphere320):
-    """A mesh solved at fewer than 16 frequencies (over all calls) integrates point by
-    point; the call that brings the count to 16 forms the moments and uses them."""
+def test_short_calls_run_point_by_point(gpu_ctx, native, sphere320):
+    """A call of fewer than 12 frequencies integrates point by point, also on a mesh whose
+    moments an earlier, longer call formed, so its results depend on its own inputs only."""
     m = gpu_ctx.upload_mesh(sphere320.vertices, sphere320.faces)
     try:
         m.set_excitation((sphere320.tags == meshes.RADIATOR_TAG).astype(np.complex128)[None, :])
         m.set_observation_points(np.array([[0.0, 0.0, 2.0]]))
-        _, _, st = m.solve(np.geomspace(300.0, 900.0, 8), precision=native.BEM_PRECISION_MIXED)
+        short = np.geomspace(300.0, 900.0, 8)
+        p1, u1, st = m.solve(short, precision=native.BEM_PRECISION_MIXED)
         assert st["singular_cheb_freqs"] == 0
-        _, _, st = m.solve(np.geomspace(1000.0, 2500.0, 8), precision=native.BEM_PRECISION_MIXED)
-        assert st["singular_cheb_freqs"] == 8
+        _, _, st = m.solve(np.geomspace(1000.0, 2500.0, 12), precision=native.BEM_PRECISION_MIXED)
+        assert st["singular_cheb_freqs"] == 12
+        p2, u2, st = m.solve(short, precision=native.BEM_PRECISION_MIXED)
+        assert st["singular_cheb_freqs"] == 0
+        assert np.array_equal(p1, p2) and np.array_equal(u1, u2)
     finally:
         m.release()
 
