@@ -252,10 +252,10 @@ Layout layout_for(const bem::DeviceMesh& dm, bem::Precision prec) {
 }
 
 // Frequencies a mixed-form call needs before its singular remainders go through the mesh's
-// Chebyshev moments: forming them costs about as much as 15 frequencies of the point-by-
-// point singular kernel at the full 24 terms (fewer terms cost proportionally less), and
-// each frequency through them costs a tenth of one.  A shorter call runs point by point
-// even when the moments exist, so a call's results depend on its own inputs only.
+// Chebyshev moments: forming them costs about as much as six frequencies of the point-by-
+// point singular kernel at 16 terms (more at more terms, at most 24), and each frequency
+// through them costs a fifteenth of one.  A shorter call runs point by point even when the
+// moments exist, so a call's results depend on its own inputs only.
 constexpr int kChebMinFreqs = 12;
 
 // Forms (or extends) the mesh's Chebyshev moments on the side stream for the call's
