@@ -587,9 +587,12 @@ def main() -> None:
 def accuracy_sweep(m, freqs, mesh, points, opts, args, stream, mixed_rate: float) -> dict:
     """The plain FP64 GPU form on the sweep's frequencies (every one by default) and the
     mixed form's relative error against it, per frequency: far field and surface
-    pressure, with the mixed form's refinement steps and final relative residual per
-    frequency (one frequency per call).  The FP64 form runs in batches of at most 16
-    and is timed with CUDA events on the library's stream."""
+    pressure.  The mixed form is solved twice: in one call over all the frequencies with
+    the timed steps' options (batch, lanes: the production path, e.g. the singular
+    remainder through the Chebyshev moments), whose errors are the record, and one
+    frequency per call (the point-by-point singular kernel), which also gives the
+    refinement steps and final relative residual of each frequency.  The FP64 form runs
+    in batches of at most 16 and is timed with CUDA events on the library's stream."""
     import torch
 
     native = pkg("native")
@@ -615,14 +618,20 @@ def accuracy_sweep(m, freqs, mesh, points, opts, args, stream, mixed_rate: float
         ev_b.record(stream)
     torch.cuda.synchronize()
     t64 = ev_a.elapsed_time(ev_b) / 1e3
+    pw = torch.empty((len(sel), 1, mesh.n_vertices), dtype=torch.complex128, device="cuda")
+    uw = torch.empty((len(sel), 1, len(points)), dtype=torch.complex128, device="cuda")
+    stw = m.solve_device(sel, pw.data_ptr(), uw.data_ptr(), **opts)
+    torch.cuda.synchronize()
+    errs = [float(torch.linalg.norm(uw[i] - u64[i]) / torch.linalg.norm(u64[i])) for i in range(len(sel))]
+    perr = [float(torch.linalg.norm(pw[i] - p64[i]) / torch.linalg.norm(p64[i])) for i in range(len(sel))]
     pm = torch.empty((1, 1, mesh.n_vertices), dtype=torch.complex128, device="cuda")
     um = torch.empty((1, 1, len(points)), dtype=torch.complex128, device="cuda")
-    errs, perr, steps, resid = [], [], [], []
+    errs1, perr1, steps, resid = [], [], [], []
     for i, f in enumerate(sel):
         st = m.solve_device([f], pm.data_ptr(), um.data_ptr(), **{**opts, "batch": 1})
         torch.cuda.synchronize()
-        errs.append(float(torch.linalg.norm(um[0] - u64[i]) / torch.linalg.norm(u64[i])))
-        perr.append(float(torch.linalg.norm(pm[0] - p64[i]) / torch.linalg.norm(p64[i])))
+        errs1.append(float(torch.linalg.norm(um[0] - u64[i]) / torch.linalg.norm(u64[i])))
+        perr1.append(float(torch.linalg.norm(pm[0] - p64[i]) / torch.linalg.norm(p64[i])))
         steps.append(int(st["max_refine_steps"]))
         resid.append(float(st["max_rel_residual"]))
     v64 = len(sel) / t64
@@ -630,6 +639,11 @@ def accuracy_sweep(m, freqs, mesh, points, opts, args, stream, mixed_rate: float
         "fp64_form": {"value": v64, "unit": UNIT, "freqs_hz": [float(f) for f in sel],
                       "stage_ms_per_freq": {k: 1e3 * v / len(sel) for k, v in kernel_s.items()},
                       "far_field_err_per_freq": errs, "surface_pressure_err_per_freq": perr,
+                      "sweep_call": {"refine_steps_max": int(stw["max_refine_steps"]),
+                                     "rel_residual_max": float(stw["max_rel_residual"]),
+                                     "singular_cheb_freqs": int(stw["singular_cheb_freqs"])},
+                      "far_field_err_per_freq_single_calls": errs1,
+                      "surface_pressure_err_per_freq_single_calls": perr1,
                       "mixed_refine_steps_per_freq": steps, "mixed_rel_residual_per_freq": resid},
         "speedup_vs_fp64": mixed_rate / v64,
         "max_rel_far_field_err_vs_fp64": max(errs),
