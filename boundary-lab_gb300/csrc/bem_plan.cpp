@@ -824,44 +824,96 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
   // singular scatter plan: every (trial column 3 g + b, extended row e) entry the
   // pairs of trial face g add into, with its contributions in pair order (pair k,
   // then test vertex a), so a thread per entry adds them in the order one thread
-  // per trial face would have
+  // per trial face would have.  The entries of trial face g are its own columns, so
+  // each face's entries and contributions are planned on their own: in slices of
+  // trial faces on the planner's threads, numbered in order of first appearance
+  // within the face and concatenated in face order (the same plan as one walk over
+  // all faces).
   {
-    const size_t np = P.pairs.size();
-    std::vector<int> entry_of(3 * (size_t)std::max(P.n_ext, 1), -1);
-    std::vector<int> touched;
-    std::vector<int> contrib_entry(9 * np), contrib_src(9 * np);
-    P.scat_col.clear();
-    P.scat_row.clear();
-    size_t c = 0;
-    for (int g = 0; g < nf; ++g) {
-      touched.clear();
-      for (int k = P.pairs_by_trial_ptr[g]; k < P.pairs_by_trial_ptr[g + 1]; ++k) {
-        const int f = P.pairs[k].test;
-        for (int a = 0; a < 3; ++a) {
-          const int e = P.face_ext[3 * (size_t)f + a];
-          for (int b = 0; b < 3; ++b) {
-            int& slot = entry_of[3 * (size_t)e + b];
-            if (slot < 0) {
-              slot = (int)P.scat_col.size();
-              P.scat_col.push_back(3 * g + b);
-              P.scat_row.push_back(e);
-              touched.push_back(3 * e + b);
+    struct ScatSlice {
+      std::vector<int> col, row, cnt, src;
+    };
+    const int Ts = plan_threads(nf);
+    std::vector<ScatSlice> ss(Ts);
+    parallel_slices(nf, Ts, [&](long long gb, long long ge, int ti) {
+      ScatSlice& S = ss[ti];
+      const size_t npairs_slice = (size_t)(P.pairs_by_trial_ptr[ge] - P.pairs_by_trial_ptr[gb]);
+      S.src.reserve(9 * npairs_slice);
+      S.col.reserve(4 * npairs_slice);
+      S.row.reserve(4 * npairs_slice);
+      S.cnt.reserve(4 * npairs_slice);
+      std::vector<int> entry_of(3 * (size_t)std::max(P.n_ext, 1), -1);
+      std::vector<int> touched, off;
+      for (long long g = gb; g < ge; ++g) {
+        const int k0 = P.pairs_by_trial_ptr[g], k1 = P.pairs_by_trial_ptr[g + 1];
+        const int e0 = (int)S.col.size();
+        touched.clear();
+        for (int k = k0; k < k1; ++k) {
+          const int f = P.pairs[k].test;
+          for (int a = 0; a < 3; ++a) {
+            const int e = P.face_ext[3 * (size_t)f + a];
+            for (int b = 0; b < 3; ++b) {
+              int& slot = entry_of[3 * (size_t)e + b];
+              if (slot < 0) {
+                slot = (int)S.col.size();
+                S.col.push_back(3 * (int)g + b);
+                S.row.push_back(e);
+                S.cnt.push_back(0);
+                touched.push_back(3 * e + b);
+              }
+              S.cnt[slot]++;
             }
-            contrib_entry[c] = slot;
-            contrib_src[c] = 12 * k + 3 * a + b;
-            ++c;
           }
         }
+        // this face's contributions grouped by entry, each entry's in walk order
+        const int ne_g = (int)S.col.size() - e0;
+        off.assign(ne_g, 0);
+        size_t run = S.src.size();
+        for (int i = 0; i < ne_g; ++i) {
+          off[i] = (int)run;
+          run += S.cnt[e0 + i];
+        }
+        S.src.resize(run);
+        for (int k = k0; k < k1; ++k) {
+          const int f = P.pairs[k].test;
+          for (int a = 0; a < 3; ++a) {
+            const int e = P.face_ext[3 * (size_t)f + a];
+            for (int b = 0; b < 3; ++b) S.src[off[entry_of[3 * (size_t)e + b] - e0]++] = 12 * k + 3 * a + b;
+          }
+        }
+        for (int t : touched) entry_of[t] = -1;
       }
-      for (int t : touched) entry_of[t] = -1;
+    });
+    size_t ne = 0, nc = 0;
+    for (const ScatSlice& S : ss) {
+      ne += S.col.size();
+      nc += S.src.size();
     }
-    const size_t ne = P.scat_col.size();
-    P.scat_ptr.assign(ne + 1, 0);
-    for (size_t i = 0; i < c; ++i) P.scat_ptr[contrib_entry[i] + 1]++;
-    for (size_t i = 0; i < ne; ++i) P.scat_ptr[i + 1] += P.scat_ptr[i];
-    P.scat_src.assign(c, 0);
-    std::vector<int> fill(P.scat_ptr.begin(), P.scat_ptr.end() - 1);
-    for (size_t i = 0; i < c; ++i) P.scat_src[fill[contrib_entry[i]]++] = contrib_src[i];
+    P.scat_col.resize(ne);
+    P.scat_row.resize(ne);
+    P.scat_ptr.resize(ne + 1);
+    P.scat_src.resize(nc);
+    std::vector<size_t> eo(Ts + 1, 0), co(Ts + 1, 0);
+    for (int t = 0; t < Ts; ++t) {
+      eo[t + 1] = eo[t] + ss[t].col.size();
+      co[t + 1] = co[t] + ss[t].src.size();
+    }
+    P.scat_ptr[0] = 0;
+    // each slice into its own range (the copies, and the first touch of the fresh
+    // pages, spread over the threads)
+    parallel_slices(Ts, Ts, [&](long long b, long long e, int) {
+      for (long long t = b; t < e; ++t) {
+        const ScatSlice& S = ss[t];
+        std::copy(S.col.begin(), S.col.end(), P.scat_col.begin() + eo[t]);
+        std::copy(S.row.begin(), S.row.end(), P.scat_row.begin() + eo[t]);
+        std::copy(S.src.begin(), S.src.end(), P.scat_src.begin() + co[t]);
+        int run = (int)co[t];
+        for (size_t i = 0; i < S.cnt.size(); ++i) {
+          run += S.cnt[i];
+          P.scat_ptr[eo[t] + i + 1] = run;
+        }
+      }
+    });
   }
   return std::string();
 }
