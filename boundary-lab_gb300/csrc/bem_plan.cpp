@@ -636,15 +636,23 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
   }
   // lane groups: each tile's faces packed into ceil(n / 32) vertex-disjoint
   // groups of 32 where possible (pack_lane_groups), so few lanes idle.
+  // The tiles are packed independently, on the planner's threads, and appended in
+  // tile order.
   P.tile_group_ptr.assign(1, 0);
   P.lane_slots.clear();
+  std::vector<std::vector<std::vector<int>>> tile_groups(P.n_tiles);
+  parallel_slices(P.n_tiles, std::min(plan_threads(nf), std::max(1, P.n_tiles)), [&](long long tb, long long te, int) {
+    for (long long t = tb; t < te; ++t) {
+      std::vector<std::array<int, 3>> fl;
+      fl.reserve(tile_face_list[t].size());
+      for (int f : tile_face_list[t]) fl.push_back({face_loc[3 * f], face_loc[3 * f + 1], face_loc[3 * f + 2]});
+      tile_groups[t] = pack_lane_groups(fl, (int)tile_rows[t].size());
+      for (auto& g : tile_groups[t])
+        for (int& i : g) i = tile_face_list[t][i];
+    }
+  });
   for (int t = 0; t < P.n_tiles; ++t) {
-    std::vector<std::array<int, 3>> fl;
-    fl.reserve(tile_face_list[t].size());
-    for (int f : tile_face_list[t]) fl.push_back({face_loc[3 * f], face_loc[3 * f + 1], face_loc[3 * f + 2]});
-    std::vector<std::vector<int>> groups = pack_lane_groups(fl, (int)tile_rows[t].size());
-    for (auto& g : groups)
-      for (int& i : g) i = tile_face_list[t][i];
+    const std::vector<std::vector<int>>& groups = tile_groups[t];
     for (auto& g : groups) {
       for (int l = 0; l < kLanes; ++l) {
         LaneSlot s;
@@ -669,8 +677,9 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
                 "FaceF32 word offsets");
   {
     const size_t ng = P.lane_slots.size() / kLanes;
-    P.group_faces32.assign(ng * kFaceWords * kLanes, 0.0f);
-    for (size_t g = 0; g < ng; ++g)
+    P.group_faces32.resize(ng * kFaceWords * kLanes);
+    parallel_slices((long long)ng, plan_threads(nf), [&](long long gb, long long ge, int) {
+    for (long long g = gb; g < ge; ++g)
       for (int l = 0; l < kLanes; ++l) {
         const int f = P.lane_slots[g * kLanes + l].face;
         float w[kFaceWords];
@@ -683,6 +692,7 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
         }
         for (int i = 0; i < kFaceWords; ++i) P.group_faces32[(g * kFaceWords + i) * kLanes + l] = w[i];
       }
+    });
   }
   // column gather CSR: vertex j <- (g, b)
   P.col_ptr.assign(nv + 1, 0);
