@@ -2019,23 +2019,6 @@ cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, float* 
   return cudaGetLastError();
 }
 
-double singular_pair_radius(const double* verts, const int* faces, const SingularPair* pairs, int npairs) {
-  double r2 = 0.0;
-  for (int p = 0; p < npairs; ++p) {
-    const int* ft = faces + 3 * (size_t)pairs[p].test;
-    const int* fr = faces + 3 * (size_t)pairs[p].trial;
-    const double sx = tr_sx(pairs[p].tr), sy = tr_sy(pairs[p].tr);
-    for (int a = 0; a < 3; ++a)
-      for (int b = 0; b < 3; ++b) {
-        const double* t = verts + 3 * (size_t)ft[a];
-        const double* q = verts + 3 * (size_t)fr[b];
-        const double dx = sx * q[0] - t[0], dy = sy * q[1] - t[1], dz = q[2] - t[2];
-        r2 = std::max(r2, dx * dx + dy * dy + dz * dz);
-      }
-  }
-  return std::sqrt(r2);
-}
-
 namespace {
 // Chebyshev coefficients on r in [0, R] of f1(r) = (e^{ikr} - 1) / r and
 // g2(r) = (1 - (1 - ikr) e^{ikr}) / r^2 (FP64), by interpolation at the N <= kChebN

@@ -141,7 +141,7 @@ struct UploadPack {
   };
   std::vector<Part> parts;
   size_t total = 0;
-  template <typename T> void add(T*& dst, const std::vector<T>& v) {
+  template <typename T, typename A> void add(T*& dst, const std::vector<T, A>& v) {
     dst = nullptr;
     if (v.empty()) return;
     const size_t off = (total + 255) & ~(size_t)255;
@@ -165,10 +165,36 @@ struct UploadPack {
       ctx->stage_bytes = want;
     }
     char* base = (char*)mesh_alloc(m, total, "allocate mesh data");
+    // the host copies into the staging buffer, in pieces of at most 1 MB spread
+    // over a few threads (one thread below 4 MB)
+    struct Piece {
+      size_t off, bytes;
+      const char* src;
+    };
+    std::vector<Piece> pieces;
+    constexpr size_t kPiece = (size_t)1 << 20;
     for (const Part& p : parts) {
-      std::memcpy((char*)ctx->stage + p.off, p.src, p.bytes);
       p.bind(base);
+      for (size_t o = 0; o < p.bytes; o += kPiece)
+        pieces.push_back({p.off + o, std::min(kPiece, p.bytes - o), (const char*)p.src + o});
     }
+    const int nt = total < ((size_t)4 << 20)
+                       ? 1
+                       : (int)std::min<size_t>({8, pieces.size(), std::max(1u, std::thread::hardware_concurrency())});
+    auto copy = [&](int t) {
+      for (size_t i = t; i < pieces.size(); i += nt)
+        std::memcpy((char*)ctx->stage + pieces[i].off, pieces[i].src, pieces[i].bytes);
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) {
+      try {
+        th.emplace_back(copy, t);
+      } catch (...) {  // no thread: this one copies that share
+        copy(t);
+      }
+    }
+    copy(0);
+    for (auto& t : th) t.join();
     ck(cudaMemcpyAsync(base, ctx->stage, total, cudaMemcpyHostToDevice, ctx->stream), "upload");
   }
 };
@@ -593,7 +619,7 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
           d.rule_cw[a * P.Q + q] = phi[a] * P.rule_w[q];
         }
       }
-      for (const auto& sp : P.pairs) m->singular_points += P.rule_ptr[sp.rule + 1] - P.rule_ptr[sp.rule];
+      m->singular_points = P.singular_points;
       for (int i = 0; i < 12; ++i) d.m11m10f[i] = (float)mm[i];
       if (d.npairs > 0) {
         d.moments = (double*)mesh_alloc(m, (size_t)d.npairs * 24 * sizeof(double), "allocate singular moments");
@@ -602,7 +628,7 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
         // the Chebyshev expansion interval of the singular remainder: every point distance
         // of a pair lies below the largest distance between its vertices (a little margin
         // for rounding); the moments themselves are formed by the first sweep that uses them
-        d.cheb_R = 1.000001 * bem::singular_pair_radius(P.verts.data(), P.faces.data(), P.pairs.data(), d.npairs);
+        d.cheb_R = 1.000001 * P.pair_radius;
       }
       ck(cudaStreamSynchronize(ctx->stream), "mesh upload");
       if (d.npairs > 0) {

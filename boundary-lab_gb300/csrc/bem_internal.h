@@ -3,10 +3,26 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace bem {
+
+// std::allocator whose value-initialisation of a trivial element does nothing, so
+// a vector resized before being filled in parallel is not first zero-filled (and
+// its pages are first touched by the threads that fill them).
+template <typename T> struct UninitAlloc : std::allocator<T> {
+  template <typename U> struct rebind {
+    using other = UninitAlloc<U>;
+  };
+  UninitAlloc() = default;
+  template <typename U> UninitAlloc(const UninitAlloc<U>&) noexcept {}
+  template <typename U> void construct(U*) noexcept {}
+  template <typename U, typename... A> void construct(U* p, A&&... a) { ::new ((void*)p) U(std::forward<A>(a)...); }
+};
+template <typename T> using FillVec = std::vector<T, UninitAlloc<T>>;
 
 // Regular (6-point) rule and Duffy rules use the reference's orders; the
 // planner supports regular orders 1 (1 point), 2/3 (3 points) and 4 (6 points)
@@ -118,9 +134,11 @@ struct MeshPlan {
   // singular scatter: the distinct extended-row entries (column 3 g + b of trial
   // face g, extended row e) that the pairs' 3 x 3 blocks add into, each with its
   // contributions (block element 12 k + 3 a + b of pair k) in pair order
-  std::vector<int> scat_col, scat_row;  // per entry
-  std::vector<int> scat_ptr;            // entries + 1
-  std::vector<int> scat_src;            // 9 per pair
+  FillVec<int> scat_col, scat_row;  // per entry
+  FillVec<int> scat_ptr;            // entries + 1
+  FillVec<int> scat_src;            // 9 per pair
+  double pair_radius = 0.0;         // largest vertex distance of a pair (its trial face reflected for image pairs)
+  long long singular_points = 0;    // Duffy points over all pairs
   // Duffy rules: concatenated points; rule r occupies [rule_ptr[r], rule_ptr[r+1])
   std::vector<int> rule_ptr;
   std::vector<double> duffy;  // 5 doubles per point: test xi, test eta, trial xi, trial eta, w

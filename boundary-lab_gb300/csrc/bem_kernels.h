@@ -125,9 +125,6 @@ cudaError_t launch_singular_dyn(const DeviceMesh& m, Precision prec, int nfreq, 
 int cheb_terms(double k, double R);
 // The mesh's Chebyshev moments for the first nterms terms into m.cheb (after the pair setup).
 cudaError_t launch_cheb_moments(const DeviceMesh& m, int nterms, cudaStream_t stream);
-// Largest distance between a point of a vertex-sharing pair's test face and one of its trial
-// face (the trial face reflected for image pairs): the maximum over vertex pairs.
-double singular_pair_radius(const double* verts, const int* faces, const SingularPair* pairs, int npairs);
 cudaError_t launch_singular_scatter(const DeviceMesh& m, Precision prec, const void* blocks, void* Rext,
                                     long long ldR, cudaStream_t stream);
 cudaError_t launch_gather(const DeviceMesh& m, Precision prec, const void* Rext, long long ldR, void* A, long long lda,

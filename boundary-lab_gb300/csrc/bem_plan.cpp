@@ -842,6 +842,8 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
   {
     struct ScatSlice {
       std::vector<int> col, row, cnt, src;
+      double r2 = 0.0;     // largest squared vertex distance of a pair
+      long long npts = 0;  // Duffy points of the pairs
     };
     const int Ts = plan_threads(nf);
     std::vector<ScatSlice> ss(Ts);
@@ -860,6 +862,19 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
         touched.clear();
         for (int k = k0; k < k1; ++k) {
           const int f = P.pairs[k].test;
+          {
+            const SingularPair& sp = P.pairs[k];
+            const double sx = tr_sx(sp.tr), sy = tr_sy(sp.tr);
+            for (int a = 0; a < 3; ++a) {
+              const double* t = &P.verts[3 * (size_t)P.faces[3 * (size_t)f + a]];
+              for (int b = 0; b < 3; ++b) {
+                const double* q = &P.verts[3 * (size_t)P.faces[3 * (size_t)g + b]];
+                const double dx = sx * q[0] - t[0], dy = sy * q[1] - t[1], dz = q[2] - t[2];
+                S.r2 = std::max(S.r2, dx * dx + dy * dy + dz * dz);
+              }
+            }
+            S.npts += P.rule_ptr[sp.rule + 1] - P.rule_ptr[sp.rule];
+          }
           for (int a = 0; a < 3; ++a) {
             const int e = P.face_ext[3 * (size_t)f + a];
             for (int b = 0; b < 3; ++b) {
@@ -895,10 +910,15 @@ std::string build_mesh_plan(const double* verts_in, int nv, const int* faces, in
       }
     });
     size_t ne = 0, nc = 0;
+    double r2 = 0.0;
+    P.singular_points = 0;
     for (const ScatSlice& S : ss) {
       ne += S.col.size();
       nc += S.src.size();
+      r2 = std::max(r2, S.r2);
+      P.singular_points += S.npts;
     }
+    P.pair_radius = std::sqrt(r2);
     P.scat_col.resize(ne);
     P.scat_row.resize(ne);
     P.scat_ptr.resize(ne + 1);
