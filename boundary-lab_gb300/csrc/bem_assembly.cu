@@ -743,41 +743,12 @@ __global__ void pair_setup_kernel(SingularGeom geo, const SingularPair* __restri
   for (int i = kRecMom + kStatic; i < kPairRec; ++i) o[i] = 0.0f;
 }
 
-// Warp reduce-scatter by recursive halving of N = 3 x 2^j values per lane (N <= 96).  At
-// exchange offset O a lane keeps one half of its values (the upper half when bit O of its
-// lane index is set) and adds its partner's copy of that half, so each level moves half as
-// many values as the one before; once three values remain, the remaining offsets are plain
-// butterflies.  Afterwards v[0..3) of lane l hold the warp sums of entries 3 (l >> s) ..
-// 3 (l >> s) + 2, s = 5 - log2(N / 3).  For 96 values the five levels move 48 + 24 + 12 +
-// 6 + 3 values per lane, against 5 x 96 for a butterfly of every value.
-template <int N, int O>
-__device__ __forceinline__ void warp_reduce_halving(float* v, int lane) {
-  if constexpr (O > 0) {
-    if constexpr (N > 3) {
-      constexpr int H = N / 2;
-      const bool upper = (lane & O) != 0;
-#pragma unroll
-      for (int i = 0; i < H; ++i) {
-        const float send = upper ? v[i] : v[H + i];
-        const float keep = upper ? v[H + i] : v[i];
-        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, O);
-      }
-      warp_reduce_halving<H, O / 2>(v, lane);
-    } else {
-#pragma unroll
-      for (int i = 0; i < 3; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], O);
-      warp_reduce_halving<N, O / 2>(v, lane);
-    }
-  }
-}
-
-// The 24 k-independent moments of a pair for the plain FP64 form (one warp per
-// pair, lanes over the Duffy points), in double-float arithmetic on the FP32
-// pipe: every product, sum, the reciprocal root and the accumulation carry about
-// 44 bits, which is FP64 accuracy for these sums at the FP32 rate (this part's
-// FP64 rate is 1/64 of it).  Lane i < 24 then writes moment i = jac * sum_i in
-// FP64 (and, when rec is given, its float copy and the S0 term into the pair
-// record).
+// The 24 k-independent moments of a pair (one warp per pair, lanes over the
+// Duffy points), in double-float arithmetic on the FP32 pipe: every product,
+// sum, the reciprocal root and the accumulation carry about 44 bits, which is
+// FP64 accuracy for these sums at the FP32 rate (this part's FP64 rate is
+// 1/64 of it).  Lane i < 24 then writes moment i = jac * sum_i in FP64 and its
+// float copy into the pair record; lane 0 also writes the record's S0 term.
 __global__ void __launch_bounds__(256)
     singular_moments_df_kernel(const SingularPair* __restrict__ pairs, int npairs, const int* __restrict__ rule_ptr,
                                const float* __restrict__ duffy_df, const float* __restrict__ geo_df,
@@ -851,81 +822,16 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
   for (int i = 0; i < kStatic; ++i)
     if (lane == i) mine = df_to_double(acc[i]) * P.jac;
-  if (lane < kStatic) moments[(size_t)kStatic * warp + lane] = mine;
-  if (!rec) return;
   float* o = rec + (size_t)kPairRec * warp;
-  if (lane < kStatic) o[kRecMom + lane] = (float)mine;
+  if (lane < kStatic) {
+    moments[(size_t)kStatic * warp + lane] = mine;
+    o[kRecMom + lane] = (float)mine;
+  }
   if (lane == 0) {
     const double m0 = df_to_double(acc[0]) * P.jac, m1 = df_to_double(acc[1]) * P.jac,
                  m2 = df_to_double(acc[2]) * P.jac;
     o[kRecS0] = (float)(m0 + m1 + m2);
   }
-}
-
-// The same 24 moments for the mixed form's pair record, in FP32 (one warp per
-// pair, lanes over the Duffy points, from the record's rounded geometry): the
-// mixed form reads them as floats, and FP32 sums of the Duffy points carry a
-// relative error of a few 1e-7, the size of the float rounding of the FP64
-// values.  Afterwards lanes 4j hold the sums 3j .. 3j + 2; lane 0 also writes
-// the record's S0 term.
-__global__ void __launch_bounds__(256)
-    singular_moments_f32_kernel(const SingularPair* __restrict__ pairs, int npairs, const int* __restrict__ rule_ptr,
-                                const float* __restrict__ duffy, float* __restrict__ rec) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= npairs) return;
-  const SingularPair P = pairs[warp];
-  float* G = rec + (size_t)kPairRec * warp;
-  float g[21];
-#pragma unroll
-  for (int i = 0; i < 21; ++i) g[i] = G[kRecGeom + i];
-  const float* e1t = g;
-  const float* e2t = g + 3;
-  const float* d0 = g + 6;
-  const float* e1r = g + 9;
-  const float* e2r = g + 12;
-  const float* nt = g + 15;
-  const float* nr = g + 18;
-  const float inv4pi = (float)(0.25 / CUDART_PI);
-  float v[kStatic];
-#pragma unroll
-  for (int i = 0; i < kStatic; ++i) v[i] = 0.f;
-  const int q0 = rule_ptr[P.rule], q1 = rule_ptr[P.rule + 1];
-  for (int q = q0 + lane; q < q1; q += 32) {
-    const float tu = __ldg(duffy + 5 * (size_t)q), tv = __ldg(duffy + 5 * (size_t)q + 1);
-    const float ru = __ldg(duffy + 5 * (size_t)q + 2), rvv = __ldg(duffy + 5 * (size_t)q + 3);
-    const float w = __ldg(duffy + 5 * (size_t)q + 4);
-    const float px[3] = {1.f - tu - tv, tu, tv};
-    const float py[3] = {1.f - ru - rvv, ru, rvv};
-    float rv[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) rv[d] = (d0[d] + ru * e1r[d] + rvv * e2r[d]) - (tu * e1t[d] + tv * e2t[d]);
-    const float r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
-    if (r2 == 0.f) continue;
-    const float rinv = rsqrt_ftz(r2);
-    const float ws = w * rinv * inv4pi;                // w G0
-    const float srr = ws * rinv * rinv;                // w G0 / r^2
-    const float wd = -(rv[0] * nr[0] + rv[1] * nr[1] + rv[2] * nr[2]) * srr;  // w dG0/dn_y
-    const float wn = (rv[0] * nt[0] + rv[1] * nt[1] + rv[2] * nt[2]) * srr;   // w dG0/dn_x
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const float was = ws * px[a], wad = wd * px[a];
-      v[a] += was;
-      v[21 + a] = fmaf(wn, px[a], v[21 + a]);
-#pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        v[3 + 3 * a + b] = fmaf(was, py[b], v[3 + 3 * a + b]);
-        v[12 + 3 * a + b] = fmaf(wad, py[b], v[12 + 3 * a + b]);
-      }
-    }
-  }
-  warp_reduce_halving<kStatic, 16>(v, lane);
-  const float jac = G[kRecJac];
-  if ((lane & 3) == 0) {
-#pragma unroll
-    for (int j = 0; j < 3; ++j) G[kRecMom + 3 * (lane >> 2) + j] = v[j] * jac;
-  }
-  if (lane == 0) G[kRecS0] = ((v[0] + v[1]) + v[2]) * jac;
 }
 
 template <typename R> struct SingParams;
@@ -1065,6 +971,34 @@ __global__ void __launch_bounds__(256, 1)
     C2 rhs = cadd(cmul(p.cS, S), cmul(p.cK, K));
     if (coincident) rhs = cadd(rhs, cscale(p.cM10, a2 * (R)m11m10[9 + a]));
     o[9 + a] = rhs;
+  }
+}
+
+// Warp reduce-scatter by recursive halving of N = 3 x 2^j values per lane (N <= 96).  At
+// exchange offset O a lane keeps one half of its values (the upper half when bit O of its
+// lane index is set) and adds its partner's copy of that half, so each level moves half as
+// many values as the one before; once three values remain, the remaining offsets are plain
+// butterflies.  Afterwards v[0..3) of lane l hold the warp sums of entries 3 (l >> s) ..
+// 3 (l >> s) + 2, s = 5 - log2(N / 3).  For 96 values the five levels move 48 + 24 + 12 +
+// 6 + 3 values per lane, against 5 x 96 for a butterfly of every value.
+template <int N, int O>
+__device__ __forceinline__ void warp_reduce_halving(float* v, int lane) {
+  if constexpr (O > 0) {
+    if constexpr (N > 3) {
+      constexpr int H = N / 2;
+      const bool upper = (lane & O) != 0;
+#pragma unroll
+      for (int i = 0; i < H; ++i) {
+        const float send = upper ? v[i] : v[H + i];
+        const float keep = upper ? v[H + i] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, O);
+      }
+      warp_reduce_halving<H, O / 2>(v, lane);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], O);
+      warp_reduce_halving<N, O / 2>(v, lane);
+    }
   }
 }
 
@@ -2073,23 +2007,15 @@ cudaError_t launch_regular_f64(const DeviceMesh& m, double k, double2 cD, double
   return cudaGetLastError();
 }
 
-cudaError_t launch_singular_static(const DeviceMesh& m, float* pairrec, cudaStream_t stream) {
+cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, float* pairrec, cudaStream_t stream) {
   if (m.npairs == 0) return cudaSuccess;
   SingularGeom geo{m.verts, m.faces, m.normal};
   pair_setup_kernel<<<(m.npairs + 127) / 128, 128, 0, stream>>>(geo, m.pairs, m.npairs, m.curls, m.area, m.pairgeo_df,
                                                                 pairrec);
   const int threads = 256;
   const int blocks = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
-  singular_moments_f32_kernel<<<blocks, threads, 0, stream>>>(m.pairs, m.npairs, m.rule_ptr, m.duffy32, pairrec);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_singular_moments64(const DeviceMesh& m, double* moments, cudaStream_t stream) {
-  if (m.npairs == 0) return cudaSuccess;
-  const int threads = 256;
-  const int blocks = (int)(((long long)m.npairs * 32 + threads - 1) / threads);
   singular_moments_df_kernel<<<blocks, threads, 0, stream>>>(m.pairs, m.npairs, m.rule_ptr, m.duffy_df, m.pairgeo_df,
-                                                             moments, nullptr);
+                                                             moments, pairrec);
   return cudaGetLastError();
 }
 

@@ -116,9 +116,8 @@ struct bem_mesh {
   DevBuf drive32, drive64, obs;
   int nobs = 0;
   DevBuf driven;
-  cudaEvent_t moments_ready = nullptr;    // recorded on ctx->side after the pair setup and FP32 moments
-  cudaEvent_t moments64_ready = nullptr;  // recorded on ctx->side after the FP64 form's moments kernel
-  cudaEvent_t cheb_ready = nullptr;       // recorded on ctx->side after the Chebyshev moments kernel
+  cudaEvent_t moments_ready = nullptr;  // recorded on ctx->side after the singular moments kernel
+  cudaEvent_t cheb_ready = nullptr;     // recorded on ctx->side after the Chebyshev moments kernel
   long long singular_points = 0;
 };
 
@@ -317,24 +316,6 @@ void ensure_cheb(bem_context* ctx, bem_mesh* m, const double* k, int n) {
   d.cheb_n = nterms;
 }
 
-// The plain FP64 form's static moments of the mesh, formed once at the form's first
-// use on the side stream (after the pair setup, which precedes them there).  Called
-// on the solving thread before any lane starts.
-void ensure_moments64(bem_mesh* m) {
-  bem::DeviceMesh& d = m->dm;
-  if (d.npairs == 0 || m->moments64_ready) return;
-  bem_context* ctx = m->ctx;
-  d.moments = (double*)mesh_alloc(m, (size_t)d.npairs * 24 * sizeof(double), "allocate singular moments");
-  cudaEvent_t ev = nullptr;  // the side stream must see the allocation, made on the context's stream
-  ck(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "create event");
-  ck(cudaEventRecord(ev, ctx->stream), "record event");
-  ck(cudaStreamWaitEvent(ctx->side, ev, 0), "wait for the allocation");
-  cudaEventDestroy(ev);
-  ck(bem::launch_singular_moments64(d, d.moments, ctx->side), "FP64 singular moments kernel");
-  ck(cudaEventCreateWithFlags(&m->moments64_ready, cudaEventDisableTiming), "create event");
-  ck(cudaEventRecord(m->moments64_ready, ctx->side), "record event");
-}
-
 // Assemble the LHS (c[i].cD, cH, cM) of cnt frequencies into A[i] (and A2[i] if
 // given; column-major, leading dimension lda) and, if nc > 0, the RHS into b[i]
 // (nc columns, leading dimension ldb, permuted rows).  lda / ldb <= 0: the mesh's
@@ -374,12 +355,6 @@ long long assemble_frequencies(bem_context* ctx, bem_mesh* m, bem::Precision pre
        "regular kernel");
     prof_mark(ctx, BEM_K_REGULAR);
     if (m->moments_ready) ck(cudaStreamWaitEvent(ctx->stream, m->moments_ready, 0), "wait for singular moments");
-    if (prec == bem::Precision::FP64 && dm.npairs > 0) {
-      // formed before any lane starts (bem_solve_frequencies); single-threaded callers
-      // form them here on first use
-      if (!m->moments64_ready) ensure_moments64(m);
-      ck(cudaStreamWaitEvent(ctx->stream, m->moments64_ready, 0), "wait for FP64 singular moments");
-    }
     if (m->cheb_ready) ck(cudaStreamWaitEvent(ctx->stream, m->cheb_ready, 0), "wait for Chebyshev moments");
     long long sing_launches = 0;
     ck(bem::launch_singular_dyn(dm, prec, g, k + f0, c + f0, sblk(0), (long long)sblk_n, ctx->stream,
@@ -430,11 +405,6 @@ void free_mesh_device(bem_mesh* m) {
     cudaStreamWaitEvent(m->ctx->stream, m->cheb_ready, 0);
     cudaEventDestroy(m->cheb_ready);
     m->cheb_ready = nullptr;
-  }
-  if (m->moments64_ready) {
-    cudaStreamWaitEvent(m->ctx->stream, m->moments64_ready, 0);
-    cudaEventDestroy(m->moments64_ready);
-    m->moments64_ready = nullptr;
   }
   if (m->moments_ready) {
     cudaStreamWaitEvent(m->ctx->stream, m->moments_ready, 0);
@@ -652,6 +622,7 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
       m->singular_points = P.singular_points;
       for (int i = 0; i < 12; ++i) d.m11m10f[i] = (float)mm[i];
       if (d.npairs > 0) {
+        d.moments = (double*)mesh_alloc(m, (size_t)d.npairs * 24 * sizeof(double), "allocate singular moments");
         d.pairrec = (float*)mesh_alloc(m, (size_t)d.npairs * bem::kPairRec * sizeof(float), "allocate pair records");
         d.pairgeo_df = (float*)mesh_alloc(m, (size_t)d.npairs * bem::kPairGeoDf * sizeof(float), "allocate pair geometry");
         // the Chebyshev expansion interval of the singular remainder: every point distance
@@ -661,10 +632,9 @@ int bem_upload_mesh_symmetric(bem_context* ctx, const double* vertices, int n_ve
       }
       ck(cudaStreamSynchronize(ctx->stream), "mesh upload");
       if (d.npairs > 0) {
-        // the pair records with the k-independent moments (FP32) on the side stream; the
-        // first singular kernel of a solve waits for them, the regular assembly before it
-        // does not.  The FP64 form's moments are formed at its first use (ensure_moments64).
-        ck(bem::launch_singular_static(d, d.pairrec, ctx->side), "singular moments kernel");
+        // the k-independent moments (FP64) on the side stream; the first singular kernel
+        // of a solve waits for them, the regular assembly before it does not
+        ck(bem::launch_singular_static(d, d.moments, d.pairrec, ctx->side), "singular moments kernel");
         ck(cudaEventCreateWithFlags(&m->moments_ready, cudaEventDisableTiming), "create event");
         ck(cudaEventRecord(m->moments_ready, ctx->side), "record event");
       }
@@ -1182,7 +1152,6 @@ int bem_solve_frequencies(bem_mesh* m, const double* freqs_hz, int n_freq, const
     if (!valid_options(ctx, o)) return BEM_ERR_INVALID_ARGUMENT;
     const bem::Precision prec = o.precision == BEM_PRECISION_MIXED ? bem::Precision::Mixed : bem::Precision::FP64;
     const bool cheb = prec == bem::Precision::Mixed && n_freq >= kChebMinFreqs;
-    if (prec == bem::Precision::FP64) ensure_moments64(m);
     if (cheb) {
       std::vector<double> kw(n_freq);
       for (int i = 0; i < n_freq; ++i) kw[i] = 2.0 * M_PI * freqs_hz[i] / o.sound_speed;

@@ -110,10 +110,7 @@ constexpr int kPairRec = 64;
 // Chebyshev terms of the mixed form's singular remainder expansion (bem_assembly.cu).
 constexpr int kChebN = 24;
 constexpr int kPairGeoDf = 48;
-// The pair setup and the FP32 static moments of the mixed form's pair records (at upload).
-cudaError_t launch_singular_static(const DeviceMesh& m, float* pairrec, cudaStream_t stream);
-// The FP64-accurate static moments of the plain FP64 form (at its first use; after the pair setup).
-cudaError_t launch_singular_moments64(const DeviceMesh& m, double* moments, cudaStream_t stream);
+cudaError_t launch_singular_static(const DeviceMesh& m, double* moments, float* pairrec, cudaStream_t stream);
 // Singular blocks of nfreq frequencies; frequency f's blocks start at element
 // f * blocks_stride of blocks (the mixed form takes two frequencies per launch).
 // use_cheb (mixed form): take the mesh's Chebyshev moments for the frequencies whose
