@@ -743,12 +743,59 @@ __global__ void pair_setup_kernel(SingularGeom geo, const SingularPair* __restri
   for (int i = kRecMom + kStatic; i < kPairRec; ++i) o[i] = 0.0f;
 }
 
+// Compensated accumulation in the style of Dot2 (Ogita, Rump and Oishi, "Accurate
+// sum and dot product", SIAM J. Sci. Comput. 26, 2005): a double-float
+// accumulator whose high part takes each term through two-sum and whose low part
+// sums the rounding errors and the terms' low parts in plain FP32.  A term is a
+// double-float value or the exact product of two (two-product of the high parts
+// plus the cross terms), so a term costs 8 or 12 FP32 instructions instead of the
+// 20 of a df_add (27 with the df_mul before it); the low part is folded back by
+// two-sum every few terms.  The result carries about 44 bits, as df arithmetic does.
+__device__ __forceinline__ void dacc_add(df& a, float th, float tl) {
+  const df s = two_sum(a.hi, th);
+  a.hi = s.hi;
+  a.lo += s.lo + tl;
+}
+__device__ __forceinline__ void dacc_mul(df& a, df x, df y) {
+  const float p = x.hi * y.hi;
+  dacc_add(a, p, fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, fmaf(x.hi, y.hi, -p))));
+}
+__device__ __forceinline__ df dacc_norm(df a) { return two_sum(a.hi, a.lo); }
+
+// warp_reduce_halving for double-float values, every addition a full df_add:
+// afterwards v[0..3) of lane l hold the warp sums of entries 3 (l >> s) ..
+// 3 (l >> s) + 2, s = 5 - log2(N / 3).
+template <int N, int O>
+__device__ __forceinline__ void warp_reduce_halving_df(df* v, int lane) {
+  if constexpr (O > 0) {
+    if constexpr (N > 3) {
+      constexpr int H = N / 2;
+      const bool upper = (lane & O) != 0;
+#pragma unroll
+      for (int i = 0; i < H; ++i) {
+        const df send = upper ? v[i] : v[H + i];
+        const df keep = upper ? v[H + i] : v[i];
+        v[i] = df_add(keep, df{__shfl_xor_sync(0xffffffffu, send.hi, O), __shfl_xor_sync(0xffffffffu, send.lo, O)});
+      }
+      warp_reduce_halving_df<H, O / 2>(v, lane);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        v[i] = df_add(v[i], df{__shfl_xor_sync(0xffffffffu, v[i].hi, O), __shfl_xor_sync(0xffffffffu, v[i].lo, O)});
+      warp_reduce_halving_df<N, O / 2>(v, lane);
+    }
+  }
+}
+
 // The 24 k-independent moments of a pair (one warp per pair, lanes over the
 // Duffy points), in double-float arithmetic on the FP32 pipe: every product,
 // sum, the reciprocal root and the accumulation carry about 44 bits, which is
 // FP64 accuracy for these sums at the FP32 rate (this part's FP64 rate is
-// 1/64 of it).  Lane i < 24 then writes moment i = jac * sum_i in FP64 and its
-// float copy into the pair record; lane 0 also writes the record's S0 term.
+// 1/64 of it).  The 24 moments are summed by the compensated accumulation
+// above (renormalised every eight points).  The lanes' partial
+// sums are combined by a reduce-scatter in full df_add; lane 4 j then holds
+// sums 3 j .. 3 j + 2 and writes moments = jac * sum in FP64 and their float
+// copies into the pair record; lane 0 also writes the record's S0 term.
 __global__ void __launch_bounds__(256)
     singular_moments_df_kernel(const SingularPair* __restrict__ pairs, int npairs, const int* __restrict__ rule_ptr,
                                const float* __restrict__ duffy_df, const float* __restrict__ geo_df,
@@ -772,13 +819,18 @@ __global__ void __launch_bounds__(256)
   df acc[kStatic];
 #pragma unroll
   for (int i = 0; i < kStatic; ++i) acc[i] = df{0.0f, 0.0f};
-  const df one = {1.0f, 0.0f};
   const int q0 = rule_ptr[P.rule], q1 = rule_ptr[P.rule + 1];
+  int it = 0;
   for (int q = q0 + lane; q < q1; q += 32) {
     const float* pt = duffy_df + 10 * (size_t)q;
     const df tu = {pt[0], pt[1]}, tv = {pt[2], pt[3]}, ru = {pt[4], pt[5]}, rvv = {pt[6], pt[7]}, w = {pt[8], pt[9]};
+    const df one = {1.0f, 0.0f};
     const df px[3] = {df_sub(df_sub(one, tu), tv), tu, tv};
     const df py[3] = {df_sub(df_sub(one, ru), rvv), ru, rvv};
+    // the point and the normal components in full df arithmetic: on a coincident
+    // pair (r . n = 0 in exact arithmetic) this keeps the double-layer moments at
+    // their rounding level; a compensated sum of the five terms of r left them
+    // about 50 times larger
     df rv[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -800,32 +852,30 @@ __global__ void __launch_bounds__(256)
     for (int a = 0; a < 3; ++a) {
       const df was = df_mul(ws, px[a]);
       const df wad = df_mul(wd, px[a]);
-      acc[a] = df_add(acc[a], was);
-      acc[21 + a] = df_add(acc[21 + a], df_mul(wn, px[a]));
+      dacc_add(acc[a], was.hi, was.lo);
+      dacc_mul(acc[21 + a], wn, px[a]);
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
-        acc[3 + 3 * a + b] = df_add(acc[3 + 3 * a + b], df_mul(was, py[b]));
-        acc[12 + 3 * a + b] = df_add(acc[12 + 3 * a + b], df_mul(wad, py[b]));
+        dacc_mul(acc[3 + 3 * a + b], was, py[b]);
+        dacc_mul(acc[12 + 3 * a + b], wad, py[b]);
       }
     }
-  }
-  // butterfly reduction: every lane ends with every sum
+    if ((++it & 7) == 0) {
 #pragma unroll
-  for (int i = 0; i < kStatic; ++i) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const df other = {__shfl_xor_sync(0xffffffffu, acc[i].hi, o), __shfl_xor_sync(0xffffffffu, acc[i].lo, o)};
-      acc[i] = df_add(acc[i], other);
+      for (int i = 0; i < kStatic; ++i) acc[i] = dacc_norm(acc[i]);
     }
   }
-  double mine = 0.0;
 #pragma unroll
-  for (int i = 0; i < kStatic; ++i)
-    if (lane == i) mine = df_to_double(acc[i]) * P.jac;
+  for (int i = 0; i < kStatic; ++i) acc[i] = dacc_norm(acc[i]);
+  warp_reduce_halving_df<kStatic, 16>(acc, lane);
   float* o = rec + (size_t)kPairRec * warp;
-  if (lane < kStatic) {
-    moments[(size_t)kStatic * warp + lane] = mine;
-    o[kRecMom + lane] = (float)mine;
+  if ((lane & 3) == 0) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double mine = df_to_double(acc[j]) * P.jac;
+      moments[(size_t)kStatic * warp + 3 * (lane >> 2) + j] = mine;
+      o[kRecMom + 3 * (lane >> 2) + j] = (float)mine;
+    }
   }
   if (lane == 0) {
     const double m0 = df_to_double(acc[0]) * P.jac, m1 = df_to_double(acc[1]) * P.jac,
