@@ -24,6 +24,7 @@
 #include <array>
 #include <cmath>
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <thread>
@@ -174,8 +175,13 @@ Adjacency classify(const int* fa, const int* fb) {
 }
 
 // Worker threads of the planner's parallel loops: the hardware threads, at most
-// 8; one for meshes too small to gain from it.
+// 8 (16 measured slower on a 16-core Grace host); one for meshes too small to gain
+// from it.  BEM_PLAN_THREADS (1-64) overrides the count; the plan does not depend on it.
 int plan_threads(int nf) {
+  if (const char* e = std::getenv("BEM_PLAN_THREADS")) {
+    const int t = std::atoi(e);
+    if (t >= 1 && t <= 64) return t;
+  }
   const unsigned hc = std::thread::hardware_concurrency();
   if (nf < 2000) return 1;
   return (int)std::max(1u, std::min(hc ? hc : 1u, 8u));

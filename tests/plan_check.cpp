@@ -1,7 +1,9 @@
 // Test driver: runs the mesh planner of the library on a mesh read from a
 // binary file (int32 nv, nf; float64 vertices[nv][3]; int32 faces[nf][3]) and
 // prints the tile and lane-group layout as text for the Python checks.
+// Arguments: mesh file, faces per tile, optional symmetry (0 none, 1 x, 2 xy).
 #include <cstdio>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -19,7 +21,8 @@ int main(int argc, char** argv) {
   std::fclose(f);
   if (!ok) return 2;
   bem::MeshPlan p;
-  const std::string err = bem::build_mesh_plan(v.data(), nv, fc.data(), nf, 4, 4, std::atoi(argv[2]), p);
+  const int symmetry = argc > 3 ? std::atoi(argv[3]) : 0;  // 0 none, 1 x, 2 xy
+  const std::string err = bem::build_mesh_plan(v.data(), nv, fc.data(), nf, 4, 4, std::atoi(argv[2]), p, symmetry);
   if (!err.empty()) {
     std::printf("error %s\n", err.c_str());
     return 1;
@@ -36,7 +39,10 @@ int main(int argc, char** argv) {
   }
   // singular pairs (trial, test), the faces' extended rows and the scatter plan
   std::printf("npairs %zu next %d\n", p.pairs.size(), p.n_ext);
-  for (size_t k = 0; k < p.pairs.size(); ++k) std::printf("pair %d %d\n", p.pairs[k].trial, p.pairs[k].test);
+  std::printf("radius %.17g points %lld\n", p.pair_radius, p.singular_points);
+  for (size_t k = 0; k < p.pairs.size(); ++k)
+    std::printf("pair %d %d %d %d\n", p.pairs[k].trial, p.pairs[k].test, p.pairs[k].tr,
+                p.rule_ptr[p.pairs[k].rule + 1] - p.rule_ptr[p.pairs[k].rule]);
   for (int f = 0; f < nf; ++f) std::printf("fext %d %d %d\n", p.face_ext[3 * f], p.face_ext[3 * f + 1], p.face_ext[3 * f + 2]);
   for (size_t i = 0; i < p.scat_col.size(); ++i) {
     std::printf("scat %d %d", p.scat_col[i], p.scat_row[i]);

@@ -143,3 +143,64 @@ def test_singular_scatter_plan_keeps_the_pair_order(plan_tool, tmp_path):
     assert np.array_equal(walk.view(np.int32), planned.view(np.int32))
     assert len({(c, r) for c, r, _ in scat}) == len(scat)
     assert np.all(used.reshape(-1, 12)[:, :9] == 1) and np.all(used.reshape(-1, 12)[:, 9:] == 0)
+
+
+def _mesh_file(tmp_path, mesh):
+    path = tmp_path / "mesh.bin"
+    with open(path, "wb") as f:
+        np.array([mesh.n_vertices, len(mesh.faces)], np.int32).tofile(f)
+        np.ascontiguousarray(mesh.vertices, np.float64).tofile(f)
+        np.ascontiguousarray(mesh.faces, np.int32).tofile(f)
+    return path
+
+
+def test_plan_does_not_depend_on_the_thread_count(plan_tool, tmp_path):
+    """The planner cuts its loops (face geometry, pair enumeration, lane packing,
+    field-major copies, scatter plan) into contiguous slices on worker threads and
+    joins them in slice order: the whole printed plan is the same for 1, 3 and 8
+    threads (BEM_PLAN_THREADS) on a mesh large enough to be planned in parallel."""
+    import os
+
+    path = _mesh_file(tmp_path, meshes.box_with_piston((0.3, 0.2, 0.25), 5000, 0.05, "+z"))
+    outs = []
+    for t in ("1", "3", "8"):
+        env = {**os.environ, "BEM_PLAN_THREADS": t}
+        outs.append(subprocess.run([str(plan_tool), str(path), "512"], check=True, capture_output=True, text=True,
+                                   env=env).stdout)
+    assert outs[0] == outs[1] == outs[2]
+
+
+def test_pair_radius_and_duffy_points(plan_tool, tmp_path):
+    """The planner's pair radius (the interval of the singular remainder's
+    Chebyshev expansion) is the largest distance between a vertex of a pair's test
+    face and one of its trial face, the trial face reflected for image pairs; the
+    Duffy point count is the sum of the pairs' rule sizes.  Checked against numpy
+    on a half model planned with symmetry x, whose image pairs carry reflected
+    trial faces."""
+    mesh = meshes.fundamental_domain(meshes.box_with_piston((0.3, 0.2, 0.25), 2000, 0.05, "+z"), "x")
+    out = subprocess.run([str(plan_tool), str(_mesh_file(tmp_path, mesh)), "512", "1"], check=True,
+                         capture_output=True, text=True).stdout
+    radius = points = None
+    pairs = []
+    for line in out.splitlines():
+        w = line.split()
+        if w[0] == "radius":
+            radius, points = float(w[1]), int(w[3])
+        elif w[0] == "pair":
+            pairs.append(tuple(map(int, w[1:5])))
+    assert pairs and radius is not None
+    p = np.array(pairs)
+    assert np.any(p[:, 2] == 1), "the half model has image pairs"
+    v = np.asarray(mesh.vertices, np.float64)
+    fc = np.asarray(mesh.faces)
+    sx = np.where(p[:, 2] & 1, -1.0, 1.0)
+    sy = np.where(p[:, 2] & 2, -1.0, 1.0)
+    best = 0.0
+    for a in range(3):
+        t = v[fc[p[:, 1], a]]
+        for b in range(3):
+            q = v[fc[p[:, 0], b]]
+            d = np.stack([sx * q[:, 0] - t[:, 0], sy * q[:, 1] - t[:, 1], q[:, 2] - t[:, 2]], 1)
+            best = max(best, float(np.max(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])))
+    assert radius == pytest.approx(np.sqrt(best), rel=1e-15)
+    assert points == int(p[:, 3].sum())
